@@ -1,0 +1,224 @@
+/*
+ * rsrgpu.h -- C ABI of the GB300 rasteriser (tile binning, per-tile coverage,
+ * depth test, fragment shading, sRGB8 resolve) that replaces the rglv
+ * virtual GPU of rsr.
+ *
+ * The calling surface mirrors rglv::GPU (src/rgl/rglv/rglv_gpu.hxx:97-277)
+ * and the command protocol recorded by rglv::GL (src/rgl/rglv/rglv_gl.hxx:
+ * 182-345, src/rgl/rglv/rglv_gpu_protocol.hxx:7-56).  Everything crosses the
+ * boundary as plain pointers and sizes; no C++ or torch types appear here.
+ *
+ * Command stream
+ * --------------
+ * A frame is a byte stream in rsr's own protocol (same opcodes, same field
+ * order and widths as rglv::GL writes them), with one difference: the 8-byte
+ * field after CMD_STATE carries the index of the state snapshot in the
+ * `states` array passed to rsrgpu_submit(), instead of a GLState address.
+ * Every other pointer field is an address supplied by the caller:
+ *   CMD_DRAW_ELEMENTS   op u8, 0x14 u8, hint u8, count i32, indices u16*
+ *   CMD_DRAW_ARRAYS     op u8, count i32
+ *   CMD_CLEAR           op u8, bits u8
+ *   CMD_STORE_COLOR_FULL_LINEAR_TC  op u8, gamma u8, rsrgpu_truecolor_canvas*
+ *   CMD_STORE_DEPTH_FULL_LINEAR_FP  op u8, float* (width*height, row-major)
+ *   CMD_EOF (optional; the stream may simply end)
+ *
+ * Memory
+ * ------
+ * Pointers in the stream and in the state snapshots may be device pointers
+ * (used in place) or host pointers previously declared with
+ * rsrgpu_register_host_buffer(); host inputs are copied to the device and
+ * host outputs copied back inside every rsrgpu_run(), so the caller's buffers
+ * keep the reference's meaning of "read when the frame runs".
+ *
+ * Errors
+ * ------
+ * Every entry point returns 0 on success and a negative RSRGPU_E* code
+ * otherwise; rsrgpu_last_error() gives the message.  The reference
+ * terminates the process on the same conditions (std::exit(1) at
+ * src/rgl/rglv/rglv_gpu.cxx:202-242,301-431).
+ */
+#ifndef RSRGPU_H
+#define RSRGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- protocol constants (src/rgl/rglv/rglv_gpu_protocol.hxx:7-56) ---- */
+#define RSRGPU_CMD_EOF                        0x8d
+#define RSRGPU_CMD_STATE                      1
+#define RSRGPU_CMD_CLEAR                      10
+#define RSRGPU_CMD_DRAW_ELEMENTS              11
+#define RSRGPU_CMD_DRAW_ARRAYS                12
+#define RSRGPU_CMD_DRAW_ELEMENTS_INSTANCED    13
+#define RSRGPU_CMD_DRAW_ARRAYS_INSTANCED      14
+#define RSRGPU_CMD_DRAW_INLINE                15
+#define RSRGPU_CMD_DRAW_INLINE_INSTANCED      16
+#define RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP 20
+#define RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP 21
+#define RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC 22
+#define RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP  23
+#define RSRGPU_CMD_STORE_DEPTH_FULL_QUADS_FP  24
+#define RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP 25
+#define RSRGPU_CMD_CLIPPED_TRI                100
+
+/* ---- GL enums (src/rgl/rglv/rglv_gl.hxx:20-62) ---- */
+#define RSRGPU_GL_FRONT            1
+#define RSRGPU_GL_BACK             2
+#define RSRGPU_GL_LESS             0
+#define RSRGPU_GL_LEQUAL           1
+#define RSRGPU_GL_EQUAL            2
+#define RSRGPU_GL_COLOR_BUFFER_BIT 1
+#define RSRGPU_GL_DEPTH_BUFFER_BIT 2
+#define RSRGPU_HINT_READ4          1
+#define RSRGPU_HINT_DENSE          2
+#define RSRGPU_RB_COLOR_DEPTH      0
+#define RSRGPU_RB_RGBF32           1
+#define RSRGPU_RB_RGBAF32          2
+#define RSRGPU_RB_F32              3
+
+/* ---- program ids (src/viewer/shaders.hxx, rglv_gpu_shaders.hxx) ---- */
+#define RSRGPU_PROGRAM_DEFAULT_POST  1   /* DefaultPostProgram, shaders.hxx:32 */
+#define RSRGPU_PROGRAM_EXPOSURE_POST 2   /* ExposurePostProgram, shaders.hxx:40 */
+#define RSRGPU_PROGRAM_AMY           4   /* AmyProgram (textured), shaders.hxx:69 */
+#define RSRGPU_PROGRAM_OBJ1          7   /* OBJ1Program (lit Gouraud), shaders.hxx:586 */
+#define RSRGPU_PROGRAM_GOURAUD       90  /* test program: per-vertex rgb, no lighting */
+
+/* ---- error codes ---- */
+#define RSRGPU_OK            0
+#define RSRGPU_EINVAL       -1   /* bad argument / malformed stream */
+#define RSRGPU_ENODISPATCH  -2   /* no program installed for a state key */
+#define RSRGPU_ECUDA        -3   /* CUDA runtime error */
+#define RSRGPU_ECAPACITY    -4   /* a device capacity was exceeded and could not be grown */
+#define RSRGPU_ETIMEOUT     -5   /* rsrgpu_wait() timed out */
+#define RSRGPU_EUNSUPPORTED -6   /* a protocol feature this build does not implement */
+
+/* Texture unit binding, mirrors rglv::TextureState (rglv_gl.hxx:64-77).
+ * ptr: RGBA float32 pixels (PixelToaster::FloatingPointPixel).  For square
+ * power-of-two textures the buffer holds the stacked mip chain built as in
+ * rglr::Texture::maybe_make_mipmap (rglr_texture.cxx:33-80): 2*width*width
+ * pixels. */
+typedef struct rsrgpu_texture_state {
+    const float* ptr;
+    int32_t width;
+    int32_t height;
+    int32_t stride;
+    int32_t filter;   /* 0 = nearest, 1 = bilinear (GL_LINEAR_MIPMAP_NEAREST) */
+} rsrgpu_texture_state;
+
+/* State snapshot, mirrors rglv::GLState (rglv_gl.hxx:80-179).  Matrices are
+ * column-major exactly as rmlm::mat4::ff. */
+typedef struct rsrgpu_glstate {
+    float clear_color[4];
+    float clear_depth;
+    int32_t clear_stencil;
+    int32_t culling_enabled;
+    int32_t cull_face;
+    int32_t scissor_enabled;
+    int32_t scissor_origin[2];
+    int32_t scissor_size[2];
+    int32_t viewport_origin[2];
+    int32_t viewport_size[2];      /* {0,0}: unset (std::nullopt) */
+    int32_t blending_enabled;
+    int32_t color_write_mask;
+    int32_t depth_write_mask;
+    int32_t depth_test_enabled;
+    int32_t depth_func;
+    int32_t program_id;
+    int32_t uniforms_ofs;          /* -1: no uniform block */
+    int32_t color0_attachment_type;
+    int32_t depth_attachment_type;
+    int32_t reserved0;
+    float uniforms[32];            /* the 32-float uniform block (UNIFORM_BUFFER_SIZE) */
+    const float* buffers[16];      /* SoA vertex attribute arrays */
+    rsrgpu_texture_state tus[2];
+    const float* tu3ptr;
+    int32_t tu3dim;
+    int32_t reserved1;
+    float view_matrix[16];
+    float normal_matrix[16];
+    float projection_matrix[16];
+} rsrgpu_glstate;
+
+/* Output target of CMD_STORE_COLOR_FULL_LINEAR_TC, mirrors
+ * rglr::TrueColorCanvas: 0x00RRGGBB pixels, row-major. */
+typedef struct rsrgpu_truecolor_canvas {
+    uint32_t* data;
+    int32_t width;
+    int32_t height;
+    int32_t stride;   /* in pixels */
+    int32_t reserved;
+} rsrgpu_truecolor_canvas;
+
+/* One clipped vertex as stored by the clipper, mirrors rglv::ClippedVertex
+ * (rglv_gpu.hxx:38-40): device coordinate + the program's VertexOutputSD. */
+typedef struct rsrgpu_clipped_vertex {
+    float coord[4];
+    float data[16];
+} rsrgpu_clipped_vertex;
+
+/* Per-frame statistics, mirrors rglv::GPUStats (rglv_gpu.hxx:51-62). */
+typedef struct rsrgpu_stats {
+    int64_t total_tiles;
+    int64_t total_tile_records;      /* triangle records over all tile lists */
+    int64_t total_clipped_records;
+    int64_t max_tile_records;
+    int64_t primitives_submitted;
+    int64_t primitives_clipped;
+    int64_t gpu_launches;            /* kernels launched by the last run */
+} rsrgpu_stats;
+
+typedef struct rsrgpu_ctx rsrgpu_ctx;
+
+/* GPU::GPU(concurrency, guid) -- rglv_gpu.cxx:18-24.  device: CUDA ordinal. */
+int rsrgpu_create(int device, rsrgpu_ctx** out);
+int rsrgpu_destroy(rsrgpu_ctx* ctx);
+
+/* GPU::Install(programId, stateKey, ptrs) -- rglv_gpu.cxx:26-47.  kind:
+ * 0 = bin (vertex) program, 1 = draw (fragment) program, 2 = blt program.
+ * Fails with RSRGPU_ENODISPATCH when this build has no device implementation
+ * of the program for that state key. */
+int rsrgpu_install(rsrgpu_ctx* ctx, int program_id, uint32_t state_key, int kind);
+
+/* GPU::Reset(sizeInPixels, tileSizeInBlocks) -- rglv_gpu.cxx:50-56.  Tiles are
+ * tile_blocks_x*8 by tile_blocks_y*8 pixels (kBlockDimensionsInPixels,
+ * rglv_gpu.hxx:27); width must be a multiple of 4 and height of 2, and tiles
+ * at most 128 pixels on a side (the reference's quad stride). */
+int rsrgpu_reset(rsrgpu_ctx* ctx, int width, int height, int tile_blocks_x, int tile_blocks_y);
+
+/* Declare a host buffer the stream or a state may point to. */
+int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t bytes);
+int rsrgpu_unregister_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr);
+
+/* Hand over one frame's commands (GL::commands_ plus its state deque). */
+int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes,
+                  const rsrgpu_glstate* states, int nstates);
+
+/* GPU::Run() -- rglv_gpu.hxx:167, rglv_gpu.cxx:90-116.  Enqueues the frame on
+ * `stream` (a cudaStream_t; NULL = the context's own stream). */
+int rsrgpu_run(rsrgpu_ctx* ctx, void* stream);
+
+/* Wait for the last run; timeout_ms < 0 waits without limit. */
+int rsrgpu_wait(rsrgpu_ctx* ctx, int timeout_ms);
+
+/* Debug/parity access to the bins of the last run.  Tile streams are written
+ * in the canonical form shared with the oracle: for each tile (row-major) a
+ * u32 byte length followed by the tile's command bytes with every pointer
+ * field removed and CMD_STATE carrying a u32 state ordinal.  *needed receives
+ * the full size. */
+int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* needed);
+int rsrgpu_dump_clipped(rsrgpu_ctx* ctx, rsrgpu_clipped_vertex* out, int capacity, int* count);
+int rsrgpu_get_stats(rsrgpu_ctx* ctx, rsrgpu_stats* out);
+
+/* Device timing of the last run's kernels (CUDA events on the run stream). */
+int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms);
+
+int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RSRGPU_H */

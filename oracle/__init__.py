@@ -1,0 +1,121 @@
+"""Oracle for the rasteriser path -- test infrastructure, not product code.
+
+Two CPU implementations live here, both driven by the same (command stream,
+state snapshots) input that rsrgpu_submit() takes:
+
+  * oracle/rsr_oracle.c  -- a plain-C restatement of rsr's binner, clipper,
+    tile rasteriser, fragment programs and resolve (each function cites the
+    reference lines it follows).  Portable (x86-64 and aarch64), built into
+    oracle/librsroracle.so.  Runs on every machine, including the GPU machine,
+    and is the CPU baseline there.
+  * oracle/_ref/librsrref.so -- rsr's own sources compiled by
+    oracle/ref/Makefile (x86-64 only, SSE4.1), used to pin the restatement.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline may load
+this package.
+"""
+import atexit
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_LIB = os.path.join(HERE, "_ref", "librsrref.so")
+ORACLE_LIB = os.path.join(HERE, "librsroracle.so")
+SRGB_LUT = os.path.join(os.path.dirname(HERE), "tests", "golden", "srgb8_lut.bin")
+
+_ref = None
+_oracle = None
+
+
+def _declare(lib, prefix):
+    from rsr_gb300 import abi
+    getattr(lib, prefix + "_init").argtypes = [ctypes.c_int]
+    getattr(lib, prefix + "_render").argtypes = [
+        ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(abi.GLStateC), ctypes.c_int,
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    getattr(lib, prefix + "_dump_tiles").argtypes = [
+        ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    getattr(lib, prefix + "_dump_clipped").argtypes = [
+        ctypes.POINTER(abi.ClippedVertexC), ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+
+
+def ref_available():
+    return os.path.exists(REF_LIB)
+
+
+def load_ref(threads=None):
+    global _ref
+    if _ref is None:
+        _ref = ctypes.CDLL(REF_LIB)
+        _declare(_ref, "rsrref")
+        _ref.rsrref_init(threads or os.cpu_count())
+        atexit.register(_ref.rsrref_shutdown)
+    return _ref
+
+
+def load_oracle(threads=None):
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_LIB):
+            raise RuntimeError("oracle not built: %s" % ORACLE_LIB)
+        _oracle = ctypes.CDLL(ORACLE_LIB)
+        _declare(_oracle, "rsroracle")
+        _oracle.rsroracle_init(threads or os.cpu_count())
+        lut = np.fromfile(SRGB_LUT, np.uint8)
+        _oracle.rsroracle_set_srgb_lut(lut.ctypes.data_as(ctypes.c_void_p), len(lut))
+    return _oracle
+
+
+class CpuRenderer:
+    """Renders scenes through one of the CPU implementations."""
+
+    def __init__(self, which="oracle", threads=None):
+        self.which = which
+        self.lib = load_ref(threads) if which == "ref" else load_oracle(threads)
+        self.prefix = "rsrref" if which == "ref" else "rsroracle"
+
+    def render_gl(self, gl, width, height, tile_blocks):
+        cmds = gl.stream()
+        states = gl.c_states()
+        buf = ctypes.create_string_buffer(cmds, len(cmds))
+        rc = getattr(self.lib, self.prefix + "_render")(
+            ctypes.cast(buf, ctypes.c_void_p), len(cmds), states, len(gl.states),
+            width, height, tile_blocks[0], tile_blocks[1])
+        if rc != 0:
+            raise RuntimeError("%s render failed: %d" % (self.which, rc))
+
+    def render(self, scene, gamma=True):
+        gl = scene.record(gamma=gamma)
+        self.render_gl(gl, scene.width, scene.height, scene.tile_blocks)
+        return scene.color.copy(), scene.depth.copy()
+
+    def tiles(self):
+        need = ctypes.c_size_t(0)
+        fn = getattr(self.lib, self.prefix + "_dump_tiles")
+        fn(None, 0, ctypes.byref(need))
+        out = (ctypes.c_uint8 * max(1, need.value))()
+        fn(out, need.value, ctypes.byref(need))
+        return split_tiles(bytes(out)[:need.value])
+
+    def clipped(self):
+        from rsr_gb300 import abi
+        n = ctypes.c_int(0)
+        fn = getattr(self.lib, self.prefix + "_dump_clipped")
+        fn(None, 0, ctypes.byref(n))
+        out = (abi.ClippedVertexC * max(1, n.value))()
+        fn(out, n.value, ctypes.byref(n))
+        return np.ctypeslib.as_array(ctypes.cast(out, ctypes.POINTER(ctypes.c_float)),
+                                     shape=(max(1, n.value) * 20,))[:n.value * 20].reshape(n.value, 20).copy()
+
+
+def split_tiles(blob):
+    """Splits a canonical tile dump (u32 length + bytes per tile) into a list."""
+    out = []
+    p = 0
+    while p < len(blob):
+        n = int.from_bytes(blob[p:p + 4], "little")
+        out.append(blob[p + 4:p + 4 + n])
+        p += 4 + n
+    return out

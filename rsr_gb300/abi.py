@@ -1,0 +1,154 @@
+"""ctypes mirror of include/rsrgpu.h (structs, constants) and the library loader.
+
+The product library is rsr_gb300/librsrgpu.so, built in-tree by
+rsr_gb300/build.py.  Loading it never falls back to anything else: if the
+shared object is missing the import of the GPU entry points fails loudly.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librsrgpu.so")
+
+# protocol (src/rgl/rglv/rglv_gpu_protocol.hxx:7-56)
+CMD_EOF = 0x8D
+CMD_STATE = 1
+CMD_CLEAR = 10
+CMD_DRAW_ELEMENTS = 11
+CMD_DRAW_ARRAYS = 12
+CMD_DRAW_INLINE = 15
+CMD_STORE_COLOR_FULL_LINEAR_TC = 22
+CMD_STORE_DEPTH_FULL_LINEAR_FP = 25
+CMD_CLIPPED_TRI = 100
+
+# GL enums (src/rgl/rglv/rglv_gl.hxx:20-62)
+GL_CULL_FACE = 1
+GL_SCISSOR_TEST = 2
+GL_BLEND = 3
+GL_DEPTH_TEST = 4
+GL_FRONT = 1
+GL_BACK = 2
+GL_LESS = 0
+GL_LEQUAL = 1
+GL_EQUAL = 2
+GL_COLOR_BUFFER_BIT = 1
+GL_DEPTH_BUFFER_BIT = 2
+GL_DEPTH_ATTACHMENT = 0
+GL_COLOR_ATTACHMENT0 = 2
+RGL_HINT_READ4 = 1
+RGL_HINT_DENSE = 2
+RB_COLOR_DEPTH = 0
+RB_RGBF32 = 1
+RB_RGBAF32 = 2
+RB_F32 = 3
+GL_NEAREST_MIPMAP_NEAREST = 0
+GL_LINEAR_MIPMAP_NEAREST = 1
+
+PROGRAM_DEFAULT_POST = 1
+PROGRAM_EXPOSURE_POST = 2
+PROGRAM_AMY = 4
+PROGRAM_OBJ1 = 7
+PROGRAM_GOURAUD = 90
+
+KIND_BIN, KIND_DRAW, KIND_BLT = 0, 1, 2
+
+RSRGPU_OK = 0
+
+
+class TextureState(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("stride", ctypes.c_int32),
+                ("filter", ctypes.c_int32)]
+
+
+class GLStateC(ctypes.Structure):
+    """rsrgpu_glstate, mirrors rglv::GLState (rglv_gl.hxx:80-179)."""
+    _fields_ = [
+        ("clear_color", ctypes.c_float * 4),
+        ("clear_depth", ctypes.c_float),
+        ("clear_stencil", ctypes.c_int32),
+        ("culling_enabled", ctypes.c_int32),
+        ("cull_face", ctypes.c_int32),
+        ("scissor_enabled", ctypes.c_int32),
+        ("scissor_origin", ctypes.c_int32 * 2),
+        ("scissor_size", ctypes.c_int32 * 2),
+        ("viewport_origin", ctypes.c_int32 * 2),
+        ("viewport_size", ctypes.c_int32 * 2),
+        ("blending_enabled", ctypes.c_int32),
+        ("color_write_mask", ctypes.c_int32),
+        ("depth_write_mask", ctypes.c_int32),
+        ("depth_test_enabled", ctypes.c_int32),
+        ("depth_func", ctypes.c_int32),
+        ("program_id", ctypes.c_int32),
+        ("uniforms_ofs", ctypes.c_int32),
+        ("color0_attachment_type", ctypes.c_int32),
+        ("depth_attachment_type", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("uniforms", ctypes.c_float * 32),
+        ("buffers", ctypes.c_void_p * 16),
+        ("tus", TextureState * 2),
+        ("tu3ptr", ctypes.c_void_p),
+        ("tu3dim", ctypes.c_int32),
+        ("reserved1", ctypes.c_int32),
+        ("view_matrix", ctypes.c_float * 16),
+        ("normal_matrix", ctypes.c_float * 16),
+        ("projection_matrix", ctypes.c_float * 16),
+    ]
+
+
+class TrueColorCanvasC(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("stride", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class ClippedVertexC(ctypes.Structure):
+    _fields_ = [("coord", ctypes.c_float * 4), ("data", ctypes.c_float * 16)]
+
+
+class StatsC(ctypes.Structure):
+    _fields_ = [("total_tiles", ctypes.c_int64),
+                ("total_tile_records", ctypes.c_int64),
+                ("total_clipped_records", ctypes.c_int64),
+                ("max_tile_records", ctypes.c_int64),
+                ("primitives_submitted", ctypes.c_int64),
+                ("primitives_clipped", ctypes.c_int64),
+                ("gpu_launches", ctypes.c_int64)]
+
+
+_LIB = None
+
+SYMBOLS = {
+    "rsrgpu_create": ([ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rsrgpu_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_install": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_reset": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_register_host_buffer": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t], ctypes.c_int),
+    "rsrgpu_unregister_host_buffer": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_submit": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int], ctypes.c_int),
+    "rsrgpu_run": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_wait": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_dump_tiles": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "rsrgpu_dump_clipped": ([ctypes.c_void_p, ctypes.POINTER(ClippedVertexC), ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "rsrgpu_get_stats": ([ctypes.c_void_p, ctypes.POINTER(StatsC)], ctypes.c_int),
+    "rsrgpu_last_timings": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "rsrgpu_last_error": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+}
+
+
+def load_library(path=LIB_PATH):
+    """Loads librsrgpu.so and declares every entry point of include/rsrgpu.h."""
+    global _LIB
+    if _LIB is not None and path == LIB_PATH:
+        return _LIB
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "librsrgpu.so is not built (%s); run __graft_entry__.build()" % path)
+    lib = ctypes.CDLL(path)
+    for name, (argtypes, restype) in SYMBOLS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = restype
+    if path == LIB_PATH:
+        _LIB = lib
+    return lib

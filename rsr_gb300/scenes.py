@@ -1,0 +1,275 @@
+"""Seeded synthetic scenes for the rasteriser path.
+
+RNG: splitmix64(seed); each draw u = (x >> 40) * 2^-24 in float32 and a value
+in [a, b) is a + (b - a) * u, also in float32.  Values are generated per
+triangle, per vertex, then per field in the listed order.  The same bytes
+feed the reference, the oracle and the GPU library.
+
+Scenes:
+  plain_raster      640x360, 10 000 random NDC triangles, Gouraud, no culling
+  textured_sphere   1920x1080, icosphere (subdivision 7: 327 680 triangles),
+                    60 degree camera at distance 3, back-face culling,
+                    1024x1024 value-noise texture with bilinear sampling
+Every scene ends with a STORE_COLOR (sRGB8) and STORE_DEPTH (fp32).
+"""
+import math
+
+import numpy as np
+
+from . import abi
+from .gl import GL
+
+GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(seed, n):
+    """The first n outputs of splitmix64(seed) as uint64."""
+    with np.errstate(over="ignore"):
+        i = np.arange(1, n + 1, dtype=np.uint64)
+        z = np.uint64(seed) + i * GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed, n):
+    return ((splitmix64(seed, n) >> np.uint64(40)).astype(np.float32)
+            * np.float32(1.0 / (1 << 24)))
+
+
+def lerp(a, b, u):
+    return (np.float32(a) + (np.float32(b) - np.float32(a)) * u).astype(np.float32)
+
+
+def pad4(a, fill=0.0):
+    n = (len(a) + 3) & ~3
+    out = np.full(n, fill, np.float32)
+    out[:len(a)] = a
+    return out
+
+
+# ---- matrices (column-major, rmlm::mat4::ff) ----
+def mat_from_rows(rows):
+    """rmlm::mat4's 16-float constructor takes rows (rmlm_mat4.hxx); ff is column-major."""
+    return np.asarray(rows, np.float32).reshape(4, 4).T.reshape(16).copy()
+
+
+def look_at(eye, center, up):
+    eye, center, up = (np.asarray(v, np.float64) for v in (eye, center, up))
+    f = center - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    rot = np.array([[s[0], s[1], s[2], 0], [u[0], u[1], u[2], 0],
+                    [-f[0], -f[1], -f[2], 0], [0, 0, 0, 1]])
+    tr = np.eye(4)
+    tr[:3, 3] = -eye
+    return mat_from_rows(rot @ tr)
+
+
+def perspective(fovy_deg, aspect, znear, zfar):
+    h = math.tan(math.radians(fovy_deg) / 2) * znear
+    w = h * aspect
+    l, r, b, t, n, f = -w, w, -h, h, znear, zfar
+    rows = [[2 * n / (r - l), 0, (r + l) / (r - l), 0],
+            [0, 2 * n / (t - b), (t + b) / (t - b), 0],
+            [0, 0, -(f + n) / (f - n), -2 * f * n / (f - n)],
+            [0, 0, -1, 0]]
+    return mat_from_rows(rows)
+
+
+class Scene:
+    """A frame description: dimensions, tile size, and a recorder callback.
+
+    `arrays` holds the host inputs by name; `record(gl, ref)` writes the frame
+    into a GL using ref(name) to obtain the buffer object to point at (the
+    numpy array itself, or a device tensor holding a copy of it)."""
+
+    def __init__(self, name, width, height, tile_blocks, arrays, record_fn, ntris):
+        self.name = name
+        self.width = width
+        self.height = height
+        self.tile_blocks = tile_blocks
+        self.arrays = arrays
+        self._record = record_fn
+        self.ntris = ntris
+        self.color = np.zeros(width * height, np.uint32)
+        self.depth = np.zeros(width * height, np.float32)
+
+    def record(self, ref=None, color=None, depth=None, gamma=True):
+        gl = GL()
+        ref = ref or (lambda k: self.arrays[k])
+        self._record(gl, ref)
+        gl.UseProgram(abi.PROGRAM_DEFAULT_POST)
+        gl.StoreColor(self.color if color is None else color, self.width, self.height, gamma)
+        gl.StoreDepth(self.depth if depth is None else depth)
+        return gl
+
+
+def _begin_frame(gl, clear_rgb=(0.0, 0.0, 0.0)):
+    gl.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, abi.RB_RGBF32)
+    gl.RenderbufferType(abi.GL_DEPTH_ATTACHMENT, abi.RB_F32)
+    gl.ClearColor(clear_rgb)
+    gl.ClearDepth(1.0)
+    gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
+
+
+def plain_raster(seed=0, ntris=10000, width=640, height=360, tile_blocks=(8, 8)):
+    """Random NDC triangles (xyz in [-1,1], w=1), rgb in [0,1], Gouraud, LESS,
+    no culling; one DrawElements of 3*ntris sequential indices."""
+    nverts = 3 * ntris
+    u = uniform01(seed, nverts * 6).reshape(ntris, 3, 6)
+    pos = lerp(-1.0, 1.0, u[:, :, 0:3]).reshape(nverts, 3)
+    rgb = lerp(0.0, 1.0, u[:, :, 3:6]).reshape(nverts, 3)
+    arrays = {
+        "px": pad4(pos[:, 0]), "py": pad4(pos[:, 1]), "pz": pad4(pos[:, 2]),
+        "cr": pad4(rgb[:, 0]), "cg": pad4(rgb[:, 1]), "cb": pad4(rgb[:, 2]),
+        "idx": np.arange(nverts, dtype=np.uint16),
+    }
+    if nverts > 32767:
+        raise ValueError("a draw holds at most 32767 vertices (u16 indices, bit 15 = back-face flag)")
+
+    def record(gl, ref):
+        _begin_frame(gl)
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
+        gl.UseBuffer(3, (ref("cr"), ref("cg"), ref("cb")))
+        gl.DrawElements(nverts, ref("idx"), 0)
+
+    return Scene("plain_raster", width, height, tile_blocks, arrays, record, ntris)
+
+
+# ---- icosphere ----
+def icosphere(divs):
+    """Unit icosphere: vertices (float32, normalised) and CCW-outward triangles."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+             (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(v, np.float64) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11),
+             (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6), (7, 1, 8),
+             (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9),
+             (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(divs):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+        nf = []
+        for (a, b, c) in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (ab, b, bc), (ab, bc, ca), (ca, bc, c)]
+        faces = nf
+    return np.array(verts, np.float32), np.array(faces, np.int64)
+
+
+def value_noise_rgba8(seed, dim=1024, cells=(8, 16, 32, 64)):
+    """Seeded multi-octave value noise, RGBA8 (alpha = 255)."""
+    img = np.zeros((dim, dim, 3), np.float64)
+    total = 0.0
+    for k, c in enumerate(cells):
+        lat = uniform01(seed * 7919 + k + 1, (c + 1) * (c + 1) * 3).reshape(c + 1, c + 1, 3).astype(np.float64)
+        lat[c, :, :] = lat[0, :, :]
+        lat[:, c, :] = lat[:, 0, :]
+        g = (np.arange(dim) + 0.5) * c / dim
+        i0 = np.floor(g).astype(int)
+        f = g - i0
+        f = f * f * (3 - 2 * f)
+        a = lat[i0][:, i0] * (1 - f)[None, :, None] + lat[i0][:, i0 + 1] * f[None, :, None]
+        b = lat[i0 + 1][:, i0] * (1 - f)[None, :, None] + lat[i0 + 1][:, i0 + 1] * f[None, :, None]
+        layer = a * (1 - f)[:, None, None] + b * f[:, None, None]
+        w = 1.0 / (1 << k)
+        img += w * layer
+        total += w
+    rgb = np.clip(np.round(img / total * 255.0), 0, 255).astype(np.uint8)
+    out = np.full((dim, dim, 4), 255, np.uint8)
+    out[:, :, :3] = rgb
+    return out
+
+
+def srgb8_to_linear(c):
+    c = c.astype(np.float64) / 255.0
+    return np.where(c <= 0.04045, c / 12.92, ((c + 0.055) / 1.055) ** 2.4).astype(np.float32)
+
+
+def make_mip_chain(rgba):
+    """Stacked mip chain as rglr::Texture::maybe_make_mipmap builds it
+    (rglr_texture.cxx:33-80): level 0 in rows [0, W), each next level below
+    the previous one with the same row stride; each texel the float32 sum of
+    its 2x2 parents ((a+b)+c)+d divided by 4."""
+    dim = rgba.shape[0]
+    buf = np.zeros((2 * dim, dim, 4), np.float32)
+    buf[:dim] = rgba
+    src_row, size = 0, dim
+    dst_row = dim
+    while size > 1:
+        s = buf[src_row:src_row + size, :size]
+        a, b = s[0::2, 0::2], s[0::2, 1::2]
+        c, d = s[1::2, 0::2], s[1::2, 1::2]
+        buf[dst_row:dst_row + size // 2, :size // 2] = (((a + b) + c) + d) / np.float32(4.0)
+        src_row = dst_row
+        dst_row += size // 2
+        size //= 2
+    return buf.reshape(-1)
+
+
+def textured_sphere(seed=1, divs=7, width=1920, height=1080, tile_blocks=(4, 4), tex_dim=1024):
+    """AmyProgram on an icosphere, chunked into draws of at most 32767 vertices."""
+    verts, faces = icosphere(divs)
+    # spherical uv
+    uu = (np.arctan2(verts[:, 2], verts[:, 0]) / (2 * np.pi) + 0.5).astype(np.float32)
+    vv = (np.arcsin(np.clip(verts[:, 1], -1, 1)) / np.pi + 0.5).astype(np.float32)
+    arrays = {}
+    draws = []
+    start = 0
+    nfaces = len(faces)
+    while start < nfaces:
+        local = {}
+        end = start
+        while end < nfaces:
+            new = [v for v in faces[end] if v not in local]
+            if len(local) + len(new) > 32764:
+                break
+            for v in new:
+                local[v] = len(local)
+            end += 1
+        gidx = np.fromiter(local.keys(), np.int64, len(local))
+        k = len(draws)
+        arrays["px%d" % k] = pad4(verts[gidx, 0])
+        arrays["py%d" % k] = pad4(verts[gidx, 1])
+        arrays["pz%d" % k] = pad4(verts[gidx, 2])
+        arrays["u%d" % k] = pad4(uu[gidx])
+        arrays["v%d" % k] = pad4(vv[gidx])
+        arrays["idx%d" % k] = np.array([local[v] for f in faces[start:end] for v in f], np.uint16)
+        draws.append((k, 3 * (end - start)))
+        start = end
+    rgba8 = value_noise_rgba8(seed, tex_dim)
+    lin = np.empty((tex_dim, tex_dim, 4), np.float32)
+    lin[:, :, :3] = srgb8_to_linear(rgba8[:, :, :3])
+    lin[:, :, 3] = rgba8[:, :, 3].astype(np.float32) / np.float32(255.0)
+    arrays["tex"] = make_mip_chain(lin)
+    view = look_at((0.0, 0.0, 3.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0))
+    proj = perspective(60.0, width / height, 0.1, 100.0)
+
+    def record(gl, ref):
+        _begin_frame(gl, (0.1, 0.1, 0.1))
+        gl.UseProgram(abi.PROGRAM_AMY)
+        gl.Enable(abi.GL_CULL_FACE)
+        gl.CullFace(abi.GL_BACK)
+        gl.ViewMatrix(view)
+        gl.ProjectionMatrix(proj)
+        gl.BindTexture(0, ref("tex"), tex_dim, tex_dim, tex_dim, abi.GL_LINEAR_MIPMAP_NEAREST)
+        for k, count in draws:
+            gl.UseBuffer(0, (ref("px%d" % k), ref("py%d" % k), ref("pz%d" % k)))
+            gl.UseBuffer(9, ref("u%d" % k))
+            gl.UseBuffer(10, ref("v%d" % k))
+            gl.DrawElements(count, ref("idx%d" % k), abi.RGL_HINT_DENSE | abi.RGL_HINT_READ4)
+
+    return Scene("textured_sphere", width, height, tile_blocks, arrays, record, nfaces)
