@@ -1,0 +1,349 @@
+"""Benchmark of the rasteriser hot path on GB300.
+
+Workload (one step = one frame): the textured perspective mesh at 1920x1080 --
+an icosphere subdivided 7 times (327 680 triangles, the subdivision level
+closest to "about 500k"), 60 degree camera at distance 3, back-face culling,
+1024x1024 value-noise texture sampled bilinearly (AmyProgram), depth LESS,
+sRGB8 colour + fp32 depth stores; 32x32-pixel tiles.  Synthetic seeded data.
+
+Reported (one JSON line from rank 0):
+  value      Mtris/s with inputs resident in HBM, device time of the frame's
+             kernels (CUDA events on the launching stream), L2 flushed with a
+             256 MiB write before every timed frame (outside the event pair)
+  e2e        the same metric through the C ABI with host (pinned) buffers:
+             every frame copies its inputs to the device and its colour and
+             depth back, inside the timed region
+  roofline   dominant kernel (raster) against measured HBM bandwidth
+  cpu_baseline  the CPU implementation on this machine's cores, bounded sample
+
+`--impl reference` times the CPU implementation of the same frame instead:
+rsr itself (oracle/_ref) where it can run (x86-64 hosts), else the oracle's
+C restatement (the reference's SSE code does not build for aarch64).
+
+Multi-GPU: frames are independent, so N ranks render N replicas (weak
+scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "Mtris/s (1080p textured perspective mesh, 1 GB300)"
+UNIT = "Mtris/s"
+PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload():
+    from rsr_gb300 import scenes
+    return scenes.textured_sphere(seed=1, divs=7, width=1920, height=1080, tile_blocks=(4, 4))
+
+
+def config_dict(sc):
+    return {"workload": "textured_sphere_1080p", "triangles": sc.ntris, "width": sc.width,
+            "height": sc.height, "tile_px": sc.tile_blocks[0] * 8, "texture": "1024x1024 RGBA mip chain, bilinear",
+            "program": "AmyProgram", "culling": "back", "l2": "flushed (256 MiB write) before each timed frame",
+            "parallelism": "replicas"}
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, device_index=0):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        rows = [r for r in rows if r[0] == str(device_index)] or rows
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(which, sc, seconds=15.0, max_frames=200, threads=None):
+    """Times the CPU implementation on a bounded sample of frames."""
+    import oracle
+    threads = threads or os.cpu_count()
+    r = oracle.CpuRenderer(which, threads=threads)
+    r.render(sc, True)   # warm-up (page-in, allocation)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while len(times) < max_frames and (time.perf_counter() < t_end or len(times) < 3):
+        t0 = time.perf_counter()
+        gl = sc.record(gamma=True)
+        r.render_gl(gl, sc.width, sc.height, sc.tile_blocks)
+        times.append(time.perf_counter() - t0)
+    med = statistics.median(times)
+    return {"value": sc.ntris / med / 1e6, "unit": UNIT, "cores": threads,
+            "kind": "reference" if which == "ref" else "port",
+            "sample": "%d frames of the same 1080p frame, median %.2f ms/frame (%s)" % (
+                len(times), med * 1e3, "rsr built from source" if which == "ref" else "C restatement of rsr's path"),
+            "frames_per_s": 1.0 / med}
+
+
+def cpu_impl_available():
+    import oracle
+    if platform.machine() in ("x86_64", "AMD64") and oracle.ref_available():
+        return "ref"
+    return "oracle"
+
+
+def run_reference(args):
+    world, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    from rsr_gb300 import build
+    build.build_oracle()
+    sc = workload()
+    which = cpu_impl_available()
+    import oracle
+    threads = os.cpu_count()
+    r = oracle.CpuRenderer(which, threads=threads)
+    for _ in range(args.warmup):
+        r.render(sc, True)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        gl = sc.record(gamma=True)
+        r.render_gl(gl, sc.width, sc.height, sc.tile_blocks)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sc.ntris * args.steps / total / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "config": config_dict(sc),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
+                             "kind": "reference" if which == "ref" else "port",
+                             "sample": "%d timed frames after %d warm-up, all host threads" % (args.steps, args.warmup)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "frames_per_s": args.steps / total}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    from rsr_gb300 import build
+    build.build_gpu()
+    from rsr_gb300.gpu import GPU
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    sc = workload()
+    gpu = GPU(local)
+    gpu.InstallDefaults()
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+
+    # ---- device-resident inputs and outputs ----
+    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+    col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+    dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+    gl = sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)
+    gpu.submit(gl)
+    torch.cuda.synchronize()
+    for _ in range(max(args.warmup, 3)):
+        gpu.run(sptr)
+        gpu.Wait()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    raster_ms = []
+    clocks = ClockSampler(os.path.join(REPO, "gpurun_out", "bench_clocks_%d.csv" % rank)
+                          if os.path.isdir(os.path.join(REPO, "gpurun_out")) else "/tmp/bench_clocks_%d.csv" % rank)
+    barrier(world)
+    torch.cuda.synchronize()
+    with clocks, torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 0xff)                     # evict L2 (outside the timed pair)
+            ev[i][0].record(stream)
+            gpu.run(sptr)
+            ev[i][1].record(stream)
+            gpu.Wait()
+            raster_ms.append(gpu.timings()[1])
+        torch.cuda.synchronize()
+    barrier(world)
+    dev_ms = sum(s.elapsed_time(e) for s, e in ev)
+    dev_ms = max_over_ranks(world, dev_ms)
+    value = sc.ntris * args.steps * world / (dev_ms / 1e3) / 1e6
+    ms_per_step = dev_ms / args.steps
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    host = {k: torch.from_numpy(v).pin_memory() for k, v in sc.arrays.items()}
+    hcol = torch.zeros(sc.width * sc.height, dtype=torch.int32).pin_memory()
+    hdep = torch.zeros(sc.width * sc.height, dtype=torch.float32).pin_memory()
+    for t in list(host.values()) + [hcol, hdep]:
+        gpu.register_host_buffer(t)
+    gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+    gl2 = sc.record(ref=host.__getitem__, color=hcol, depth=hdep, gamma=True)
+    gpu.submit(gl2)
+    for _ in range(max(args.warmup, 3)):
+        gpu.run(sptr)
+        gpu.Wait()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = hcol.numel() * 4 + hdep.numel() * 4
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gpu.run(sptr)
+        gpu.Wait()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    e2e_ms = max_over_ranks(world, max(wall_ms, e0.elapsed_time(e1)))
+    e2e_value = sc.ntris * args.steps * world / (e2e_ms / 1e3) / 1e6
+    # the frame is correct end to end (depth of the last host frame equals the device one)
+    assert torch.equal(hdep, dep.cpu())
+
+    if rank != 0:
+        return
+    peak, peak_kind = hbm_peak()
+    raster_avg = statistics.mean(raster_ms)
+    # algorithmic DRAM bytes of one raster launch: the triangle records it reads
+    # (96 B per tile-list entry), the colour and depth it writes (8 B per
+    # pixel) and the sampled mip level-0 texels (16 B each, read once)
+    st = gpu.stats() if False else None
+    gpu_tiles_bytes = _raster_bytes(gpu, sc)
+    achieved = gpu_tiles_bytes / (raster_avg / 1e3) / 1e9
+    roof = {"kernel": "raster_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": _ncu_traffic(), "algorithmic_bytes_per_launch": gpu_tiles_bytes,
+            "avg_launch_ms": raster_avg}
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_sample(cpu_impl_available(), sc, seconds=args.cpu_seconds)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere + value-noise texture)",
+            "config": config_dict(sc),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms / args.steps},
+            "frames_per_s": 1e3 / ms_per_step, "e2e_frames_per_s": 1e3 * args.steps / e2e_ms,
+            "gpu_launches": 3 * args.steps, "roofline": roof, "cpu_baseline": cpu,
+            "clocks": clocks.summary(local)}
+    print(json.dumps(line))
+
+
+_RASTER_BYTES = {}
+
+
+def _raster_bytes(gpu, sc):
+    """Algorithmic bytes of one raster launch for this frame (see run_gpu)."""
+    tiles = gpu.tiles()
+    st = gpu.stats()
+    records = st["total_tile_records"] + st["total_clipped_records"]
+    texels = 1024 * 1024
+    return int(records * 96 + sc.width * sc.height * 8 + texels * 16)
+
+
+def _ncu_traffic():
+    """DRAM bytes per raster launch from the committed ncu capture, if any."""
+    p = os.path.join(REPO, "profiles", "raster_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)["dram_bytes_per_launch"]
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

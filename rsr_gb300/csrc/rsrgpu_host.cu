@@ -1,0 +1,820 @@
+// rsrgpu_host.cu -- host runtime behind include/rsrgpu.h.
+//
+// Replaces the host half of rglv::GPU (src/rgl/rglv/rglv_gpu.cxx): program
+// installation, Reset/Retile, the command interpreter of BinImpl (here it only
+// decodes the stream into device tables: states, draws and the frame's op
+// list, since state/clear/store commands are identical for every tile), and
+// RunImpl, which becomes a fixed sequence of stream-ordered device work:
+//   H2D of host inputs -> memset(counters) -> setup -> bin -> raster -> D2H.
+// Errors are reported as status codes instead of std::exit(1).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <set>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "../../include/rsrgpu.h"
+#include "rsrgpu_internal.h"
+
+namespace rsrgpu {
+cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+
+static const uint32_t kRcpTable[2048] = {
+#include "rcpps_table.inc"
+};
+}  // namespace rsrgpu
+
+using namespace rsrgpu;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t n = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) cap = n;
+        return e;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+    template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct HostBuffer {
+    const uint8_t* host = nullptr;
+    size_t bytes = 0;
+    void* dev = nullptr;
+    bool in = false, out = false;
+};
+
+struct Copy { void* dst; const void* src; size_t bytes; };
+
+}  // namespace
+
+struct rsrgpu_ctx {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t run_stream = nullptr;
+    std::string err;
+    // render target (GPU::Reset)
+    int width = 0, height = 0, tile_w = 64, tile_h = 64, tiles_x = 0, tiles_y = 0, ntiles = 0;
+    std::set<uint64_t> installed;   // (kind << 56) | (program << 24) | key
+    std::map<const uint8_t*, HostBuffer> host;
+    // frame tables
+    std::vector<DevState> states;
+    std::vector<int32_t> state_ordinal;
+    std::vector<DevDraw> draws;
+    std::vector<FrameOp> ops;
+    int ntris = 0;
+    bool submitted = false;
+    bool ran = false;
+    // device memory
+    DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
+        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb;
+    uint32_t clip_cap = 1u << 18;
+    uint32_t bin_cap = 1u << 22;
+    FrameCounters* h_counters = nullptr;   // pinned
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    FrameView fv{};
+    rsrgpu_stats stats{};
+};
+
+namespace {
+
+int fail(rsrgpu_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+int cuda_fail(rsrgpu_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, RSRGPU_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what) do { cudaError_t e_ = (expr); if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); } while (0)
+
+// float op order of rmlm::operator*(mat4, mat4) (rmlm_mat4.hxx:196-207); the
+// host compiler runs with -ffp-contract=off so each product and sum rounds
+void mat4_mul(const float* l, const float* r, float* out) {
+    for (int row = 0; row < 4; ++row) {
+        for (int col = 0; col < 4; ++col) {
+            float ax = l[0 * 4 + row] * r[col * 4 + 0];
+            ax = ax + l[1 * 4 + row] * r[col * 4 + 1];
+            ax = ax + l[2 * 4 + row] * r[col * 4 + 2];
+            ax = ax + l[3 * 4 + row] * r[col * 4 + 3];
+            out[col * 4 + row] = ax;
+        }
+    }
+}
+
+int ilog2u(unsigned x) { int p = 0; while (x) { x >>= 1; ++p; } return p - 1; }
+
+uint32_t fragment_state_key(const rsrgpu_glstate& s) {   // GLState::FragmentStateKey (rglv_gl.hxx:136-146)
+    uint32_t key = uint32_t(s.program_id) << 24;
+    key |= uint32_t(s.scissor_enabled != 0);
+    key |= uint32_t(s.depth_test_enabled != 0) << 1;
+    if (s.depth_test_enabled) key |= uint32_t(s.depth_func) << 2;
+    key |= uint32_t(s.blending_enabled != 0) << 4;
+    key |= uint32_t(s.depth_write_mask != 0) << 5;
+    key |= uint32_t(s.color_write_mask != 0) << 6;
+    key |= uint32_t(s.color0_attachment_type) << 7;
+    key |= uint32_t(s.depth_attachment_type) << 9;
+    return key;
+}
+
+bool draw_program_supported(int pid) { return pid == kProgGouraud || pid == kProgAmy; }
+bool blt_program_supported(int pid) { return pid == kProgDefaultPost || pid == kProgExposurePost || pid == kProgGouraud; }
+
+// the fragment state keys this device implementation covers: no scissor, depth
+// test on with LESS/LEQUAL/EQUAL, RGB f32 colour with f32 depth, or colour and
+// depth packed in RGBA (RB_COLOR_DEPTH)
+bool draw_key_supported(uint32_t key) {
+    key &= 0xffffffu;
+    if (key & 1u) return false;
+    if (!(key & 2u)) return false;
+    if (((key >> 2) & 3u) > 2u) return false;
+    const uint32_t ct = (key >> 7) & 3u, dt = (key >> 9) & 3u;
+    if (ct == RSRGPU_RB_RGBF32 && dt == RSRGPU_RB_F32) return true;
+    if (ct == RSRGPU_RB_COLOR_DEPTH && dt == RSRGPU_RB_COLOR_DEPTH) return true;
+    return false;
+}
+
+// sRGB8 encode table of this library: for each of the 13*2048 float classes
+// the clamped input falls into (exponent and top 11 mantissa bits), the
+// correctly rounded 8-bit sRGB value of the class midpoint.
+void build_srgb_lut(std::vector<uint8_t>& lut) {
+    lut.resize(26624);
+    for (uint32_t k = 0; k < 26624; ++k) {
+        const uint32_t bits = ((k + ((127u - 13u) << 11)) << 12) | 0x800u;
+        float f;
+        std::memcpy(&f, &bits, 4);
+        const double x = f;
+        const double s = x <= 0.0031308 ? 12.92 * x : 1.055 * std::pow(x, 1.0 / 2.4) - 0.055;
+        double v = std::floor(s * 255.0 + 0.5);
+        lut[k] = uint8_t(v < 0 ? 0 : (v > 255 ? 255 : v));
+    }
+}
+
+// Maps a caller pointer to a device address and the number of bytes that
+// are valid from it (to the end of the registered host buffer, or of the
+// device allocation containing it).
+int resolve(rsrgpu_ctx* ctx, const void* p, bool output, void** out, const char* what, size_t* avail = nullptr) {
+    *out = nullptr;
+    if (avail) *avail = 0;
+    if (p == nullptr) return 0;
+    const uint8_t* bp = static_cast<const uint8_t*>(p);
+    auto it = ctx->host.upper_bound(bp);
+    if (it != ctx->host.begin()) {
+        --it;
+        HostBuffer& hb = it->second;
+        if (bp >= hb.host && bp < hb.host + hb.bytes) {
+            if (output) hb.out = true; else hb.in = true;
+            *out = static_cast<uint8_t*>(hb.dev) + (bp - hb.host);
+            if (avail) *avail = hb.bytes - size_t(bp - hb.host);
+            return 0;
+        }
+    }
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e == cudaSuccess && (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)) {
+        // cuMemGetAddressRange through the runtime's driver entry point, so the
+        // library itself does not link libcuda (it loads on machines without a GPU)
+        using RangeFn = CUresult (*)(CUdeviceptr*, size_t*, CUdeviceptr);
+        static RangeFn range_fn = nullptr;
+        if (range_fn == nullptr) {
+            void* fn = nullptr;
+            cudaDriverEntryPointQueryResult q{};
+            if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+                range_fn = reinterpret_cast<RangeFn>(fn);
+        }
+        CUdeviceptr base = 0;
+        size_t size = 0;
+        if (range_fn == nullptr || range_fn(&base, &size, CUdeviceptr(uintptr_t(p))) != CUDA_SUCCESS)
+            return fail(ctx, RSRGPU_EINVAL, "%s pointer %p: allocation range unknown", what, p);
+        *out = const_cast<void*>(p);
+        if (avail) *avail = size_t(base + size - CUdeviceptr(uintptr_t(p)));
+        return 0;
+    }
+    cudaGetLastError();
+    return fail(ctx, RSRGPU_EINVAL, "%s pointer %p is neither device memory nor a registered host buffer", what, p);
+}
+
+template <typename T>
+bool rd(const uint8_t*& p, const uint8_t* end, T& v) {
+    if (p + sizeof(T) > end) return false;
+    std::memcpy(&v, p, sizeof(T));
+    p += sizeof(T);
+    return true;
+}
+
+int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
+    std::memset(&d, 0, sizeof(d));
+    mat4_mul(s.projection_matrix, s.view_matrix, d.vpm);   // MakeMatrices: vpm = P * V
+    int vx = ctx->width, vy = ctx->height;                 // GPU::DSDO (rglv_gpu.hxx:265-270)
+    if (s.viewport_size[0] != 0 || s.viewport_size[1] != 0) { vx = s.viewport_size[0]; vy = s.viewport_size[1]; }
+    d.DS[0] = float(vx / 2);
+    d.DS[1] = float(-vy / 2);
+    d.DO[0] = float(vx / 2 + s.viewport_origin[0]);
+    d.DO[1] = float(ctx->height - (vy / 2 + s.viewport_origin[1]));
+    {   // CalcGuardBandFactor (rglv_view_frustum.hxx:36-39)
+        const int longSide = std::max(ctx->width, ctx->height);
+        const int half = longSide / 2;
+        d.guard = (2048.0f - float(half)) / float(half);
+    }
+    if (!s.scissor_enabled) {   // GPU::ScissorRect (rglv_gpu.hxx:272-276)
+        d.scissor[0] = 0; d.scissor[1] = 0; d.scissor[2] = ctx->width; d.scissor[3] = ctx->height;
+    } else {
+        const int left = s.scissor_origin[0], right = left + s.scissor_size[0];
+        const int bottom = ctx->height - s.scissor_origin[1] - 1, top = bottom - s.scissor_size[1];
+        d.scissor[0] = left; d.scissor[1] = top; d.scissor[2] = right; d.scissor[3] = bottom;
+    }
+    d.program = s.program_id;
+    d.nvary = s.program_id == kProgGouraud ? 3 : (s.program_id == kProgAmy ? 2 : 0);
+    d.keep_backs = !(s.culling_enabled && s.cull_face == RSRGPU_GL_BACK);
+    d.keep_fronts = !(s.culling_enabled && s.cull_face == RSRGPU_GL_FRONT);
+    d.cull_enabled = s.culling_enabled != 0;
+    d.cull_face = s.cull_face;
+    d.depth_test = s.depth_test_enabled != 0;
+    d.depth_func = s.depth_func;
+    d.depth_write = s.depth_write_mask != 0;
+    d.color_write = s.color_write_mask != 0;
+    d.blend = s.blending_enabled != 0;
+    d.color_type = s.color0_attachment_type;
+    d.depth_type = s.depth_attachment_type;
+    std::memcpy(d.clear_color, s.clear_color, sizeof(d.clear_color));
+    d.clear_depth = s.clear_depth;
+    std::memcpy(d.uniforms, s.uniforms, sizeof(d.uniforms));
+    for (int i = 0; i < 16; ++i) {
+        void* dp = nullptr;
+        size_t avail = 0;
+        int rc = resolve(ctx, s.buffers[i], false, &dp, "vertex buffer", &avail);
+        if (rc) return rc;
+        d.buffers[i] = static_cast<const float*>(dp);
+        d.buffer_len[i] = int32_t(std::min<size_t>(avail / sizeof(float), size_t(INT32_MAX)));
+    }
+    // MakeTextureUnit (rglr_texture_sampler.cxx:314-363)
+    const rsrgpu_texture_state& t = s.tus[0];
+    d.tu0.width = t.width; d.tu0.height = t.height; d.tu0.stride = t.stride;
+    d.tu0.power = ilog2u(unsigned(t.width));
+    const bool pow2 = t.width > 0 && (1 << d.tu0.power) == t.width && t.width == t.height && t.stride == t.width;
+    d.tu0.kind = pow2 ? (t.filter ? 1 : 0) : 2;
+    if (s.program_id == kProgAmy) {
+        if (t.ptr == nullptr) return fail(ctx, RSRGPU_EINVAL, "AmyProgram draw without a texture on unit 0");
+        if (pow2 && (t.width < 4 || t.width > 1024))
+            return fail(ctx, RSRGPU_EUNSUPPORTED, "can't make TextureUnit for pow2 size %d", t.width);
+        void* dp = nullptr;
+        size_t avail = 0;
+        int rc = resolve(ctx, t.ptr, false, &dp, "texture", &avail);
+        if (rc) return rc;
+        // the mip chain of a square power-of-two texture (2*W*W texels), else H rows of stride texels
+        const size_t need = pow2 ? size_t(2) * size_t(t.width) * size_t(t.width) * 16u
+                                 : size_t(std::max(t.height, 1)) * size_t(std::max(t.stride, 1)) * 16u;
+        if (t.width <= 0 || t.height <= 0 || t.stride < t.width || avail < need)
+            return fail(ctx, RSRGPU_EINVAL, "texture buffer holds %zu bytes, its %dx%d (stride %d) layout needs %zu",
+                        avail, t.width, t.height, t.stride, need);
+        d.tu0.buf = static_cast<const float*>(dp);
+        d.tu0.texels = int32_t(std::min<size_t>(avail / 16u, size_t(INT32_MAX)));
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsrgpu_create(int device, rsrgpu_ctx** out) {
+    if (out == nullptr) return RSRGPU_EINVAL;
+    *out = nullptr;
+    rsrgpu_ctx* ctx = new rsrgpu_ctx;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete ctx; return RSRGPU_ECUDA; }
+    if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_counters), sizeof(FrameCounters), cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev2) != cudaSuccess || cudaEventCreate(&ctx->ev3) != cudaSuccess) {
+        rsrgpu_destroy(ctx);
+        return RSRGPU_ECUDA;
+    }
+    std::vector<uint8_t> lut;
+    build_srgb_lut(lut);
+    if (ctx->d_rcp.ensure(sizeof(kRcpTable)) != cudaSuccess || ctx->d_srgb.ensure(lut.size()) != cudaSuccess ||
+        cudaMemcpy(ctx->d_rcp.p, kRcpTable, sizeof(kRcpTable), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(ctx->d_srgb.p, lut.data(), lut.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        rsrgpu_destroy(ctx);
+        return RSRGPU_ECUDA;
+    }
+    std::memset(ctx->h_counters, 0, sizeof(FrameCounters));
+    *out = ctx;
+    return 0;
+}
+
+int rsrgpu_destroy(rsrgpu_ctx* ctx) {
+    if (ctx == nullptr) return 0;
+    if (ctx->own) cudaStreamSynchronize(ctx->own);
+    for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
+    DevBuf* bufs[] = { &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+                       &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
+                       &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
+                       &ctx->d_rcp, &ctx->d_srgb };
+    for (DevBuf* b : bufs) b->release();
+    if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3 };
+    for (cudaEvent_t ev : evs) if (ev) cudaEventDestroy(ev);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return 0;
+}
+
+int rsrgpu_install(rsrgpu_ctx* ctx, int program_id, uint32_t state_key, int kind) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (kind == 0) {
+        if (!draw_program_supported(program_id))
+            return fail(ctx, RSRGPU_ENODISPATCH, "no device vertex program for pid(%d)", program_id);
+    } else if (kind == 1) {
+        if (!draw_program_supported(program_id) || !draw_key_supported(state_key))
+            return fail(ctx, RSRGPU_ENODISPATCH, "no device fragment program for pid(%d) state(0x%x)", program_id, state_key);
+    } else if (kind == 2) {
+        if (!blt_program_supported(program_id))
+            return fail(ctx, RSRGPU_ENODISPATCH, "no device blt program for pid(%d)", program_id);
+    } else {
+        return fail(ctx, RSRGPU_EINVAL, "unknown program kind %d", kind);
+    }
+    ctx->installed.insert((uint64_t(kind) << 56) | (uint64_t(uint32_t(program_id) & 0xff) << 24) | (state_key & 0xffffffu));
+    return 0;
+}
+
+int rsrgpu_reset(rsrgpu_ctx* ctx, int width, int height, int tile_blocks_x, int tile_blocks_y) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (width <= 0 || height <= 0 || (width & 3) || (height & 1))
+        return fail(ctx, RSRGPU_EINVAL, "target %dx%d: width must be a multiple of 4 and height of 2", width, height);
+    if (tile_blocks_x <= 0 || tile_blocks_y <= 0 || tile_blocks_x > 16 || tile_blocks_y > 16)
+        return fail(ctx, RSRGPU_EINVAL, "tile size in blocks must be 1..16");
+    ctx->width = width;
+    ctx->height = height;
+    ctx->tile_w = tile_blocks_x * 8;   // kBlockDimensionsInPixels (rglv_gpu.hxx:27)
+    ctx->tile_h = tile_blocks_y * 8;
+    ctx->tiles_x = (width + ctx->tile_w - 1) / ctx->tile_w;   // GPU::Retile (rglv_gpu.cxx:67-87)
+    ctx->tiles_y = (height + ctx->tile_h - 1) / ctx->tile_h;
+    ctx->ntiles = ctx->tiles_x * ctx->tiles_y;
+    if (ctx->tiles_x > 32767 || ctx->tiles_y > 32767) return fail(ctx, RSRGPU_EINVAL, "too many tiles");
+    ctx->submitted = false;
+    return 0;
+}
+
+int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t bytes) {
+    if (ctx == nullptr || host_ptr == nullptr || bytes == 0) return RSRGPU_EINVAL;
+    const uint8_t* p = static_cast<const uint8_t*>(host_ptr);
+    auto it = ctx->host.find(p);
+    if (it != ctx->host.end()) {
+        if (it->second.bytes >= bytes) return 0;
+        cudaFree(it->second.dev);
+        ctx->host.erase(it);
+    }
+    // drop registrations the new range overlaps (their memory was reused)
+    for (auto jt = ctx->host.begin(); jt != ctx->host.end();) {
+        if (jt->second.host < p + bytes && p < jt->second.host + jt->second.bytes) {
+            cudaStreamSynchronize(ctx->own);
+            cudaFree(jt->second.dev);
+            jt = ctx->host.erase(jt);
+        } else {
+            ++jt;
+        }
+    }
+    HostBuffer hb;
+    hb.host = p;
+    hb.bytes = bytes;
+    CK(cudaMalloc(&hb.dev, bytes), "cudaMalloc(host mirror)");
+    ctx->host[p] = hb;
+    return 0;
+}
+
+int rsrgpu_unregister_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    auto it = ctx->host.find(static_cast<const uint8_t*>(host_ptr));
+    if (it == ctx->host.end()) return fail(ctx, RSRGPU_EINVAL, "buffer %p is not registered", host_ptr);
+    cudaStreamSynchronize(ctx->own);
+    cudaFree(it->second.dev);
+    ctx->host.erase(it);
+    return 0;
+}
+
+int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates) {
+    if (ctx == nullptr || (commands == nullptr && nbytes) || nstates < 0) return RSRGPU_EINVAL;
+    if (ctx->ntiles == 0) return fail(ctx, RSRGPU_EINVAL, "rsrgpu_reset() has not been called");
+    for (auto& kv : ctx->host) kv.second.in = kv.second.out = false;
+    ctx->states.assign(size_t(nstates), DevState{});
+    ctx->state_ordinal.assign(size_t(nstates), -1);
+    ctx->draws.clear();
+    ctx->ops.clear();
+    ctx->ntris = 0;
+    ctx->submitted = false;
+    std::vector<bool> decoded(size_t(nstates), false);
+    int ordinals = 0;
+    int cur = -1;
+    const uint8_t* p = commands;
+    const uint8_t* end = commands + nbytes;
+    while (p < end) {
+        uint8_t op = 0;
+        rd(p, end, op);
+        if (op == RSRGPU_CMD_EOF) break;
+        FrameOp fo{};
+        switch (op) {
+        case RSRGPU_CMD_STATE: {
+            uint64_t idx;
+            if (!rd(p, end, idx) || idx >= uint64_t(nstates)) return fail(ctx, RSRGPU_EINVAL, "CMD_STATE index out of range");
+            if (!decoded[idx]) {
+                int rc = decode_state(ctx, states[idx], ctx->states[idx]);
+                if (rc) return rc;
+                decoded[idx] = true;
+            }
+            if (ctx->state_ordinal[idx] < 0) ctx->state_ordinal[idx] = ordinals++;
+            cur = int(idx);
+            fo.kind = kOpState;
+            fo.arg = int(idx);
+            fo.ordinal = ctx->state_ordinal[idx];
+            ctx->ops.push_back(fo);
+        } break;
+        case RSRGPU_CMD_CLEAR: {
+            uint8_t bits;
+            if (!rd(p, end, bits)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_CLEAR");
+            if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "CMD_CLEAR before any state");
+            if (bits & 4) return fail(ctx, RSRGPU_EUNSUPPORTED, "CLEAR on STENCIL not implemented");
+            const auto& s = states[cur];
+            if (s.color0_attachment_type == RSRGPU_RB_COLOR_DEPTH && bits != 3)
+                return fail(ctx, RSRGPU_EINVAL, "must clear color and depth when using RB_COLOR_DEPTH");
+            fo.kind = kOpClear;
+            fo.arg = bits;
+            ctx->ops.push_back(fo);
+        } break;
+        case RSRGPU_CMD_DRAW_ELEMENTS:
+        case RSRGPU_CMD_DRAW_ARRAYS: {
+            int32_t count = 0;
+            uint64_t iptr = 0;
+            if (op == RSRGPU_CMD_DRAW_ELEMENTS) {
+                uint8_t flags, hint;
+                if (!rd(p, end, flags) || !rd(p, end, hint) || !rd(p, end, count) || !rd(p, end, iptr))
+                    return fail(ctx, RSRGPU_EINVAL, "truncated CMD_DRAW_ELEMENTS");
+                if (flags != 0x14) return fail(ctx, RSRGPU_EINVAL, "CMD_DRAW_ELEMENTS flags must be 0x14");
+            } else {
+                if (!rd(p, end, count)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_DRAW_ARRAYS");
+            }
+            if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "draw before any state");
+            const auto& s = states[cur];
+            const uint32_t vkey = (uint32_t(s.program_id) & 0xff) << 24;
+            if (!ctx->installed.count((uint64_t(0) << 56) | vkey))
+                return fail(ctx, RSRGPU_ENODISPATCH, "BIN:DRAW no dispatch entry for 0x%x", vkey);
+            const uint32_t fkey = fragment_state_key(s) & 0xffffffu;
+            if (!ctx->installed.count((uint64_t(1) << 56) | vkey | fkey))
+                return fail(ctx, RSRGPU_ENODISPATCH, "no dispatch entry for 0x%x found for CMD_DRAW_INLINE", vkey | fkey);
+            if (count < 0) return fail(ctx, RSRGPU_EINVAL, "negative draw count");
+            if (s.program_id == kProgGouraud && (!s.buffers[0] || !s.buffers[3] || !s.buffers[4] || !s.buffers[5]))
+                return fail(ctx, RSRGPU_EINVAL, "Gouraud program needs buffers 0-5");
+            DevDraw dd{};
+            dd.state = cur;
+            dd.first_tri = ctx->ntris;
+            dd.ntris = count / 3;
+            dd.is_arrays = op == RSRGPU_CMD_DRAW_ARRAYS;
+            if (!dd.is_arrays) {
+                void* dp = nullptr;
+                size_t avail = 0;
+                int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(iptr)), false, &dp, "index", &avail);
+                if (rc) return rc;
+                if (dp == nullptr || avail < size_t(dd.ntris) * 3u * sizeof(uint16_t))
+                    return fail(ctx, RSRGPU_EINVAL, "index buffer holds %zu bytes, draw needs %zu", avail, size_t(dd.ntris) * 6u);
+                dd.indices = static_cast<const uint16_t*>(dp);
+            }
+            if (int64_t(ctx->ntris) + dd.ntris > (int64_t(1) << 30)) return fail(ctx, RSRGPU_ECAPACITY, "too many triangles");
+            ctx->ntris += dd.ntris;
+            fo.kind = kOpDraw;
+            fo.arg = int(ctx->draws.size());
+            ctx->draws.push_back(dd);
+            ctx->ops.push_back(fo);
+        } break;
+        case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC: {
+            uint8_t gamma;
+            uint64_t cp;
+            if (!rd(p, end, gamma) || !rd(p, end, cp)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_STORE_COLOR_FULL_LINEAR_TC");
+            if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "store before any state");
+            const auto& s = states[cur];
+            const uint32_t bkey = (uint32_t(s.program_id) & 0xff) << 24;
+            if (!ctx->installed.count((uint64_t(2) << 56) | bkey))
+                return fail(ctx, RSRGPU_ENODISPATCH, "no dispatch entry for %x found for CMD_STORE_COLOR_FULL_LINEAR_TC", bkey);
+            const auto* cv = reinterpret_cast<const rsrgpu_truecolor_canvas*>(uintptr_t(cp));
+            if (cv == nullptr || cv->width != ctx->width || cv->height != ctx->height || cv->stride < cv->width || (cv->stride & 1))
+                return fail(ctx, RSRGPU_EINVAL, "TrueColor canvas must match the %dx%d target (even stride)", ctx->width, ctx->height);
+            void* dp = nullptr;
+            size_t avail = 0;
+            int rc = resolve(ctx, cv->data, true, &dp, "color output", &avail);
+            if (rc) return rc;
+            if (dp == nullptr || avail < size_t(cv->stride) * size_t(cv->height) * 4u)
+                return fail(ctx, RSRGPU_EINVAL, "color output holds %zu bytes, needs %zu", avail, size_t(cv->stride) * size_t(cv->height) * 4u);
+            if (reinterpret_cast<uintptr_t>(dp) & 7) return fail(ctx, RSRGPU_EINVAL, "color output must be 8-byte aligned");
+            fo.kind = kOpStoreTC;
+            fo.arg = gamma ? 1 : 0;
+            fo.ptr = dp;
+            fo.width = cv->width; fo.height = cv->height; fo.stride = cv->stride;
+            ctx->ops.push_back(fo);
+        } break;
+        case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: {
+            uint64_t dp64;
+            if (!rd(p, end, dp64)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_STORE_DEPTH_FULL_LINEAR_FP");
+            if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "store before any state");
+            if (states[cur].depth_attachment_type != RSRGPU_RB_F32)
+                return fail(ctx, RSRGPU_EUNSUPPORTED, "STORE_DEPTH_FULL_LINEAR_FP not implemented for attachment type %d", states[cur].depth_attachment_type);
+            void* dp = nullptr;
+            size_t avail = 0;
+            int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(dp64)), true, &dp, "depth output", &avail);
+            if (rc) return rc;
+            if (dp == nullptr || avail < size_t(ctx->width) * size_t(ctx->height) * 4u)
+                return fail(ctx, RSRGPU_EINVAL, "depth output holds %zu bytes, needs %zu", avail, size_t(ctx->width) * size_t(ctx->height) * 4u);
+            if (reinterpret_cast<uintptr_t>(dp) & 7) return fail(ctx, RSRGPU_EINVAL, "depth output must be 8-byte aligned");
+            fo.kind = kOpStoreDepth;
+            fo.ptr = dp;
+            fo.width = ctx->width; fo.height = ctx->height; fo.stride = ctx->width;
+            ctx->ops.push_back(fo);
+        } break;
+        default:
+            return fail(ctx, RSRGPU_EUNSUPPORTED, "command 0x%02x is not supported", op);
+        }
+    }
+    if (nstates == 0) ctx->states.assign(1, DevState{});
+    ctx->submitted = true;
+    return 0;
+}
+
+namespace {
+
+int prepare_view(rsrgpu_ctx* ctx) {
+    const int ntris = ctx->ntris;
+    const int nchunks = (ntris + kChunk - 1) / kChunk;
+    const int nsupers = (ntris + kSuper - 1) / kSuper;
+    const size_t nt = size_t(std::max(ntris, 1));
+    CK(ctx->d_states.ensure(sizeof(DevState) * ctx->states.size()), "alloc states");
+    CK(ctx->d_draws.ensure(sizeof(DevDraw) * std::max<size_t>(ctx->draws.size(), 1)), "alloc draws");
+    CK(ctx->d_ops.ensure(sizeof(FrameOp) * std::max<size_t>(ctx->ops.size(), 1)), "alloc ops");
+    CK(ctx->d_tris.ensure(sizeof(TriRecord) * nt), "alloc tris");
+    CK(ctx->d_bin_rect.ensure(sizeof(uint64_t) * nt), "alloc bin_rect");
+    CK(ctx->d_rec16.ensure(sizeof(uint32_t) * 2 * nt), "alloc rec16");
+    CK(ctx->d_chunk.ensure(sizeof(int4) * std::max(nchunks, 1)), "alloc chunk rects");
+    CK(ctx->d_super.ensure(sizeof(int4) * std::max(nsupers, 1)), "alloc super rects");
+    CK(ctx->d_clip_info.ensure(sizeof(ClipInfo) * nt), "alloc clip info");
+    CK(ctx->d_clip_verts.ensure(sizeof(ClipVert) * size_t(ctx->clip_cap)), "alloc clip verts");
+    CK(ctx->d_clip_poly.ensure(sizeof(int32_t) * size_t(ctx->clip_cap)), "alloc clip poly");
+    CK(ctx->d_clip_src.ensure(sizeof(int32_t) * size_t(ctx->clip_cap)), "alloc clip src");
+    CK(ctx->d_clip_fan.ensure(sizeof(uint64_t) * size_t(ctx->clip_cap)), "alloc clip fans");
+    CK(ctx->d_bins.ensure(sizeof(TileBin) * size_t(ctx->ntiles)), "alloc bins");
+    CK(ctx->d_pool.ensure(sizeof(uint32_t) * size_t(ctx->bin_cap)), "alloc bin pool");
+    CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
+    FrameView& fv = ctx->fv;
+    fv.states = ctx->d_states.as<DevState>();
+    fv.draws = ctx->d_draws.as<DevDraw>();
+    fv.ndraws = int(ctx->draws.size());
+    fv.ntris = ntris;
+    fv.ops = ctx->d_ops.as<FrameOp>();
+    fv.nops = int(ctx->ops.size());
+    fv.width = ctx->width; fv.height = ctx->height;
+    fv.tile_w = ctx->tile_w; fv.tile_h = ctx->tile_h;
+    fv.tiles_x = ctx->tiles_x; fv.tiles_y = ctx->tiles_y; fv.ntiles = ctx->ntiles;
+    fv.nchunks = nchunks; fv.nsupers = nsupers;
+    fv.tris = ctx->d_tris.as<TriRecord>();
+    fv.bin_rect = ctx->d_bin_rect.as<uint64_t>();
+    fv.rec16 = ctx->d_rec16.as<uint32_t>();
+    fv.chunk_rect = ctx->d_chunk.as<int4>();
+    fv.super_rect = ctx->d_super.as<int4>();
+    fv.clip_info = ctx->d_clip_info.as<ClipInfo>();
+    fv.clip_verts = ctx->d_clip_verts.as<ClipVert>();
+    fv.clip_poly = ctx->d_clip_poly.as<int32_t>();
+    fv.clip_src = ctx->d_clip_src.as<int32_t>();
+    fv.clip_fan_rect = ctx->d_clip_fan.as<uint64_t>();
+    fv.clip_cap = ctx->clip_cap;
+    fv.bins = ctx->d_bins.as<TileBin>();
+    fv.bin_pool = ctx->d_pool.as<uint32_t>();
+    fv.bin_cap = ctx->bin_cap;
+    fv.counters = ctx->d_counters.as<FrameCounters>();
+    fv.rcp_table = ctx->d_rcp.as<uint32_t>();
+    fv.srgb_lut = ctx->d_srgb.as<uint8_t>();
+    return 0;
+}
+
+int enqueue(rsrgpu_ctx* ctx, cudaStream_t st) {
+    int rc = prepare_view(ctx);
+    if (rc) return rc;
+    const FrameView& fv = ctx->fv;
+    // inputs that live in registered host buffers travel with every run
+    for (auto& kv : ctx->host)
+        if (kv.second.in) CK(cudaMemcpyAsync(kv.second.dev, kv.second.host, kv.second.bytes, cudaMemcpyHostToDevice, st), "H2D input");
+    CK(cudaMemcpyAsync(ctx->d_states.p, ctx->states.data(), sizeof(DevState) * ctx->states.size(), cudaMemcpyHostToDevice, st), "H2D states");
+    if (!ctx->draws.empty())
+        CK(cudaMemcpyAsync(ctx->d_draws.p, ctx->draws.data(), sizeof(DevDraw) * ctx->draws.size(), cudaMemcpyHostToDevice, st), "H2D draws");
+    if (!ctx->ops.empty())
+        CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
+    CK(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(FrameCounters), st), "memset counters");
+    if (fv.nsupers > 0) CK(cudaMemsetAsync(ctx->d_super.p, 0x7f, sizeof(int4) * size_t(fv.nsupers), st), "memset super rects");
+    CK(cudaEventRecord(ctx->ev0, st), "event");
+    CK(launch_setup(fv, st), "setup_kernel");
+    CK(launch_bin(fv, st), "bin_kernel");
+    CK(cudaEventRecord(ctx->ev1, st), "event");
+    CK(launch_raster(fv, st), "raster_kernel");
+    CK(cudaEventRecord(ctx->ev2, st), "event");
+    for (auto& kv : ctx->host)
+        if (kv.second.out) CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
+    CK(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, st), "D2H counters");
+    CK(cudaEventRecord(ctx->ev3, st), "event");
+    ctx->stats.gpu_launches = 3;
+    return 0;
+}
+
+}  // namespace
+
+int rsrgpu_run(rsrgpu_ctx* ctx, void* stream) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (!ctx->submitted) return fail(ctx, RSRGPU_EINVAL, "nothing submitted");
+    ctx->run_stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    int rc = enqueue(ctx, ctx->run_stream);
+    if (rc) return rc;
+    ctx->ran = true;
+    return 0;
+}
+
+int rsrgpu_wait(rsrgpu_ctx* ctx, int timeout_ms) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (!ctx->ran) return 0;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        const auto t0 = std::chrono::steady_clock::now();
+        while (true) {
+            cudaError_t q = cudaEventQuery(ctx->ev3);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return cuda_fail(ctx, q, "run");
+            if (timeout_ms >= 0) {
+                const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+                if (ms > timeout_ms) return fail(ctx, RSRGPU_ETIMEOUT, "rsrgpu_wait timed out after %d ms", timeout_ms);
+            }
+            std::this_thread::yield();
+        }
+        const FrameCounters c = *ctx->h_counters;
+        if (c.overflow == 0) return 0;
+        if (c.overflow & 4u) return fail(ctx, RSRGPU_EINVAL, "a vertex index lies outside its attribute buffer");
+        // a capacity was too small: grow from the counts the frame requested and run again
+        if (c.overflow & 1u) ctx->clip_cap = std::max<uint32_t>(ctx->clip_cap * 2, c.clip_verts + c.clip_verts / 4 + 1024);
+        if (c.overflow & 2u) ctx->bin_cap = std::max<uint32_t>(ctx->bin_cap * 2, c.bin_used + c.bin_used / 4 + 4096);
+        if (ctx->clip_cap > (1u << 28) || ctx->bin_cap > (1u << 30))
+            return fail(ctx, RSRGPU_ECAPACITY, "frame needs %u clipped vertices and %u tile entries", c.clip_verts, c.bin_used);
+        int rc = enqueue(ctx, ctx->run_stream);
+        if (rc) return rc;
+    }
+    return fail(ctx, RSRGPU_ECAPACITY, "capacity growth did not converge");
+}
+
+int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms) {
+    if (ctx == nullptr || !ctx->ran) return RSRGPU_EINVAL;
+    float t = 0, r = 0;
+    CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev2), "elapsed");
+    CK(cudaEventElapsedTime(&r, ctx->ev1, ctx->ev2), "elapsed");
+    if (total_ms) *total_ms = t;
+    if (raster_ms) *raster_ms = r;
+    return 0;
+}
+
+int rsrgpu_get_stats(rsrgpu_ctx* ctx, rsrgpu_stats* out) {
+    if (ctx == nullptr || out == nullptr) return RSRGPU_EINVAL;
+    *out = ctx->stats;
+    out->total_tiles = ctx->ntiles;
+    out->primitives_submitted = ctx->ntris;
+    return 0;
+}
+
+int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* needed) {
+    if (ctx == nullptr || needed == nullptr || !ctx->ran) return RSRGPU_EINVAL;
+    CK(cudaStreamSynchronize(ctx->run_stream), "sync");
+    const int nt = ctx->ntris, ntiles = ctx->ntiles;
+    std::vector<TileBin> bins(static_cast<size_t>(ntiles));
+    std::vector<uint32_t> rec16(static_cast<size_t>(2) * size_t(std::max(nt, 1)));
+    std::vector<ClipInfo> ci(static_cast<size_t>(std::max(nt, 1)));
+    const FrameCounters c = *ctx->h_counters;
+    std::vector<uint32_t> pool(static_cast<size_t>(c.bin_used));
+    std::vector<int32_t> poly(size_t(c.clip_verts) + 1), src(size_t(c.clip_verts) + 1);
+    CK(cudaMemcpy(bins.data(), ctx->d_bins.p, sizeof(TileBin) * bins.size(), cudaMemcpyDeviceToHost), "D2H bins");
+    if (nt) {
+        CK(cudaMemcpy(rec16.data(), ctx->d_rec16.p, sizeof(uint32_t) * 2 * size_t(nt), cudaMemcpyDeviceToHost), "D2H rec16");
+        CK(cudaMemcpy(ci.data(), ctx->d_clip_info.p, sizeof(ClipInfo) * size_t(nt), cudaMemcpyDeviceToHost), "D2H clip info");
+    }
+    if (c.bin_used) CK(cudaMemcpy(pool.data(), ctx->d_pool.p, sizeof(uint32_t) * pool.size(), cudaMemcpyDeviceToHost), "D2H pool");
+    if (c.clip_verts) {
+        CK(cudaMemcpy(poly.data(), ctx->d_clip_poly.p, sizeof(int32_t) * c.clip_verts, cudaMemcpyDeviceToHost), "D2H clip poly");
+        CK(cudaMemcpy(src.data(), ctx->d_clip_src.p, sizeof(int32_t) * c.clip_verts, cudaMemcpyDeviceToHost), "D2H clip src");
+    }
+    // canonical clipped-vertex numbering: polygons in source-triangle order
+    std::vector<int32_t> canon(size_t(std::max(nt, 1)), 0);
+    int32_t running = 0;
+    for (int g = 0; g < nt; ++g) if (ci[g].nverts > 0) { canon[g] = running; running += ci[g].nverts; }
+    std::vector<uint8_t> all;
+    auto put8 = [&](std::vector<uint8_t>& v, uint8_t x) { v.push_back(x); };
+    auto put16 = [&](std::vector<uint8_t>& v, uint16_t x) { v.push_back(x & 0xff); v.push_back(x >> 8); };
+    auto put32 = [&](std::vector<uint8_t>& v, uint32_t x) { for (int i = 0; i < 4; ++i) v.push_back((x >> (8 * i)) & 0xff); };
+    int64_t total_rec = 0, total_clip = 0, max_rec = 0;
+    for (int t = 0; t < ntiles; ++t) {
+        std::vector<uint8_t> one;
+        const TileBin b = bins[t];
+        total_rec += b.inl_cnt; total_clip += b.clip_cnt; max_rec = std::max<int64_t>(max_rec, b.inl_cnt + b.clip_cnt);
+        uint32_t ic = 0, cc = 0;
+        for (const FrameOp& o : ctx->ops) {
+            if (o.kind == kOpState) { put8(one, RSRGPU_CMD_STATE); put32(one, uint32_t(o.ordinal)); }
+            else if (o.kind == kOpClear) { put8(one, RSRGPU_CMD_CLEAR); put8(one, uint8_t(o.arg)); }
+            else if (o.kind == kOpStoreTC) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC); put8(one, uint8_t(o.arg)); }
+            else if (o.kind == kOpStoreDepth) { put8(one, RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP); }
+            else if (o.kind == kOpDraw) {
+                const DevDraw& d = ctx->draws[size_t(o.arg)];
+                const uint32_t endg = uint32_t(d.first_tri + d.ntris);
+                bool opened = false;
+                while (ic < b.inl_cnt && pool[b.inl_off + ic] < endg) {
+                    const uint32_t g = pool[b.inl_off + ic++];
+                    if (!opened) { put8(one, RSRGPU_CMD_DRAW_INLINE); opened = true; }
+                    put16(one, uint16_t(rec16[2 * g] & 0xffff));
+                    put16(one, uint16_t(rec16[2 * g] >> 16));
+                    put16(one, uint16_t(rec16[2 * g + 1]));
+                }
+                if (opened) put16(one, 0xffff);
+                while (cc < b.clip_cnt) {
+                    const uint32_t e = pool[b.clip_off + cc];
+                    const int32_t pb = poly[e];
+                    const int32_t g = src[pb];
+                    if (uint32_t(g) >= endg) break;
+                    ++cc;
+                    const int32_t bi = canon[g];
+                    const int32_t vi = int32_t(e) - pb;
+                    put8(one, RSRGPU_CMD_CLIPPED_TRI);
+                    put16(one, uint16_t((bi + 0) | (ci[g].backfacing ? 0x8000 : 0)));
+                    put16(one, uint16_t(bi + vi));
+                    put16(one, uint16_t(bi + vi + 1));
+                }
+            }
+        }
+        put8(one, RSRGPU_CMD_EOF);
+        put32(all, uint32_t(one.size()));
+        all.insert(all.end(), one.begin(), one.end());
+    }
+    ctx->stats.total_tile_records = total_rec;
+    ctx->stats.total_clipped_records = total_clip;
+    ctx->stats.max_tile_records = max_rec;
+    *needed = all.size();
+    if (out && capacity >= all.size()) std::memcpy(out, all.data(), all.size());
+    return 0;
+}
+
+int rsrgpu_dump_clipped(rsrgpu_ctx* ctx, rsrgpu_clipped_vertex* out, int capacity, int* count) {
+    if (ctx == nullptr || count == nullptr || !ctx->ran) return RSRGPU_EINVAL;
+    CK(cudaStreamSynchronize(ctx->run_stream), "sync");
+    const int nt = ctx->ntris;
+    std::vector<ClipInfo> ci(static_cast<size_t>(std::max(nt, 1)));
+    if (nt) CK(cudaMemcpy(ci.data(), ctx->d_clip_info.p, sizeof(ClipInfo) * size_t(nt), cudaMemcpyDeviceToHost), "D2H clip info");
+    const FrameCounters c = *ctx->h_counters;
+    std::vector<ClipVert> verts(size_t(c.clip_verts) + 1);
+    if (c.clip_verts) CK(cudaMemcpy(verts.data(), ctx->d_clip_verts.p, sizeof(ClipVert) * c.clip_verts, cudaMemcpyDeviceToHost), "D2H clip verts");
+    int n = 0;
+    size_t d = 0;
+    for (int g = 0; g < nt; ++g) {
+        if (ci[g].nverts <= 0) continue;
+        while (d + 1 < ctx->draws.size() && ctx->draws[d + 1].first_tri <= g) ++d;
+        const int nvary = ctx->states[size_t(ctx->draws[d].state)].nvary;
+        for (int i = 0; i < ci[g].nverts; ++i, ++n) {
+            if (out && n < capacity) {
+                std::memset(&out[n], 0, sizeof(out[n]));
+                const ClipVert& v = verts[size_t(ci[g].vbase + i)];
+                std::memcpy(out[n].coord, v.coord, 16);
+                for (int k = 0; k < nvary && k < kMaxVary; ++k) out[n].data[k] = v.vary[k];
+            }
+        }
+    }
+    *count = n;
+    return 0;
+}
+
+int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len) {
+    if (ctx == nullptr || buf == nullptr || len == 0) return RSRGPU_EINVAL;
+    std::snprintf(buf, len, "%s", ctx->err.c_str());
+    return 0;
+}
+
+}  // extern "C"

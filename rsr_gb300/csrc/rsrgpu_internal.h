@@ -1,0 +1,144 @@
+// rsrgpu_internal.h -- device-side data layout shared by the host runtime
+// (rsrgpu_host.cu) and the kernels (rsrgpu_kernels.cu).
+//
+// One frame in HBM:
+//   DevState[nstates]   decoded GLState snapshots (matrices premultiplied on
+//                       the host in the reference's float order)
+//   DevDraw[ndraws]     draws in submission order; triangles are numbered
+//                       globally g = draw.first_tri + t
+//   TriRecord[ntris]    per-triangle setup (fixed-point device coords, z/w,
+//                       varyings) in the reference's post-swap vertex order
+//   bin_rect[ntris]     u16x4 tile rectangle used for binning (union of the
+//                       inline rectangle and the clipped fans' rectangles)
+//   chunk/super rects   hierarchy over 32 / 1024 consecutive triangles
+//   ClipPoly/ClipVert   clipped polygons (staging order) for clip-source tris
+//   tile lists          per tile: ordered inline triangle ids and ordered
+//                       clipped fan-triangle ids
+#pragma once
+#include <cstdint>
+
+namespace rsrgpu {
+
+constexpr int kMaxVary = 4;
+constexpr int kChunk = 32;        // triangles per chunk (one warp)
+constexpr int kSuper = 1024;      // triangles per super-chunk
+constexpr int kSetupBlock = 256;
+constexpr int kMaxClipVerts = 8;  // 3 + one per clipping plane (5 planes)
+constexpr int kRegionPx = 32;     // raster CTA covers at most 32x32 px of one tile
+constexpr int kRasterBatch = 256; // triangles set up per shared-memory batch
+
+enum ProgramId : int32_t {
+    kProgDefaultPost = 1,
+    kProgExposurePost = 2,
+    kProgAmy = 4,
+    kProgOBJ1 = 7,
+    kProgGouraud = 90,
+};
+
+struct DevTexture {
+    const float* buf;
+    int32_t kind;   // 0 nearest-mip, 1 linear-mip, 2 non-pow2 nearest
+    int32_t power;
+    int32_t width, height, stride;
+    int32_t texels;   // RGBA texels addressable from buf
+};
+
+struct DevState {
+    float vpm[16];
+    float DS[2], DO[2];
+    float guard;
+    int32_t scissor[4];   // left, top, right, bottom
+    int32_t program;
+    int32_t nvary;
+    int32_t keep_backs, keep_fronts;
+    int32_t cull_enabled, cull_face;
+    int32_t depth_test, depth_func, depth_write, color_write, blend;
+    int32_t color_type, depth_type;
+    float clear_color[4];
+    float clear_depth;
+    const float* buffers[16];
+    int32_t buffer_len[16];   // floats readable from each buffer pointer
+    DevTexture tu0;
+    float uniforms[32];
+};
+
+struct DevDraw {
+    int32_t state;
+    int32_t first_tri;
+    int32_t ntris;
+    int32_t is_arrays;
+    const uint16_t* indices;
+};
+
+enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4 };
+
+struct FrameOp {
+    int32_t kind;
+    int32_t arg;      // state index / clear bits / draw index / gamma
+    int32_t ordinal;  // state ordinal for the canonical dump
+    int32_t pad;
+    void* ptr;        // output base (device address)
+    int32_t width, height, stride, pad2;
+};
+
+struct TriRecord {        // 96 bytes, 16-byte aligned
+    int32_t fx[3], fy[3];
+    float z[3], w[3];
+    float vary[3][kMaxVary];
+};
+
+struct ClipVert {         // clipped vertex: device coord + varyings
+    float coord[4];
+    float vary[kMaxVary];
+};
+
+struct ClipInfo {         // per source triangle (valid when nverts > 0)
+    int32_t vbase;        // staging index of the polygon's first vertex
+    int32_t nverts;       // polygon vertex count (0: not clipped or culled away)
+    int32_t backfacing;
+    int32_t pad;
+};
+
+// frame-global counters, cleared at the start of every run
+struct FrameCounters {
+    uint32_t clip_verts;      // staging vertices allocated
+    uint32_t bin_used;        // tile-list entries allocated
+    uint32_t overflow;        // bit 0: clip staging, bit 1: bin pool, bit 2: vertex index out of range
+    uint32_t pad;
+};
+
+struct TileBin {
+    uint32_t inl_off, inl_cnt;
+    uint32_t clip_off, clip_cnt;
+};
+
+struct FrameView {
+    const DevState* states;
+    const DevDraw* draws;
+    int32_t ndraws;
+    int32_t ntris;
+    const FrameOp* ops;
+    int32_t nops;
+    int32_t width, height;
+    int32_t tile_w, tile_h, tiles_x, tiles_y, ntiles;
+    int32_t nchunks, nsupers;
+    TriRecord* tris;
+    uint64_t* bin_rect;       // tx0 | ty0<<16 | tx1<<32 | ty1<<48; empty when tx0 > tx1
+    uint32_t* rec16;          // 2 words per tri: (i0|bf) | i1<<16, i2
+    int4* chunk_rect;
+    int4* super_rect;         // (minx, miny, -maxx, -maxy), atomically reduced
+    ClipInfo* clip_info;
+    ClipVert* clip_verts;
+    int32_t* clip_poly;       // per staging vertex: polygon base
+    int32_t* clip_src;        // per staging vertex: source triangle (valid at the base)
+    uint64_t* clip_fan_rect;  // per staging vertex v (fan apex index), tile rect of fan (base, v, v+1)
+    uint32_t clip_cap;
+    TileBin* bins;
+    uint32_t* bin_pool;
+    uint32_t bin_cap;
+    FrameCounters* counters;
+    const uint32_t* rcp_table;
+    const uint8_t* srgb_lut;
+};
+
+}  // namespace rsrgpu

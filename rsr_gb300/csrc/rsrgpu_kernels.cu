@@ -1,0 +1,869 @@
+// rsrgpu_kernels.cu -- sm_103a kernels of the rasteriser path.
+//
+//   setup_kernel   one thread per triangle: vertex program, frustum flags,
+//                  rcpps-based perspective divide, viewport, fixed point,
+//                  area/cull, tile rectangle; clip-source triangles run the
+//                  Sutherland-Hodgman clipper in place.  Replaces
+//                  GPUBinImpl::BinTriangles1P/2P + ClipTriangles
+//                  (src/rgl/rglv/rglv_gpu_impl.hxx:315-793).
+//   bin_kernel     one warp per tile: walks the triangle stream in submission
+//                  order through a 1024/32-triangle rectangle hierarchy and
+//                  compacts the triangles touching the tile with ballot +
+//                  popc, so every tile list comes out in the reference's
+//                  append order without sorting or atomics on list slots.
+//   raster_kernel  one CTA per (tile, 32x32 px region): the region's colour
+//                  and depth live in registers (one 2x2 quad per thread);
+//                  triangles are set up per tile in shared memory in batches
+//                  and walked in list order; coverage, depth test, fragment
+//                  program, blend and the sRGB8/fp32 stores follow
+//                  GPU::DrawImpl, VTriangleRasterizer/TriangleRasterizer and
+//                  TriangleProgram::Render (rglv_gpu.cxx:263-432,
+//                  rglv_triangle.hxx:79-304, rglv_gpu_impl.hxx:166-222).
+//
+// Built with -fmad=false: every float expression keeps the reference's
+// separate multiply and add roundings and its evaluation order.
+#include <cstdint>
+#include <climits>
+#include <cuda_runtime.h>
+
+#include "rsrgpu_internal.h"
+
+namespace rsrgpu {
+
+#define FULL_MASK 0xffffffffu
+
+// ---------------------------------------------------------------------------
+// SSE lane semantics (src/rml/rmlv/rmlv_mvec4.hxx)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(u); }
+
+// _mm_rcp_ps through the table measured on the reference's host
+__device__ __forceinline__ float rcpps(const uint32_t* __restrict__ T, float x) {
+    const uint32_t b = f2u(x), s = b & 0x80000000u, e = (b >> 23) & 255u, m = b & 0x7fffffu;
+    if (e == 255u) return u2f(m ? (b | 0x00400000u) : s);
+    if (e == 0u) return u2f(s | 0x7f800000u);
+    const uint32_t t = __ldg(T + (m >> 12));
+    const int er = int((t >> 23) & 255u) - (int(e) - 127);
+    if (er <= 0) return u2f(s);
+    return u2f(s | (uint32_t(er) << 23) | (t & 0x7fffffu));
+}
+
+// rmlv::oneover (rmlv_mvec4.hxx:631-651)
+__device__ __forceinline__ float oneover(const uint32_t* __restrict__ T, float a) {
+    const float r = rcpps(T, a);
+    const float muls = __fmul_rn(a, __fmul_rn(r, r));
+    return __fsub_rn(__fadd_rn(r, r), muls);
+}
+
+// _mm_cvttps_epi32: truncation, INT_MIN when out of range or NaN
+__device__ __forceinline__ int32_t ftoi(float f) {
+    return (f >= -2147483648.0f && f < 2147483648.0f) ? __float2int_rz(f) : INT_MIN;
+}
+__device__ __forceinline__ float itof(int32_t i) { return __int2float_rn(i); }
+__device__ __forceinline__ float sse_min(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float sse_max(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ int32_t wadd(int32_t a, int32_t b) { return int32_t(uint32_t(a) + uint32_t(b)); }
+__device__ __forceinline__ int32_t wsub(int32_t a, int32_t b) { return int32_t(uint32_t(a) - uint32_t(b)); }
+__device__ __forceinline__ int32_t wmul(int32_t a, int32_t b) { return int32_t(uint32_t(a) * uint32_t(b)); }
+__device__ __forceinline__ float fract(float a) { return a - itof(ftoi(a)); }
+
+// ---------------------------------------------------------------------------
+// vertex programs
+// ---------------------------------------------------------------------------
+// SHADER::ShadeVertex: gl_Position = vpm * (position, 1) (qmat4 * qfloat4,
+// rmlm_soa.hxx:59-65) and the program's VertexOutputSD.
+// Attribute fetch with a bounds check: an index past the end of a buffer
+// raises the frame's error bit and reads 0 instead of faulting.
+__device__ __forceinline__ float fetch(const DevState& s, int b, int idx, FrameCounters* ctr) {
+    if (idx >= s.buffer_len[b]) {
+        atomicOr(&ctr->overflow, 4u);
+        return 0.f;
+    }
+    return __ldg(s.buffers[b] + idx);
+}
+
+__device__ __forceinline__ void shade_vertex(const DevState& s, int idx, float pos[4], float vary[kMaxVary],
+                                             FrameCounters* ctr) {
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (s.buffers[0] != nullptr && s.buffers[1] != nullptr && s.buffers[2] != nullptr) {
+        x = fetch(s, 0, idx, ctr);
+        y = fetch(s, 1, idx, ctr);
+        z = fetch(s, 2, idx, ctr);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        pos[r] = ((s.vpm[r] * x + s.vpm[4 + r] * y) + s.vpm[8 + r] * z) + s.vpm[12 + r] * 1.0f;
+#pragma unroll
+    for (int k = 0; k < kMaxVary; ++k) vary[k] = 0.f;
+    if (s.program == kProgGouraud) {
+        vary[0] = fetch(s, 3, idx, ctr);
+        vary[1] = fetch(s, 4, idx, ctr);
+        vary[2] = fetch(s, 5, idx, ctr);
+    } else if (s.program == kProgAmy) {
+        vary[0] = s.buffers[9] ? fetch(s, 9, idx, ctr) : 0.f;
+        vary[1] = s.buffers[10] ? fetch(s, 10, idx, ctr) : 0.f;
+    }
+}
+
+// ViewFrustum::Test, SIMD version (rglv_view_frustum.hxx:60-73)
+__device__ __forceinline__ uint32_t frustum_test(float factor, const float p[4]) {
+    const float w = p[3] * factor;
+    const uint32_t left = (w + p[0]) <= 0.f;
+    const uint32_t bottom = (w + p[1]) <= 0.f;
+    const uint32_t nearp = (p[3] + p[2]) <= 0.f;
+    const uint32_t right = (w - p[0]) <= 0.f;
+    const uint32_t top = (w - p[1]) <= 0.f;
+    return left | (bottom << 1) | (nearp << 2) | (right << 3) | (top << 4);
+}
+
+constexpr uint64_t kEmptyRect = 0x0000'0000'ffff'ffffull;   // tx0=ty0=0xffff > tx1=ty1=0
+// a rectangle whose far corner lies before its near corner covers no tile (the
+// reference's tile loops run zero times)
+__device__ __forceinline__ uint64_t pack_rect(int tx0, int ty0, int tx1, int ty1) {
+    if (tx1 < tx0 || ty1 < ty0) return kEmptyRect;
+    return uint64_t(uint16_t(tx0)) | (uint64_t(uint16_t(ty0)) << 16) | (uint64_t(uint16_t(tx1)) << 32) |
+           (uint64_t(uint16_t(ty1) & 0x7fffu) << 48);
+}
+__device__ __forceinline__ bool rect_has(uint64_t r, int tx, int ty) {
+    const int x0 = int(r & 0xffff), y0 = int((r >> 16) & 0xffff);
+    const int x1 = int((r >> 32) & 0xffff), y1 = int((r >> 48) & 0x7fff);
+    return x0 <= tx && tx <= x1 && y0 <= ty && ty <= y1;
+}
+
+__device__ __forceinline__ int find_draw(const DevDraw* __restrict__ draws, int ndraws, int g) {
+    int lo = 0, hi = ndraws - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&draws[mid].first_tri) <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// clipping: GPUBinImpl::ClipTriangles for one triangle (rglv_gpu_impl.hxx:678-793)
+// ---------------------------------------------------------------------------
+struct CV { float c[4]; float d[kMaxVary]; };
+
+__device__ __forceinline__ bool is_inside(int plane, const float* p) {
+    switch (plane) {
+    case 0: return p[3] + p[0] >= 0.f;   // left
+    case 1: return p[3] + p[1] >= 0.f;   // bottom
+    case 2: return p[3] + p[2] >= 0.f;   // near
+    case 3: return p[3] - p[0] >= 0.f;   // right
+    default: return p[3] - p[1] >= 0.f;  // top
+    }
+}
+__device__ __forceinline__ float plane_distance(int plane, const float* a, const float* b) {
+    switch (plane) {
+    case 0: return (a[3] + a[0]) / ((a[3] + a[0]) - (b[3] + b[0]));
+    case 1: return (a[3] + a[1]) / ((a[3] + a[1]) - (b[3] + b[1]));
+    case 2: return (a[3] + a[2]) / ((a[3] + a[2]) - (b[3] + b[2]));
+    case 3: return (a[3] - a[0]) / ((a[3] - a[0]) - (b[3] - b[0]));
+    default: return (a[3] - a[1]) / ((a[3] - a[1]) - (b[3] - b[1]));
+    }
+}
+
+// ForEachCoveredTile's rectangle (rglv_gpu_impl.hxx:796-808)
+__device__ __forceinline__ uint64_t fan_rect(const FrameView& fv, const int sc[4], const float* a, const float* b, const float* c) {
+    const int x0 = __float2int_rz(a[0]), y0 = __float2int_rz(a[1]);
+    const int x1 = __float2int_rz(b[0]), y1 = __float2int_rz(b[1]);
+    const int x2 = __float2int_rz(c[0]), y2 = __float2int_rz(c[1]);
+    const int vminx = max(min(x0, min(x1, x2)), sc[0]);
+    const int vminy = max(min(y0, min(y1, y2)), sc[1]);
+    const int vmaxx = min(max(x0, max(x1, x2)) + 1, sc[2] - 1);
+    const int vmaxy = min(max(y0, max(y1, y2)) + 1, sc[3] - 1);
+    return pack_rect(vminx / fv.tile_w, vminy / fv.tile_h, vmaxx / fv.tile_w, vmaxy / fv.tile_h);
+}
+
+__device__ __noinline__ void clip_triangle(const FrameView& fv, const DevState& s, int g,
+                                           const float pos[3][4], const float vary[3][kMaxVary],
+                                           uint64_t& rect_union) {
+    CV A[kMaxClipVerts + 1], B[kMaxClipVerts + 1];
+    int na = 3;
+    for (int i = 0; i < 3; ++i) {
+        for (int k = 0; k < 4; ++k) A[i].c[k] = pos[i][k];
+        for (int k = 0; k < kMaxVary; ++k) A[i].d[k] = vary[i][k];
+    }
+    const int nv = s.nvary;
+    for (int plane = 0; plane < 5 && na > 0; ++plane) {   // clipping_panes order L,B,N,R,T
+        bool hereIsInside = is_inside(plane, A[0].c);
+        int nb = 0;
+        for (int h = 0; h < na; ++h) {
+            const int n = (h + 1) % na;
+            const bool nextIsInside = is_inside(plane, A[n].c);
+            if (hereIsInside && nb <= kMaxClipVerts) B[nb++] = A[h];
+            if (hereIsInside != nextIsInside) {
+                const CV& from = hereIsInside ? A[h] : A[n];
+                const CV& to = hereIsInside ? A[n] : A[h];
+                const float d = plane_distance(plane, from.c, to.c);
+                CV o;
+                for (int k = 0; k < 4; ++k) o.c[k] = (1.0f - d) * from.c[k] + d * to.c[k];
+                for (int k = 0; k < kMaxVary; ++k) o.d[k] = k < nv ? (1.0f - d) * from.d[k] + d * to.d[k] : 0.f;
+                if (nb <= kMaxClipVerts) B[nb++] = o;
+                hereIsInside = !hereIsInside;
+            }
+        }
+        for (int i = 0; i < nb; ++i) A[i] = B[i];
+        na = nb > kMaxClipVerts ? kMaxClipVerts : nb;
+    }
+    ClipInfo info{0, 0, 0, 0};
+    if (na >= 3) {
+        for (int i = 0; i < na; ++i) {
+            const float iw = oneover(fv.rcp_table, A[i].c[3]);   // pdiv (rglv_math.hxx:143-152)
+            A[i].c[0] = A[i].c[0] * iw; A[i].c[1] = A[i].c[1] * iw; A[i].c[2] = A[i].c[2] * iw; A[i].c[3] = iw;
+            A[i].c[0] = A[i].c[0] * s.DS[0] + s.DO[0];
+            A[i].c[1] = A[i].c[1] * s.DS[1] + s.DO[1];
+        }
+        const float d31x = A[2].c[0] - A[0].c[0], d31y = A[2].c[1] - A[0].c[1];
+        const float d21x = A[1].c[0] - A[0].c[0], d21y = A[1].c[1] - A[0].c[1];
+        const bool backfacing = (d31x * d21y - d31y * d21x) < 0.f;
+        bool willCull = true;
+        if (backfacing) { if (!s.cull_enabled || (s.cull_face & 2) == 0) willCull = false; }
+        else { if (!s.cull_enabled || (s.cull_face & 1) == 0) willCull = false; }
+        if (!willCull) {
+            if (backfacing) {
+                for (int i = 0; i < na / 2; ++i) { CV t = A[i]; A[i] = A[na - 1 - i]; A[na - 1 - i] = t; }
+            }
+            const uint32_t vbase = atomicAdd(&fv.counters->clip_verts, uint32_t(na));
+            if (vbase + uint32_t(na) > fv.clip_cap) {
+                atomicOr(&fv.counters->overflow, 1u);
+            } else {
+                for (int i = 0; i < na; ++i) {
+                    ClipVert cvx;
+                    for (int k = 0; k < 4; ++k) cvx.coord[k] = A[i].c[k];
+                    for (int k = 0; k < kMaxVary; ++k) cvx.vary[k] = A[i].d[k];
+                    fv.clip_verts[vbase + i] = cvx;
+                    fv.clip_poly[vbase + i] = int32_t(vbase);
+                }
+                fv.clip_src[vbase] = g;
+                int sc[4] = { s.scissor[0], s.scissor[1], s.scissor[2], s.scissor[3] };
+                int ux0 = INT_MAX, uy0 = INT_MAX, ux1 = INT_MIN, uy1 = INT_MIN;
+                for (int vi = 1; vi < na - 1; ++vi) {
+                    const uint64_t r = fan_rect(fv, sc, A[0].c, A[vi].c, A[vi + 1].c);
+                    fv.clip_fan_rect[vbase + vi] = r;
+                    const int x0 = int(r & 0xffff), y0 = int((r >> 16) & 0xffff);
+                    const int x1 = int((r >> 32) & 0xffff), y1 = int((r >> 48) & 0x7fff);
+                    if (x0 <= x1 && y0 <= y1) {
+                        ux0 = min(ux0, x0); uy0 = min(uy0, y0); ux1 = max(ux1, x1); uy1 = max(uy1, y1);
+                    }
+                }
+                info.vbase = int32_t(vbase);
+                info.nverts = na;
+                info.backfacing = backfacing ? 1 : 0;
+                if (ux0 <= ux1) rect_union = pack_rect(ux0, uy0, ux1, uy1) | (1ull << 63);
+            }
+        }
+    }
+    fv.clip_info[g] = info;
+}
+
+// ---------------------------------------------------------------------------
+// setup
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSetupBlock) setup_kernel(FrameView fv) {
+    const int g = blockIdx.x * kSetupBlock + threadIdx.x;
+    uint64_t rect = kEmptyRect;
+    if (g < fv.ntris) {
+        const int d = find_draw(fv.draws, fv.ndraws, g);
+        const DevDraw dr = fv.draws[d];
+        const DevState& s = fv.states[dr.state];
+        const int t = g - dr.first_tri;
+        int idx[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) idx[k] = dr.is_arrays ? 3 * t + k : int(__ldg(dr.indices + 3 * t + k));
+        float pos[3][4], vary[3][kMaxVary];
+        float dx[3], dy[3], zz[3], ww[3];
+        uint32_t cf[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            shade_vertex(s, idx[k], pos[k], vary[k], fv.counters);
+            cf[k] = frustum_test(s.guard, pos[k]);
+            const float iw = oneover(fv.rcp_table, pos[k][3]);
+            dx[k] = (pos[k][0] * iw) * s.DS[0] + s.DO[0];
+            dy[k] = (pos[k][1] * iw) * s.DS[1] + s.DO[1];
+            zz[k] = pos[k][2] * iw;
+            ww[k] = iw;
+        }
+        // BinTriangles1P (rglv_gpu_impl.hxx:605-661)
+        const bool pointsOutside = int32_t(cf[0] | cf[1] | cf[2]) > 0;
+        const bool primsOutside = int32_t(cf[0] & cf[1] & cf[2]) > 0;
+        const bool needClip = !primsOutside && pointsOutside;
+        const float d31x = dx[2] - dx[0], d31y = dy[2] - dy[0];
+        const float d21x = dx[1] - dx[0], d21y = dy[1] - dy[0];
+        const bool front = (d31x * d21y - d31y * d21x) > 0.f;
+        const int32_t ix0 = ftoi(dx[0]), iy0 = ftoi(dy[0]);
+        const int32_t ix1 = ftoi(dx[1]), iy1 = ftoi(dy[1]);
+        const int32_t ix2 = ftoi(dx[2]), iy2 = ftoi(dy[2]);
+        const int32_t vminx = max(min(ix0, min(ix1, ix2)), s.scissor[0]);
+        const int32_t vminy = max(min(iy0, min(iy1, iy2)), s.scissor[1]);
+        const int32_t vmaxx = min(wadd(max(ix0, max(ix1, ix2)), 1), s.scissor[2] - 1);
+        const int32_t vmaxy = min(wadd(max(iy0, max(iy1, iy2)), 1), s.scissor[3] - 1);
+        bool notCulled = (!front && s.keep_backs) || (front && s.keep_fronts);
+        notCulled = notCulled && !pointsOutside;
+        const bool accept = notCulled && vmaxx > vminx && vmaxy > vminy;
+        if (accept) {
+            const int o0 = front ? 0 : 2, o2 = front ? 2 : 0;
+            const int ord[3] = { o0, 1, o2 };
+            TriRecord r;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int v = ord[k];
+                r.fx[k] = ftoi(16.0f * dx[v]);
+                r.fy[k] = ftoi(16.0f * dy[v]);
+                r.z[k] = zz[v];
+                r.w[k] = ww[v];
+#pragma unroll
+                for (int q = 0; q < kMaxVary; ++q) r.vary[k][q] = vary[v][q];
+            }
+            const float4* src = reinterpret_cast<const float4*>(&r);
+            float4* dst = reinterpret_cast<float4*>(fv.tris + g);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) dst[q] = src[q];
+            const uint32_t ni0 = uint32_t(uint16_t(idx[o0])) | (front ? 0u : 0x8000u);
+            fv.rec16[2 * g] = (ni0 & 0xffffu) | (uint32_t(uint16_t(idx[1])) << 16);
+            fv.rec16[2 * g + 1] = uint32_t(uint16_t(idx[o2]));
+            rect = pack_rect(vminx / fv.tile_w, vminy / fv.tile_h, vmaxx / fv.tile_w, vmaxy / fv.tile_h);
+        }
+        if (needClip) {
+            clip_triangle(fv, s, g, pos, vary, rect);
+        } else {
+            fv.clip_info[g] = ClipInfo{0, 0, 0, 0};
+        }
+        fv.bin_rect[g] = rect;
+    }
+    // chunk and super-chunk rectangles
+    const bool nonempty = (rect & 0xffff) <= ((rect >> 32) & 0xffff) && ((rect >> 16) & 0xffff) <= ((rect >> 48) & 0x7fff);
+    int x0 = nonempty ? int(rect & 0xffff) : INT_MAX;
+    int y0 = nonempty ? int((rect >> 16) & 0xffff) : INT_MAX;
+    int x1 = nonempty ? int((rect >> 32) & 0xffff) : INT_MIN;
+    int y1 = nonempty ? int((rect >> 48) & 0x7fff) : INT_MIN;
+    x0 = __reduce_min_sync(FULL_MASK, x0);
+    y0 = __reduce_min_sync(FULL_MASK, y0);
+    x1 = __reduce_max_sync(FULL_MASK, x1);
+    y1 = __reduce_max_sync(FULL_MASK, y1);
+    const int chunk = (blockIdx.x * kSetupBlock + threadIdx.x) >> 5;
+    if ((threadIdx.x & 31) == 0 && chunk < fv.nchunks) {
+        fv.chunk_rect[chunk] = make_int4(x0, y0, x1, y1);
+        if (x0 <= x1) {
+            int4* sr = fv.super_rect + (chunk >> 5);
+            atomicMin(&sr->x, x0);
+            atomicMin(&sr->y, y0);
+            atomicMin(&sr->z, -x1);
+            atomicMin(&sr->w, -y1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// binning
+// ---------------------------------------------------------------------------
+template <bool WRITE>
+__device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, int lane,
+                                         uint32_t& ninl, uint32_t& nclip,
+                                         uint32_t* __restrict__ inl_out, uint32_t* __restrict__ clip_out) {
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int sb = 0; sb < fv.nsupers; sb += 32) {
+        const int sidx = sb + lane;
+        bool hs = false;
+        if (sidx < fv.nsupers) {
+            const int4 r = fv.super_rect[sidx];
+            hs = r.x <= tx && tx <= -r.z && r.y <= ty && ty <= -r.w;
+        }
+        uint32_t ms = __ballot_sync(FULL_MASK, hs);
+        while (ms) {
+            const int s2 = sb + __ffs(ms) - 1;
+            ms &= ms - 1;
+            const int c = s2 * 32 + lane;
+            bool hc = false;
+            if (c < fv.nchunks) {
+                const int4 r = fv.chunk_rect[c];
+                hc = r.x <= tx && tx <= r.z && r.y <= ty && ty <= r.w;
+            }
+            uint32_t mc = __ballot_sync(FULL_MASK, hc);
+            while (mc) {
+                const int c2 = s2 * 32 + __ffs(mc) - 1;
+                mc &= mc - 1;
+                const int g = c2 * 32 + lane;
+                bool inl = false;
+                int cnt = 0;
+                uint64_t br = kEmptyRect;
+                if (g < fv.ntris) {
+                    br = fv.bin_rect[g];
+                    if (rect_has(br, tx, ty)) {
+                        if ((br >> 63) == 0) {
+                            inl = true;
+                        } else {
+                            const ClipInfo ci = fv.clip_info[g];
+                            for (int vi = 1; vi < ci.nverts - 1; ++vi)
+                                cnt += rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty) ? 1 : 0;
+                        }
+                    }
+                }
+                const uint32_t mi = __ballot_sync(FULL_MASK, inl);
+                if (WRITE && inl) inl_out[ninl + __popc(mi & lt)] = uint32_t(g);
+                ninl += __popc(mi);
+                // clipped fans: warp exclusive scan of per-lane counts
+                int incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(FULL_MASK, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                const int total = __shfl_sync(FULL_MASK, incl, 31);
+                if (WRITE && cnt) {
+                    const ClipInfo ci = fv.clip_info[g];
+                    uint32_t pos = nclip + uint32_t(incl - cnt);
+                    for (int vi = 1; vi < ci.nverts - 1; ++vi)
+                        if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
+                }
+                nclip += uint32_t(total);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) bin_kernel(FrameView fv) {
+    const int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (tile >= fv.ntiles) return;
+    if (fv.counters->overflow & 1u) {
+        if (lane == 0) fv.bins[tile] = TileBin{0, 0, 0, 0};
+        return;
+    }
+    const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
+    uint32_t ninl = 0, nclip = 0;
+    bin_walk<false>(fv, tx, ty, lane, ninl, nclip, nullptr, nullptr);
+    uint32_t off = 0;
+    if (lane == 0) {
+        off = atomicAdd(&fv.counters->bin_used, ninl + nclip);
+        if (off + ninl + nclip > fv.bin_cap) {
+            atomicOr(&fv.counters->overflow, 2u);
+            fv.bins[tile] = TileBin{0, 0, 0, 0};
+            off = 0xffffffffu;
+        } else {
+            fv.bins[tile] = TileBin{off, ninl, off + ninl, nclip};
+        }
+    }
+    off = __shfl_sync(FULL_MASK, off, 0);
+    if (off == 0xffffffffu) return;
+    uint32_t w_inl = 0, w_clip = 0;
+    bin_walk<true>(fv, tx, ty, lane, w_inl, w_clip, fv.bin_pool + off, fv.bin_pool + off + ninl);
+}
+
+// ---------------------------------------------------------------------------
+// raster
+// ---------------------------------------------------------------------------
+// per-(triangle, tile) setup, structure of arrays in shared memory
+struct RasterSmem {
+    int32_t minx[kRasterBatch], miny[kRasterBatch], maxx[kRasterBatch], maxy[kRasterBatch];
+    int32_t c1[kRasterBatch], c2[kRasterBatch], c3[kRasterBatch];
+    int32_t dy12[kRasterBatch], dx12[kRasterBatch], dy23[kRasterBatch], dx23[kRasterBatch];
+    int32_t dy31[kRasterBatch], dx31[kRasterBatch];
+    float scale[kRasterBatch];
+    float z[3][kRasterBatch], w[3][kRasterBatch];
+    float vary[3][kMaxVary][kRasterBatch];
+    uint32_t entry[kRasterBatch];
+};
+
+// VTriangleRasterizer setup for one lane (rglv_triangle.hxx:209-240), int32 wrap
+__device__ __forceinline__ void setup_vector(RasterSmem& S, int i, const int rect[4],
+                                             int32_t x1, int32_t x2, int32_t x3, int32_t y1, int32_t y2, int32_t y3) {
+    int32_t vminx = max(min(min(x1, x2), x3) >> 4, rect[0]);
+    const int32_t vmaxx = min(wadd(max(max(x1, x2), x3), 15) >> 4, rect[2]);
+    int32_t vminy = max(min(min(y1, y2), y3) >> 4, rect[1]);
+    const int32_t vmaxy = min(wadd(max(max(y1, y2), y3), 15) >> 4, rect[3]);
+    vminx &= ~1; vminy &= ~1;
+    const int32_t dx12 = wsub(x1, x2), dy12 = wsub(y2, y1);
+    const int32_t dx23 = wsub(x2, x3), dy23 = wsub(y3, y2);
+    const int32_t dx31 = wsub(x3, x1), dy31 = wsub(y1, y3);
+    const int32_t sx = wadd(int32_t(uint32_t(vminx) << 4), 8);
+    const int32_t sy = wadd(int32_t(uint32_t(vminy) << 4), 8);
+    int32_t c1 = wadd(wmul(dy12, wsub(sx, x1)), wmul(dx12, wsub(sy, y1)));
+    int32_t c2 = wadd(wmul(dy23, wsub(sx, x2)), wmul(dx23, wsub(sy, y2)));
+    int32_t c3 = wadd(wmul(dy31, wsub(sx, x3)), wmul(dx31, wsub(sy, y3)));
+    const int tl12 = dy12 > 0 || (dy12 == 0 && dx12 > 0);
+    const int tl23 = dy23 > 0 || (dy23 == 0 && dx23 > 0);
+    const int tl31 = dy31 > 0 || (dy31 == 0 && dx31 > 0);
+    c1 = wsub(wadd(c1, tl12), 1) >> 4;
+    c2 = wsub(wadd(c2, tl23), 1) >> 4;
+    c3 = wsub(wadd(c3, tl31), 1) >> 4;
+    S.minx[i] = vminx; S.miny[i] = vminy; S.maxx[i] = vmaxx; S.maxy[i] = vmaxy;
+    S.c1[i] = c1; S.c2[i] = c2; S.c3[i] = c3;
+    S.dy12[i] = dy12; S.dx12[i] = dx12; S.dy23[i] = dy23; S.dx23[i] = dx23; S.dy31[i] = dy31; S.dx31[i] = dx31;
+    S.scale[i] = __fdiv_rn(1.0f, itof(wadd(wadd(c1, c2), c3)));
+}
+
+// TriangleRasterizer setup (rglv_triangle.hxx:79-131), int64
+__device__ __forceinline__ void setup_scalar(RasterSmem& S, int i, const int rect[4],
+                                             int x1, int x2, int x3, int y1, int y2, int y3) {
+    int minx = max(min(x1, min(x2, x3)) >> 4, rect[0]);
+    const int endx = min((max(x1, max(x2, x3)) + 15) >> 4, rect[2]);
+    int miny = max(min(y1, min(y2, y3)) >> 4, rect[1]);
+    const int endy = min((max(y1, max(y2, y3)) + 15) >> 4, rect[3]);
+    minx &= ~1; miny &= ~1;
+    const int64_t dx12 = x1 - x2, dy12 = y2 - y1;
+    const int64_t dx23 = x2 - x3, dy23 = y3 - y2;
+    const int64_t dx31 = x3 - x1, dy31 = y1 - y3;
+    const int64_t sx = (minx << 4) + 8, sy = (miny << 4) + 8;
+    int64_t c1 = dy12 * (sx - x1) + dx12 * (sy - y1);
+    int64_t c2 = dy23 * (sx - x2) + dx23 * (sy - y2);
+    int64_t c3 = dy31 * (sx - x3) + dx31 * (sy - y3);
+    if (dy12 > 0 || (dy12 == 0 && dx12 > 0)) c1++;
+    --c1;
+    if (dy23 > 0 || (dy23 == 0 && dx23 > 0)) c2++;
+    --c2;
+    if (dy31 > 0 || (dy31 == 0 && dx31 > 0)) c3++;
+    --c3;
+    c1 >>= 4; c2 >>= 4; c3 >>= 4;
+    S.minx[i] = minx; S.miny[i] = miny; S.maxx[i] = endx; S.maxy[i] = endy;
+    S.c1[i] = int32_t(c1); S.c2[i] = int32_t(c2); S.c3[i] = int32_t(c3);
+    S.dy12[i] = int32_t(dy12); S.dx12[i] = int32_t(dx12);
+    S.dy23[i] = int32_t(dy23); S.dx23[i] = int32_t(dx23);
+    S.dy31[i] = int32_t(dy31); S.dx31[i] = int32_t(dx31);
+    S.scale[i] = __fdiv_rn(1.0f, __ll2float_rn(c1 + c2 + c3));
+}
+
+// Texel fetch for the nearest samplers: their offsets come from fract() of
+// the coordinate, which is negative for coordinates below -10 (-100 for the
+// non-power-of-two unit), where the reference reads outside the texture;
+// here such texels read as zero.
+__device__ __forceinline__ float4 texel(const DevTexture& tu, int32_t ofs4) {
+    const int32_t t = ofs4 >> 2;
+    if (t < 0 || t >= tu.texels) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return __ldg(reinterpret_cast<const float4*>(tu.buf) + t);
+}
+
+// texture units (src/rgl/rglr/rglr_texture_sampler.cxx)
+__device__ __forceinline__ void tex_sample(const DevTexture& tu, const float u[4], const float v[4], float out[4][4]) {
+    const float almostone = u2f(0x3f7fffffu);
+    if (tu.kind == 2) {   // NM_ONEMAP_WRAP_NEAREST (:289-311)
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int32_t pu = ftoi(fract(u[l] + 100.0f) * float(tu.width));
+            const int32_t pv = ftoi((almostone - fract(v[l] + 100.0f)) * float(tu.height));
+            const float4 px = texel(tu, wmul(wadd(wmul(pv, tu.stride), pu), 4));
+            out[l][0] = px.x; out[l][1] = px.y; out[l][2] = px.z; out[l][3] = px.w;
+        }
+        return;
+    }
+    const int P = tu.power;
+    const float baseDim = float(1 << P);
+    // LevelOfDetail (:25-42), coarse: lanes 1 - 0
+    const float dux = u[1] * baseDim - u[0] * baseDim;
+    const float dvx = v[1] * baseDim - v[0] * baseDim;
+    const float sqd = dux * dux + dvx * dvx;
+    int lod = (int32_t(f2u(sqd)) - (127 << 23)) >> 24;
+    lod = lod < 0 ? 0 : (lod > P ? P : lod);
+    if (tu.kind == 0) {   // P2_MIPMAP_WRAP_NEAREST (:63-109)
+        const float levelDim = float(1 << (P - lod));
+        const int32_t levelBeginRow = int32_t((0xfffffffeu << (P - lod)) & ((1u << (P + 1)) - 1u));
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int32_t lx = ftoi(fract(u[l] + 10.0f) * levelDim);
+            const int32_t ly = ftoi((almostone - fract(v[l] + 10.0f)) * levelDim);
+            const float4 px = texel(tu, wmul(wadd(int32_t(uint32_t(wadd(levelBeginRow, ly)) << P), lx), 4));
+            out[l][0] = px.x; out[l][1] = px.y; out[l][2] = px.z; out[l][3] = px.w;
+        }
+        return;
+    }
+    // P2_MIPMAP_WRAP_LINEAR (:172-286)
+    const int levelDim = 1 << (P - lod);
+    const int32_t wrapMask = levelDim - 1;
+    const int32_t levelLastRow = int32_t(((0xffffffffu << (P - lod)) & ((1u << (P + 1)) - 1u)) - 1u);
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        const float levelX = u[l] * float(levelDim);
+        const float levelY = v[l] * float(levelDim);
+        int32_t tx0 = ftoi(levelX - 0.5f), ty0 = ftoi(levelY - 0.5f);
+        int32_t tx1 = wadd(tx0, 1), ty1 = wadd(ty0, 1);
+        const float fx = (levelX - itof(tx0)) - 0.5f;
+        const float fy = (levelY - itof(ty0)) - 0.5f;
+        const float fx1 = 1.0f - fx, fy1 = 1.0f - fy;
+        const float w00 = fx1 * fy1, w10 = fx * fy1, w01 = fx1 * fy, w11 = fx * fy;
+        tx0 &= wrapMask; ty0 &= wrapMask; tx1 &= wrapMask; ty1 &= wrapMask;
+        const int32_t y0 = wsub(levelLastRow, ty0), y1 = wsub(levelLastRow, ty1);
+        const float4 p00 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y0) << P), tx0));
+        const float4 p10 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y0) << P), tx1));
+        const float4 p01 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y1) << P), tx0));
+        const float4 p11 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y1) << P), tx1));
+        out[l][0] = ((p00.x * w00 + p10.x * w10) + p01.x * w01) + p11.x * w11;
+        out[l][1] = ((p00.y * w00 + p10.y * w10) + p01.y * w01) + p11.y * w11;
+        out[l][2] = ((p00.z * w00 + p10.z * w10) + p01.z * w01) + p11.z * w11;
+        out[l][3] = ((p00.w * w00 + p10.w * w10) + p01.w * w01) + p11.w * w11;
+    }
+}
+
+// fragment-stage constants of the current state, held in registers
+struct FragState {
+    int program, nvary;
+    int depth_test, depth_func, depth_write, color_write, blend;
+    DevTexture tu0;
+};
+
+__device__ __forceinline__ void load_frag_state(const DevState& s, FragState& f) {
+    f.program = s.program; f.nvary = s.nvary;
+    f.depth_test = s.depth_test; f.depth_func = s.depth_func; f.depth_write = s.depth_write;
+    f.color_write = s.color_write; f.blend = s.blend;
+    f.tu0 = s.tu0;
+}
+
+// sRGB8 encode with this library's own table (see rsrgpu_host.cu)
+__device__ __forceinline__ uint32_t srgb8(const uint8_t* __restrict__ lut, float v) {
+    const float c = sse_min(sse_max(v, u2f((127u - 13u) << 23)), u2f(0x3f7fffffu));
+    return __ldg(lut + ((f2u(c) >> 12) - ((127u - 13u) << 11)));
+}
+__device__ __forceinline__ uint32_t basic8(float v) {   // to_tc_basic (rglr_canvas_util.hxx:22-31)
+    return uint32_t(ftoi(sse_max(sse_min(v, 1.0f), 0.0f) * 255.0f));
+}
+
+__global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
+    __shared__ RasterSmem S;
+    if (fv.counters->overflow != 0u) return;
+
+    const int sub_x = (fv.tile_w + kRegionPx - 1) / kRegionPx;
+    const int sub_y = (fv.tile_h + kRegionPx - 1) / kRegionPx;
+    const int subs = sub_x * sub_y;
+    const int tile = blockIdx.x / subs;
+    const int sub = blockIdx.x % subs;
+    const int ttx = tile % fv.tiles_x, tty = tile / fv.tiles_x;
+    int rect[4];   // the tile rectangle (GPU::TileRect, rglv_gpu.hxx:292-299)
+    rect[0] = ttx * fv.tile_w; rect[1] = tty * fv.tile_h;
+    rect[2] = min(rect[0] + fv.tile_w, fv.width); rect[3] = min(rect[1] + fv.tile_h, fv.height);
+    const int rx0 = rect[0] + (sub % sub_x) * kRegionPx, ry0 = rect[1] + (sub / sub_x) * kRegionPx;
+    const int rx1 = min(rx0 + kRegionPx, rect[2]), ry1 = min(ry0 + kRegionPx, rect[3]);
+    if (rx0 >= rx1 || ry0 >= ry1) return;
+    const int qw = (rx1 - rx0) >> 1, qh = (ry1 - ry0) >> 1;
+    const int tid = threadIdx.x;
+    const bool active = tid < qw * qh;
+    const int qx = rx0 + 2 * (active ? tid % qw : 0);
+    const int qy = ry0 + 2 * (active ? tid / qw : 0);
+    // the warp's quad footprint, for whole-warp triangle rejection
+    const int wx0 = __reduce_min_sync(FULL_MASK, active ? qx : INT_MAX);
+    const int wy0 = __reduce_min_sync(FULL_MASK, active ? qy : INT_MAX);
+    const int wx1 = __reduce_max_sync(FULL_MASK, active ? qx : INT_MIN);
+    const int wy1 = __reduce_max_sync(FULL_MASK, active ? qy : INT_MIN);
+
+    const TileBin bin = fv.bins[tile];
+    float col[4][3], dep[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) { col[l][0] = col[l][1] = col[l][2] = 0.f; dep[l] = 1.f; }
+    uint32_t inl_cur = 0, clip_cur = 0;
+    int cur_state = 0;
+    FragState fs;
+    load_frag_state(fv.states[0], fs);
+
+    for (int op = 0; op < fv.nops; ++op) {
+        const FrameOp o = fv.ops[op];
+        if (o.kind == kOpState) {
+            cur_state = o.arg;
+            load_frag_state(fv.states[cur_state], fs);
+        } else if (o.kind == kOpClear) {
+            const DevState& s = fv.states[cur_state];
+            const bool packed = s.color_type == 0;   // RB_COLOR_DEPTH clears both
+            if (packed || (o.arg & 1)) {
+#pragma unroll
+                for (int l = 0; l < 4; ++l) { col[l][0] = s.clear_color[0]; col[l][1] = s.clear_color[1]; col[l][2] = s.clear_color[2]; }
+            }
+            if (packed || (o.arg & 2)) {
+#pragma unroll
+                for (int l = 0; l < 4; ++l) dep[l] = s.clear_depth;
+            }
+        } else if (o.kind == kOpDraw) {
+            const DevDraw dr = fv.draws[o.arg];
+            const int end_tri = dr.first_tri + dr.ntris;
+            // inline triangles of this draw, then its clipped fans (rglv_gpu_impl.hxx:506-508)
+            for (int pass = 0; pass < 2; ++pass) {
+                const uint32_t base = pass == 0 ? bin.inl_off : bin.clip_off;
+                const uint32_t cnt = pass == 0 ? bin.inl_cnt : bin.clip_cnt;
+                uint32_t& cur = pass == 0 ? inl_cur : clip_cur;
+                while (true) {
+                    __syncthreads();
+                    bool valid = false;
+                    uint32_t e = 0;
+                    if (cur + uint32_t(tid) < cnt) {
+                        e = fv.bin_pool[base + cur + tid];
+                        const int src = pass == 0 ? int(e) : fv.clip_src[fv.clip_poly[e]];
+                        valid = src < end_tri;
+                    }
+                    const int n = __syncthreads_count(valid);
+                    if (n == 0) break;
+                    if (valid) {
+                        if (pass == 0) {
+                            const float4* rp = reinterpret_cast<const float4*>(fv.tris + e);
+                            TriRecord r;
+                            float4* rr = reinterpret_cast<float4*>(&r);
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) rr[q] = __ldg(rp + q);
+                            setup_vector(S, tid, rect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) {
+                                S.z[k][tid] = r.z[k]; S.w[k][tid] = r.w[k];
+#pragma unroll
+                                for (int q = 0; q < kMaxVary; ++q) S.vary[k][q][tid] = r.vary[k][q];
+                            }
+                        } else {
+                            const int pbase = fv.clip_poly[e];
+                            const ClipVert v0 = fv.clip_verts[pbase], v1 = fv.clip_verts[e], v2 = fv.clip_verts[e + 1];
+                            // DrawClipped: int(dev.x * FP_MUL) (rglv_gpu_impl.hxx:997-998)
+                            setup_scalar(S, tid, rect,
+                                         __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
+                                         __float2int_rz(v0.coord[1] * 16.0f), __float2int_rz(v1.coord[1] * 16.0f), __float2int_rz(v2.coord[1] * 16.0f));
+                            S.z[0][tid] = v0.coord[2]; S.z[1][tid] = v1.coord[2]; S.z[2][tid] = v2.coord[2];
+                            S.w[0][tid] = v0.coord[3]; S.w[1][tid] = v1.coord[3]; S.w[2][tid] = v2.coord[3];
+#pragma unroll
+                            for (int q = 0; q < kMaxVary; ++q) {
+                                S.vary[0][q][tid] = v0.vary[q]; S.vary[1][q][tid] = v1.vary[q]; S.vary[2][q][tid] = v2.vary[q];
+                            }
+                        }
+                    }
+                    __syncthreads();
+                    for (int i = 0; i < n; ++i) {
+                        const int minx = S.minx[i], maxx = S.maxx[i], miny = S.miny[i], maxy = S.maxy[i];
+                        if (maxx <= wx0 || minx > wx1 || maxy <= wy0 || miny > wy1) continue;   // warp-uniform
+                        if (!active || qx < minx || qx >= maxx || qy < miny || qy >= maxy) continue;
+                        const int32_t kx = qx - minx, ky = qy - miny;
+                        const int32_t dy12 = S.dy12[i], dx12 = S.dx12[i];
+                        const int32_t dy23 = S.dy23[i], dx23 = S.dx23[i];
+                        const int32_t dy31 = S.dy31[i], dx31 = S.dx31[i];
+                        const int32_t e1 = wadd(wadd(S.c1[i], wmul(kx, dy12)), wmul(ky, dx12));
+                        const int32_t e2 = wadd(wadd(S.c2[i], wmul(kx, dy23)), wmul(ky, dx23));
+                        const int32_t e3 = wadd(wadd(S.c3[i], wmul(kx, dy31)), wmul(ky, dx31));
+                        int32_t l1[4], l2[4], l3[4];
+                        l1[0] = e1; l1[1] = wadd(e1, dy12); l1[2] = wadd(e1, dx12); l1[3] = wadd(wadd(e1, dx12), dy12);
+                        l2[0] = e2; l2[1] = wadd(e2, dy23); l2[2] = wadd(e2, dx23); l2[3] = wadd(wadd(e2, dx23), dy23);
+                        l3[0] = e3; l3[1] = wadd(e3, dy31); l3[2] = wadd(e3, dx31); l3[3] = wadd(wadd(e3, dx31), dy31);
+                        bool inside[4];
+                        bool anyin = false;
+#pragma unroll
+                        for (int l = 0; l < 4; ++l) { inside[l] = (l1[l] | l2[l] | l3[l]) >= 0; anyin |= inside[l]; }
+                        if (!anyin) continue;
+                        const float scale = S.scale[i];
+                        const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];
+                        float bx[4], by[4], bz[4], fz[4];
+                        bool mask[4];
+                        bool any = false;
+#pragma unroll
+                        for (int l = 0; l < 4; ++l) {
+                            bx[l] = itof(l2[l]) * scale;
+                            bz[l] = itof(l1[l]) * scale;
+                            by[l] = (1.0f - bx[l]) - bz[l];
+                            fz[l] = (bx[l] * z0 + by[l] * z1) + bz[l] * z2;
+                            bool pass = true;
+                            if (fs.depth_test) {
+                                pass = fs.depth_func == 0 ? (fz[l] < dep[l]) : (fs.depth_func == 1 ? (fz[l] <= dep[l]) : (fz[l] == dep[l]));
+                            }
+                            mask[l] = inside[l] && pass;
+                            any |= mask[l];
+                        }
+                        if (!any) continue;
+                        if (fs.depth_write) {
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) if (mask[l]) dep[l] = fz[l];
+                        }
+                        const float w0 = S.w[0][i], w1 = S.w[1][i], w2 = S.w[2][i];
+                        float bpx[4], bpy[4], bpz[4];
+#pragma unroll
+                        for (int l = 0; l < 4; ++l) {
+                            const float fragW = oneover(fv.rcp_table, (bx[l] * w0 + by[l] * w1) + bz[l] * w2);
+                            bpx[l] = (w0 * bx[l]) * fragW;
+                            bpz[l] = (w2 * bz[l]) * fragW;
+                            bpy[l] = (1.0f - bpx[l]) - bpz[l];
+                        }
+                        float frag[4][4];
+                        if (fs.program == kProgAmy) {
+                            float uu[4], vv[4];
+                            const float u0 = S.vary[0][0][i], u1 = S.vary[1][0][i], u2 = S.vary[2][0][i];
+                            const float v0 = S.vary[0][1][i], v1 = S.vary[1][1][i], v2 = S.vary[2][1][i];
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) {
+                                uu[l] = (bpx[l] * u0 + bpy[l] * u1) + bpz[l] * u2;
+                                vv[l] = (bpx[l] * v0 + bpy[l] * v1) + bpz[l] * v2;
+                            }
+                            tex_sample(fs.tu0, uu, vv, frag);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < 3; ++q) {
+                                const float a0 = S.vary[0][q][i], a1 = S.vary[1][q][i], a2 = S.vary[2][q][i];
+#pragma unroll
+                                for (int l = 0; l < 4; ++l) frag[l][q] = (bpx[l] * a0 + bpy[l] * a1) + bpz[l] * a2;
+                            }
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) frag[l][3] = 1.0f;
+                        }
+                        if (fs.color_write) {
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) {
+                                if (!mask[l]) continue;
+                                if (fs.blend) {   // BlendAlpha (rglv_gpu_impl.hxx:80-84)
+                                    const float a = frag[l][3], oma = 1.0f - a;
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) col[l][c] = frag[l][c] * a + col[l][c] * oma;
+                                } else {
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) col[l][c] = frag[l][c];
+                                }
+                            }
+                        }
+                    }
+                    cur += uint32_t(n);
+                    if (n < int(blockDim.x)) break;
+                }
+            }
+        } else if (o.kind == kOpStoreTC) {
+            // GPUBltImpl::StoreTrueColor -> FilterTile (rglr_algorithm.hxx:31-104)
+            if (active) {
+                const DevState& s = fv.states[cur_state];
+                const float ex = s.program == kProgExposurePost ? s.uniforms[0] : 1.0f;
+                uint32_t px[4];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    float c3[3] = { col[l][0], col[l][1], col[l][2] };
+                    if (s.program == kProgExposurePost) { c3[0] = c3[0] * ex; c3[1] = c3[1] * ex; c3[2] = c3[2] * ex; }
+                    if (o.arg) px[l] = (srgb8(fv.srgb_lut, c3[0]) << 16) | (srgb8(fv.srgb_lut, c3[1]) << 8) | srgb8(fv.srgb_lut, c3[2]);
+                    else px[l] = (basic8(c3[0]) << 16) | (basic8(c3[1]) << 8) | basic8(c3[2]);
+                }
+                uint32_t* dst = static_cast<uint32_t*>(o.ptr);
+                *reinterpret_cast<uint2*>(dst + size_t(qy) * o.stride + qx) = make_uint2(px[0], px[1]);
+                *reinterpret_cast<uint2*>(dst + size_t(qy + 1) * o.stride + qx) = make_uint2(px[2], px[3]);
+            }
+        } else if (o.kind == kOpStoreDepth) {
+            // Copy(QFloatCanvas -> FloatCanvas) (rglr_algorithm.cxx:227-244)
+            if (active) {
+                float* dst = static_cast<float*>(o.ptr);
+                *reinterpret_cast<float2*>(dst + size_t(qy) * o.stride + qx) = make_float2(dep[0], dep[1]);
+                *reinterpret_cast<float2*>(dst + size_t(qy + 1) * o.stride + qx) = make_float2(dep[2], dep[3]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launch wrappers
+// ---------------------------------------------------------------------------
+cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
+    const int blocks = (fv.ntris + kSetupBlock - 1) / kSetupBlock;
+    if (blocks == 0) return cudaSuccess;
+    setup_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
+    const int warps_per_block = 8;
+    const int blocks = (fv.ntiles + warps_per_block - 1) / warps_per_block;
+    bin_kernel<<<blocks, warps_per_block * 32, 0, st>>>(fv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
+    const int sub_x = (fv.tile_w + kRegionPx - 1) / kRegionPx;
+    const int sub_y = (fv.tile_h + kRegionPx - 1) / kRegionPx;
+    const int blocks = fv.ntiles * sub_x * sub_y;
+    const int qx = (fv.tile_w < kRegionPx ? fv.tile_w : kRegionPx) / 2;
+    const int qy = (fv.tile_h < kRegionPx ? fv.tile_h : kRegionPx) / 2;
+    int threads = ((qx * qy + 31) / 32) * 32;
+    raster_kernel<<<blocks, threads, 0, st>>>(fv);
+    return cudaGetLastError();
+}
+
+}  // namespace rsrgpu

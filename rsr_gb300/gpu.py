@@ -1,0 +1,172 @@
+"""rglv::GPU over the C ABI of librsrgpu.so.
+
+Mirrors src/rgl/rglv/rglv_gpu.hxx:97-277: Install(programId, stateKey, ...),
+Reset(size, tileBlocks), IC() -> GL recorder, Run().  Run() submits the
+recorded stream and enqueues the frame; Wait() blocks until the outputs have
+landed.  Failures raise RsrGpuError carrying the library's message (the
+reference calls std::exit(1) on the same conditions).
+"""
+import ctypes
+
+import numpy as np
+
+from . import abi
+from .gl import GL
+
+
+class RsrGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("rsrgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+# The fragment state keys rsr's viewer installs (src/viewer/shaders.cxx:49-53,
+# 71-126) plus LEQUAL and the no-depth-write variant of the RGB f32 layout.
+DRAW_STATE_KEYS = (0x6E2, 0x6E6, 0x6F2, 0x6C2, 0x62, 0x72)
+
+
+class GPU:
+    def __init__(self, device=0):
+        self.lib = abi.load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.rsrgpu_create(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise RsrGpuError(rc, "rsrgpu_create failed")
+        self.ctx = h
+        self._gl = GL()
+        self._keep = None
+        self.width = self.height = 0
+        self.tile_blocks = (8, 8)
+
+    def close(self):
+        if self.ctx:
+            self.lib.rsrgpu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.rsrgpu_last_error(self.ctx, buf, 512)
+            raise RsrGpuError(rc, buf.value.decode(errors="replace"))
+
+    # ---- rglv::GPU surface ----
+    def Install(self, program_id, state_key, kind):
+        self._check(self.lib.rsrgpu_install(self.ctx, int(program_id), int(state_key), int(kind)))
+
+    def InstallDefaults(self):
+        """The device counterpart of rqv::Install (src/viewer/shaders.cxx:54-126)
+        for the programs this library implements."""
+        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY):
+            self.Install(pid, 0, abi.KIND_BIN)
+            for key in DRAW_STATE_KEYS:
+                self.Install(pid, key, abi.KIND_DRAW)
+        for pid in (abi.PROGRAM_DEFAULT_POST, abi.PROGRAM_EXPOSURE_POST, abi.PROGRAM_GOURAUD):
+            self.Install(pid, 0, abi.KIND_BLT)
+
+    def Reset(self, width, height, tile_blocks=(8, 8)):
+        self._check(self.lib.rsrgpu_reset(self.ctx, int(width), int(height),
+                                          int(tile_blocks[0]), int(tile_blocks[1])))
+        self.width, self.height, self.tile_blocks = width, height, tuple(tile_blocks)
+        self._gl = GL()
+
+    def IC(self):
+        return self._gl
+
+    def register_host_buffer(self, arr):
+        nbytes = arr.nbytes if isinstance(arr, np.ndarray) else arr.numel() * arr.element_size()
+        ptr = arr.ctypes.data if isinstance(arr, np.ndarray) else arr.data_ptr()
+        self._check(self.lib.rsrgpu_register_host_buffer(self.ctx, ctypes.c_void_p(ptr), nbytes))
+
+    def unregister_host_buffer(self, arr):
+        ptr = arr.ctypes.data if isinstance(arr, np.ndarray) else arr.data_ptr()
+        self._check(self.lib.rsrgpu_unregister_host_buffer(self.ctx, ctypes.c_void_p(ptr)))
+
+    def submit(self, gl=None):
+        gl = gl or self._gl
+        cmds = gl.stream()
+        states = gl.c_states()
+        buf = ctypes.create_string_buffer(cmds, max(1, len(cmds)))
+        self._keep = (buf, states, gl)
+        self._check(self.lib.rsrgpu_submit(self.ctx, ctypes.cast(buf, ctypes.c_void_p), len(cmds),
+                                           states, len(gl.states)))
+
+    def Run(self, gl=None, stream=None):
+        """Submit the recorded frame and enqueue it (GPU::Run)."""
+        self.submit(gl)
+        self.run(stream)
+
+    def run(self, stream=None):
+        self._check(self.lib.rsrgpu_run(self.ctx, ctypes.c_void_p(stream) if stream else None))
+
+    def Wait(self, timeout_ms=-1):
+        self._check(self.lib.rsrgpu_wait(self.ctx, int(timeout_ms)))
+
+    # ---- inspection ----
+    def tiles(self):
+        need = ctypes.c_size_t(0)
+        self._check(self.lib.rsrgpu_dump_tiles(self.ctx, None, 0, ctypes.byref(need)))
+        out = (ctypes.c_uint8 * max(1, need.value))()
+        self._check(self.lib.rsrgpu_dump_tiles(self.ctx, out, need.value, ctypes.byref(need)))
+        blob = bytes(out)[:need.value]
+        res, p = [], 0
+        while p < len(blob):
+            n = int.from_bytes(blob[p:p + 4], "little")
+            res.append(blob[p + 4:p + 4 + n])
+            p += 4 + n
+        return res
+
+    def clipped(self):
+        n = ctypes.c_int(0)
+        self._check(self.lib.rsrgpu_dump_clipped(self.ctx, None, 0, ctypes.byref(n)))
+        out = (abi.ClippedVertexC * max(1, n.value))()
+        self._check(self.lib.rsrgpu_dump_clipped(self.ctx, out, n.value, ctypes.byref(n)))
+        flat = np.ctypeslib.as_array(ctypes.cast(out, ctypes.POINTER(ctypes.c_float)),
+                                     shape=(max(1, n.value) * 20,))
+        return flat[:n.value * 20].reshape(n.value, 20).copy()
+
+    def stats(self):
+        s = abi.StatsC()
+        self._check(self.lib.rsrgpu_get_stats(self.ctx, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.StatsC._fields_}
+
+    def timings(self):
+        t, r = ctypes.c_float(), ctypes.c_float()
+        self._check(self.lib.rsrgpu_last_timings(self.ctx, ctypes.byref(t), ctypes.byref(r)))
+        return t.value, r.value
+
+
+def render_scene(gpu, scene, gamma=True, device_inputs=None, color=None, depth=None):
+    """Render a scenes.Scene.  With device_inputs (name -> device tensor) the
+    inputs are used in place; otherwise the scene's host arrays are
+    registered and copied inside the run.  Returns (color, depth) on the
+    host."""
+    gpu.Reset(scene.width, scene.height, scene.tile_blocks)
+    if device_inputs is None:
+        for arr in scene.arrays.values():
+            gpu.register_host_buffer(arr)
+        if color is None:
+            gpu.register_host_buffer(scene.color)
+            gpu.register_host_buffer(scene.depth)
+        ref = None
+    else:
+        ref = device_inputs.__getitem__
+    gl = scene.record(ref=ref, color=color, depth=depth, gamma=gamma)
+    try:
+        gpu.Run(gl)
+        gpu.Wait()
+    finally:
+        if device_inputs is None:
+            for arr in scene.arrays.values():
+                gpu.unregister_host_buffer(arr)
+            if color is None:
+                gpu.unregister_host_buffer(scene.color)
+                gpu.unregister_host_buffer(scene.depth)
+    if color is None:
+        return scene.color.copy(), scene.depth.copy()
+    return color, depth

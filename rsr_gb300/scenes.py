@@ -273,3 +273,32 @@ def textured_sphere(seed=1, divs=7, width=1920, height=1080, tile_blocks=(4, 4),
             gl.DrawElements(count, ref("idx%d" % k), abi.RGL_HINT_DENSE | abi.RGL_HINT_READ4)
 
     return Scene("textured_sphere", width, height, tile_blocks, arrays, record, nfaces)
+
+
+def clip_stress(seed=3, ntris=3000, width=640, height=360, tile_blocks=(8, 8), extent=6.0):
+    """Random triangles around a perspective camera at the origin: many cross
+    the near plane or the guard band and go through the Sutherland-Hodgman
+    clipper and the scalar rasteriser.  Culling of back faces is on so the
+    clipper's winding handling is exercised too."""
+    nverts = 3 * ntris
+    u = uniform01(seed, nverts * 6).reshape(ntris, 3, 6)
+    pos = lerp(-extent, extent, u[:, :, 0:3]).reshape(nverts, 3)
+    rgb = lerp(0.0, 1.0, u[:, :, 3:6]).reshape(nverts, 3)
+    arrays = {
+        "px": pad4(pos[:, 0]), "py": pad4(pos[:, 1]), "pz": pad4(pos[:, 2]),
+        "cr": pad4(rgb[:, 0]), "cg": pad4(rgb[:, 1]), "cb": pad4(rgb[:, 2]),
+        "idx": np.arange(nverts, dtype=np.uint16),
+    }
+    proj = perspective(90.0, width / height, 0.5, 50.0)
+
+    def record(gl, ref):
+        _begin_frame(gl)
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        gl.Enable(abi.GL_CULL_FACE)
+        gl.CullFace(abi.GL_BACK)
+        gl.ProjectionMatrix(proj)
+        gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
+        gl.UseBuffer(3, (ref("cr"), ref("cg"), ref("cb")))
+        gl.DrawElements(nverts, ref("idx"), 0)
+
+    return Scene("clip_stress", width, height, tile_blocks, arrays, record, ntris)

@@ -1,0 +1,78 @@
+"""Generates tests/golden/frames.json from rsr's own CPU rasteriser.
+
+Runs oracle/_ref/librsrref.so (rsr's sources built by oracle/ref/Makefile,
+x86-64 only) on the seeded scenes of GOLDEN_SCENES and records, per scene
+and gamma setting, SHA-256 digests of the sRGB8/linear colour buffer, the fp32
+depth buffer, the canonical per-tile command streams, and the clipped vertex
+buffer (coordinates + the program's varyings).  The oracle is checked
+against these digests on every machine, including ones without the
+reference.
+
+    python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from rsr_gb300 import scenes  # noqa: E402
+
+# name -> (factory, kwargs, varyings kept per clipped vertex)
+GOLDEN_SCENES = {
+    "plain_640_t64": ("plain_raster", {}, 3),
+    "plain_320_t8": ("plain_raster", dict(seed=7, ntris=2000, width=320, height=180, tile_blocks=(1, 1)), 3),
+    "plain_1080_t128": ("plain_raster", dict(seed=8, ntris=500, width=1920, height=1080, tile_blocks=(16, 16)), 3),
+    "plain_640_t16x32": ("plain_raster", dict(seed=9, ntris=3000, width=640, height=360, tile_blocks=(2, 4)), 3),
+    "sphere_1080_t32": ("textured_sphere", dict(divs=6), 2),
+    "clip_640_t64": ("clip_stress", {}, 3),
+    "clip_2160_t32": ("clip_stress", dict(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0), 3),
+}
+
+
+def make_scene(name):
+    fn, kw, _ = GOLDEN_SCENES[name]
+    kw = dict(kw)
+    if "tile_blocks" in kw:
+        kw["tile_blocks"] = tuple(kw["tile_blocks"])
+    return getattr(scenes, fn)(**kw)
+
+
+def digest(b):
+    return hashlib.sha256(b).hexdigest()
+
+
+def frame_digests(color, depth, tiles, clipped, nvary):
+    return {
+        "color": digest(np.ascontiguousarray(color).tobytes()),
+        "depth": digest(np.ascontiguousarray(depth).view(np.uint32).tobytes()),
+        "tiles": digest(b"".join(len(t).to_bytes(4, "little") + t for t in tiles)),
+        "clipped": digest(np.ascontiguousarray(clipped[:, :4 + nvary]).view(np.uint32).tobytes()),
+        "nclipped": int(clipped.shape[0]),
+        "covered": int((depth < 1.0).sum()),
+    }
+
+
+def main():
+    import oracle
+    if not oracle.ref_available():
+        raise SystemExit("oracle/_ref/librsrref.so is not built (x86-64 host with the reference needed)")
+    ref = oracle.CpuRenderer("ref")
+    out = {}
+    for name, (_, _, nvary) in GOLDEN_SCENES.items():
+        sc = make_scene(name)
+        for gamma in (False, True):
+            c, d = ref.render(sc, gamma)
+            out["%s/gamma%d" % (name, int(gamma))] = frame_digests(c, d, ref.tiles(), ref.clipped(), nvary)
+            print(name, gamma, out["%s/gamma%d" % (name, int(gamma))]["covered"])
+    with open(os.path.join(HERE, "frames.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()
