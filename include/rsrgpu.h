@@ -218,6 +218,34 @@ int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms);
 
 int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
 
+/* ---- rendering without any device allocation ----
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that cannot call cudaMalloc (for example a host framework that owns all
+ * device memory through its own pool, or a real-time loop that must never
+ * allocate): it renders one frame through the same kernels as rsrgpu_run()
+ * but keeps all frame scratch in one fixed file-scope device array of
+ * RSRGPU_STATIC_SCRATCH_BYTES (about 7 MiB) that every GPU loading this
+ * library holds until the process exits.  Inputs and outputs must be device
+ * pointers; there is no context and no host staging.  The first call on a
+ * device sets the array up (symbol address lookup and two synchronous table
+ * uploads), so make it before any stream capture.  Calls share the array
+ * (the counters that must start at zero are cleared on every call), so
+ * calls that overlap on the GPU race: serialise them.  The call returns once
+ * the frame has finished on `stream` (a cudaStream_t, NULL = legacy stream);
+ * frames larger than the limits below fail with RSRGPU_ECAPACITY and the
+ * reason in errbuf (may be NULL). */
+#define RSRGPU_STATIC_MAX_TRIANGLES    32768
+#define RSRGPU_STATIC_MAX_TILES        8192
+#define RSRGPU_STATIC_MAX_TILE_ENTRIES 524288
+#define RSRGPU_STATIC_MAX_CLIP_VERTS   16384
+#define RSRGPU_STATIC_MAX_STATES       64
+#define RSRGPU_STATIC_MAX_DRAWS        256
+#define RSRGPU_STATIC_MAX_OPS          1024
+#define RSRGPU_STATIC_SCRATCH_BYTES    7341824
+int rsrgpu_render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates,
+                         int width, int height, int tile_blocks_x, int tile_blocks_y, void* stream,
+                         char* errbuf, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

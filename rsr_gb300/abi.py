@@ -133,6 +133,9 @@ SYMBOLS = {
     "rsrgpu_get_stats": ([ctypes.c_void_p, ctypes.POINTER(StatsC)], ctypes.c_int),
     "rsrgpu_last_timings": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     "rsrgpu_last_error": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
+                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                              ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
 }
 
 

@@ -818,3 +818,40 @@ int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Frame decode for callers without a context (rsrgpu_static.cu): runs the
+// same stream parser as rsrgpu_submit() on a temporary context that owns no
+// device memory, with every program this library implements installed.
+// Pointers must therefore be device pointers.
+// ---------------------------------------------------------------------------
+namespace rsrgpu {
+int decode_frame_without_context(int width, int height, int tile_blocks_x, int tile_blocks_y,
+                                 const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates,
+                                 std::vector<DevState>& out_states, std::vector<DevDraw>& out_draws,
+                                 std::vector<FrameOp>& out_ops, int& ntris, int& ntiles, std::string& err) {
+    rsrgpu_ctx tmp;
+    int rc = rsrgpu_reset(&tmp, width, height, tile_blocks_x, tile_blocks_y);
+    const int programs[] = { kProgGouraud, kProgAmy };
+    const uint32_t keys[] = { 0x6e2, 0x6e6, 0x6ea, 0x6f2, 0x6f6, 0x6c2, 0x6c6, 0x62, 0x66, 0x72, 0x42, 0x6a };
+    for (int pid : programs) {
+        if (rc == 0) rc = rsrgpu_install(&tmp, pid, 0, 0);
+        for (uint32_t k : keys)
+            if (rc == 0 && draw_key_supported(k)) rc = rsrgpu_install(&tmp, pid, k, 1);
+    }
+    const int blts[] = { kProgDefaultPost, kProgExposurePost, kProgGouraud };
+    for (int pid : blts)
+        if (rc == 0) rc = rsrgpu_install(&tmp, pid, 0, 2);
+    if (rc == 0) rc = rsrgpu_submit(&tmp, commands, nbytes, states, nstates);
+    if (rc != 0) {
+        err = tmp.err;
+        return rc;
+    }
+    out_states = std::move(tmp.states);
+    out_draws = std::move(tmp.draws);
+    out_ops = std::move(tmp.ops);
+    ntris = tmp.ntris;
+    ntiles = tmp.ntiles;
+    return 0;
+}
+}  // namespace rsrgpu
