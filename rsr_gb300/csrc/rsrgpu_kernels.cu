@@ -454,7 +454,17 @@ __global__ void __launch_bounds__(256) bin_kernel(FrameView fv) {
 // ---------------------------------------------------------------------------
 // raster
 // ---------------------------------------------------------------------------
-// per-(triangle, tile) setup, structure of arrays in shared memory
+// per-(triangle, tile) rasteriser setup: the bounding box clamped to the tile
+// and aligned to quads, the three edge values at its first quad and their
+// steps, and 1 / (c1 + c2 + c3)
+struct TriSetup {
+    int32_t minx, miny, maxx, maxy;
+    int32_t c1, c2, c3;
+    int32_t dy12, dx12, dy23, dx23, dy31, dx31;
+    float scale;
+};
+
+// structure of arrays in shared memory, one batch of triangles
 struct RasterSmem {
     int32_t minx[kRasterBatch], miny[kRasterBatch], maxx[kRasterBatch], maxy[kRasterBatch];
     int32_t c1[kRasterBatch], c2[kRasterBatch], c3[kRasterBatch];
@@ -463,11 +473,11 @@ struct RasterSmem {
     float scale[kRasterBatch];
     float z[3][kRasterBatch], w[3][kRasterBatch];
     float vary[3][kMaxVary][kRasterBatch];
-    uint32_t entry[kRasterBatch];
+    uint32_t code[kRasterBatch];   // fragment owner: triangle id, or clipped fan id | bit 31
 };
 
 // VTriangleRasterizer setup for one lane (rglv_triangle.hxx:209-240), int32 wrap
-__device__ __forceinline__ void setup_vector(RasterSmem& S, int i, const int rect[4],
+__device__ __forceinline__ void setup_vector(TriSetup& t, const int rect[4],
                                              int32_t x1, int32_t x2, int32_t x3, int32_t y1, int32_t y2, int32_t y3) {
     int32_t vminx = max(min(min(x1, x2), x3) >> 4, rect[0]);
     const int32_t vmaxx = min(wadd(max(max(x1, x2), x3), 15) >> 4, rect[2]);
@@ -488,14 +498,14 @@ __device__ __forceinline__ void setup_vector(RasterSmem& S, int i, const int rec
     c1 = wsub(wadd(c1, tl12), 1) >> 4;
     c2 = wsub(wadd(c2, tl23), 1) >> 4;
     c3 = wsub(wadd(c3, tl31), 1) >> 4;
-    S.minx[i] = vminx; S.miny[i] = vminy; S.maxx[i] = vmaxx; S.maxy[i] = vmaxy;
-    S.c1[i] = c1; S.c2[i] = c2; S.c3[i] = c3;
-    S.dy12[i] = dy12; S.dx12[i] = dx12; S.dy23[i] = dy23; S.dx23[i] = dx23; S.dy31[i] = dy31; S.dx31[i] = dx31;
-    S.scale[i] = __fdiv_rn(1.0f, itof(wadd(wadd(c1, c2), c3)));
+    t.minx = vminx; t.miny = vminy; t.maxx = vmaxx; t.maxy = vmaxy;
+    t.c1 = c1; t.c2 = c2; t.c3 = c3;
+    t.dy12 = dy12; t.dx12 = dx12; t.dy23 = dy23; t.dx23 = dx23; t.dy31 = dy31; t.dx31 = dx31;
+    t.scale = __fdiv_rn(1.0f, itof(wadd(wadd(c1, c2), c3)));
 }
 
 // TriangleRasterizer setup (rglv_triangle.hxx:79-131), int64
-__device__ __forceinline__ void setup_scalar(RasterSmem& S, int i, const int rect[4],
+__device__ __forceinline__ void setup_scalar(TriSetup& t, const int rect[4],
                                              int x1, int x2, int x3, int y1, int y2, int y3) {
     int minx = max(min(x1, min(x2, x3)) >> 4, rect[0]);
     const int endx = min((max(x1, max(x2, x3)) + 15) >> 4, rect[2]);
@@ -516,12 +526,30 @@ __device__ __forceinline__ void setup_scalar(RasterSmem& S, int i, const int rec
     if (dy31 > 0 || (dy31 == 0 && dx31 > 0)) c3++;
     --c3;
     c1 >>= 4; c2 >>= 4; c3 >>= 4;
-    S.minx[i] = minx; S.miny[i] = miny; S.maxx[i] = endx; S.maxy[i] = endy;
-    S.c1[i] = int32_t(c1); S.c2[i] = int32_t(c2); S.c3[i] = int32_t(c3);
-    S.dy12[i] = int32_t(dy12); S.dx12[i] = int32_t(dx12);
-    S.dy23[i] = int32_t(dy23); S.dx23[i] = int32_t(dx23);
-    S.dy31[i] = int32_t(dy31); S.dx31[i] = int32_t(dx31);
-    S.scale[i] = __fdiv_rn(1.0f, __ll2float_rn(c1 + c2 + c3));
+    t.minx = minx; t.miny = miny; t.maxx = endx; t.maxy = endy;
+    t.c1 = int32_t(c1); t.c2 = int32_t(c2); t.c3 = int32_t(c3);
+    t.dy12 = int32_t(dy12); t.dx12 = int32_t(dx12);
+    t.dy23 = int32_t(dy23); t.dx23 = int32_t(dx23);
+    t.dy31 = int32_t(dy31); t.dx31 = int32_t(dx31);
+    t.scale = __fdiv_rn(1.0f, __ll2float_rn(c1 + c2 + c3));
+}
+
+__device__ __forceinline__ void put_setup(RasterSmem& S, int i, const TriSetup& t) {
+    S.minx[i] = t.minx; S.miny[i] = t.miny; S.maxx[i] = t.maxx; S.maxy[i] = t.maxy;
+    S.c1[i] = t.c1; S.c2[i] = t.c2; S.c3[i] = t.c3;
+    S.dy12[i] = t.dy12; S.dx12[i] = t.dx12; S.dy23[i] = t.dy23; S.dx23[i] = t.dx23;
+    S.dy31[i] = t.dy31; S.dx31[i] = t.dx31;
+    S.scale[i] = t.scale;
+}
+
+// Edge values of one lane of quad (qx, qy): the quad walk adds 2*dy per quad
+// column and 2*dx per quad row to the first quad's values, lane l adds dy for
+// x+1 and dx for y+1 -- all wrapping 32-bit sums, so the direct form is equal.
+__device__ __forceinline__ void lane_edges(const TriSetup& t, int qx, int qy, int l, int32_t& e1, int32_t& e2, int32_t& e3) {
+    const int32_t kx = qx - t.minx + (l & 1), ky = qy - t.miny + (l >> 1);
+    e1 = wadd(wadd(t.c1, wmul(kx, t.dy12)), wmul(ky, t.dx12));
+    e2 = wadd(wadd(t.c2, wmul(kx, t.dy23)), wmul(ky, t.dx23));
+    e3 = wadd(wadd(t.c3, wmul(kx, t.dy31)), wmul(ky, t.dx31));
 }
 
 // Texel fetch for the nearest samplers: their offsets come from fract() of
@@ -594,6 +622,48 @@ __device__ __forceinline__ void tex_sample(const DevTexture& tu, const float u[4
     }
 }
 
+// LINEAR mip sampler for one lane, with the quad's coarse LoD taken from
+// lanes 0 and 1 (u0,v0), (u1,v1) exactly as the four-lane sampler does
+__device__ __forceinline__ void tex_sample_lane(const DevTexture& tu, float u0, float v0, float u1, float v1,
+                                                float ul, float vl, float out[4]) {
+    float u[4] = { u0, u1, ul, ul }, v[4] = { v0, v1, vl, vl };
+    float o[4][4];
+    if (tu.kind == 1) {
+        // only the LoD needs lanes 0 and 1; sample lane l alone
+        const int P = tu.power;
+        const float baseDim = float(1 << P);
+        const float dux = u1 * baseDim - u0 * baseDim;
+        const float dvx = v1 * baseDim - v0 * baseDim;
+        const float sqd = dux * dux + dvx * dvx;
+        int lod = (int32_t(f2u(sqd)) - (127 << 23)) >> 24;
+        lod = lod < 0 ? 0 : (lod > P ? P : lod);
+        const int levelDim = 1 << (P - lod);
+        const int32_t wrapMask = levelDim - 1;
+        const int32_t levelLastRow = int32_t(((0xffffffffu << (P - lod)) & ((1u << (P + 1)) - 1u)) - 1u);
+        const float levelX = ul * float(levelDim);
+        const float levelY = vl * float(levelDim);
+        int32_t tx0 = ftoi(levelX - 0.5f), ty0 = ftoi(levelY - 0.5f);
+        int32_t tx1 = wadd(tx0, 1), ty1 = wadd(ty0, 1);
+        const float fx = (levelX - itof(tx0)) - 0.5f;
+        const float fy = (levelY - itof(ty0)) - 0.5f;
+        const float fx1 = 1.0f - fx, fy1 = 1.0f - fy;
+        const float w00 = fx1 * fy1, w10 = fx * fy1, w01 = fx1 * fy, w11 = fx * fy;
+        tx0 &= wrapMask; ty0 &= wrapMask; tx1 &= wrapMask; ty1 &= wrapMask;
+        const int32_t y0 = wsub(levelLastRow, ty0), y1 = wsub(levelLastRow, ty1);
+        const float4 p00 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y0) << P), tx0));
+        const float4 p10 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y0) << P), tx1));
+        const float4 p01 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y1) << P), tx0));
+        const float4 p11 = __ldg(reinterpret_cast<const float4*>(tu.buf) + wadd(int32_t(uint32_t(y1) << P), tx1));
+        out[0] = ((p00.x * w00 + p10.x * w10) + p01.x * w01) + p11.x * w11;
+        out[1] = ((p00.y * w00 + p10.y * w10) + p01.y * w01) + p11.y * w11;
+        out[2] = ((p00.z * w00 + p10.z * w10) + p01.z * w01) + p11.z * w11;
+        out[3] = ((p00.w * w00 + p10.w * w10) + p01.w * w01) + p11.w * w11;
+        return;
+    }
+    tex_sample(tu, u, v, o);
+    out[0] = o[2][0]; out[1] = o[2][1]; out[2] = o[2][2]; out[3] = o[2][3];
+}
+
 // fragment-stage constants of the current state, held in registers
 struct FragState {
     int program, nvary;
@@ -617,6 +687,99 @@ __device__ __forceinline__ uint32_t basic8(float v) {   // to_tc_basic (rglr_can
     return uint32_t(ftoi(sse_max(sse_min(v, 1.0f), 0.0f) * 255.0f));
 }
 
+__device__ __forceinline__ bool depth_pass(int func, float frag, float dest) {
+    return func == 0 ? (frag < dest) : (func == 1 ? (frag <= dest) : (frag == dest));
+}
+
+constexpr uint32_t kNoOwner = 0xffffffffu;
+constexpr uint32_t kClippedBit = 0x80000000u;
+
+// Per-(triangle, tile) setup and vertex data of one list entry, for the
+// resolve pass: the triangle that last wrote a pixel is set up again exactly
+// as when it was rasterised.
+__device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int rect[4], TriSetup& t,
+                                         float w[3], float vary[3][kMaxVary], int& state) {
+    int g;
+    if (code & kClippedBit) {
+        const uint32_t e = code & ~kClippedBit;
+        const int pbase = fv.clip_poly[e];
+        g = fv.clip_src[pbase];
+        const ClipVert v0 = fv.clip_verts[pbase], v1 = fv.clip_verts[e], v2 = fv.clip_verts[e + 1];
+        setup_scalar(t, rect,
+                     __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
+                     __float2int_rz(v0.coord[1] * 16.0f), __float2int_rz(v1.coord[1] * 16.0f), __float2int_rz(v2.coord[1] * 16.0f));
+        w[0] = v0.coord[3]; w[1] = v1.coord[3]; w[2] = v2.coord[3];
+        for (int q = 0; q < kMaxVary; ++q) { vary[0][q] = v0.vary[q]; vary[1][q] = v1.vary[q]; vary[2][q] = v2.vary[q]; }
+    } else {
+        g = int(code);
+        const float4* rp = reinterpret_cast<const float4*>(fv.tris + g);
+        TriRecord r;
+        float4* rr = reinterpret_cast<float4*>(&r);
+        for (int q = 0; q < 6; ++q) rr[q] = __ldg(rp + q);
+        setup_vector(t, rect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
+        for (int k = 0; k < 3; ++k) {
+            w[k] = r.w[k];
+            for (int q = 0; q < kMaxVary; ++q) vary[k][q] = r.vary[k][q];
+        }
+    }
+    state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+}
+
+// perspective-correct barycentrics of one lane (TriangleProgram::Render,
+// rglv_gpu_impl.hxx:187-191)
+__device__ __forceinline__ void lane_bary(const FrameView& fv, const TriSetup& t, const float w[3], int qx, int qy, int l,
+                                          float& px, float& py, float& pz) {
+    int32_t e1, e2, e3;
+    lane_edges(t, qx, qy, l, e1, e2, e3);
+    const float bx = itof(e2) * t.scale;
+    const float bz = itof(e1) * t.scale;
+    const float by = (1.0f - bx) - bz;
+    const float fragW = oneover(fv.rcp_table, (bx * w[0] + by * w[1]) + bz * w[2]);
+    px = (w[0] * bx) * fragW;
+    pz = (w[2] * bz) * fragW;
+    py = (1.0f - px) - pz;
+}
+
+// Shades every pixel of the quad whose last visible fragment is still
+// pending, with the owning triangle's program, and writes the colour.
+__device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect[4], int qx, int qy,
+                                             uint32_t own[4], float col[4][3]) {
+    uint32_t cur = kNoOwner;
+    TriSetup t;
+    float w[3], vary[3][kMaxVary];
+    int state = 0;
+#pragma unroll 1
+    for (int l = 0; l < 4; ++l) {
+        if (own[l] == kNoOwner) continue;
+        if (own[l] != cur) {
+            cur = own[l];
+            owner_setup(fv, cur, rect, t, w, vary, state);
+        }
+        const DevState& s = fv.states[state];
+        float bpx, bpy, bpz;
+        lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
+        if (s.program == kProgAmy) {
+            float b0x, b0y, b0z, b1x, b1y, b1z;
+            lane_bary(fv, t, w, qx, qy, 0, b0x, b0y, b0z);
+            lane_bary(fv, t, w, qx, qy, 1, b1x, b1y, b1z);
+            const float u0 = (b0x * vary[0][0] + b0y * vary[1][0]) + b0z * vary[2][0];
+            const float v0 = (b0x * vary[0][1] + b0y * vary[1][1]) + b0z * vary[2][1];
+            const float u1 = (b1x * vary[0][0] + b1y * vary[1][0]) + b1z * vary[2][0];
+            const float v1 = (b1x * vary[0][1] + b1y * vary[1][1]) + b1z * vary[2][1];
+            const float ul = (bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0];
+            const float vl = (bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1];
+            float o[4];
+            const DevTexture tu = s.tu0;
+            tex_sample_lane(tu, u0, v0, u1, v1, ul, vl, o);
+            col[l][0] = o[0]; col[l][1] = o[1]; col[l][2] = o[2];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) col[l][q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
+        }
+        own[l] = kNoOwner;
+    }
+}
+
 __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
     __shared__ RasterSmem S;
     if (fv.counters->overflow != 0u) return;
@@ -635,6 +798,7 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
     if (rx0 >= rx1 || ry0 >= ry1) return;
     const int qw = (rx1 - rx0) >> 1, qh = (ry1 - ry0) >> 1;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const bool active = tid < qw * qh;
     const int qx = rx0 + 2 * (active ? tid % qw : 0);
     const int qy = ry0 + 2 * (active ? tid / qw : 0);
@@ -646,8 +810,10 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
 
     const TileBin bin = fv.bins[tile];
     float col[4][3], dep[4];
+    uint32_t own[4];   // pending last visible fragment of each pixel (visibility mode)
 #pragma unroll
-    for (int l = 0; l < 4; ++l) { col[l][0] = col[l][1] = col[l][2] = 0.f; dep[l] = 1.f; }
+    for (int l = 0; l < 4; ++l) { col[l][0] = col[l][1] = col[l][2] = 0.f; dep[l] = 1.f; own[l] = kNoOwner; }
+    bool pending = false;
     uint32_t inl_cur = 0, clip_cur = 0;
     int cur_state = 0;
     FragState fs;
@@ -658,7 +824,18 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
         if (o.kind == kOpState) {
             cur_state = o.arg;
             load_frag_state(fv.states[cur_state], fs);
-        } else if (o.kind == kOpClear) {
+            continue;
+        }
+        // Without blending the colour of a pixel is that of the last fragment
+        // that passed the depth test, so draws without blending only track
+        // that fragment's owner and shade it once; anything that reads or
+        // replaces colour first resolves the pending pixels.
+        const bool visibility = o.kind == kOpDraw && !fs.blend;
+        if (!visibility && pending) {
+            if (active) resolve_quad(fv, rect, qx, qy, own, col);
+            pending = false;
+        }
+        if (o.kind == kOpClear) {
             const DevState& s = fv.states[cur_state];
             const bool packed = s.color_type == 0;   // RB_COLOR_DEPTH clears both
             if (packed || (o.arg & 1)) {
@@ -672,6 +849,7 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
         } else if (o.kind == kOpDraw) {
             const DevDraw dr = fv.draws[o.arg];
             const int end_tri = dr.first_tri + dr.ntris;
+            if (visibility) pending = true;
             // inline triangles of this draw, then its clipped fans (rglv_gpu_impl.hxx:506-508)
             for (int pass = 0; pass < 2; ++pass) {
                 const uint32_t base = pass == 0 ? bin.inl_off : bin.clip_off;
@@ -689,24 +867,26 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
                     const int n = __syncthreads_count(valid);
                     if (n == 0) break;
                     if (valid) {
+                        TriSetup t;
                         if (pass == 0) {
                             const float4* rp = reinterpret_cast<const float4*>(fv.tris + e);
                             TriRecord r;
                             float4* rr = reinterpret_cast<float4*>(&r);
 #pragma unroll
                             for (int q = 0; q < 6; ++q) rr[q] = __ldg(rp + q);
-                            setup_vector(S, tid, rect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
+                            setup_vector(t, rect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
 #pragma unroll
                             for (int k = 0; k < 3; ++k) {
                                 S.z[k][tid] = r.z[k]; S.w[k][tid] = r.w[k];
 #pragma unroll
                                 for (int q = 0; q < kMaxVary; ++q) S.vary[k][q][tid] = r.vary[k][q];
                             }
+                            S.code[tid] = e;
                         } else {
                             const int pbase = fv.clip_poly[e];
                             const ClipVert v0 = fv.clip_verts[pbase], v1 = fv.clip_verts[e], v2 = fv.clip_verts[e + 1];
                             // DrawClipped: int(dev.x * FP_MUL) (rglv_gpu_impl.hxx:997-998)
-                            setup_scalar(S, tid, rect,
+                            setup_scalar(t, rect,
                                          __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
                                          __float2int_rz(v0.coord[1] * 16.0f), __float2int_rz(v1.coord[1] * 16.0f), __float2int_rz(v2.coord[1] * 16.0f));
                             S.z[0][tid] = v0.coord[2]; S.z[1][tid] = v1.coord[2]; S.z[2][tid] = v2.coord[2];
@@ -715,94 +895,105 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
                             for (int q = 0; q < kMaxVary; ++q) {
                                 S.vary[0][q][tid] = v0.vary[q]; S.vary[1][q][tid] = v1.vary[q]; S.vary[2][q][tid] = v2.vary[q];
                             }
+                            S.code[tid] = e | kClippedBit;
                         }
+                        put_setup(S, tid, t);
                     }
                     __syncthreads();
-                    for (int i = 0; i < n; ++i) {
-                        const int minx = S.minx[i], maxx = S.maxx[i], miny = S.miny[i], maxy = S.maxy[i];
-                        if (maxx <= wx0 || minx > wx1 || maxy <= wy0 || miny > wy1) continue;   // warp-uniform
-                        if (!active || qx < minx || qx >= maxx || qy < miny || qy >= maxy) continue;
-                        const int32_t kx = qx - minx, ky = qy - miny;
-                        const int32_t dy12 = S.dy12[i], dx12 = S.dx12[i];
-                        const int32_t dy23 = S.dy23[i], dx23 = S.dx23[i];
-                        const int32_t dy31 = S.dy31[i], dx31 = S.dx31[i];
-                        const int32_t e1 = wadd(wadd(S.c1[i], wmul(kx, dy12)), wmul(ky, dx12));
-                        const int32_t e2 = wadd(wadd(S.c2[i], wmul(kx, dy23)), wmul(ky, dx23));
-                        const int32_t e3 = wadd(wadd(S.c3[i], wmul(kx, dy31)), wmul(ky, dx31));
-                        int32_t l1[4], l2[4], l3[4];
-                        l1[0] = e1; l1[1] = wadd(e1, dy12); l1[2] = wadd(e1, dx12); l1[3] = wadd(wadd(e1, dx12), dy12);
-                        l2[0] = e2; l2[1] = wadd(e2, dy23); l2[2] = wadd(e2, dx23); l2[3] = wadd(wadd(e2, dx23), dy23);
-                        l3[0] = e3; l3[1] = wadd(e3, dy31); l3[2] = wadd(e3, dx31); l3[3] = wadd(wadd(e3, dx31), dy31);
-                        bool inside[4];
-                        bool anyin = false;
-#pragma unroll
-                        for (int l = 0; l < 4; ++l) { inside[l] = (l1[l] | l2[l] | l3[l]) >= 0; anyin |= inside[l]; }
-                        if (!anyin) continue;
-                        const float scale = S.scale[i];
-                        const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];
-                        float bx[4], by[4], bz[4], fz[4];
-                        bool mask[4];
-                        bool any = false;
-#pragma unroll
-                        for (int l = 0; l < 4; ++l) {
-                            bx[l] = itof(l2[l]) * scale;
-                            bz[l] = itof(l1[l]) * scale;
-                            by[l] = (1.0f - bx[l]) - bz[l];
-                            fz[l] = (bx[l] * z0 + by[l] * z1) + bz[l] * z2;
-                            bool pass = true;
-                            if (fs.depth_test) {
-                                pass = fs.depth_func == 0 ? (fz[l] < dep[l]) : (fs.depth_func == 1 ? (fz[l] <= dep[l]) : (fz[l] == dep[l]));
-                            }
-                            mask[l] = inside[l] && pass;
-                            any |= mask[l];
+                    // triangles of the batch in list order; a warp visits only
+                    // those whose box meets its quads (ballot over 32 at a time)
+                    for (int b0 = 0; b0 < n; b0 += 32) {
+                        bool hit = false;
+                        if (b0 + lane < n) {
+                            const int j = b0 + lane;
+                            hit = !(S.maxx[j] <= wx0 || S.minx[j] > wx1 || S.maxy[j] <= wy0 || S.miny[j] > wy1);
                         }
-                        if (!any) continue;
-                        if (fs.depth_write) {
+                        uint32_t m = __ballot_sync(FULL_MASK, hit);
+                        while (m) {
+                            const int i = b0 + __ffs(m) - 1;
+                            m &= m - 1;
+                            if (!active || qx < S.minx[i] || qx >= S.maxx[i] || qy < S.miny[i] || qy >= S.maxy[i]) continue;
+                            const int32_t kx = qx - S.minx[i], ky = qy - S.miny[i];
+                            const int32_t dy12 = S.dy12[i], dx12 = S.dx12[i];
+                            const int32_t dy23 = S.dy23[i], dx23 = S.dx23[i];
+                            const int32_t dy31 = S.dy31[i], dx31 = S.dx31[i];
+                            const int32_t e1 = wadd(wadd(S.c1[i], wmul(kx, dy12)), wmul(ky, dx12));
+                            const int32_t e2 = wadd(wadd(S.c2[i], wmul(kx, dy23)), wmul(ky, dx23));
+                            const int32_t e3 = wadd(wadd(S.c3[i], wmul(kx, dy31)), wmul(ky, dx31));
+                            int32_t l1[4], l2[4], l3[4];
+                            l1[0] = e1; l1[1] = wadd(e1, dy12); l1[2] = wadd(e1, dx12); l1[3] = wadd(wadd(e1, dx12), dy12);
+                            l2[0] = e2; l2[1] = wadd(e2, dy23); l2[2] = wadd(e2, dx23); l2[3] = wadd(wadd(e2, dx23), dy23);
+                            l3[0] = e3; l3[1] = wadd(e3, dy31); l3[2] = wadd(e3, dx31); l3[3] = wadd(wadd(e3, dx31), dy31);
+                            bool inside[4];
+                            bool anyin = false;
 #pragma unroll
-                            for (int l = 0; l < 4; ++l) if (mask[l]) dep[l] = fz[l];
-                        }
-                        const float w0 = S.w[0][i], w1 = S.w[1][i], w2 = S.w[2][i];
-                        float bpx[4], bpy[4], bpz[4];
-#pragma unroll
-                        for (int l = 0; l < 4; ++l) {
-                            const float fragW = oneover(fv.rcp_table, (bx[l] * w0 + by[l] * w1) + bz[l] * w2);
-                            bpx[l] = (w0 * bx[l]) * fragW;
-                            bpz[l] = (w2 * bz[l]) * fragW;
-                            bpy[l] = (1.0f - bpx[l]) - bpz[l];
-                        }
-                        float frag[4][4];
-                        if (fs.program == kProgAmy) {
-                            float uu[4], vv[4];
-                            const float u0 = S.vary[0][0][i], u1 = S.vary[1][0][i], u2 = S.vary[2][0][i];
-                            const float v0 = S.vary[0][1][i], v1 = S.vary[1][1][i], v2 = S.vary[2][1][i];
+                            for (int l = 0; l < 4; ++l) { inside[l] = (l1[l] | l2[l] | l3[l]) >= 0; anyin |= inside[l]; }
+                            if (!anyin) continue;
+                            const float scale = S.scale[i];
+                            const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];
+                            float bx[4], by[4], bz[4], fz[4];
+                            bool mask[4];
+                            bool any = false;
 #pragma unroll
                             for (int l = 0; l < 4; ++l) {
-                                uu[l] = (bpx[l] * u0 + bpy[l] * u1) + bpz[l] * u2;
-                                vv[l] = (bpx[l] * v0 + bpy[l] * v1) + bpz[l] * v2;
+                                bx[l] = itof(l2[l]) * scale;
+                                bz[l] = itof(l1[l]) * scale;
+                                by[l] = (1.0f - bx[l]) - bz[l];
+                                fz[l] = (bx[l] * z0 + by[l] * z1) + bz[l] * z2;
+                                const bool pass = fs.depth_test ? depth_pass(fs.depth_func, fz[l], dep[l]) : true;
+                                mask[l] = inside[l] && pass;
+                                any |= mask[l];
                             }
-                            tex_sample(fs.tu0, uu, vv, frag);
-                        } else {
+                            if (!any) continue;
+                            if (fs.depth_write) {
 #pragma unroll
-                            for (int q = 0; q < 3; ++q) {
-                                const float a0 = S.vary[0][q][i], a1 = S.vary[1][q][i], a2 = S.vary[2][q][i];
-#pragma unroll
-                                for (int l = 0; l < 4; ++l) frag[l][q] = (bpx[l] * a0 + bpy[l] * a1) + bpz[l] * a2;
+                                for (int l = 0; l < 4; ++l) if (mask[l]) dep[l] = fz[l];
                             }
+                            if (!fs.color_write) continue;
+                            if (visibility) {
+                                const uint32_t code = S.code[i];
 #pragma unroll
-                            for (int l = 0; l < 4; ++l) frag[l][3] = 1.0f;
-                        }
-                        if (fs.color_write) {
+                                for (int l = 0; l < 4; ++l) if (mask[l]) own[l] = code;
+                                continue;
+                            }
+                            // immediate shading (blending draws)
+                            const float w0 = S.w[0][i], w1 = S.w[1][i], w2 = S.w[2][i];
+                            float bpx[4], bpy[4], bpz[4];
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) {
+                                const float fragW = oneover(fv.rcp_table, (bx[l] * w0 + by[l] * w1) + bz[l] * w2);
+                                bpx[l] = (w0 * bx[l]) * fragW;
+                                bpz[l] = (w2 * bz[l]) * fragW;
+                                bpy[l] = (1.0f - bpx[l]) - bpz[l];
+                            }
+                            float frag[4][4];
+                            if (fs.program == kProgAmy) {
+                                float uu[4], vv[4];
+                                const float u0 = S.vary[0][0][i], u1 = S.vary[1][0][i], u2 = S.vary[2][0][i];
+                                const float v0 = S.vary[0][1][i], v1 = S.vary[1][1][i], v2 = S.vary[2][1][i];
+#pragma unroll
+                                for (int l = 0; l < 4; ++l) {
+                                    uu[l] = (bpx[l] * u0 + bpy[l] * u1) + bpz[l] * u2;
+                                    vv[l] = (bpx[l] * v0 + bpy[l] * v1) + bpz[l] * v2;
+                                }
+                                tex_sample(fs.tu0, uu, vv, frag);
+                            } else {
+#pragma unroll
+                                for (int q = 0; q < 3; ++q) {
+                                    const float a0 = S.vary[0][q][i], a1 = S.vary[1][q][i], a2 = S.vary[2][q][i];
+#pragma unroll
+                                    for (int l = 0; l < 4; ++l) frag[l][q] = (bpx[l] * a0 + bpy[l] * a1) + bpz[l] * a2;
+                                }
+#pragma unroll
+                                for (int l = 0; l < 4; ++l) frag[l][3] = 1.0f;
+                            }
 #pragma unroll
                             for (int l = 0; l < 4; ++l) {
                                 if (!mask[l]) continue;
-                                if (fs.blend) {   // BlendAlpha (rglv_gpu_impl.hxx:80-84)
-                                    const float a = frag[l][3], oma = 1.0f - a;
+                                // BlendAlpha (rglv_gpu_impl.hxx:80-84)
+                                const float a = frag[l][3], oma = 1.0f - a;
 #pragma unroll
-                                    for (int c = 0; c < 3; ++c) col[l][c] = frag[l][c] * a + col[l][c] * oma;
-                                } else {
-#pragma unroll
-                                    for (int c = 0; c < 3; ++c) col[l][c] = frag[l][c];
-                                }
+                                for (int c = 0; c < 3; ++c) col[l][c] = frag[l][c] * a + col[l][c] * oma;
                             }
                         }
                     }
