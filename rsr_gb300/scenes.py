@@ -87,7 +87,8 @@ class Scene:
     into a GL using ref(name) to obtain the buffer object to point at (the
     numpy array itself, or a device tensor holding a copy of it)."""
 
-    def __init__(self, name, width, height, tile_blocks, arrays, record_fn, ntris):
+    def __init__(self, name, width, height, tile_blocks, arrays, record_fn, ntris, post_program=None):
+        self.post_program = post_program
         self.name = name
         self.width = width
         self.height = height
@@ -102,7 +103,8 @@ class Scene:
         gl = GL()
         ref = ref or (lambda k: self.arrays[k])
         self._record(gl, ref)
-        gl.UseProgram(abi.PROGRAM_DEFAULT_POST)
+        if self.post_program is None:
+            gl.UseProgram(abi.PROGRAM_DEFAULT_POST)
         gl.StoreColor(self.color if color is None else color, self.width, self.height, gamma)
         gl.StoreDepth(self.depth if depth is None else depth)
         return gl
@@ -302,3 +304,78 @@ def clip_stress(seed=3, ntris=3000, width=640, height=360, tile_blocks=(8, 8), e
         gl.DrawElements(nverts, ref("idx"), 0)
 
     return Scene("clip_stress", width, height, tile_blocks, arrays, record, ntris)
+
+
+def mixed_states(seed=13, width=640, height=360, tile_blocks=(4, 4)):
+    """Several draws with different states in one frame: opaque Gouraud with
+    LESS, a textured sphere with alpha blending (texture alpha from noise),
+    Gouraud with LEQUAL, Gouraud with depth writes off, then an exposure
+    post program for the store.  Exercises every ordering rule of the tile
+    interpreter and the switches between them."""
+    n1, n2, n3 = 1500, 800, 600
+    u = uniform01(seed, (n1 + n2 + n3) * 3 * 6).reshape(-1, 3, 6)
+    arrays = {}
+
+    def tri_set(tag, rows, zlo, zhi):
+        pos = np.concatenate([lerp(-1.0, 1.0, rows[:, :, 0:2]), lerp(zlo, zhi, rows[:, :, 2:3])], -1).reshape(-1, 3)
+        rgb = lerp(0.0, 1.0, rows[:, :, 3:6]).reshape(-1, 3)
+        for k, c in enumerate("xyz"):
+            arrays["%s_p%s" % (tag, c)] = pad4(pos[:, k])
+        for k, c in enumerate("rgb"):
+            arrays["%s_c%s" % (tag, c)] = pad4(rgb[:, k])
+        arrays["%s_idx" % tag] = np.arange(len(pos), dtype=np.uint16)
+        return len(pos)
+
+    c1 = tri_set("a", u[:n1], -1.0, 1.0)
+    c3 = tri_set("c", u[n1:n1 + n2], -0.5, 0.5)
+    c4 = tri_set("d", u[n1 + n2:], -1.0, 0.0)
+    verts, faces = icosphere(3)
+    uu = (np.arctan2(verts[:, 2], verts[:, 0]) / (2 * np.pi) + 0.5).astype(np.float32)
+    vv = (np.arcsin(np.clip(verts[:, 1], -1, 1)) / np.pi + 0.5).astype(np.float32)
+    arrays["s_px"], arrays["s_py"], arrays["s_pz"] = (pad4(verts[:, k]) for k in range(3))
+    arrays["s_u"], arrays["s_v"] = pad4(uu), pad4(vv)
+    arrays["s_idx"] = faces.reshape(-1).astype(np.uint16)
+    rgba8 = value_noise_rgba8(seed, 64, cells=(4, 8))
+    alpha = value_noise_rgba8(seed + 1, 64, cells=(4,))[:, :, 0]
+    lin = np.empty((64, 64, 4), np.float32)
+    lin[:, :, :3] = srgb8_to_linear(rgba8[:, :, :3])
+    lin[:, :, 3] = alpha.astype(np.float32) / np.float32(255.0)
+    arrays["tex"] = make_mip_chain(lin)
+    view = look_at((0.0, 0.0, 2.2), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0))
+    proj = perspective(60.0, width / height, 0.1, 100.0)
+    ident = np.eye(4, dtype=np.float32).reshape(16)
+
+    def gouraud(gl, ref, tag, count):
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        gl.UseBuffer(0, (ref(tag + "_px"), ref(tag + "_py"), ref(tag + "_pz")))
+        gl.UseBuffer(3, (ref(tag + "_cr"), ref(tag + "_cg"), ref(tag + "_cb")))
+        gl.DrawElements(count, ref(tag + "_idx"), 0)
+
+    def record(gl, ref):
+        _begin_frame(gl, (0.2, 0.1, 0.05))
+        gouraud(gl, ref, "a", c1)                          # 0x6e2
+        gl.UseProgram(abi.PROGRAM_AMY)                     # 0x6f2: alpha blending
+        gl.Enable(abi.GL_BLEND)
+        gl.Enable(abi.GL_CULL_FACE)
+        gl.ViewMatrix(view)
+        gl.ProjectionMatrix(proj)
+        gl.BindTexture(0, ref("tex"), 64, 64, 64, abi.GL_LINEAR_MIPMAP_NEAREST)
+        gl.UseBuffer(0, (ref("s_px"), ref("s_py"), ref("s_pz")))
+        gl.UseBuffer(9, ref("s_u"))
+        gl.UseBuffer(10, ref("s_v"))
+        gl.DrawElements(len(faces) * 3, ref("s_idx"), abi.RGL_HINT_DENSE | abi.RGL_HINT_READ4)
+        gl.Disable(abi.GL_BLEND)
+        gl.Disable(abi.GL_CULL_FACE)
+        gl.ViewMatrix(ident)
+        gl.ProjectionMatrix(ident)
+        gl.DepthFunc(abi.GL_LEQUAL)                        # 0x6e6
+        gouraud(gl, ref, "c", c3)
+        gl.DepthFunc(abi.GL_LESS)
+        gl.DepthWriteMask(False)                           # 0x6c2
+        gouraud(gl, ref, "d", c4)
+        gl.DepthWriteMask(True)
+        gl.UseProgram(abi.PROGRAM_EXPOSURE_POST)
+        gl.UseUniforms([1.5])
+
+    return Scene("mixed_states", width, height, tile_blocks, arrays, record,
+                 c1 // 3 + len(faces) + c3 // 3 + c4 // 3, post_program=abi.PROGRAM_EXPOSURE_POST)

@@ -32,6 +32,7 @@ GOLDEN_SCENES = {
     "sphere_1080_t32": ("textured_sphere", dict(divs=6), 2),
     "clip_640_t64": ("clip_stress", {}, 3),
     "clip_2160_t32": ("clip_stress", dict(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0), 3),
+    "mixed_640_t32": ("mixed_states", {}, 3),
 }
 
 

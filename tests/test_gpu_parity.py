@@ -25,6 +25,8 @@ SCENES = {
     "sphere_1080_t32": lambda: scenes.textured_sphere(divs=6),
     "clip_640_t64": lambda: scenes.clip_stress(),
     "clip_2160_t32": lambda: scenes.clip_stress(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0),
+    "mixed_640_t32": lambda: scenes.mixed_states(),
+    "mixed_640_t8": lambda: scenes.mixed_states(seed=14, tile_blocks=(1, 1)),
 }
 
 
