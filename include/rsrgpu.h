@@ -64,6 +64,13 @@ extern "C" {
 #define RSRGPU_CMD_STORE_DEPTH_FULL_QUADS_FP  24
 #define RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP 25
 #define RSRGPU_CMD_CLIPPED_TRI                100
+/* Extension of this library (rsr has no deferred path): op u8,
+ * rsrgpu_gbuffer*.  Stores the depth buffer and, for pixels whose visible
+ * fragment comes from RSRGPU_PROGRAM_GBUFFER, its interpolated normal and
+ * albedo; other pixels get normal 0 and albedo 0.  The frame's draws must
+ * all use RSRGPU_PROGRAM_GBUFFER without blending and the store must follow
+ * them with no other store in between. */
+#define RSRGPU_CMD_STORE_GBUFFER              40
 
 /* ---- GL enums (src/rgl/rglv/rglv_gl.hxx:20-62) ---- */
 #define RSRGPU_GL_FRONT            1
@@ -86,6 +93,8 @@ extern "C" {
 #define RSRGPU_PROGRAM_AMY           4   /* AmyProgram (textured), shaders.hxx:69 */
 #define RSRGPU_PROGRAM_OBJ1          7   /* OBJ1Program (lit Gouraud), shaders.hxx:586 */
 #define RSRGPU_PROGRAM_GOURAUD       90  /* test program: per-vertex rgb, no lighting */
+#define RSRGPU_PROGRAM_GBUFFER       91  /* G-buffer program: position 0-2, normal 3-5,
+                                            RGBA8 albedo bits (as float) in 6 */
 
 /* ---- error codes ---- */
 #define RSRGPU_OK            0
@@ -153,6 +162,27 @@ typedef struct rsrgpu_truecolor_canvas {
     int32_t reserved;
 } rsrgpu_truecolor_canvas;
 
+/* G-buffer written by RSRGPU_CMD_STORE_GBUFFER: fp32 NDC depth, the normal
+ * as three fp16 planes (IEEE binary16 bits, round to nearest even), and
+ * RGBA8 albedo (R in the low byte); all row-major width*height. */
+typedef struct rsrgpu_gbuffer {
+    float* depth;
+    uint16_t* normal_x;
+    uint16_t* normal_y;
+    uint16_t* normal_z;
+    uint32_t* albedo;
+    int32_t width;
+    int32_t height;
+} rsrgpu_gbuffer;
+
+/* Point light of the deferred shader. */
+typedef struct rsrgpu_light {
+    float position[3];
+    float radius;
+    float color[3];
+    float reserved;
+} rsrgpu_light;
+
 /* One clipped vertex as stored by the clipper, mirrors rglv::ClippedVertex
  * (rglv_gpu.hxx:38-40): device coordinate + the program's VertexOutputSD. */
 typedef struct rsrgpu_clipped_vertex {
@@ -217,6 +247,19 @@ int rsrgpu_get_stats(rsrgpu_ctx* ctx, rsrgpu_stats* out);
 int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms);
 
 int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
+
+/* ---- deferred shading (extension; no counterpart in rsr) ----
+ * Plain multi-light Blinn-Phong over a G-buffer: for each pixel with albedo
+ * != 0, world position from depth through inv_view_proj (column-major), then
+ * for every light closer than its radius: att = (1 - d/r)^2, diffuse
+ * max(N.L, 0) * albedo, specular max(N.H, 0)^32, summed and packed to sRGB8
+ * (0x00RRGGBB) into out_srgb and/or as linear RGB float triples into
+ * out_linear (either may be NULL).  Pixels with albedo 0 get
+ * `background` (linear RGB).  All pointers are device pointers; the call is
+ * enqueued on `stream`. */
+int rsrgpu_shade_plain(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const float inv_view_proj[16],
+                       const float eye[3], const rsrgpu_light* lights, int nlights,
+                       const float background[3], uint32_t* out_srgb, float* out_linear, void* stream);
 
 /* ---- rendering without any device allocation ----
  * This entry point has no counterpart in the reference.  It is for callers

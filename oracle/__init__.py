@@ -91,6 +91,26 @@ class CpuRenderer:
         self.render_gl(gl, scene.width, scene.height, scene.tile_blocks)
         return scene.color.copy(), scene.depth.copy()
 
+    def render_gbuffer(self, scene):
+        """Renders a scenes.DeferredScene and returns copies of its G-buffer planes."""
+        gl = scene.record()
+        self.render_gl(gl, scene.width, scene.height, scene.tile_blocks)
+        return {k: v.copy() for k, v in scene.gbuf.items()}
+
+    def shade_plain(self, gbuf, width, height, ivp, eye, lights, background=(0.0, 0.0, 0.0)):
+        """The deferred plain shader (oracle restatement); linear RGB float32 (H*W, 3)."""
+        from rsr_gb300 import abi
+        if self.which != "oracle":
+            raise RuntimeError("rsr has no deferred shader; only the oracle implements it")
+        g = abi.GBufferC(gbuf["depth"].ctypes.data, gbuf["nx"].ctypes.data, gbuf["ny"].ctypes.data,
+                         gbuf["nz"].ctypes.data, gbuf["albedo"].ctypes.data, width, height)
+        out = np.zeros((width * height, 3), np.float32)
+        lights = np.ascontiguousarray(lights, np.float32)
+        f16 = lambda a: (ctypes.c_float * len(a))(*[float(x) for x in a])
+        self.lib.rsroracle_shade_plain(ctypes.byref(g), f16(ivp), f16(eye), lights.ctypes.data_as(ctypes.c_void_p),
+                                       len(lights), f16(background), out.ctypes.data_as(ctypes.c_void_p))
+        return out
+
     def tiles(self):
         need = ctypes.c_size_t(0)
         fn = getattr(self.lib, self.prefix + "_dump_tiles")

@@ -108,6 +108,7 @@ static int program_nvary(int pid) {
     switch (pid) {
     case RSRGPU_PROGRAM_GOURAUD: return 3;
     case RSRGPU_PROGRAM_AMY: return 2;
+    case RSRGPU_PROGRAM_GBUFFER: return 4;
     default: return -1;
     }
 }
@@ -127,6 +128,10 @@ static void shade_vertex(const rsrgpu_glstate* s, const float* vpm, int idx, flo
     } else if (s->program_id == RSRGPU_PROGRAM_AMY) {
         vary[0] = s->buffers[9] ? s->buffers[9][idx] : 0.0f;
         vary[1] = s->buffers[10] ? s->buffers[10][idx] : 0.0f;
+    } else if (s->program_id == RSRGPU_PROGRAM_GBUFFER) {
+        /* G-buffer program (this library's extension): interpolated normal, flat packed-RGB albedo */
+        vary[0] = s->buffers[3][idx]; vary[1] = s->buffers[4][idx]; vary[2] = s->buffers[5][idx];
+        vary[3] = s->buffers[6][idx];
     }
 }
 
@@ -418,11 +423,12 @@ static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices,
 /* ClipTriangles (rglv_gpu_impl.hxx:678-793) */
 typedef struct CV { float c[4]; float d[MAX_VARY]; } CV;
 
-static CV cv_mix(const CV* a, const CV* b, float t, int nvary) {  /* CVMix, rmlv::mix (rmlv_math.hxx:87-90) */
+static CV cv_mix(const CV* a, const CV* b, float t, int nvary, int program) {  /* CVMix, rmlv::mix (rmlv_math.hxx:87-90) */
     CV o;
     memset(&o, 0, sizeof(o));
     for (int k = 0; k < 4; ++k) o.c[k] = (1.0f - t) * a->c[k] + t * b->c[k];
     for (int k = 0; k < nvary; ++k) o.d[k] = (1.0f - t) * a->d[k] + t * b->d[k];
+    if (program == RSRGPU_PROGRAM_GBUFFER) o.d[3] = a->d[3];   /* flat albedo */
     return o;
 }
 
@@ -455,7 +461,7 @@ static int clip_triangles(Frame* f, const rsrgpu_glstate* s, const ClipEntry* q,
                     const CV* from = hereIsInside ? &A[h] : &A[n];
                     const CV* to = hereIsInside ? &A[n] : &A[h];
                     float d = plane_distance(plane, from->c, to->c);
-                    B[nb++] = cv_mix(from, to, d, nvary);
+                    B[nb++] = cv_mix(from, to, d, nvary, s->program_id);
                     hereIsInside = !hereIsInside;
                 }
             }
@@ -547,7 +553,8 @@ static int bin_frame(Frame* f, const uint8_t* cmds, size_t n) {
             RD(uint64_t, ptr);
             for (int t = 0; t < f->ntiles; ++t) { bb_u8(&f->tiles[t], op); bb_u8(&f->tiles[t], gamma); bb_u64(&f->tiles[t], ptr); }
         } break;
-        case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: {
+        case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP:
+        case RSRGPU_CMD_STORE_GBUFFER: {
             RD(uint64_t, ptr);
             for (int t = 0; t < f->ntiles; ++t) { bb_u8(&f->tiles[t], op); bb_u64(&f->tiles[t], ptr); }
         } break;
@@ -581,6 +588,7 @@ typedef struct TileCtx {
     int rect[4];                 /* left, top, right, bottom */
     float* color;                /* tile-local rgba, row-major, tile_w*tile_h */
     float* depth;
+    uint8_t* gbflag;             /* pixel's colour written by the G-buffer program */
     const rsrgpu_glstate* s;
     float vpm[16];
     float DS[2], DO[2];
@@ -604,6 +612,7 @@ static uint32_t fragment_state_key(const rsrgpu_glstate* s) {  /* rglv_gl.hxx:13
 }
 static int draw_dispatch_ok(const rsrgpu_glstate* s) {
     if (program_nvary(s->program_id) < 0) return 0;
+    if (s->program_id == RSRGPU_PROGRAM_GBUFFER && s->blending_enabled) return 0;
     uint32_t k = fragment_state_key(s) & 0xffffffu;
     return k == 0x6e2 || k == 0x6e6 || k == 0x6f2 || k == 0x6c2 || k == 0x62 || k == 0x72;
 }
@@ -656,6 +665,9 @@ static void render_quad(TileCtx* tc, const TriSetup* tri, int qx, int qy, const 
         float uv[4][2];
         for (int l = 0; l < 4; ++l) { uv[l][0] = attr[l][0]; uv[l][1] = attr[l][1]; }
         tex_sample(&tc->tu0, uv, frag);
+    } else if (s->program_id == RSRGPU_PROGRAM_GBUFFER) {
+        /* colour = interpolated normal, alpha = flat albedo of the record's first vertex */
+        for (int l = 0; l < 4; ++l) { frag[l][0] = attr[l][0]; frag[l][1] = attr[l][1]; frag[l][2] = attr[l][2]; frag[l][3] = tri->vary[0][3]; }
     } else {
         for (int l = 0; l < 4; ++l) { frag[l][0] = attr[l][0]; frag[l][1] = attr[l][1]; frag[l][2] = attr[l][2]; frag[l][3] = 1.0f; }
     }
@@ -669,6 +681,8 @@ static void render_quad(TileCtx* tc, const TriSetup* tri, int qx, int qy, const 
             } else {
                 for (int c = 0; c < 3; ++c) dst[c] = frag[l][c];
             }
+            if (s->program_id == RSRGPU_PROGRAM_GBUFFER) { dst[3] = frag[l][3]; tc->gbflag[ly[l] * tw + lx[l]] = 1; }
+            else tc->gbflag[ly[l] * tw + lx[l]] = 0;
         }
     }
 }
@@ -815,6 +829,44 @@ static const uint8_t* draw_clipped(TileCtx* tc, const uint8_t* p) {
     return p;
 }
 
+/* IEEE binary32 -> binary16, round to nearest even (finite inputs) */
+static uint16_t f32_to_f16(float f) {
+    const uint32_t x = f2u(f);
+    const uint16_t sign = (uint16_t)((x >> 16) & 0x8000u);
+    const uint32_t e = (x >> 23) & 255u;
+    uint32_t m = x & 0x7fffffu;
+    if (e == 255u) return (uint16_t)(sign | 0x7c00u | (m ? 0x200u : 0u));
+    const int exp = (int)e - 127 + 15;
+    if (exp >= 31) return (uint16_t)(sign | 0x7c00u);
+    if (exp <= 0) {
+        if (exp < -10) return sign;
+        m |= 0x800000u;
+        const int shift = 14 - exp;
+        uint32_t hm = m >> shift;
+        const uint32_t rem = m & ((1u << shift) - 1u), halfway = 1u << (shift - 1);
+        if (rem > halfway || (rem == halfway && (hm & 1u))) ++hm;
+        return (uint16_t)(sign | hm);
+    }
+    uint32_t h = ((uint32_t)exp << 10) | (m >> 13);
+    const uint32_t rem = m & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+    return (uint16_t)(sign | h);
+}
+
+static float f16_to_f32(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    uint32_t e = (h >> 10) & 31u, m = h & 0x3ffu;
+    if (e == 0) {
+        if (m == 0) return u2f(sign);
+        int k = 0;
+        while (!(m & 0x400u)) { m <<= 1; ++k; }
+        m &= 0x3ffu;
+        return u2f(sign | ((uint32_t)(113 - k) << 23) | (m << 13));
+    }
+    if (e == 31) return u2f(sign | 0x7f800000u | (m << 13));
+    return u2f(sign | ((e + 112u) << 23) | (m << 13));
+}
+
 static uint8_t srgb8(const uint8_t* lut, float v) {
     /* float_to_srgb8_var2_SSE2 (ryg-srgb.h:183-219) reproduced through the
        golden output table: clamp with maxps/minps then index by bits >> 12 */
@@ -825,10 +877,11 @@ static int32_t basic8(float v) {   /* to_tc_basic (rglr_canvas_util.hxx:22-31) *
     return ftoi(sse_max(sse_min(v, 1.0f), 0.0f) * 255.0f);
 }
 
-static int draw_tile(const Frame* f, int tile, float* color, float* depth) {
+static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8_t* gbflag) {
     TileCtx tc;
     memset(&tc, 0, sizeof(tc));
     tc.f = f;
+    tc.gbflag = gbflag;
     const int tx = tile % f->tiles_x, ty = tile / f->tiles_x;
     tc.rect[0] = tx * f->tile_w; tc.rect[1] = ty * f->tile_h;
     tc.rect[2] = imin(tc.rect[0] + f->tile_w, f->width);
@@ -858,9 +911,9 @@ static int draw_tile(const Frame* f, int tile, float* color, float* depth) {
             const rsrgpu_glstate* s = tc.s;
             if (s->color0_attachment_type == RSRGPU_RB_COLOR_DEPTH) {
                 if (bits != (RSRGPU_GL_COLOR_BUFFER_BIT | RSRGPU_GL_DEPTH_BUFFER_BIT)) return RSRGPU_EINVAL;
-                for (int i = 0; i < n; ++i) { memcpy(&color[i * 4], s->clear_color, 12); color[i * 4 + 3] = s->clear_depth; depth[i] = s->clear_depth; }
+                for (int i = 0; i < n; ++i) { memcpy(&color[i * 4], s->clear_color, 12); color[i * 4 + 3] = s->clear_depth; depth[i] = s->clear_depth; gbflag[i] = 0; }
             } else {
-                if (bits & RSRGPU_GL_COLOR_BUFFER_BIT) for (int i = 0; i < n; ++i) memcpy(&color[i * 4], s->clear_color, 16);
+                if (bits & RSRGPU_GL_COLOR_BUFFER_BIT) for (int i = 0; i < n; ++i) { memcpy(&color[i * 4], s->clear_color, 16); gbflag[i] = 0; }
                 if (bits & RSRGPU_GL_DEPTH_BUFFER_BIT) for (int i = 0; i < n; ++i) depth[i] = s->clear_depth;
             }
         } break;
@@ -895,6 +948,27 @@ static int draw_tile(const Frame* f, int tile, float* color, float* depth) {
                 }
             }
         } break;
+        case RSRGPU_CMD_STORE_GBUFFER: {
+            uint64_t gp;
+            memcpy(&gp, p, 8); p += 8;
+            const rsrgpu_gbuffer* gb = (const rsrgpu_gbuffer*)(uintptr_t)gp;
+            for (int y = tc.rect[1]; y < tc.rect[3]; ++y) {
+                for (int x = tc.rect[0]; x < tc.rect[2]; ++x) {
+                    const int li = (y - tc.rect[1]) * f->tile_w + (x - tc.rect[0]);
+                    const size_t o = (size_t)y * f->width + x;
+                    gb->depth[o] = depth[li];
+                    if (gbflag[li]) {
+                        gb->normal_x[o] = f32_to_f16(color[li * 4 + 0]);
+                        gb->normal_y[o] = f32_to_f16(color[li * 4 + 1]);
+                        gb->normal_z[o] = f32_to_f16(color[li * 4 + 2]);
+                        gb->albedo[o] = (uint32_t)color[li * 4 + 3] | 0xff000000u;
+                    } else {
+                        gb->normal_x[o] = gb->normal_y[o] = gb->normal_z[o] = 0;
+                        gb->albedo[o] = 0;
+                    }
+                }
+            }
+        } break;
         case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: {
             uint64_t dp;
             memcpy(&dp, p, 8); p += 8;
@@ -923,15 +997,16 @@ static void* tile_worker(void* arg) {
     const Frame* f = pool->f;
     float* color = (float*)malloc(sizeof(float) * 4 * (size_t)f->tile_w * (size_t)f->tile_h);
     float* depth = (float*)malloc(sizeof(float) * (size_t)f->tile_w * (size_t)f->tile_h);
+    uint8_t* gbflag = (uint8_t*)calloc((size_t)f->tile_w * (size_t)f->tile_h, 1);
     while (1) {
         pthread_mutex_lock(&pool->mu);
         int t = pool->next++;
         pthread_mutex_unlock(&pool->mu);
         if (t >= f->ntiles) break;
-        int rc = draw_tile(f, t, color, depth);
+        int rc = draw_tile(f, t, color, depth, gbflag);
         if (rc) { pthread_mutex_lock(&pool->mu); pool->rc = rc; pthread_mutex_unlock(&pool->mu); }
     }
-    free(color); free(depth);
+    free(color); free(depth); free(gbflag);
     return NULL;
 }
 
@@ -1016,6 +1091,7 @@ int rsroracle_dump_tiles(uint8_t* out, size_t capacity, size_t* needed) {
             case RSRGPU_CMD_CLEAR: bb_u8(&one, *p++); break;
             case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC: bb_u8(&one, *p++); p += 8; break;
             case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: p += 8; break;
+            case RSRGPU_CMD_STORE_GBUFFER: p += 8; break;
             case RSRGPU_CMD_DRAW_INLINE:
                 while (1) {
                     uint16_t w; p = rd_u16(p, &w); bb_u16(&one, w);
@@ -1089,5 +1165,94 @@ int rsroracle_kat_top_left(const float pts[6], int w, int h, uint8_t* mask) {
             }
         }
     }
+    return 0;
+}
+
+
+/* ======================================================================
+ * deferred plain shading (this library's extension; no rsr counterpart)
+ * Same definition and operation order as shade_plain_kernel in
+ * rsr_gb300/csrc/rsrgpu_deferred.cu.
+ * ====================================================================== */
+static float dot3(float ax, float ay, float az, float bx, float by, float bz) { return (ax * bx + ay * by) + az * bz; }
+static float pos0(float x) { return x > 0.0f ? x : 0.0f; }
+
+typedef struct PlainJob {
+    const rsrgpu_gbuffer* gb;
+    const float* ivp; const float* eye; const rsrgpu_light* lights; int nlights;
+    const float* bg; float* out_linear; int next; pthread_mutex_t mu;
+} PlainJob;
+
+static void plain_row(const PlainJob* j, int y) {
+    const rsrgpu_gbuffer* g = j->gb;
+    const float* m = j->ivp;
+    for (int x = 0; x < g->width; ++x) {
+        const size_t i = (size_t)y * g->width + x;
+        float* o = j->out_linear + 3 * i;
+        const uint32_t alb = g->albedo[i];
+        if (alb == 0) { o[0] = j->bg[0]; o[1] = j->bg[1]; o[2] = j->bg[2]; continue; }
+        const float z = g->depth[i];
+        const float ndcx = (2.0f * ((float)x + 0.5f)) / (float)g->width - 1.0f;
+        const float ndcy = 1.0f - (2.0f * ((float)y + 0.5f)) / (float)g->height;
+        const float cx = ((m[0] * ndcx + m[4] * ndcy) + m[8] * z) + m[12];
+        const float cy = ((m[1] * ndcx + m[5] * ndcy) + m[9] * z) + m[13];
+        const float cz = ((m[2] * ndcx + m[6] * ndcy) + m[10] * z) + m[14];
+        const float cw = ((m[3] * ndcx + m[7] * ndcy) + m[11] * z) + m[15];
+        const float px = cx / cw, py = cy / cw, pz = cz / cw;
+        float nx = f16_to_f32(g->normal_x[i]), ny = f16_to_f32(g->normal_y[i]), nz = f16_to_f32(g->normal_z[i]);
+        const float nlen = sqrtf(dot3(nx, ny, nz, nx, ny, nz));
+        nx = nx / nlen; ny = ny / nlen; nz = nz / nlen;
+        float vx = j->eye[0] - px, vy = j->eye[1] - py, vz = j->eye[2] - pz;
+        const float vlen = sqrtf(dot3(vx, vy, vz, vx, vy, vz));
+        vx = vx / vlen; vy = vy / vlen; vz = vz / vlen;
+        const float ar = (float)(alb & 255u) / 255.0f, ag = (float)((alb >> 8) & 255u) / 255.0f, ab = (float)((alb >> 16) & 255u) / 255.0f;
+        float sr = 0.0f, sg = 0.0f, sb = 0.0f;
+        for (int k = 0; k < j->nlights; ++k) {
+            const rsrgpu_light* L = &j->lights[k];
+            float lx = L->position[0] - px, ly = L->position[1] - py, lz = L->position[2] - pz;
+            const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
+            if (!(d < L->radius)) continue;
+            lx = lx / d; ly = ly / d; lz = lz / d;
+            const float t = 1.0f - d / L->radius;
+            const float att = t * t;
+            const float ndl = pos0(dot3(nx, ny, nz, lx, ly, lz));
+            float hx = lx + vx, hy = ly + vy, hz = lz + vz;
+            const float hlen = sqrtf(dot3(hx, hy, hz, hx, hy, hz));
+            hx = hx / hlen; hy = hy / hlen; hz = hz / hlen;
+            float sp = pos0(dot3(nx, ny, nz, hx, hy, hz));
+            sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;
+            sr = sr + (L->color[0] * att) * (ar * ndl + sp);
+            sg = sg + (L->color[1] * att) * (ag * ndl + sp);
+            sb = sb + (L->color[2] * att) * (ab * ndl + sp);
+        }
+        o[0] = sr + 0.03f * ar; o[1] = sg + 0.03f * ag; o[2] = sb + 0.03f * ab;
+    }
+}
+
+static void* plain_worker(void* arg) {
+    PlainJob* j = (PlainJob*)arg;
+    while (1) {
+        pthread_mutex_lock(&j->mu);
+        int y = j->next++;
+        pthread_mutex_unlock(&j->mu);
+        if (y >= j->gb->height) break;
+        plain_row(j, y);
+    }
+    return NULL;
+}
+
+int rsroracle_shade_plain(const rsrgpu_gbuffer* gb, const float ivp[16], const float eye[3],
+                          const rsrgpu_light* lights, int nlights, const float background[3], float* out_linear) {
+    PlainJob j;
+    j.gb = gb; j.ivp = ivp; j.eye = eye; j.lights = lights; j.nlights = nlights; j.bg = background;
+    j.out_linear = out_linear; j.next = 0;
+    pthread_mutex_init(&j.mu, NULL);
+    int nt = g_session.threads;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
+    for (int i = 1; i < nt; ++i) pthread_create(&th[i], NULL, plain_worker, &j);
+    plain_worker(&j);
+    for (int i = 1; i < nt; ++i) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&j.mu);
     return 0;
 }

@@ -20,6 +20,7 @@ CMD_DRAW_INLINE = 15
 CMD_STORE_COLOR_FULL_LINEAR_TC = 22
 CMD_STORE_DEPTH_FULL_LINEAR_FP = 25
 CMD_CLIPPED_TRI = 100
+CMD_STORE_GBUFFER = 40
 
 # GL enums (src/rgl/rglv/rglv_gl.hxx:20-62)
 GL_CULL_FACE = 1
@@ -49,6 +50,7 @@ PROGRAM_EXPOSURE_POST = 2
 PROGRAM_AMY = 4
 PROGRAM_OBJ1 = 7
 PROGRAM_GOURAUD = 90
+PROGRAM_GBUFFER = 91
 
 KIND_BIN, KIND_DRAW, KIND_BLT = 0, 1, 2
 
@@ -106,6 +108,17 @@ class ClippedVertexC(ctypes.Structure):
     _fields_ = [("coord", ctypes.c_float * 4), ("data", ctypes.c_float * 16)]
 
 
+class GBufferC(ctypes.Structure):
+    _fields_ = [("depth", ctypes.c_void_p), ("normal_x", ctypes.c_void_p), ("normal_y", ctypes.c_void_p),
+                ("normal_z", ctypes.c_void_p), ("albedo", ctypes.c_void_p), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32)]
+
+
+class LightC(ctypes.Structure):
+    _fields_ = [("position", ctypes.c_float * 3), ("radius", ctypes.c_float),
+                ("color", ctypes.c_float * 3), ("reserved", ctypes.c_float)]
+
+
 class StatsC(ctypes.Structure):
     _fields_ = [("total_tiles", ctypes.c_int64),
                 ("total_tile_records", ctypes.c_int64),
@@ -133,6 +146,10 @@ SYMBOLS = {
     "rsrgpu_get_stats": ([ctypes.c_void_p, ctypes.POINTER(StatsC)], ctypes.c_int),
     "rsrgpu_last_timings": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
     "rsrgpu_last_error": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "rsrgpu_shade_plain": ([ctypes.c_void_p, ctypes.POINTER(GBufferC), ctypes.POINTER(ctypes.c_float),
+                            ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+                           ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

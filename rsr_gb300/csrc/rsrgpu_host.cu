@@ -29,6 +29,9 @@ namespace rsrgpu {
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
+                               const rsrgpu_light* lights, int nlights, const float background[3],
+                               uint32_t* out_srgb, float* out_linear, const uint8_t* srgb_lut, cudaStream_t st);
 
 static const uint32_t kRcpTable[2048] = {
 #include "rcpps_table.inc"
@@ -81,12 +84,13 @@ struct rsrgpu_ctx {
     std::vector<int32_t> state_ordinal;
     std::vector<DevDraw> draws;
     std::vector<FrameOp> ops;
+    std::vector<GBufferDesc> gbufs;
     int ntris = 0;
     bool submitted = false;
     bool ran = false;
     // device memory
     DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
-        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb;
+        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs;
     uint32_t clip_cap = 1u << 18;
     uint32_t bin_cap = 1u << 22;
     FrameCounters* h_counters = nullptr;   // pinned
@@ -142,7 +146,7 @@ uint32_t fragment_state_key(const rsrgpu_glstate& s) {   // GLState::FragmentSta
     return key;
 }
 
-bool draw_program_supported(int pid) { return pid == kProgGouraud || pid == kProgAmy; }
+bool draw_program_supported(int pid) { return pid == kProgGouraud || pid == kProgAmy || pid == kProgGBuffer; }
 bool blt_program_supported(int pid) { return pid == kProgDefaultPost || pid == kProgExposurePost || pid == kProgGouraud; }
 
 // the fragment state keys this device implementation covers: no scissor, depth
@@ -250,7 +254,7 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
         d.scissor[0] = left; d.scissor[1] = top; d.scissor[2] = right; d.scissor[3] = bottom;
     }
     d.program = s.program_id;
-    d.nvary = s.program_id == kProgGouraud ? 3 : (s.program_id == kProgAmy ? 2 : 0);
+    d.nvary = s.program_id == kProgGouraud ? 3 : (s.program_id == kProgAmy ? 2 : (s.program_id == kProgGBuffer ? 4 : 0));
     d.keep_backs = !(s.culling_enabled && s.cull_face == RSRGPU_GL_BACK);
     d.keep_fronts = !(s.culling_enabled && s.cull_face == RSRGPU_GL_FRONT);
     d.cull_enabled = s.culling_enabled != 0;
@@ -334,7 +338,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     if (ctx == nullptr) return 0;
     if (ctx->own) cudaStreamSynchronize(ctx->own);
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
-    DevBuf* bufs[] = { &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -428,7 +432,9 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
     ctx->state_ordinal.assign(size_t(nstates), -1);
     ctx->draws.clear();
     ctx->ops.clear();
+    ctx->gbufs.clear();
     ctx->ntris = 0;
+    bool gbuffer_frame = false, other_op_since_draw = false, any_draw = false;
     ctx->submitted = false;
     std::vector<bool> decoded(size_t(nstates), false);
     int ordinals = 0;
@@ -467,6 +473,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             fo.kind = kOpClear;
             fo.arg = bits;
             ctx->ops.push_back(fo);
+            other_op_since_draw = true;
         } break;
         case RSRGPU_CMD_DRAW_ELEMENTS:
         case RSRGPU_CMD_DRAW_ARRAYS: {
@@ -491,6 +498,12 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             if (count < 0) return fail(ctx, RSRGPU_EINVAL, "negative draw count");
             if (s.program_id == kProgGouraud && (!s.buffers[0] || !s.buffers[3] || !s.buffers[4] || !s.buffers[5]))
                 return fail(ctx, RSRGPU_EINVAL, "Gouraud program needs buffers 0-5");
+            if (s.program_id == kProgGBuffer && (!s.buffers[0] || !s.buffers[3] || !s.buffers[4] || !s.buffers[5] || !s.buffers[6]))
+                return fail(ctx, RSRGPU_EINVAL, "G-buffer program needs buffers 0-6");
+            if (s.program_id == kProgGBuffer && s.blending_enabled)
+                return fail(ctx, RSRGPU_EUNSUPPORTED, "the G-buffer program does not blend");
+            any_draw = true;
+            other_op_since_draw = false;
             DevDraw dd{};
             dd.state = cur;
             dd.first_tri = ctx->ntris;
@@ -531,6 +544,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             if (dp == nullptr || avail < size_t(cv->stride) * size_t(cv->height) * 4u)
                 return fail(ctx, RSRGPU_EINVAL, "color output holds %zu bytes, needs %zu", avail, size_t(cv->stride) * size_t(cv->height) * 4u);
             if (reinterpret_cast<uintptr_t>(dp) & 7) return fail(ctx, RSRGPU_EINVAL, "color output must be 8-byte aligned");
+            other_op_since_draw = true;
             fo.kind = kOpStoreTC;
             fo.arg = gamma ? 1 : 0;
             fo.ptr = dp;
@@ -550,14 +564,53 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             if (dp == nullptr || avail < size_t(ctx->width) * size_t(ctx->height) * 4u)
                 return fail(ctx, RSRGPU_EINVAL, "depth output holds %zu bytes, needs %zu", avail, size_t(ctx->width) * size_t(ctx->height) * 4u);
             if (reinterpret_cast<uintptr_t>(dp) & 7) return fail(ctx, RSRGPU_EINVAL, "depth output must be 8-byte aligned");
+            other_op_since_draw = true;
             fo.kind = kOpStoreDepth;
             fo.ptr = dp;
             fo.width = ctx->width; fo.height = ctx->height; fo.stride = ctx->width;
             ctx->ops.push_back(fo);
         } break;
+        case RSRGPU_CMD_STORE_GBUFFER: {
+            uint64_t gp;
+            if (!rd(p, end, gp)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_STORE_GBUFFER");
+            if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "store before any state");
+            if (other_op_since_draw && any_draw)
+                return fail(ctx, RSRGPU_EINVAL, "CMD_STORE_GBUFFER must directly follow the G-buffer draws");
+            const auto* g = reinterpret_cast<const rsrgpu_gbuffer*>(uintptr_t(gp));
+            if (g == nullptr || g->width != ctx->width || g->height != ctx->height)
+                return fail(ctx, RSRGPU_EINVAL, "G-buffer must match the %dx%d target", ctx->width, ctx->height);
+            const size_t npx = size_t(ctx->width) * size_t(ctx->height);
+            GBufferDesc gd{};
+            void* dp = nullptr;
+            size_t avail = 0;
+            const void* srcs[5] = { g->depth, g->normal_x, g->normal_y, g->normal_z, g->albedo };
+            const size_t need[5] = { npx * 4, npx * 2, npx * 2, npx * 2, npx * 4 };
+            void** dsts[5] = { reinterpret_cast<void**>(&gd.depth), reinterpret_cast<void**>(&gd.nx),
+                               reinterpret_cast<void**>(&gd.ny), reinterpret_cast<void**>(&gd.nz),
+                               reinterpret_cast<void**>(&gd.albedo) };
+            for (int k = 0; k < 5; ++k) {
+                int rc = resolve(ctx, srcs[k], true, &dp, "G-buffer", &avail);
+                if (rc) return rc;
+                if (dp == nullptr || avail < need[k] || (reinterpret_cast<uintptr_t>(dp) & 7))
+                    return fail(ctx, RSRGPU_EINVAL, "G-buffer plane %d: need %zu bytes, 8-byte aligned", k, need[k]);
+                *dsts[k] = dp;
+            }
+            gbuffer_frame = true;
+            other_op_since_draw = true;
+            fo.kind = kOpStoreGBuffer;
+            fo.arg = int(ctx->gbufs.size());
+            fo.width = ctx->width; fo.height = ctx->height; fo.stride = ctx->width;
+            ctx->gbufs.push_back(gd);
+            ctx->ops.push_back(fo);
+        } break;
         default:
             return fail(ctx, RSRGPU_EUNSUPPORTED, "command 0x%02x is not supported", op);
         }
+    }
+    if (gbuffer_frame) {
+        for (const DevDraw& d : ctx->draws)
+            if (ctx->states[size_t(d.state)].program != kProgGBuffer)
+                return fail(ctx, RSRGPU_EINVAL, "a frame with CMD_STORE_GBUFFER draws only with the G-buffer program");
     }
     if (nstates == 0) ctx->states.assign(1, DevState{});
     ctx->submitted = true;
@@ -587,6 +640,7 @@ int prepare_view(rsrgpu_ctx* ctx) {
     CK(ctx->d_bins.ensure(sizeof(TileBin) * size_t(ctx->ntiles)), "alloc bins");
     CK(ctx->d_pool.ensure(sizeof(uint32_t) * size_t(ctx->bin_cap)), "alloc bin pool");
     CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
+    CK(ctx->d_gbufs.ensure(sizeof(GBufferDesc) * std::max<size_t>(ctx->gbufs.size(), 1)), "alloc gbuffer table");
     FrameView& fv = ctx->fv;
     fv.states = ctx->d_states.as<DevState>();
     fv.draws = ctx->d_draws.as<DevDraw>();
@@ -594,6 +648,7 @@ int prepare_view(rsrgpu_ctx* ctx) {
     fv.ntris = ntris;
     fv.ops = ctx->d_ops.as<FrameOp>();
     fv.nops = int(ctx->ops.size());
+    fv.gbufs = ctx->d_gbufs.as<GBufferDesc>();
     fv.width = ctx->width; fv.height = ctx->height;
     fv.tile_w = ctx->tile_w; fv.tile_h = ctx->tile_h;
     fv.tiles_x = ctx->tiles_x; fv.tiles_y = ctx->tiles_y; fv.ntiles = ctx->ntiles;
@@ -630,6 +685,8 @@ int enqueue(rsrgpu_ctx* ctx, cudaStream_t st) {
         CK(cudaMemcpyAsync(ctx->d_draws.p, ctx->draws.data(), sizeof(DevDraw) * ctx->draws.size(), cudaMemcpyHostToDevice, st), "H2D draws");
     if (!ctx->ops.empty())
         CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
+    if (!ctx->gbufs.empty())
+        CK(cudaMemcpyAsync(ctx->d_gbufs.p, ctx->gbufs.data(), sizeof(GBufferDesc) * ctx->gbufs.size(), cudaMemcpyHostToDevice, st), "H2D gbuffers");
     CK(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(FrameCounters), st), "memset counters");
     if (fv.nsupers > 0) CK(cudaMemsetAsync(ctx->d_super.p, 0x7f, sizeof(int4) * size_t(fv.nsupers), st), "memset super rects");
     CK(cudaEventRecord(ctx->ev0, st), "event");
@@ -744,6 +801,7 @@ int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* ne
             else if (o.kind == kOpClear) { put8(one, RSRGPU_CMD_CLEAR); put8(one, uint8_t(o.arg)); }
             else if (o.kind == kOpStoreTC) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC); put8(one, uint8_t(o.arg)); }
             else if (o.kind == kOpStoreDepth) { put8(one, RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP); }
+            else if (o.kind == kOpStoreGBuffer) { put8(one, RSRGPU_CMD_STORE_GBUFFER); }
             else if (o.kind == kOpDraw) {
                 const DevDraw& d = ctx->draws[size_t(o.arg)];
                 const uint32_t endg = uint32_t(d.first_tri + d.ntris);
@@ -811,6 +869,40 @@ int rsrgpu_dump_clipped(rsrgpu_ctx* ctx, rsrgpu_clipped_vertex* out, int capacit
     return 0;
 }
 
+int rsrgpu_shade_plain(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const float inv_view_proj[16],
+                       const float eye[3], const rsrgpu_light* lights, int nlights,
+                       const float background[3], uint32_t* out_srgb, float* out_linear, void* stream) {
+    if (ctx == nullptr || gbuffer == nullptr || inv_view_proj == nullptr || eye == nullptr || background == nullptr)
+        return RSRGPU_EINVAL;
+    if (nlights < 0 || nlights > 256) return fail(ctx, RSRGPU_EINVAL, "1..256 lights");
+    if (gbuffer->width <= 0 || gbuffer->height <= 0) return fail(ctx, RSRGPU_EINVAL, "empty G-buffer");
+    const size_t npx = size_t(gbuffer->width) * size_t(gbuffer->height);
+    const void* ins[6] = { gbuffer->depth, gbuffer->normal_x, gbuffer->normal_y, gbuffer->normal_z, gbuffer->albedo, lights };
+    const size_t need[6] = { npx * 4, npx * 2, npx * 2, npx * 2, npx * 4, size_t(nlights) * sizeof(rsrgpu_light) };
+    rsrgpu_gbuffer g = *gbuffer;
+    void* dp = nullptr;
+    size_t avail = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (need[k] == 0) continue;
+        int rc = resolve(ctx, ins[k], false, &dp, "deferred input", &avail);
+        if (rc) return rc;
+        if (dp == nullptr || avail < need[k]) return fail(ctx, RSRGPU_EINVAL, "deferred input %d holds %zu bytes, needs %zu", k, avail, need[k]);
+        if (dp != ins[k]) return fail(ctx, RSRGPU_EINVAL, "rsrgpu_shade_plain takes device pointers");
+    }
+    const void* outs[2] = { out_srgb, out_linear };
+    const size_t oneed[2] = { npx * 4, npx * 12 };
+    for (int k = 0; k < 2; ++k) {
+        if (outs[k] == nullptr) continue;
+        int rc = resolve(ctx, outs[k], true, &dp, "deferred output", &avail);
+        if (rc) return rc;
+        if (dp != outs[k] || avail < oneed[k]) return fail(ctx, RSRGPU_EINVAL, "deferred output %d: device pointer with %zu bytes needed", k, oneed[k]);
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_shade_plain(g, inv_view_proj, eye, lights, nlights, background, out_srgb, out_linear,
+                          ctx->d_srgb.as<uint8_t>(), st), "shade_plain_kernel");
+    return 0;
+}
+
 int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len) {
     if (ctx == nullptr || buf == nullptr || len == 0) return RSRGPU_EINVAL;
     std::snprintf(buf, len, "%s", ctx->err.c_str());
@@ -846,6 +938,10 @@ int decode_frame_without_context(int width, int height, int tile_blocks_x, int t
     if (rc != 0) {
         err = tmp.err;
         return rc;
+    }
+    if (!tmp.gbufs.empty()) {
+        err = "CMD_STORE_GBUFFER is not available without a context";
+        return RSRGPU_EUNSUPPORTED;
     }
     out_states = std::move(tmp.states);
     out_draws = std::move(tmp.draws);

@@ -33,6 +33,7 @@ enum ProgramId : int32_t {
     kProgAmy = 4,
     kProgOBJ1 = 7,
     kProgGouraud = 90,
+    kProgGBuffer = 91,
 };
 
 struct DevTexture {
@@ -70,7 +71,16 @@ struct DevDraw {
     const uint16_t* indices;
 };
 
-enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4 };
+enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4, kOpStoreGBuffer = 5 };
+
+// device addresses of one G-buffer target (RSRGPU_CMD_STORE_GBUFFER)
+struct GBufferDesc {
+    float* depth;
+    uint16_t* nx;
+    uint16_t* ny;
+    uint16_t* nz;
+    uint32_t* albedo;
+};
 
 struct FrameOp {
     int32_t kind;
@@ -119,6 +129,7 @@ struct FrameView {
     int32_t ntris;
     const FrameOp* ops;
     int32_t nops;
+    const GBufferDesc* gbufs;
     int32_t width, height;
     int32_t tile_w, tile_h, tiles_x, tiles_y, ntiles;
     int32_t nchunks, nsupers;

@@ -24,6 +24,7 @@
 // separate multiply and add roundings and its evaluation order.
 #include <cstdint>
 #include <climits>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "rsrgpu_internal.h"
@@ -103,6 +104,12 @@ __device__ __forceinline__ void shade_vertex(const DevState& s, int idx, float p
     } else if (s.program == kProgAmy) {
         vary[0] = s.buffers[9] ? fetch(s, 9, idx, ctr) : 0.f;
         vary[1] = s.buffers[10] ? fetch(s, 10, idx, ctr) : 0.f;
+    } else if (s.program == kProgGBuffer) {
+        // normal (interpolated) and the packed RGB albedo (flat)
+        vary[0] = fetch(s, 3, idx, ctr);
+        vary[1] = fetch(s, 4, idx, ctr);
+        vary[2] = fetch(s, 5, idx, ctr);
+        vary[3] = fetch(s, 6, idx, ctr);
     }
 }
 
@@ -200,6 +207,7 @@ __device__ __noinline__ void clip_triangle(const FrameView& fv, const DevState& 
                 CV o;
                 for (int k = 0; k < 4; ++k) o.c[k] = (1.0f - d) * from.c[k] + d * to.c[k];
                 for (int k = 0; k < kMaxVary; ++k) o.d[k] = k < nv ? (1.0f - d) * from.d[k] + d * to.d[k] : 0.f;
+                if (s.program == kProgGBuffer) o.d[3] = from.d[3];   // the albedo is flat
                 if (nb <= kMaxClipVerts) B[nb++] = o;
                 hereIsInside = !hereIsInside;
             }
@@ -831,7 +839,7 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
         // that fragment's owner and shade it once; anything that reads or
         // replaces colour first resolves the pending pixels.
         const bool visibility = o.kind == kOpDraw && !fs.blend;
-        if (!visibility && pending) {
+        if (!visibility && o.kind != kOpStoreGBuffer && pending) {
             if (active) resolve_quad(fv, rect, qx, qy, own, col);
             pending = false;
         }
@@ -1017,6 +1025,40 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
                 uint32_t* dst = static_cast<uint32_t*>(o.ptr);
                 *reinterpret_cast<uint2*>(dst + size_t(qy) * o.stride + qx) = make_uint2(px[0], px[1]);
                 *reinterpret_cast<uint2*>(dst + size_t(qy + 1) * o.stride + qx) = make_uint2(px[2], px[3]);
+            }
+        } else if (o.kind == kOpStoreGBuffer) {
+            if (active) {
+                const GBufferDesc gb = fv.gbufs[o.arg];
+                uint16_t nx[4], ny[4], nz[4];
+                uint32_t alb[4];
+#pragma unroll 1
+                for (int l = 0; l < 4; ++l) {
+                    nx[l] = ny[l] = nz[l] = 0;
+                    alb[l] = 0;
+                    if (own[l] == kNoOwner) continue;
+                    TriSetup t;
+                    float w[3], vary[3][kMaxVary];
+                    int state;
+                    owner_setup(fv, own[l], rect, t, w, vary, state);
+                    if (fv.states[state].program != kProgGBuffer) continue;
+                    float bpx, bpy, bpz;
+                    lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
+                    nx[l] = __half_as_ushort(__float2half_rn((bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0]));
+                    ny[l] = __half_as_ushort(__float2half_rn((bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1]));
+                    nz[l] = __half_as_ushort(__float2half_rn((bpx * vary[0][2] + bpy * vary[1][2]) + bpz * vary[2][2]));
+                    alb[l] = uint32_t(vary[0][3]) | 0xff000000u;
+                }
+                const size_t r0 = size_t(qy) * o.stride + qx, r1 = r0 + o.stride;
+                *reinterpret_cast<float2*>(gb.depth + r0) = make_float2(dep[0], dep[1]);
+                *reinterpret_cast<float2*>(gb.depth + r1) = make_float2(dep[2], dep[3]);
+                *reinterpret_cast<uint32_t*>(gb.nx + r0) = uint32_t(nx[0]) | (uint32_t(nx[1]) << 16);
+                *reinterpret_cast<uint32_t*>(gb.nx + r1) = uint32_t(nx[2]) | (uint32_t(nx[3]) << 16);
+                *reinterpret_cast<uint32_t*>(gb.ny + r0) = uint32_t(ny[0]) | (uint32_t(ny[1]) << 16);
+                *reinterpret_cast<uint32_t*>(gb.ny + r1) = uint32_t(ny[2]) | (uint32_t(ny[3]) << 16);
+                *reinterpret_cast<uint32_t*>(gb.nz + r0) = uint32_t(nz[0]) | (uint32_t(nz[1]) << 16);
+                *reinterpret_cast<uint32_t*>(gb.nz + r1) = uint32_t(nz[2]) | (uint32_t(nz[3]) << 16);
+                *reinterpret_cast<uint2*>(gb.albedo + r0) = make_uint2(alb[0], alb[1]);
+                *reinterpret_cast<uint2*>(gb.albedo + r1) = make_uint2(alb[2], alb[3]);
             }
         } else if (o.kind == kOpStoreDepth) {
             // Copy(QFloatCanvas -> FloatCanvas) (rglr_algorithm.cxx:227-244)

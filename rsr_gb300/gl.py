@@ -264,6 +264,16 @@ class GL:
         self._maybe_update_state()
         self.commands += struct.pack("<BQ", abi.CMD_STORE_DEPTH_FULL_LINEAR_FP, _addr(data))
 
+    def StoreGBuffer(self, depth, normal_x, normal_y, normal_z, albedo, width, height):
+        """RSRGPU_CMD_STORE_GBUFFER (this library's extension): depth, fp16
+        normal planes and RGBA8 albedo of the pixels drawn with the G-buffer
+        program."""
+        self._maybe_update_state()
+        g = abi.GBufferC(_addr(depth), _addr(normal_x), _addr(normal_y), _addr(normal_z), _addr(albedo),
+                         width, height)
+        self._keep.append(g)
+        self.commands += struct.pack("<BQ", abi.CMD_STORE_GBUFFER, ctypes.addressof(g))
+
     # ---- hand-off ----
     def c_states(self):
         arr = (abi.GLStateC * max(1, len(self.states)))()

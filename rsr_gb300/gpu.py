@@ -62,7 +62,7 @@ class GPU:
     def InstallDefaults(self):
         """The device counterpart of rqv::Install (src/viewer/shaders.cxx:54-126)
         for the programs this library implements."""
-        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY):
+        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY, abi.PROGRAM_GBUFFER):
             self.Install(pid, 0, abi.KIND_BIN)
             for key in DRAW_STATE_KEYS:
                 self.Install(pid, key, abi.KIND_DRAW)
@@ -130,6 +130,18 @@ class GPU:
                                      shape=(max(1, n.value) * 20,))
         return flat[:n.value * 20].reshape(n.value, 20).copy()
 
+    def shade_plain(self, gbuf, width, height, ivp, eye, lights, background=(0.0, 0.0, 0.0),
+                    out_srgb=None, out_linear=None, stream=None):
+        """Deferred plain shading (include/rsrgpu.h rsrgpu_shade_plain); device tensors."""
+        g = abi.GBufferC(gbuf["depth"].data_ptr(), gbuf["nx"].data_ptr(), gbuf["ny"].data_ptr(),
+                         gbuf["nz"].data_ptr(), gbuf["albedo"].data_ptr(), width, height)
+        fa = lambda a: (ctypes.c_float * len(a))(*[float(x) for x in a])
+        self._check(self.lib.rsrgpu_shade_plain(
+            self.ctx, ctypes.byref(g), fa(ivp), fa(eye), ctypes.c_void_p(lights.data_ptr()), lights.shape[0],
+            fa(background), ctypes.c_void_p(out_srgb.data_ptr() if out_srgb is not None else None),
+            ctypes.c_void_p(out_linear.data_ptr() if out_linear is not None else None),
+            ctypes.c_void_p(stream) if stream else None))
+
     def stats(self):
         s = abi.StatsC()
         self._check(self.lib.rsrgpu_get_stats(self.ctx, ctypes.byref(s)))
@@ -170,3 +182,23 @@ def render_scene(gpu, scene, gamma=True, device_inputs=None, color=None, depth=N
     if color is None:
         return scene.color.copy(), scene.depth.copy()
     return color, depth
+
+
+def render_gbuffer(gpu, scene, dev=None, gbuf=None, stream=None):
+    """Renders a scenes.DeferredScene with device-resident inputs and G-buffer.
+    dev: name -> device tensor copies of scene.arrays (made here if None)."""
+    import torch
+    if dev is None:
+        dev = {k: torch.from_numpy(v).cuda() for k, v in scene.arrays.items()}
+    n = scene.width * scene.height
+    if gbuf is None:
+        gbuf = {"depth": torch.zeros(n, dtype=torch.float32, device="cuda"),
+                "nx": torch.zeros(n, dtype=torch.int16, device="cuda"),
+                "ny": torch.zeros(n, dtype=torch.int16, device="cuda"),
+                "nz": torch.zeros(n, dtype=torch.int16, device="cuda"),
+                "albedo": torch.zeros(n, dtype=torch.int32, device="cuda")}
+    gpu.Reset(scene.width, scene.height, scene.tile_blocks)
+    gl = scene.record(ref=lambda k, off=0: dev[k][off:], gbuffer=gbuf)
+    gpu.Run(gl, stream=stream)
+    gpu.Wait()
+    return gbuf, dev

@@ -379,3 +379,139 @@ def mixed_states(seed=13, width=640, height=360, tile_blocks=(4, 4)):
 
     return Scene("mixed_states", width, height, tile_blocks, arrays, record,
                  c1 // 3 + len(faces) + c3 // 3 + c4 // 3, post_program=abi.PROGRAM_EXPOSURE_POST)
+
+
+# ---- deferred scene: many small objects, G-buffer program, 64 point lights ----
+def _random_rotations(u):
+    """Uniform random rotation matrices from three uniforms per object (Shoemake)."""
+    u1, u2, u3 = (u[:, k].astype(np.float64) for k in range(3))
+    a, b = np.sqrt(1 - u1), np.sqrt(u1)
+    qx, qy = a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2)
+    qz, qw = b * np.sin(2 * np.pi * u3), b * np.cos(2 * np.pi * u3)
+    r = np.empty((len(u), 3, 3))
+    r[:, 0, 0] = 1 - 2 * (qy * qy + qz * qz); r[:, 0, 1] = 2 * (qx * qy - qz * qw); r[:, 0, 2] = 2 * (qx * qz + qy * qw)
+    r[:, 1, 0] = 2 * (qx * qy + qz * qw); r[:, 1, 1] = 1 - 2 * (qx * qx + qz * qz); r[:, 1, 2] = 2 * (qy * qz - qx * qw)
+    r[:, 2, 0] = 2 * (qx * qz - qy * qw); r[:, 2, 1] = 2 * (qy * qz + qx * qw); r[:, 2, 2] = 1 - 2 * (qx * qx + qy * qy)
+    return r
+
+
+def _cube_mesh():
+    """Unit cube, 24 vertices (flat face normals), 12 CCW-outward triangles."""
+    faces = [((1, 0, 0), (0, 1, 0)), ((-1, 0, 0), (0, 0, 1)), ((0, 1, 0), (0, 0, 1)),
+             ((0, -1, 0), (1, 0, 0)), ((0, 0, 1), (1, 0, 0)), ((0, 0, -1), (0, 1, 0))]
+    pos, nrm, tri = [], [], []
+    for n, t in faces:
+        n, t = np.array(n, float), np.array(t, float)
+        b = np.cross(n, t)
+        base = len(pos)
+        for (su, sv) in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+            pos.append(0.5 * (n + su * t + sv * b))
+            nrm.append(n)
+        tri += [(base, base + 1, base + 2), (base, base + 2, base + 3)]
+    return np.array(pos), np.array(nrm), np.array(tri)
+
+
+def _morton3(p):
+    q = np.clip(((p + 10.0) / 20.0 * 1023).astype(np.int64), 0, 1023)
+    code = np.zeros(len(p), np.int64)
+    for bit in range(10):
+        for k in range(3):
+            code |= ((q[:, k] >> bit) & 1) << (3 * bit + k)
+    return code
+
+
+def deferred_scene(nobj=2_000_000, seed=3, width=1920, height=1080, tile_blocks=(4, 4),
+                   size=(0.05, 0.15), sphere_every=8, nlights=64, gouraud=False):
+    """Config-3 G-buffer scene: nobj objects in [-10,10]^3 with random
+    orientation and size (every sphere_every-th one an icosahedron with
+    smooth normals, the others cubes with flat normals), random RGB albedo,
+    drawn with the G-buffer program (chunked into <= 32760-vertex draws,
+    objects in 3D Morton order of their centre), camera at (0,0,30) looking
+    at the origin with a 60 degree field of view; plus nlights point lights
+    (position in the box, colour in [0,1], radius in [2,6]).  gouraud=True
+    draws the same geometry with the Gouraud test program (normals as colour)
+    and ordinary colour/depth stores, so rsr itself can render it."""
+    u = uniform01(seed, nobj * 10).reshape(nobj, 10)
+    centre = lerp(-10.0, 10.0, u[:, 0:3]).astype(np.float64)
+    rot = _random_rotations(u[:, 3:6])
+    scale = lerp(size[0], size[1], u[:, 6]).astype(np.float64)
+    rgb = np.clip((lerp(0.2, 1.0, u[:, 7:10]) * 255.0).astype(np.int64), 0, 255)
+    order = np.argsort(_morton3(centre), kind="stable")
+    centre, rot, scale, rgb = centre[order], rot[order], scale[order], rgb[order]
+    is_sphere = (np.arange(nobj) % sphere_every) == sphere_every - 1
+    cpos, cnrm, ctri = _cube_mesh()
+    iverts, ifaces = icosphere(0)
+    ipos, inrm = iverts.astype(np.float64) * 0.6, iverts.astype(np.float64)
+    arrays, draws = {}, []
+    for kind, mpos, mnrm, mtri, sel in (("c", cpos, cnrm, ctri, ~is_sphere), ("s", ipos, inrm, ifaces, is_sphere)):
+        n = int(sel.sum())
+        if n == 0:
+            continue
+        nv = len(mpos)
+        per_draw = 32760 // nv
+        wp = np.einsum("oij,vj->ovi", rot[sel], mpos) * scale[sel][:, None, None] + centre[sel][:, None, :]
+        wn = np.einsum("oij,vj->ovi", rot[sel], mnrm)
+        alb = (rgb[sel][:, 0] | (rgb[sel][:, 1] << 8) | (rgb[sel][:, 2] << 16)).astype(np.float32)
+        for k, c in enumerate("xyz"):
+            arrays["%s_p%s" % (kind, c)] = pad4(wp[:, :, k].reshape(-1).astype(np.float32))
+            arrays["%s_n%s" % (kind, c)] = pad4(wn[:, :, k].reshape(-1).astype(np.float32))
+        arrays["%s_alb" % kind] = pad4(np.repeat(alb, nv))
+        arrays["%s_idx" % kind] = (np.arange(per_draw)[:, None, None] * nv + mtri[None]).reshape(-1).astype(np.uint16)
+        for first in range(0, n, per_draw):
+            cnt = min(per_draw, n - first)
+            draws.append((kind, first * nv, cnt * len(mtri) * 3))
+    lu = uniform01(seed + 101, nlights * 7).reshape(nlights, 7)
+    lights = np.zeros((nlights, 8), np.float32)
+    lights[:, 0:3] = lerp(-10.0, 10.0, lu[:, 0:3])
+    lights[:, 3] = lerp(2.0, 6.0, lu[:, 3])
+    lights[:, 4:7] = lerp(0.0, 1.0, lu[:, 4:7])
+    view = look_at((0.0, 0.0, 30.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0))
+    proj = perspective(60.0, width / height, 1.0, 100.0)
+    vp = proj.reshape(4, 4).T.astype(np.float64) @ view.reshape(4, 4).T.astype(np.float64)
+    ivp = np.linalg.inv(vp).T.reshape(16).astype(np.float32)   # column-major inverse
+    ntris = sum(c // 3 for _, _, c in draws)
+
+    def record(gl, ref):
+        gl.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, abi.RB_RGBF32)
+        gl.RenderbufferType(abi.GL_DEPTH_ATTACHMENT, abi.RB_F32)
+        gl.ClearColor((0.0, 0.0, 0.0))
+        gl.ClearDepth(1.0)
+        gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
+        gl.UseProgram(abi.PROGRAM_GOURAUD if gouraud else abi.PROGRAM_GBUFFER)
+        gl.ViewMatrix(view)
+        gl.ProjectionMatrix(proj)
+        for kind, vbase, count in draws:
+            gl.UseBuffer(0, tuple(ref("%s_p%s" % (kind, c), vbase) for c in "xyz"))
+            gl.UseBuffer(3, tuple(ref("%s_n%s" % (kind, c), vbase) for c in "xyz"))
+            if not gouraud:
+                gl.UseBuffer(6, ref("%s_alb" % kind, vbase))
+            gl.DrawElements(count, ref("%s_idx" % kind, 0), 0)
+
+    if gouraud:
+        sc = Scene("deferred_gouraud", width, height, tile_blocks, arrays,
+                   lambda gl, ref: record(gl, lambda k, off=0: ref(k)[off:]), ntris)
+        return sc
+    sc = DeferredScene("deferred", width, height, tile_blocks, arrays, record, ntris)
+    sc.lights, sc.ivp, sc.eye, sc.nobj, sc.ndraws = lights, ivp, np.array([0.0, 0.0, 30.0], np.float32), nobj, len(draws)
+    return sc
+
+
+class DeferredScene(Scene):
+    """A G-buffer frame.  record(ref, gbuffer=...) takes ref(name, offset)
+    (element offset into the named array) and the five G-buffer planes."""
+
+    def __init__(self, *a, **kw):
+        super().__init__(*a, **kw)
+        n = self.width * self.height
+        self.gbuf = {"depth": np.zeros(n, np.float32), "nx": np.zeros(n, np.uint16), "ny": np.zeros(n, np.uint16),
+                     "nz": np.zeros(n, np.uint16), "albedo": np.zeros(n, np.uint32)}
+
+    def record(self, ref=None, gbuffer=None, **_):
+        gl = GL()
+        if ref is None:
+            def ref(k, off=0):
+                return self.arrays[k][off:]
+        g = gbuffer or self.gbuf
+        self._record(gl, ref)
+        gl.StoreGBuffer(g["depth"], g["nx"], g["ny"], g["nz"], g["albedo"], self.width, self.height)
+        return gl

@@ -33,6 +33,9 @@ GOLDEN_SCENES = {
     "clip_640_t64": ("clip_stress", {}, 3),
     "clip_2160_t32": ("clip_stress", dict(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0), 3),
     "mixed_640_t32": ("mixed_states", {}, 3),
+    # geometry of the deferred (G-buffer) scene drawn with the Gouraud program:
+    # pins the G-buffer pass's depth to rsr
+    "deferred_gouraud_640": ("deferred_scene", dict(nobj=20000, width=640, height=360, gouraud=True), 3),
 }
 
 
