@@ -261,6 +261,26 @@ int rsrgpu_shade_plain(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const flo
                        const float eye[3], const rsrgpu_light* lights, int nlights,
                        const float background[3], uint32_t* out_srgb, float* out_linear, void* stream);
 
+/* ---- learned deferred shader (extension; no counterpart in rsr) ----
+ * MLP 24 -> 64 -> 64 -> 64 -> 3 with ReLU, BF16 weights and activations,
+ * FP32 accumulation, run on tcgen05 tensor cores.  Weights are row-major
+ * [out][in] BF16 with the input padded to 32 columns and the output layer to
+ * 16 rows (padding must be zero); biases FP32.  Device pointers. */
+typedef struct rsrgpu_mlp {
+    const uint16_t* w1;   /* [64][32] */
+    const uint16_t* w2;   /* [64][64] */
+    const uint16_t* w3;   /* [64][64] */
+    const uint16_t* w4;   /* [16][64] */
+    const float* b1;      /* [64] */
+    const float* b2;      /* [64] */
+    const float* b3;      /* [64] */
+    const float* b4;      /* [16] */
+} rsrgpu_mlp;
+
+/* out[n][3] = MLP(features[n][32]) with BF16 features (columns 24..31 zero). */
+int rsrgpu_mlp_forward(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* features, int n,
+                       float* out, void* stream);
+
 /* ---- rendering without any device allocation ----
  * This entry point has no counterpart in the reference.  It is for callers
  * that cannot call cudaMalloc (for example a host framework that owns all

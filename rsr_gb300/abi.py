@@ -119,6 +119,10 @@ class LightC(ctypes.Structure):
                 ("color", ctypes.c_float * 3), ("reserved", ctypes.c_float)]
 
 
+class MlpC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("w1", "w2", "w3", "w4", "b1", "b2", "b3", "b4")]
+
+
 class StatsC(ctypes.Structure):
     _fields_ = [("total_tiles", ctypes.c_int64),
                 ("total_tile_records", ctypes.c_int64),
@@ -150,6 +154,8 @@ SYMBOLS = {
                             ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_int,
                             ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                            ctypes.c_int),
+    "rsrgpu_mlp_forward": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                            ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

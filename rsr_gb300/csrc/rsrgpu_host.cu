@@ -29,6 +29,8 @@ namespace rsrgpu {
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_mlp_forward(const rsrgpu_mlp& w, const uint16_t* feat, int n, float* out, int* error,
+                               int num_sms, cudaStream_t st);
 cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
                                const rsrgpu_light* lights, int nlights, const float background[3],
                                uint32_t* out_srgb, float* out_linear, const uint8_t* srgb_lut, cudaStream_t st);
@@ -90,7 +92,10 @@ struct rsrgpu_ctx {
     bool ran = false;
     // device memory
     DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
-        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs;
+        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs,
+        d_mlp_err;
+    int num_sms = 0;
+    int* h_mlp_err = nullptr;   // pinned
     uint32_t clip_cap = 1u << 18;
     uint32_t bin_cap = 1u << 22;
     FrameCounters* h_counters = nullptr;   // pinned
@@ -338,7 +343,8 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     if (ctx == nullptr) return 0;
     if (ctx->own) cudaStreamSynchronize(ctx->own);
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
-    DevBuf* bufs[] = { &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
+    DevBuf* bufs[] = { &ctx->d_mlp_err, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -900,6 +906,45 @@ int rsrgpu_shade_plain(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const flo
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
     CK(launch_shade_plain(g, inv_view_proj, eye, lights, nlights, background, out_srgb, out_linear,
                           ctx->d_srgb.as<uint8_t>(), st), "shade_plain_kernel");
+    return 0;
+}
+
+namespace {
+int check_device_input(rsrgpu_ctx* ctx, const void* p, size_t need, size_t align, const char* what) {
+    void* dp = nullptr;
+    size_t avail = 0;
+    int rc = resolve(ctx, p, false, &dp, what, &avail);
+    if (rc) return rc;
+    if (dp == nullptr || dp != p || avail < need || (reinterpret_cast<uintptr_t>(p) % align))
+        return fail(ctx, RSRGPU_EINVAL, "%s: device pointer with %zu bytes, %zu-byte aligned, needed", what, need, align);
+    return 0;
+}
+}  // namespace
+
+int rsrgpu_mlp_forward(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* features, int n,
+                       float* out, void* stream) {
+    if (ctx == nullptr || mlp == nullptr || n < 0) return RSRGPU_EINVAL;
+    if (n == 0) return 0;
+    struct { const void* p; size_t bytes; size_t align; const char* what; } ins[] = {
+        { mlp->w1, 64 * 32 * 2, 16, "w1" }, { mlp->w2, 64 * 64 * 2, 16, "w2" }, { mlp->w3, 64 * 64 * 2, 16, "w3" },
+        { mlp->w4, 16 * 64 * 2, 16, "w4" }, { mlp->b1, 64 * 4, 4, "b1" }, { mlp->b2, 64 * 4, 4, "b2" },
+        { mlp->b3, 64 * 4, 4, "b3" }, { mlp->b4, 16 * 4, 4, "b4" },
+        { features, size_t(n) * 64, 16, "features" }, { out, size_t(n) * 12, 4, "mlp output" } };
+    for (const auto& in : ins) {
+        int rc = check_device_input(ctx, in.p, in.bytes, in.align, in.what);
+        if (rc) return rc;
+    }
+    if (ctx->num_sms == 0) {
+        CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+        CK(ctx->d_mlp_err.ensure(sizeof(int)), "alloc mlp error flag");
+        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_mlp_err), sizeof(int), cudaHostAllocDefault), "alloc pinned flag");
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(cudaMemsetAsync(ctx->d_mlp_err.p, 0, sizeof(int), st), "memset mlp error");
+    CK(launch_mlp_forward(*mlp, features, n, out, ctx->d_mlp_err.as<int>(), ctx->num_sms, st), "mlp_forward_kernel");
+    CK(cudaMemcpyAsync(ctx->h_mlp_err, ctx->d_mlp_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H mlp error");
+    CK(cudaStreamSynchronize(st), "mlp sync");
+    if (*ctx->h_mlp_err) return fail(ctx, RSRGPU_ETIMEOUT, "tensor-core MMA did not complete (bounded wait expired)");
     return 0;
 }
 

@@ -142,6 +142,13 @@ class GPU:
             ctypes.c_void_p(out_linear.data_ptr() if out_linear is not None else None),
             ctypes.c_void_p(stream) if stream else None))
 
+    def mlp_forward(self, weights, features, out, stream=None):
+        """rsrgpu_mlp_forward: features (n, 32) bf16 device tensor -> out (n, 3) fp32."""
+        m = abi.MlpC(*[weights[k].data_ptr() for k in ("w1", "w2", "w3", "w4", "b1", "b2", "b3", "b4")])
+        self._check(self.lib.rsrgpu_mlp_forward(self.ctx, ctypes.byref(m), ctypes.c_void_p(features.data_ptr()),
+                                                features.shape[0], ctypes.c_void_p(out.data_ptr()),
+                                                ctypes.c_void_p(stream) if stream else None))
+
     def stats(self):
         s = abi.StatsC()
         self._check(self.lib.rsrgpu_get_stats(self.ctx, ctypes.byref(s)))
