@@ -281,6 +281,23 @@ typedef struct rsrgpu_mlp {
 int rsrgpu_mlp_forward(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* features, int n,
                        float* out, void* stream);
 
+/* Gradient of the mean squared error of one batch.  Sample rows
+ * index[0..batch) of features[.][32] (BF16) against targets[.][3] (FP32).
+ * grad receives RSRGPU_MLP_PARAMS floats laid out w1 | w2 | w3 | w4 | b1 |
+ * b2 | b3 | b4 (row-major [out][in], padded shapes as in rsrgpu_mlp); loss
+ * receives the batch's sum of squared errors.  Both are zeroed here.  The
+ * forward and backward GEMMs run on tcgen05 tensor cores. */
+#define RSRGPU_MLP_WEIGHTS 11264
+#define RSRGPU_MLP_PARAMS  11472
+int rsrgpu_mlp_grad(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* features, const float* targets,
+                    int nsamples, const int32_t* index, int batch, float* grad, float* loss, void* stream);
+
+/* Adam step on FP32 master parameters (same layout as the gradient); writes
+ * the BF16 weights (RSRGPU_MLP_WEIGHTS values, the layout rsrgpu_mlp points
+ * into) and the FP32 biases. */
+int rsrgpu_mlp_adam(rsrgpu_ctx* ctx, float* params, const float* grad, float* m, float* v, int step,
+                    float lr, uint16_t* weights_bf16, float* biases, void* stream);
+
 /* ---- rendering without any device allocation ----
  * This entry point has no counterpart in the reference.  It is for callers
  * that cannot call cudaMalloc (for example a host framework that owns all

@@ -156,6 +156,10 @@ SYMBOLS = {
                            ctypes.c_int),
     "rsrgpu_mlp_forward": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                             ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_mlp_grad": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_mlp_adam": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                         ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

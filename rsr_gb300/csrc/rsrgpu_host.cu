@@ -31,6 +31,10 @@ cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_mlp_forward(const rsrgpu_mlp& w, const uint16_t* feat, int n, float* out, int* error,
                                int num_sms, cudaStream_t st);
+cudaError_t launch_mlp_train(const rsrgpu_mlp& w, const uint16_t* feat, const float* target, const int32_t* index,
+                             int batch, float* grad, float* loss, int* error, int num_sms, cudaStream_t st);
+cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int n, int nw, float lr, float b1, float b2,
+                        float eps, int step, uint16_t* wbf16, float* bias_out, cudaStream_t st);
 cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
                                const rsrgpu_light* lights, int nlights, const float background[3],
                                uint32_t* out_srgb, float* out_linear, const uint8_t* srgb_lut, cudaStream_t st);
@@ -945,6 +949,67 @@ int rsrgpu_mlp_forward(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* f
     CK(cudaMemcpyAsync(ctx->h_mlp_err, ctx->d_mlp_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H mlp error");
     CK(cudaStreamSynchronize(st), "mlp sync");
     if (*ctx->h_mlp_err) return fail(ctx, RSRGPU_ETIMEOUT, "tensor-core MMA did not complete (bounded wait expired)");
+    return 0;
+}
+
+namespace {
+int check_mlp(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp) {
+    struct { const void* p; size_t bytes; size_t align; const char* what; } ins[] = {
+        { mlp->w1, 64 * 32 * 2, 16, "w1" }, { mlp->w2, 64 * 64 * 2, 16, "w2" }, { mlp->w3, 64 * 64 * 2, 16, "w3" },
+        { mlp->w4, 16 * 64 * 2, 16, "w4" }, { mlp->b1, 64 * 4, 4, "b1" }, { mlp->b2, 64 * 4, 4, "b2" },
+        { mlp->b3, 64 * 4, 4, "b3" }, { mlp->b4, 16 * 4, 4, "b4" } };
+    for (const auto& in : ins) {
+        int rc = check_device_input(ctx, in.p, in.bytes, in.align, in.what);
+        if (rc) return rc;
+    }
+    if (ctx->num_sms == 0) {
+        CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+        CK(ctx->d_mlp_err.ensure(sizeof(int)), "alloc mlp error flag");
+        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_mlp_err), sizeof(int), cudaHostAllocDefault), "alloc pinned flag");
+    }
+    return 0;
+}
+}  // namespace
+
+int rsrgpu_mlp_grad(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* features, const float* targets,
+                    int nsamples, const int32_t* index, int batch, float* grad, float* loss, void* stream) {
+    if (ctx == nullptr || mlp == nullptr || nsamples <= 0 || batch <= 0) return RSRGPU_EINVAL;
+    int rc = check_mlp(ctx, mlp);
+    if (rc) return rc;
+    struct { const void* p; size_t bytes; size_t align; const char* what; } ins[] = {
+        { features, size_t(nsamples) * 64, 16, "features" }, { targets, size_t(nsamples) * 12, 4, "targets" },
+        { index, size_t(batch) * 4, 4, "batch index" }, { grad, RSRGPU_MLP_PARAMS * 4, 4, "gradient" },
+        { loss, 4, 4, "loss" } };
+    for (const auto& in : ins) {
+        rc = check_device_input(ctx, in.p, in.bytes, in.align, in.what);
+        if (rc) return rc;
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(cudaMemsetAsync(grad, 0, RSRGPU_MLP_PARAMS * 4, st), "memset grad");
+    CK(cudaMemsetAsync(loss, 0, 4, st), "memset loss");
+    CK(cudaMemsetAsync(ctx->d_mlp_err.p, 0, sizeof(int), st), "memset mlp error");
+    CK(launch_mlp_train(*mlp, features, targets, index, batch, grad, loss, ctx->d_mlp_err.as<int>(), ctx->num_sms, st), "mlp_train_kernel");
+    CK(cudaMemcpyAsync(ctx->h_mlp_err, ctx->d_mlp_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H mlp error");
+    CK(cudaStreamSynchronize(st), "mlp sync");
+    if (*ctx->h_mlp_err) return fail(ctx, RSRGPU_ETIMEOUT, "tensor-core MMA did not complete (bounded wait expired)");
+    return 0;
+}
+
+int rsrgpu_mlp_adam(rsrgpu_ctx* ctx, float* params, const float* grad, float* m, float* v, int step,
+                    float lr, uint16_t* weights_bf16, float* biases, void* stream) {
+    if (ctx == nullptr || step < 1) return RSRGPU_EINVAL;
+    struct { const void* p; size_t bytes; const char* what; } ins[] = {
+        { params, RSRGPU_MLP_PARAMS * 4, "params" }, { grad, RSRGPU_MLP_PARAMS * 4, "grad" },
+        { m, RSRGPU_MLP_PARAMS * 4, "adam m" }, { v, RSRGPU_MLP_PARAMS * 4, "adam v" },
+        { weights_bf16, RSRGPU_MLP_WEIGHTS * 2, "bf16 weights" },
+        { biases, (RSRGPU_MLP_PARAMS - RSRGPU_MLP_WEIGHTS) * 4, "biases" } };
+    for (const auto& in : ins) {
+        int rc = check_device_input(ctx, in.p, in.bytes, 4, in.what);
+        if (rc) return rc;
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_adam(params, grad, m, v, RSRGPU_MLP_PARAMS, RSRGPU_MLP_WEIGHTS, lr, 0.9f, 0.999f, 1e-8f, step,
+                   weights_bf16, biases, st), "adam_kernel");
     return 0;
 }
 

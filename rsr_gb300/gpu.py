@@ -149,6 +149,18 @@ class GPU:
                                                 features.shape[0], ctypes.c_void_p(out.data_ptr()),
                                                 ctypes.c_void_p(stream) if stream else None))
 
+    def mlp_grad(self, weights, features, targets, index, grad, loss, stream=None):
+        m = abi.MlpC(*[weights[k].data_ptr() for k in ("w1", "w2", "w3", "w4", "b1", "b2", "b3", "b4")])
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())
+        self._check(self.lib.rsrgpu_mlp_grad(self.ctx, ctypes.byref(m), vp(features), vp(targets), features.shape[0],
+                                             vp(index), index.shape[0], vp(grad), vp(loss),
+                                             ctypes.c_void_p(stream) if stream else None))
+
+    def mlp_adam(self, params, grad, m, v, step, lr, wbf16, biases, stream=None):
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())
+        self._check(self.lib.rsrgpu_mlp_adam(self.ctx, vp(params), vp(grad), vp(m), vp(v), int(step), float(lr),
+                                             vp(wbf16), vp(biases), ctypes.c_void_p(stream) if stream else None))
+
     def stats(self):
         s = abi.StatsC()
         self._check(self.lib.rsrgpu_get_stats(self.ctx, ctypes.byref(s)))
