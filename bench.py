@@ -286,7 +286,6 @@ def run_gpu(args):
     # algorithmic DRAM bytes of one raster launch: the triangle records it reads
     # (96 B per tile-list entry), the colour and depth it writes (8 B per
     # pixel) and the sampled mip level-0 texels (16 B each, read once)
-    st = gpu.stats() if False else None
     gpu_tiles_bytes = _raster_bytes(gpu, sc)
     achieved = gpu_tiles_bytes / (raster_avg / 1e3) / 1e9
     roof = {"kernel": "raster_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -305,10 +304,98 @@ def run_gpu(args):
             "frames_per_s": 1e3 / ms_per_step, "e2e_frames_per_s": 1e3 * args.steps / e2e_ms,
             "gpu_launches": 3 * args.steps, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks.summary(local)}
+    if not args.no_deferred:
+        line["deferred"] = run_deferred(gpu, args, stream, flush)
     print(json.dumps(line))
 
 
 _RASTER_BYTES = {}
+
+
+def _time_device(fn, steps, stream, flush):
+    """Mean device time (ms) of fn() over `steps` calls, CUDA events on
+    `stream`, L2 flushed by a 256 MiB write before each call (untimed)."""
+    import torch
+    evs = []
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.fill_(i & 0xff)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+    return statistics.mean(s.elapsed_time(e) for s, e in evs)
+
+
+def run_deferred(gpu, args, stream, flush):
+    """The 64-light deferred scene (1920x1080, 2M objects, seed 100): G-buffer
+    pass, plain shader, learned shader (committed weights) with its per-tile
+    fallback; PSNR / max-abs of the learned image against the plain one."""
+    import torch
+    from rsr_gb300 import learned
+    sptr = stream.cuda_stream
+    fr = learned.DeferredFrame(gpu, 100, 1920, 1080, 2_000_000)
+    n = fr.width * fr.height
+    plain = torch.zeros(n, dtype=torch.int32, device="cuda")
+    out = torch.zeros(n, dtype=torch.int32, device="cuda")
+    status = torch.zeros(fr.ntiles, dtype=torch.uint8, device="cuda")
+    steps = max(5, min(args.steps, 20))
+    peak, peak_kind = hbm_peak()
+    res = {"workload": "deferred_1080p: 2M cubes/icosahedra seed 100, 64 point lights, Blinn-Phong 32",
+           "steps": steps}
+    gbuf_ms = _time_device(lambda: (gpu.run(sptr), gpu.Wait()), steps, stream, flush)
+    plain_ms = _time_device(lambda: fr.shade_plain(gpu, plain, stream=sptr), steps, stream, flush)
+    # plain shader bytes: G-buffer read (14 B/px), lights, sRGB8 write (4 B/px)
+    plain_bytes = n * 18 + 64 * 32
+    res["gbuffer_ms"] = gbuf_ms
+    res["plain"] = {"ms": plain_ms, "frames_per_s_shading": 1e3 / plain_ms,
+                    "frames_per_s_frame": 1e3 / (gbuf_ms + plain_ms),
+                    "roofline": {"kernel": "shade_plain_kernel", "bound": "compute (fp32, IEEE div/sqrt)",
+                                 "achieved": plain_bytes / (plain_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                 "frac": plain_bytes / (plain_ms / 1e3) / 1e9 / peak,
+                                 "peak_source": peak_kind}}
+    if not os.path.exists(learned.WEIGHTS_PATH):
+        res["learned"] = {"unavailable": "no trained weights at rsr_gb300/weights/learned_shader.npz"}
+        return res
+    net = learned.LearnedShader.load()
+    thr = learned.PSNR_40DB_MSE
+    fr.shade_learned(gpu, net, thr, out, tile_status=status, stream=sptr)
+    gpu.shade_learned_check()
+    torch.cuda.synchronize()
+    fr.shade_plain(gpu, plain, stream=sptr)
+    torch.cuda.synchronize()
+    db, maxabs = learned.psnr(out.cpu().numpy(), plain.cpu().numpy())
+    st = status.cpu().numpy()
+    learned_ms = _time_device(lambda: fr.shade_learned(gpu, net, thr, out, stream=sptr), steps, stream, flush)
+    gpu.shade_learned_check()
+    served = float((st == 0).sum() / max(1, (st != 2).sum()))
+    covered = int(fr.covered.sum().item())
+    mlp_flops = 2 * (24 * 64 + 64 * 64 * 2 + 64 * 3)          # unpadded MACs x 2 per pixel
+    tflops = covered * served * mlp_flops / (learned_ms / 1e3) / 1e12
+    res["learned"] = {"ms": learned_ms, "frames_per_s_shading": 1e3 / learned_ms,
+                      "frames_per_s_frame": 1e3 / (gbuf_ms + learned_ms),
+                      "speedup_vs_plain_shading": plain_ms / learned_ms,
+                      "psnr_db_vs_plain": db, "max_abs_vs_plain": maxabs, "gate_max_tile_mse": thr,
+                      "served_tiles": served, "covered_pixels": covered,
+                      "mlp_tflops": tflops, "weights": {k: net.meta.get(k) for k in ("train_seeds", "samples", "steps")}}
+    # end to end: G-buffer pass + shading + sRGB8 image read back to pinned host memory, wall clock
+    host = torch.zeros(n, dtype=torch.int32).pin_memory()
+    for name, shade in (("plain", lambda: fr.shade_plain(gpu, plain, stream=sptr)),
+                        ("learned", lambda: fr.shade_learned(gpu, net, thr, plain, stream=sptr))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                gpu.run(sptr)
+                gpu.Wait()
+                shade()
+                host.copy_(plain, non_blocking=True)
+                stream.synchronize()
+        res[name]["e2e_frames_per_s"] = steps / (time.perf_counter() - t0)
+    gpu.shade_learned_check()
+    return res
 
 
 def _raster_bytes(gpu, sc):
@@ -338,6 +425,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-deferred", action="store_true", help="skip the deferred / learned shading figures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -298,6 +298,48 @@ int rsrgpu_mlp_grad(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* feat
 int rsrgpu_mlp_adam(rsrgpu_ctx* ctx, float* params, const float* grad, float* m, float* v, int step,
                     float lr, uint16_t* weights_bf16, float* biases, void* stream);
 
+/* ---- learned deferred shading, fused (extension; no counterpart in rsr) ----
+ * The G-buffer is shaded in 32x32-pixel tiles.  Per tile: the 8 candidate
+ * lights with the largest bound on their contribution to the tile's
+ * world-space box; per covered pixel (albedo != 0) 24 features: unit normal,
+ * unit view vector, albedo, eye distance / 50, and a summary of the candidate
+ * lights reaching the pixel (sum of colour * att, sum of w L, the six
+ * entries of sum w L L^T, sum of w max(N.L, 0), mean d/r weighted by w, with
+ * att = (1 - d/r)^2 and w the colour sum of colour * att).  The output is
+ * rgb = max(MLP(features) + base, 0)^2 per channel, where base is the square
+ * root of an analytic estimate from the same features (Blinn-Phong of one
+ * virtual light with direction sum w L and colour sum colour * att, plus
+ * ambient); with a zero output layer the shader is that estimate.  The gate shades min(16, covered) sample
+ * pixels of the tile (its 4x4 grid of pixels (8i+4, 8j+4) first) with the
+ * plain shader; if the mean squared difference of learned and plain sRGB8
+ * values over the samples exceeds max_tile_mse (8-bit units squared; 6.5 is
+ * 40 dB), the tile is shaded by the plain shader, bit-exact with
+ * rsrgpu_shade_plain.  A negative max_tile_mse shades every tile plain,
+ * INFINITY none.  tile_status (optional, one byte per tile in row-major
+ * order): 0 learned, 1 plain, 2 nothing covered; tile_mse (optional) the
+ * gate's estimate.  All pointers are device pointers; the call is enqueued
+ * on `stream` and returns without waiting.  A tensor-core stall is reported
+ * by the next rsrgpu_shade_learned_check(). */
+#define RSRGPU_SHADE_TILE 32
+int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gbuffer* gbuffer,
+                         const float inv_view_proj[16], const float eye[3], const rsrgpu_light* lights, int nlights,
+                         const float background[3], float max_tile_mse, uint32_t* out_srgb, float* out_linear,
+                         uint8_t* tile_status, float* tile_mse, void* stream);
+
+/* Waits for the work rsrgpu_shade_learned() enqueued and returns
+ * RSRGPU_ETIMEOUT if a tensor-core wait expired in any call since the last
+ * check (the affected tiles were left unwritten), else 0. */
+int rsrgpu_shade_learned_check(rsrgpu_ctx* ctx);
+
+/* The learned shader's inputs and training targets for every pixel:
+ * features[W*H][32] BF16 (columns 24..31 and uncovered rows zero), targets
+ * (optional) [W*H][3] = sqrt(max(plain linear RGB, 0)) - base, the network's
+ * training target (zero rows where uncovered), candidates (optional) [tiles][8] light indices (-1 pads).
+ * Device pointers; synchronous. */
+int rsrgpu_learned_features(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const float inv_view_proj[16],
+                            const float eye[3], const rsrgpu_light* lights, int nlights, uint16_t* features,
+                            float* targets, int32_t* candidates, void* stream);
+
 /* ---- rendering without any device allocation ----
  * This entry point has no counterpart in the reference.  It is for callers
  * that cannot call cudaMalloc (for example a host framework that owns all

@@ -1256,3 +1256,167 @@ int rsroracle_shade_plain(const rsrgpu_gbuffer* gb, const float ivp[16], const f
     pthread_mutex_destroy(&j.mu);
     return 0;
 }
+
+/* ---- learned deferred shader: inputs (the CUDA feature builder's restatement) ----
+ * Shading tiles of 32x32 pixels.  Per tile: the world-space box of its covered
+ * pixels, each light's score (1 - d/r)^2 * (r + g + b) at the box point nearest
+ * the light (or -1 when d >= r), and up to 8 candidates in descending score,
+ * ties to the lower index, scores > 0 only.  Per covered pixel 24 features:
+ * unit normal, unit view vector, albedo, eye distance / 50, then over the
+ * candidates reaching the pixel (att = (1 - d/r)^2, c = colour * att,
+ * w = c.r + c.g + c.b, L unit direction to the light): sum c, sum w L,
+ * sum w L L^T (xx xy xz yy yz zz), sum w max(N.L, 0), sum w (d/r) / sum w. */
+#define SHADE_TILE 32
+#define NCAND 8
+
+static void world_pos(const rsrgpu_gbuffer* g, const float* m, int x, int y, float P[3]) {
+    const float z = g->depth[(size_t)y * g->width + x];
+    const float ndcx = (2.0f * ((float)x + 0.5f)) / (float)g->width - 1.0f;
+    const float ndcy = 1.0f - (2.0f * ((float)y + 0.5f)) / (float)g->height;
+    const float cx = ((m[0] * ndcx + m[4] * ndcy) + m[8] * z) + m[12];
+    const float cy = ((m[1] * ndcx + m[5] * ndcy) + m[9] * z) + m[13];
+    const float cz = ((m[2] * ndcx + m[6] * ndcy) + m[10] * z) + m[14];
+    const float cw = ((m[3] * ndcx + m[7] * ndcy) + m[11] * z) + m[15];
+    P[0] = cx / cw; P[1] = cy / cw; P[2] = cz / cw;
+}
+
+static float light_score(const rsrgpu_light* l, const float b0[3], const float b1[3]) {
+    float e[3];
+    for (int k = 0; k < 3; ++k) {
+        const float c = fminf(fmaxf(l->position[k], b0[k]), b1[k]);
+        e[k] = l->position[k] - c;
+    }
+    const float d = sqrtf(dot3(e[0], e[1], e[2], e[0], e[1], e[2]));
+    if (!(d < l->radius)) return -1.0f;
+    const float t = 1.0f - d / l->radius;
+    return (t * t) * ((l->color[0] + l->color[1]) + l->color[2]);
+}
+
+static uint16_t bf16_rne(float x) {
+    uint32_t u = f2u(x);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+int rsroracle_learned_candidates(const rsrgpu_gbuffer* g, const float ivp[16], const rsrgpu_light* lights,
+                                 int nlights, int tile, int32_t cand[NCAND]) {
+    const int tiles_x = (g->width + SHADE_TILE - 1) / SHADE_TILE;
+    const int x0 = (tile % tiles_x) * SHADE_TILE, y0 = (tile / tiles_x) * SHADE_TILE;
+    float b0[3] = { INFINITY, INFINITY, INFINITY }, b1[3] = { -INFINITY, -INFINITY, -INFINITY };
+    for (int y = y0; y < y0 + SHADE_TILE && y < g->height; ++y)
+        for (int x = x0; x < x0 + SHADE_TILE && x < g->width; ++x) {
+            if (g->albedo[(size_t)y * g->width + x] == 0) continue;
+            float P[3];
+            world_pos(g, ivp, x, y, P);
+            for (int k = 0; k < 3; ++k) { b0[k] = fminf(b0[k], P[k]); b1[k] = fmaxf(b1[k], P[k]); }
+        }
+    float score[256];
+    const int empty = !(b0[0] <= b1[0]);
+    for (int i = 0; i < nlights && i < 256; ++i) score[i] = empty ? -1.0f : light_score(&lights[i], b0, b1);
+    for (int c = 0; c < NCAND; ++c) {
+        int best = -1;
+        float bs = 0.0f;
+        for (int i = 0; i < nlights && i < 256; ++i)
+            if (score[i] > bs) { bs = score[i]; best = i; }
+        cand[c] = best;
+        if (best >= 0) score[best] = -1.0f;
+    }
+    return 0;
+}
+
+static void pixel_features(const rsrgpu_gbuffer* g, const float* ivp, const float* eye, const rsrgpu_light* lights,
+                           const int32_t* cand, int x, int y, float f[24]) {
+    const size_t i = (size_t)y * g->width + x;
+    float P[3];
+    world_pos(g, ivp, x, y, P);
+    float nx = f16_to_f32(g->normal_x[i]), ny = f16_to_f32(g->normal_y[i]), nz = f16_to_f32(g->normal_z[i]);
+    const float nlen = sqrtf(dot3(nx, ny, nz, nx, ny, nz));
+    nx = nx / nlen; ny = ny / nlen; nz = nz / nlen;
+    float vx = eye[0] - P[0], vy = eye[1] - P[1], vz = eye[2] - P[2];
+    const float vlen = sqrtf(dot3(vx, vy, vz, vx, vy, vz));
+    vx = vx / vlen; vy = vy / vlen; vz = vz / vlen;
+    const uint32_t alb = g->albedo[i];
+    f[0] = nx; f[1] = ny; f[2] = nz; f[3] = vx; f[4] = vy; f[5] = vz;
+    f[6] = (float)(alb & 255u) / 255.0f; f[7] = (float)((alb >> 8) & 255u) / 255.0f; f[8] = (float)((alb >> 16) & 255u) / 255.0f;
+    f[9] = vlen / 50.0f;
+    for (int k = 10; k < 24; ++k) f[k] = 0.0f;
+    float wsum = 0.0f;
+    for (int c = 0; c < NCAND; ++c) {
+        if (cand[c] < 0) break;
+        const rsrgpu_light* l = &lights[cand[c]];
+        float lx = l->position[0] - P[0], ly = l->position[1] - P[1], lz = l->position[2] - P[2];
+        const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
+        if (!(d < l->radius)) continue;
+        const float q = d / l->radius;
+        const float t = 1.0f - q;
+        const float att = t * t;
+        const float cr = l->color[0] * att, cg = l->color[1] * att, cb = l->color[2] * att;
+        const float w = (cr + cg) + cb;
+        lx = lx / d; ly = ly / d; lz = lz / d;
+        const float wx = w * lx, wy = w * ly, wz = w * lz;
+        f[10] = f[10] + cr; f[11] = f[11] + cg; f[12] = f[12] + cb;
+        f[13] = f[13] + wx; f[14] = f[14] + wy; f[15] = f[15] + wz;
+        f[16] = f[16] + wx * lx; f[17] = f[17] + wx * ly; f[18] = f[18] + wx * lz;
+        f[19] = f[19] + wy * ly; f[20] = f[20] + wy * lz; f[21] = f[21] + wz * lz;
+        f[22] = f[22] + w * pos0(dot3(nx, ny, nz, lx, ly, lz));
+        f[23] = f[23] + w * q;
+        wsum = wsum + w;
+    }
+    f[23] = wsum > 0.0f ? f[23] / wsum : 0.0f;
+}
+
+/* The analytic base the network's output is added to: one virtual light with
+ * direction sum w L (normalised) and colour sum c, Blinn-Phong exponent 32 plus
+ * ambient 0.03 * albedo, square root per channel. */
+static void virtual_light_base(const float* f, float base[3]) {
+    const float dlen = sqrtf(dot3(f[13], f[14], f[15], f[13], f[14], f[15]));
+    float l[3] = { 0.0f, 0.0f, 0.0f };
+    if (dlen > 0.0f) { l[0] = f[13] / dlen; l[1] = f[14] / dlen; l[2] = f[15] / dlen; }
+    float h[3] = { l[0] + f[3], l[1] + f[4], l[2] + f[5] };
+    const float hlen = sqrtf(dot3(h[0], h[1], h[2], h[0], h[1], h[2]));
+    if (hlen > 0.0f) { h[0] = h[0] / hlen; h[1] = h[1] / hlen; h[2] = h[2] / hlen; }
+    const float ndl = pos0(dot3(f[0], f[1], f[2], l[0], l[1], l[2]));
+    float sp = pos0(dot3(f[0], f[1], f[2], h[0], h[1], h[2]));
+    sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;
+    for (int c = 0; c < 3; ++c) base[c] = sqrtf(pos0(f[10 + c] * (f[6 + c] * ndl + sp) + 0.03f * f[6 + c]));
+}
+
+/* features (bf16 [W*H][32]), features_f32 ([W*H][24], optional), targets
+ * ([W*H][3] sqrt(max(plain, 0)) - base, optional), base ([W*H][3], optional),
+ * candidates ([tiles][8], optional); uncovered pixels give zero rows */
+int rsroracle_learned_features(const rsrgpu_gbuffer* g, const float ivp[16], const float eye[3],
+                               const rsrgpu_light* lights, int nlights, uint16_t* features, float* features_f32,
+                               float* targets, float* base, int32_t* candidates) {
+    const int tiles_x = (g->width + SHADE_TILE - 1) / SHADE_TILE, tiles_y = (g->height + SHADE_TILE - 1) / SHADE_TILE;
+    const size_t npx = (size_t)g->width * g->height;
+    float* plain = NULL;
+    if (targets) {
+        static const float bg[3] = { 0.0f, 0.0f, 0.0f };
+        plain = (float*)malloc(npx * 12);
+        if (!plain) return -1;
+        rsroracle_shade_plain(g, ivp, eye, lights, nlights, bg, plain);
+    }
+    for (int tile = 0; tile < tiles_x * tiles_y; ++tile) {
+        int32_t cand[NCAND];
+        rsroracle_learned_candidates(g, ivp, lights, nlights, tile, cand);
+        if (candidates) memcpy(candidates + (size_t)tile * NCAND, cand, sizeof(cand));
+        const int x0 = (tile % tiles_x) * SHADE_TILE, y0 = (tile / tiles_x) * SHADE_TILE;
+        for (int y = y0; y < y0 + SHADE_TILE && y < g->height; ++y)
+            for (int x = x0; x < x0 + SHADE_TILE && x < g->width; ++x) {
+                const size_t i = (size_t)y * g->width + x;
+                float f[24];
+                const int covered = g->albedo[i] != 0;
+                if (covered) pixel_features(g, ivp, eye, lights, cand, x, y, f);
+                else for (int k = 0; k < 24; ++k) f[k] = 0.0f;
+                for (int k = 0; k < 32; ++k) features[i * 32 + k] = k < 24 ? bf16_rne(f[k]) : 0;
+                if (features_f32) memcpy(features_f32 + i * 24, f, sizeof(f));
+                float b[3] = { 0.0f, 0.0f, 0.0f };
+                if (covered) virtual_light_base(f, b);
+                if (base) memcpy(base + i * 3, b, sizeof(b));
+                if (targets)
+                    for (int c = 0; c < 3; ++c) targets[i * 3 + c] = covered ? sqrtf(pos0(plain[i * 3 + c])) - b[c] : 0.0f;
+            }
+    }
+    free(plain);
+    return 0;
+}

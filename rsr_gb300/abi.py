@@ -160,6 +160,14 @@ SYMBOLS = {
                          ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_mlp_adam": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                          ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_shade_learned": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.POINTER(GBufferC),
+                              ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_void_p,
+                              ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_shade_learned_check": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_learned_features": ([ctypes.c_void_p, ctypes.POINTER(GBufferC), ctypes.POINTER(ctypes.c_float),
+                                 ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

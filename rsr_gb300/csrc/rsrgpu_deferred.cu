@@ -1,90 +1,15 @@
 // rsrgpu_deferred.cu -- deferred shading over the G-buffer written by
-// RSRGPU_CMD_STORE_GBUFFER.  rsr has no deferred or multi-light path; the
-// plain shader here is this library's definition (its CPU restatement in
-// oracle/rsr_oracle.c is the oracle).  Built with -fmad=false like the
-// rasteriser, so every expression rounds once per operation in the written
-// order and the GPU matches the oracle bit for bit.
+// RSRGPU_CMD_STORE_GBUFFER: the plain multi-light shader and the learned
+// shader's dense feature/target builder (training data).  The per-pixel math
+// lives in rsrgpu_shading.cuh.
 #include <cstdint>
-#include <cuda_fp16.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/rsrgpu.h"
-#include "rsrgpu_internal.h"
+#include "rsrgpu_shading.cuh"
 
 namespace rsrgpu {
-
-constexpr int kMaxLights = 256;
-
-struct PlainParams {
-    const float* depth;
-    const uint16_t* nx;
-    const uint16_t* ny;
-    const uint16_t* nz;
-    const uint32_t* albedo;
-    int width, height;
-    float ivp[16];
-    float eye[3];
-    float background[3];
-    const rsrgpu_light* lights;
-    int nlights;
-    uint32_t* out_srgb;
-    float* out_linear;
-    const uint8_t* srgb_lut;
-};
-
-__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
-    return (ax * bx + ay * by) + az * bz;
-}
-__device__ __forceinline__ float pos0(float x) { return x > 0.0f ? x : 0.0f; }
-__device__ __forceinline__ uint32_t srgb8_lut(const uint8_t* __restrict__ lut, float v) {
-    const float lo = __uint_as_float((127u - 13u) << 23), hi = __uint_as_float(0x3f7fffffu);
-    float c = v > lo ? v : lo;
-    c = c < hi ? c : hi;
-    return __ldg(lut + ((__float_as_uint(c) >> 12) - ((127u - 13u) << 11)));
-}
-
-// Multi-light Blinn-Phong for one pixel; returns linear RGB.
-__device__ __forceinline__ void plain_pixel(const PlainParams& p, const rsrgpu_light* L, int nl, int x, int y,
-                                            float z, uint16_t hx, uint16_t hy, uint16_t hz, uint32_t alb,
-                                            float rgb[3]) {
-    const float ndcx = (2.0f * (float(x) + 0.5f)) / float(p.width) - 1.0f;
-    const float ndcy = 1.0f - (2.0f * (float(y) + 0.5f)) / float(p.height);
-    const float* m = p.ivp;
-    const float cx = ((m[0] * ndcx + m[4] * ndcy) + m[8] * z) + m[12];
-    const float cy = ((m[1] * ndcx + m[5] * ndcy) + m[9] * z) + m[13];
-    const float cz = ((m[2] * ndcx + m[6] * ndcy) + m[10] * z) + m[14];
-    const float cw = ((m[3] * ndcx + m[7] * ndcy) + m[11] * z) + m[15];
-    const float px = cx / cw, py = cy / cw, pz = cz / cw;
-    float nx = __half2float(__ushort_as_half(hx)), ny = __half2float(__ushort_as_half(hy)), nz = __half2float(__ushort_as_half(hz));
-    const float nlen = sqrtf(dot3(nx, ny, nz, nx, ny, nz));
-    nx = nx / nlen; ny = ny / nlen; nz = nz / nlen;
-    float vx = p.eye[0] - px, vy = p.eye[1] - py, vz = p.eye[2] - pz;
-    const float vlen = sqrtf(dot3(vx, vy, vz, vx, vy, vz));
-    vx = vx / vlen; vy = vy / vlen; vz = vz / vlen;
-    const float ar = float(alb & 255u) / 255.0f, ag = float((alb >> 8) & 255u) / 255.0f, ab = float((alb >> 16) & 255u) / 255.0f;
-    float sr = 0.0f, sg = 0.0f, sb = 0.0f;
-    for (int i = 0; i < nl; ++i) {
-        float lx = L[i].position[0] - px, ly = L[i].position[1] - py, lz = L[i].position[2] - pz;
-        const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
-        const float r = L[i].radius;
-        if (!(d < r)) continue;
-        lx = lx / d; ly = ly / d; lz = lz / d;
-        const float t = 1.0f - d / r;
-        const float att = t * t;
-        const float ndl = pos0(dot3(nx, ny, nz, lx, ly, lz));
-        float hx2 = lx + vx, hy2 = ly + vy, hz2 = lz + vz;
-        const float hlen = sqrtf(dot3(hx2, hy2, hz2, hx2, hy2, hz2));
-        hx2 = hx2 / hlen; hy2 = hy2 / hlen; hz2 = hz2 / hlen;
-        float s = pos0(dot3(nx, ny, nz, hx2, hy2, hz2));
-        s = s * s; s = s * s; s = s * s; s = s * s; s = s * s;   // ^32
-        sr = sr + (L[i].color[0] * att) * (ar * ndl + s);
-        sg = sg + (L[i].color[1] * att) * (ag * ndl + s);
-        sb = sb + (L[i].color[2] * att) * (ab * ndl + s);
-    }
-    rgb[0] = sr + 0.03f * ar;
-    rgb[1] = sg + 0.03f * ag;
-    rgb[2] = sb + 0.03f * ab;
-}
 
 __global__ void __launch_bounds__(256) shade_plain_kernel(PlainParams p) {
     __shared__ rsrgpu_light L[kMaxLights];
@@ -103,7 +28,7 @@ __global__ void __launch_bounds__(256) shade_plain_kernel(PlainParams p) {
         }
         if (p.out_linear) { p.out_linear[3 * i] = rgb[0]; p.out_linear[3 * i + 1] = rgb[1]; p.out_linear[3 * i + 2] = rgb[2]; }
         if (p.out_srgb)
-            p.out_srgb[i] = (srgb8_lut(p.srgb_lut, rgb[0]) << 16) | (srgb8_lut(p.srgb_lut, rgb[1]) << 8) | srgb8_lut(p.srgb_lut, rgb[2]);
+            p.out_srgb[i] = pack_srgb(p.srgb_lut, rgb);
     }
 }
 
@@ -120,6 +45,113 @@ cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], co
     int blocks = (n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
     shade_plain_kernel<<<blocks, 256, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+// ---- learned shader: dense features and training targets ----
+// One CTA of 128 threads per 32x32 shading tile (grid-stride over tiles).
+// Pass 1: the world-space box of the tile's covered pixels; warp 0 picks the
+// tile's candidate lights; pass 2: features (BF16, 32 columns,
+// 24..31 zero) and the network's targets sqrt(max(plain, 0)) - base per pixel
+// (base: virtual_light_base of the FP32 features).  Uncovered pixels
+// (albedo 0) get zero rows.
+struct FeatParams {
+    PlainParams pl;
+    uint16_t* features;    // [W*H][32] bf16
+    float* targets;        // [W*H][3] or null
+    int32_t* candidates;   // [tiles][8] or null
+};
+
+__global__ void __launch_bounds__(128) learned_features_kernel(FeatParams F) {
+    __shared__ rsrgpu_light lights[kMaxLights];
+    __shared__ float box[2][4][3];
+    __shared__ int cand[kCandidates];
+    const PlainParams& p = F.pl;
+    const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) lights[i] = p.lights[i];
+    const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile, tiles_y = (p.height + kShadeTile - 1) / kShadeTile;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
+        const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
+        // thread t: row t / 4, columns (t % 4) * 8 .. + 7
+        const int y = y0 + t / 4, xb = x0 + (t % 4) * 8;
+        float lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int x = xb + j;
+            if (x < p.width && y < p.height && p.albedo[y * p.width + x] != 0u) {
+                float P[3];
+                world_pos(p, x, y, p.depth[y * p.width + x], P);
+                for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], P[k]); hi[k] = fmaxf(hi[k], P[k]); }
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+            }
+            if (lane == 0) { box[0][warp][k] = lo[k]; box[1][warp][k] = hi[k]; }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float b0[3], b1[3];
+            for (int k = 0; k < 3; ++k) {
+                b0[k] = fminf(fminf(box[0][0][k], box[0][1][k]), fminf(box[0][2][k], box[0][3][k]));
+                b1[k] = fmaxf(fmaxf(box[1][0][k], box[1][1][k]), fmaxf(box[1][2][k], box[1][3][k]));
+            }
+            const bool empty = !(b0[0] <= b1[0]);
+            select_candidates(empty ? 0 : nl, [&](int i) { return light_score(lights[i], b0, b1); }, cand);
+            if (lane == 0 && F.candidates)
+                for (int c = 0; c < kCandidates; ++c) F.candidates[tile * kCandidates + c] = cand[c];
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int j = 0; j < 8; ++j) {
+            const int x = xb + j;
+            if (x >= p.width || y >= p.height) continue;
+            const int pi = y * p.width + x;
+            const uint32_t alb = p.albedo[pi];
+            uint4* dst = reinterpret_cast<uint4*>(F.features + size_t(pi) * 32);
+            if (alb == 0u) {
+                for (int q = 0; q < 4; ++q) dst[q] = make_uint4(0, 0, 0, 0);
+                if (F.targets) { F.targets[3 * size_t(pi)] = 0.f; F.targets[3 * size_t(pi) + 1] = 0.f; F.targets[3 * size_t(pi) + 2] = 0.f; }
+                continue;
+            }
+            float P[3], f[32];
+            world_pos(p, x, y, p.depth[pi], P);
+            pixel_features(p, lights, cand, P, p.nx[pi], p.ny[pi], p.nz[pi], alb, f);
+            for (int q = kFeatures; q < 32; ++q) f[q] = 0.0f;
+            uint32_t w[16];
+            for (int q = 0; q < 16; ++q)
+                w[q] = uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(f[2 * q]))) |
+                       (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(f[2 * q + 1]))) << 16);
+            for (int q = 0; q < 4; ++q) dst[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+            if (F.targets) {
+                float rgb[3], base[3];
+                plain_pixel(p, lights, nl, x, y, p.depth[pi], p.nx[pi], p.ny[pi], p.nz[pi], alb, rgb);
+                virtual_light_base(f, base);
+                for (int c = 0; c < 3; ++c) F.targets[3 * size_t(pi) + c] = sqrtf(pos0(rgb[c])) - base[c];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_learned_features(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
+                                    const rsrgpu_light* lights, int nlights, uint16_t* features, float* targets,
+                                    int32_t* candidates, int num_sms, cudaStream_t st) {
+    FeatParams F{};
+    PlainParams& p = F.pl;
+    p.depth = gb.depth; p.nx = gb.normal_x; p.ny = gb.normal_y; p.nz = gb.normal_z; p.albedo = gb.albedo;
+    p.width = gb.width; p.height = gb.height;
+    for (int i = 0; i < 16; ++i) p.ivp[i] = ivp[i];
+    for (int i = 0; i < 3; ++i) p.eye[i] = eye[i];
+    p.lights = lights; p.nlights = nlights;
+    F.features = features; F.targets = targets; F.candidates = candidates;
+    const int tiles = ((gb.width + kShadeTile - 1) / kShadeTile) * ((gb.height + kShadeTile - 1) / kShadeTile);
+    int grid = num_sms * 8;
+    if (grid > tiles) grid = tiles;
+    learned_features_kernel<<<grid, 128, 0, st>>>(F);
     return cudaGetLastError();
 }
 

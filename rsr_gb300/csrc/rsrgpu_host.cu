@@ -38,6 +38,13 @@ cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int n, int
 cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
                                const rsrgpu_light* lights, int nlights, const float background[3],
                                uint32_t* out_srgb, float* out_linear, const uint8_t* srgb_lut, cudaStream_t st);
+cudaError_t launch_learned_features(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
+                                    const rsrgpu_light* lights, int nlights, uint16_t* features, float* targets,
+                                    int32_t* candidates, int num_sms, cudaStream_t st);
+cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
+                                 const rsrgpu_light* lights, int nlights, const float background[3], float max_tile_mse,
+                                 uint32_t* out_srgb, float* out_linear, uint8_t* tile_status, float* tile_mse,
+                                 const uint8_t* srgb_lut, int* error, int num_sms, cudaStream_t st);
 
 static const uint32_t kRcpTable[2048] = {
 #include "rcpps_table.inc"
@@ -97,7 +104,8 @@ struct rsrgpu_ctx {
     // device memory
     DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
         d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs,
-        d_mlp_err;
+        d_mlp_err, d_learn_err;
+    std::map<cudaStream_t, cudaEvent_t> learn_events;   // last learned-shader launch per stream
     int num_sms = 0;
     int* h_mlp_err = nullptr;   // pinned
     uint32_t clip_cap = 1u << 18;
@@ -348,7 +356,8 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     if (ctx->own) cudaStreamSynchronize(ctx->own);
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
-    DevBuf* bufs[] = { &ctx->d_mlp_err, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
+    DevBuf* bufs[] = { &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -938,8 +947,9 @@ int rsrgpu_mlp_forward(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* f
         int rc = check_device_input(ctx, in.p, in.bytes, in.align, in.what);
         if (rc) return rc;
     }
-    if (ctx->num_sms == 0) {
+    if (ctx->num_sms == 0)
         CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+    if (ctx->h_mlp_err == nullptr) {
         CK(ctx->d_mlp_err.ensure(sizeof(int)), "alloc mlp error flag");
         CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_mlp_err), sizeof(int), cudaHostAllocDefault), "alloc pinned flag");
     }
@@ -962,8 +972,9 @@ int check_mlp(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp) {
         int rc = check_device_input(ctx, in.p, in.bytes, in.align, in.what);
         if (rc) return rc;
     }
-    if (ctx->num_sms == 0) {
+    if (ctx->num_sms == 0)
         CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+    if (ctx->h_mlp_err == nullptr) {
         CK(ctx->d_mlp_err.ensure(sizeof(int)), "alloc mlp error flag");
         CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_mlp_err), sizeof(int), cudaHostAllocDefault), "alloc pinned flag");
     }
@@ -1010,6 +1021,103 @@ int rsrgpu_mlp_adam(rsrgpu_ctx* ctx, float* params, const float* grad, float* m,
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
     CK(launch_adam(params, grad, m, v, RSRGPU_MLP_PARAMS, RSRGPU_MLP_WEIGHTS, lr, 0.9f, 0.999f, 1e-8f, step,
                    weights_bf16, biases, st), "adam_kernel");
+    return 0;
+}
+
+namespace {
+// device G-buffer planes and lights of a deferred call, checked for size
+int check_gbuffer(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gb, const rsrgpu_light* lights, int nlights) {
+    if (nlights < 0 || nlights > 256) return fail(ctx, RSRGPU_EINVAL, "0..256 lights");
+    if (gb->width <= 0 || gb->height <= 0) return fail(ctx, RSRGPU_EINVAL, "empty G-buffer");
+    const size_t npx = size_t(gb->width) * size_t(gb->height);
+    struct { const void* p; size_t bytes; size_t align; const char* what; } ins[] = {
+        { gb->depth, npx * 4, 4, "G-buffer depth" }, { gb->normal_x, npx * 2, 2, "G-buffer normal x" },
+        { gb->normal_y, npx * 2, 2, "G-buffer normal y" }, { gb->normal_z, npx * 2, 2, "G-buffer normal z" },
+        { gb->albedo, npx * 4, 4, "G-buffer albedo" }, { lights, size_t(nlights) * sizeof(rsrgpu_light), 4, "lights" } };
+    for (const auto& in : ins) {
+        if (in.bytes == 0) continue;
+        int rc = check_device_input(ctx, in.p, in.bytes, in.align, in.what);
+        if (rc) return rc;
+    }
+    return 0;
+}
+int check_device_output(rsrgpu_ctx* ctx, void* p, size_t need, size_t align, const char* what) {
+    if (p == nullptr) return 0;
+    void* dp = nullptr;
+    size_t avail = 0;
+    int rc = resolve(ctx, p, true, &dp, what, &avail);
+    if (rc) return rc;
+    if (dp != p || avail < need || (reinterpret_cast<uintptr_t>(p) % align))
+        return fail(ctx, RSRGPU_EINVAL, "%s: device pointer with %zu bytes, %zu-byte aligned, needed", what, need, align);
+    return 0;
+}
+}  // namespace
+
+int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gbuffer* gbuffer,
+                         const float inv_view_proj[16], const float eye[3], const rsrgpu_light* lights, int nlights,
+                         const float background[3], float max_tile_mse, uint32_t* out_srgb, float* out_linear,
+                         uint8_t* tile_status, float* tile_mse, void* stream) {
+    if (ctx == nullptr || mlp == nullptr || gbuffer == nullptr || inv_view_proj == nullptr || eye == nullptr ||
+        background == nullptr)
+        return RSRGPU_EINVAL;
+    if (max_tile_mse != max_tile_mse) return fail(ctx, RSRGPU_EINVAL, "max_tile_mse is NaN");
+    int rc = check_mlp(ctx, mlp);
+    if (rc) return rc;
+    rc = check_gbuffer(ctx, gbuffer, lights, nlights);
+    if (rc) return rc;
+    const size_t npx = size_t(gbuffer->width) * size_t(gbuffer->height);
+    const size_t tiles = size_t((gbuffer->width + RSRGPU_SHADE_TILE - 1) / RSRGPU_SHADE_TILE) *
+                         size_t((gbuffer->height + RSRGPU_SHADE_TILE - 1) / RSRGPU_SHADE_TILE);
+    if ((rc = check_device_output(ctx, out_srgb, npx * 4, 4, "sRGB output")) ||
+        (rc = check_device_output(ctx, out_linear, npx * 12, 4, "linear output")) ||
+        (rc = check_device_output(ctx, tile_status, tiles, 1, "tile status")) ||
+        (rc = check_device_output(ctx, tile_mse, tiles * 4, 4, "tile mse")))
+        return rc;
+    if (ctx->d_learn_err.p == nullptr) {
+        CK(ctx->d_learn_err.ensure(sizeof(int)), "alloc learned-shader error flag");
+        CK(cudaMemset(ctx->d_learn_err.p, 0, sizeof(int)), "clear learned-shader error flag");
+    }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_shade_learned(*mlp, *gbuffer, inv_view_proj, eye, lights, nlights, background, max_tile_mse, out_srgb,
+                            out_linear, tile_status, tile_mse, ctx->d_srgb.as<uint8_t>(), ctx->d_learn_err.as<int>(),
+                            ctx->num_sms, st), "shade_learned_kernel");
+    cudaEvent_t& ev = ctx->learn_events[st];
+    if (ev == nullptr) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "learned-shader event");
+    CK(cudaEventRecord(ev, st), "learned-shader event record");
+    return 0;
+}
+
+int rsrgpu_shade_learned_check(rsrgpu_ctx* ctx) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (ctx->d_learn_err.p == nullptr) return 0;
+    for (auto& kv : ctx->learn_events) CK(cudaEventSynchronize(kv.second), "learned shader sync");
+    int flag = 0;
+    CK(cudaMemcpy(&flag, ctx->d_learn_err.p, sizeof(int), cudaMemcpyDeviceToHost), "D2H learned-shader error");
+    if (flag == 0) return 0;
+    CK(cudaMemset(ctx->d_learn_err.p, 0, sizeof(int)), "clear learned-shader error flag");
+    return fail(ctx, RSRGPU_ETIMEOUT, "tensor-core MMA did not complete in the learned shader (bounded wait expired)");
+}
+
+int rsrgpu_learned_features(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const float inv_view_proj[16],
+                            const float eye[3], const rsrgpu_light* lights, int nlights, uint16_t* features,
+                            float* targets, int32_t* candidates, void* stream) {
+    if (ctx == nullptr || gbuffer == nullptr || inv_view_proj == nullptr || eye == nullptr || features == nullptr)
+        return RSRGPU_EINVAL;
+    int rc = check_gbuffer(ctx, gbuffer, lights, nlights);
+    if (rc) return rc;
+    const size_t npx = size_t(gbuffer->width) * size_t(gbuffer->height);
+    const size_t tiles = size_t((gbuffer->width + RSRGPU_SHADE_TILE - 1) / RSRGPU_SHADE_TILE) *
+                         size_t((gbuffer->height + RSRGPU_SHADE_TILE - 1) / RSRGPU_SHADE_TILE);
+    if ((rc = check_device_output(ctx, features, npx * 64, 16, "features")) ||
+        (rc = check_device_output(ctx, targets, npx * 12, 4, "targets")) ||
+        (rc = check_device_output(ctx, candidates, tiles * 32, 4, "candidates")))
+        return rc;
+    if (ctx->num_sms == 0)
+        CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_learned_features(*gbuffer, inv_view_proj, eye, lights, nlights, features, targets, candidates,
+                               ctx->num_sms, st), "learned_features_kernel");
+    CK(cudaStreamSynchronize(st), "learned features sync");
     return 0;
 }
 

@@ -1,0 +1,226 @@
+// rsrgpu_shading.cuh -- per-pixel deferred shading math shared by the plain
+// multi-light shader, the learned shader's feature builder and its per-tile
+// fallback.  rsr has no deferred or multi-light path; these functions are
+// this library's definition, restated on the CPU in oracle/rsr_oracle.c.
+// Every file including this header is built with -fmad=false, so each
+// expression rounds once per operation in the written order and the GPU
+// matches the CPU restatement bit for bit.
+#pragma once
+#include <cstdint>
+#include <cuda_fp16.h>
+
+#include "../../include/rsrgpu.h"
+
+namespace rsrgpu {
+
+constexpr int kMaxLights = 256;
+constexpr int kShadeTile = 32;     // learned shader: light-candidate and gate tile (pixels)
+constexpr int kCandidates = 8;     // candidate lights per shading tile
+constexpr int kFeatures = 24;      // learned-shader input features per pixel
+
+struct PlainParams {
+    const float* depth;
+    const uint16_t* nx;
+    const uint16_t* ny;
+    const uint16_t* nz;
+    const uint32_t* albedo;
+    int width, height;
+    float ivp[16];
+    float eye[3];
+    float background[3];
+    const rsrgpu_light* lights;
+    int nlights;
+    uint32_t* out_srgb;
+    float* out_linear;
+    const uint8_t* srgb_lut;
+};
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return (ax * bx + ay * by) + az * bz;
+}
+__device__ __forceinline__ float pos0(float x) { return x > 0.0f ? x : 0.0f; }
+__device__ __forceinline__ uint32_t srgb8_lut(const uint8_t* __restrict__ lut, float v) {
+    const float lo = __uint_as_float((127u - 13u) << 23), hi = __uint_as_float(0x3f7fffffu);
+    float c = v > lo ? v : lo;
+    c = c < hi ? c : hi;
+    return __ldg(lut + ((__float_as_uint(c) >> 12) - ((127u - 13u) << 11)));
+}
+__device__ __forceinline__ uint32_t pack_srgb(const uint8_t* lut, const float rgb[3]) {
+    return (srgb8_lut(lut, rgb[0]) << 16) | (srgb8_lut(lut, rgb[1]) << 8) | srgb8_lut(lut, rgb[2]);
+}
+
+// pixel centre -> NDC -> world through the column-major inverse view-projection
+__device__ __forceinline__ void world_pos(const PlainParams& p, int x, int y, float z, float P[3]) {
+    const float ndcx = (2.0f * (float(x) + 0.5f)) / float(p.width) - 1.0f;
+    const float ndcy = 1.0f - (2.0f * (float(y) + 0.5f)) / float(p.height);
+    const float* m = p.ivp;
+    const float cx = ((m[0] * ndcx + m[4] * ndcy) + m[8] * z) + m[12];
+    const float cy = ((m[1] * ndcx + m[5] * ndcy) + m[9] * z) + m[13];
+    const float cz = ((m[2] * ndcx + m[6] * ndcy) + m[10] * z) + m[14];
+    const float cw = ((m[3] * ndcx + m[7] * ndcy) + m[11] * z) + m[15];
+    P[0] = cx / cw; P[1] = cy / cw; P[2] = cz / cw;
+}
+
+// unit normal from the fp16 planes, unit view vector and its length
+__device__ __forceinline__ void surface(const PlainParams& p, const float P[3], uint16_t hx, uint16_t hy, uint16_t hz,
+                                        float n[3], float v[3], float& vlen) {
+    n[0] = __half2float(__ushort_as_half(hx)); n[1] = __half2float(__ushort_as_half(hy)); n[2] = __half2float(__ushort_as_half(hz));
+    const float nlen = sqrtf(dot3(n[0], n[1], n[2], n[0], n[1], n[2]));
+    n[0] = n[0] / nlen; n[1] = n[1] / nlen; n[2] = n[2] / nlen;
+    v[0] = p.eye[0] - P[0]; v[1] = p.eye[1] - P[1]; v[2] = p.eye[2] - P[2];
+    vlen = sqrtf(dot3(v[0], v[1], v[2], v[0], v[1], v[2]));
+    v[0] = v[0] / vlen; v[1] = v[1] / vlen; v[2] = v[2] / vlen;
+}
+
+__device__ __forceinline__ void albedo_rgb(uint32_t alb, float a[3]) {
+    a[0] = float(alb & 255u) / 255.0f; a[1] = float((alb >> 8) & 255u) / 255.0f; a[2] = float((alb >> 16) & 255u) / 255.0f;
+}
+
+// Blinn-Phong sum over lights first, first+step, ... < nl:
+// att = (1 - d/r)^2, diffuse max(N.L,0)*albedo, specular max(N.H,0)^32
+__device__ __forceinline__ void plain_sum(const rsrgpu_light* L, int first, int step, int nl, const float P[3],
+                                          const float n[3], const float v[3], const float a[3], float s[3]) {
+    for (int i = first; i < nl; i += step) {
+        float lx = L[i].position[0] - P[0], ly = L[i].position[1] - P[1], lz = L[i].position[2] - P[2];
+        const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
+        const float r = L[i].radius;
+        if (!(d < r)) continue;
+        lx = lx / d; ly = ly / d; lz = lz / d;
+        const float t = 1.0f - d / r;
+        const float att = t * t;
+        const float ndl = pos0(dot3(n[0], n[1], n[2], lx, ly, lz));
+        float hx = lx + v[0], hy = ly + v[1], hz = lz + v[2];
+        const float hlen = sqrtf(dot3(hx, hy, hz, hx, hy, hz));
+        hx = hx / hlen; hy = hy / hlen; hz = hz / hlen;
+        float sp = pos0(dot3(n[0], n[1], n[2], hx, hy, hz));
+        sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
+        s[0] = s[0] + (L[i].color[0] * att) * (a[0] * ndl + sp);
+        s[1] = s[1] + (L[i].color[1] * att) * (a[1] * ndl + sp);
+        s[2] = s[2] + (L[i].color[2] * att) * (a[2] * ndl + sp);
+    }
+}
+
+// Multi-light Blinn-Phong for one pixel plus ambient 0.03 * albedo; linear RGB.
+__device__ __forceinline__ void plain_pixel(const PlainParams& p, const rsrgpu_light* L, int nl, int x, int y,
+                                            float z, uint16_t hx, uint16_t hy, uint16_t hz, uint32_t alb,
+                                            float rgb[3]) {
+    float P[3], n[3], v[3], vlen, a[3];
+    world_pos(p, x, y, z, P);
+    surface(p, P, hx, hy, hz, n, v, vlen);
+    albedo_rgb(alb, a);
+    float s[3] = { 0.0f, 0.0f, 0.0f };
+    plain_sum(L, 0, 1, nl, P, n, v, a, s);
+    rgb[0] = s[0] + 0.03f * a[0];
+    rgb[1] = s[1] + 0.03f * a[1];
+    rgb[2] = s[2] + 0.03f * a[2];
+}
+
+// ---- learned shader inputs ----
+// Candidate score of a light for a shading tile whose covered pixels span the
+// world-space box [b0, b1]: (1 - d/r)^2 * (r + g + b) at the box point nearest
+// the light, or -1 when the light cannot reach the box.
+__device__ __forceinline__ float light_score(const rsrgpu_light& l, const float b0[3], const float b1[3]) {
+    float e[3];
+    for (int k = 0; k < 3; ++k) {
+        const float c = fminf(fmaxf(l.position[k], b0[k]), b1[k]);
+        e[k] = l.position[k] - c;
+    }
+    const float d = sqrtf(dot3(e[0], e[1], e[2], e[0], e[1], e[2]));
+    if (!(d < l.radius)) return -1.0f;
+    const float t = 1.0f - d / l.radius;
+    return (t * t) * ((l.color[0] + l.color[1]) + l.color[2]);
+}
+
+// Warp-wide choice of the tile's candidates: up to kCandidates lights in
+// descending score (ties to the lower index), only scores > 0; -1 pads.
+// score(i) is evaluated for i < nl by the calling warp.
+template <typename Score>
+__device__ __forceinline__ void select_candidates(int nl, Score score, int* cand) {
+    const int lane = threadIdx.x & 31;
+    float s[kMaxLights / 32];
+#pragma unroll
+    for (int j = 0; j < kMaxLights / 32; ++j) {
+        const int i = lane + 32 * j;
+        s[j] = i < nl ? score(i) : -1.0f;
+    }
+    for (int c = 0; c < kCandidates; ++c) {
+        float bs = 0.0f;
+        int bi = -1;
+#pragma unroll
+        for (int j = 0; j < kMaxLights / 32; ++j)
+            if (s[j] > bs) { bs = s[j]; bi = lane + 32 * j; }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float os = __shfl_xor_sync(0xffffffffu, bs, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (oi >= 0 && (bi < 0 || os > bs || (os == bs && oi < bi))) { bs = os; bi = oi; }
+        }
+        if (lane == 0) cand[c] = bi;
+        if (bi >= 0 && (bi & 31) == lane) {
+#pragma unroll
+            for (int j = 0; j < kMaxLights / 32; ++j)
+                if (lane + 32 * j == bi) s[j] = -1.0f;
+        }
+    }
+}
+
+// The 24 input features of one covered pixel:
+//   0-2 unit normal, 3-5 unit view vector, 6-8 albedo, 9 eye distance / 50,
+//   and a summary of the candidate lights that reach the pixel, each with
+//   colour c * att (att = (1 - d/r)^2), weight w = c.r + c.g + c.b (of c * att)
+//   and unit direction L:
+//   10-12 sum c*att, 13-15 sum w L, 16-21 sum w L L^T (xx xy xz yy yz zz),
+//   22 sum w max(N.L, 0), 23 sum w (d/r) / sum w (0 without lights)
+__device__ __forceinline__ void pixel_features(const PlainParams& p, const rsrgpu_light* L, const int* cand,
+                                               const float P[3], uint16_t hx, uint16_t hy, uint16_t hz,
+                                               uint32_t alb, float f[kFeatures]) {
+    float n[3], v[3], vlen, a[3];
+    surface(p, P, hx, hy, hz, n, v, vlen);
+    albedo_rgb(alb, a);
+    for (int k = 0; k < 3; ++k) { f[k] = n[k]; f[3 + k] = v[k]; f[6 + k] = a[k]; }
+    f[9] = vlen / 50.0f;
+    for (int k = 10; k < kFeatures; ++k) f[k] = 0.0f;
+    float wsum = 0.0f;
+    for (int c = 0; c < kCandidates; ++c) {
+        const int li = cand[c];
+        if (li < 0) break;
+        const rsrgpu_light& l = L[li];
+        float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
+        const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
+        if (!(d < l.radius)) continue;
+        const float q = d / l.radius;
+        const float t = 1.0f - q;
+        const float att = t * t;
+        const float cr = l.color[0] * att, cg = l.color[1] * att, cb = l.color[2] * att;
+        const float w = (cr + cg) + cb;
+        lx = lx / d; ly = ly / d; lz = lz / d;
+        const float wx = w * lx, wy = w * ly, wz = w * lz;
+        f[10] = f[10] + cr; f[11] = f[11] + cg; f[12] = f[12] + cb;
+        f[13] = f[13] + wx; f[14] = f[14] + wy; f[15] = f[15] + wz;
+        f[16] = f[16] + wx * lx; f[17] = f[17] + wx * ly; f[18] = f[18] + wx * lz;
+        f[19] = f[19] + wy * ly; f[20] = f[20] + wy * lz; f[21] = f[21] + wz * lz;
+        f[22] = f[22] + w * pos0(dot3(n[0], n[1], n[2], lx, ly, lz));
+        f[23] = f[23] + w * q;
+        wsum = wsum + w;
+    }
+    f[23] = wsum > 0.0f ? f[23] / wsum : 0.0f;
+}
+
+// The learned shader's analytic base, computed from the FP32 features: one
+// virtual light with direction sum w L (normalised) and colour sum c * att,
+// Blinn-Phong (exponent 32) plus ambient 0.03 * albedo; base = its square
+// root per channel.  The network adds its output to base, so it learns the
+// residual sqrt(plain) - base.
+__device__ __forceinline__ void virtual_light_base(const float f[kFeatures], float base[3]) {
+    const float dlen = sqrtf(dot3(f[13], f[14], f[15], f[13], f[14], f[15]));
+    float l[3] = { 0.0f, 0.0f, 0.0f };
+    if (dlen > 0.0f) { l[0] = f[13] / dlen; l[1] = f[14] / dlen; l[2] = f[15] / dlen; }
+    float h[3] = { l[0] + f[3], l[1] + f[4], l[2] + f[5] };
+    const float hlen = sqrtf(dot3(h[0], h[1], h[2], h[0], h[1], h[2]));
+    if (hlen > 0.0f) { h[0] = h[0] / hlen; h[1] = h[1] / hlen; h[2] = h[2] / hlen; }
+    const float ndl = pos0(dot3(f[0], f[1], f[2], l[0], l[1], l[2]));
+    float sp = pos0(dot3(f[0], f[1], f[2], h[0], h[1], h[2]));
+    sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
+    for (int c = 0; c < 3; ++c) base[c] = sqrtf(pos0(f[10 + c] * (f[6 + c] * ndl + sp) + 0.03f * f[6 + c]));
+}
+
+}  // namespace rsrgpu

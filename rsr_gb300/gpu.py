@@ -161,6 +161,41 @@ class GPU:
         self._check(self.lib.rsrgpu_mlp_adam(self.ctx, vp(params), vp(grad), vp(m), vp(v), int(step), float(lr),
                                              vp(wbf16), vp(biases), ctypes.c_void_p(stream) if stream else None))
 
+    @staticmethod
+    def _mlp_c(weights):
+        return abi.MlpC(*[weights[k].data_ptr() for k in ("w1", "w2", "w3", "w4", "b1", "b2", "b3", "b4")])
+
+    @staticmethod
+    def _gbuffer_c(gbuf, width, height):
+        return abi.GBufferC(gbuf["depth"].data_ptr(), gbuf["nx"].data_ptr(), gbuf["ny"].data_ptr(),
+                            gbuf["nz"].data_ptr(), gbuf["albedo"].data_ptr(), width, height)
+
+    def shade_learned(self, weights, gbuf, width, height, ivp, eye, lights, background=(0.0, 0.0, 0.0),
+                      max_tile_mse=6.5025, out_srgb=None, out_linear=None, tile_status=None, tile_mse=None,
+                      stream=None):
+        """Fused learned deferred shading (rsrgpu_shade_learned); device tensors.
+        Enqueues only: call shade_learned_check() (or synchronise) before reading."""
+        fa = lambda a: (ctypes.c_float * len(a))(*[float(x) for x in a])
+        vp = lambda t: ctypes.c_void_p(t.data_ptr() if t is not None else None)
+        m, g = self._mlp_c(weights), self._gbuffer_c(gbuf, width, height)
+        self._check(self.lib.rsrgpu_shade_learned(
+            self.ctx, ctypes.byref(m), ctypes.byref(g), fa(ivp), fa(eye), vp(lights), lights.shape[0], fa(background),
+            float(max_tile_mse), vp(out_srgb), vp(out_linear), vp(tile_status), vp(tile_mse),
+            ctypes.c_void_p(stream) if stream else None))
+
+    def shade_learned_check(self):
+        self._check(self.lib.rsrgpu_shade_learned_check(self.ctx))
+
+    def learned_features(self, gbuf, width, height, ivp, eye, lights, features, targets=None, candidates=None,
+                         stream=None):
+        """rsrgpu_learned_features: dense BF16 features (H*W, 32), optional targets and candidates."""
+        fa = lambda a: (ctypes.c_float * len(a))(*[float(x) for x in a])
+        vp = lambda t: ctypes.c_void_p(t.data_ptr() if t is not None else None)
+        g = self._gbuffer_c(gbuf, width, height)
+        self._check(self.lib.rsrgpu_learned_features(
+            self.ctx, ctypes.byref(g), fa(ivp), fa(eye), vp(lights), lights.shape[0], vp(features), vp(targets),
+            vp(candidates), ctypes.c_void_p(stream) if stream else None))
+
     def stats(self):
         s = abi.StatsC()
         self._check(self.lib.rsrgpu_get_stats(self.ctx, ctypes.byref(s)))

@@ -421,7 +421,7 @@ def _morton3(p):
 
 
 def deferred_scene(nobj=2_000_000, seed=3, width=1920, height=1080, tile_blocks=(4, 4),
-                   size=(0.05, 0.15), sphere_every=8, nlights=64, gouraud=False):
+                   size=(0.05, 0.15), sphere_every=8, nlights=64, gouraud=False, arrays=None):
     """Config-3 G-buffer scene: nobj objects in [-10,10]^3 with random
     orientation and size (every sphere_every-th one an icosahedron with
     smooth normals, the others cubes with flat normals), random RGB albedo,
@@ -430,7 +430,12 @@ def deferred_scene(nobj=2_000_000, seed=3, width=1920, height=1080, tile_blocks=
     at the origin with a 60 degree field of view; plus nlights point lights
     (position in the box, colour in [0,1], radius in [2,6]).  gouraud=True
     draws the same geometry with the Gouraud test program (normals as colour)
-    and ordinary colour/depth stores, so rsr itself can render it."""
+    and ordinary colour/depth stores, so rsr itself can render it.
+    arrays: the vertex arrays of an earlier call with the same seed and
+    sizes (scene.arrays), which skips rebuilding them."""
+    if arrays is not None:
+        return _deferred_scene_record(arrays, None, None, None, nobj, seed, width, height, tile_blocks,
+                                      sphere_every, nlights, gouraud)
     u = uniform01(seed, nobj * 10).reshape(nobj, 10)
     centre = lerp(-10.0, 10.0, u[:, 0:3]).astype(np.float64)
     rot = _random_rotations(u[:, 3:6])
@@ -438,17 +443,32 @@ def deferred_scene(nobj=2_000_000, seed=3, width=1920, height=1080, tile_blocks=
     rgb = np.clip((lerp(0.2, 1.0, u[:, 7:10]) * 255.0).astype(np.int64), 0, 255)
     order = np.argsort(_morton3(centre), kind="stable")
     centre, rot, scale, rgb = centre[order], rot[order], scale[order], rgb[order]
+    return _deferred_scene_record(None, centre, rot, (scale, rgb), nobj, seed, width, height, tile_blocks,
+                                  sphere_every, nlights, gouraud)
+
+
+def _deferred_scene_record(arrays, centre, rot, scale_rgb, nobj, seed, width, height, tile_blocks,
+                           sphere_every, nlights, gouraud):
     is_sphere = (np.arange(nobj) % sphere_every) == sphere_every - 1
     cpos, cnrm, ctri = _cube_mesh()
     iverts, ifaces = icosphere(0)
     ipos, inrm = iverts.astype(np.float64) * 0.6, iverts.astype(np.float64)
-    arrays, draws = {}, []
+    build = arrays is None
+    if build:
+        arrays = {}
+        scale, rgb = scale_rgb
+    draws = []
     for kind, mpos, mnrm, mtri, sel in (("c", cpos, cnrm, ctri, ~is_sphere), ("s", ipos, inrm, ifaces, is_sphere)):
         n = int(sel.sum())
         if n == 0:
             continue
         nv = len(mpos)
         per_draw = 32760 // nv
+        for first in range(0, n, per_draw):
+            cnt = min(per_draw, n - first)
+            draws.append((kind, first * nv, cnt * len(mtri) * 3))
+        if not build:
+            continue
         wp = np.einsum("oij,vj->ovi", rot[sel], mpos) * scale[sel][:, None, None] + centre[sel][:, None, :]
         wn = np.einsum("oij,vj->ovi", rot[sel], mnrm)
         alb = (rgb[sel][:, 0] | (rgb[sel][:, 1] << 8) | (rgb[sel][:, 2] << 16)).astype(np.float32)
@@ -457,9 +477,6 @@ def deferred_scene(nobj=2_000_000, seed=3, width=1920, height=1080, tile_blocks=
             arrays["%s_n%s" % (kind, c)] = pad4(wn[:, :, k].reshape(-1).astype(np.float32))
         arrays["%s_alb" % kind] = pad4(np.repeat(alb, nv))
         arrays["%s_idx" % kind] = (np.arange(per_draw)[:, None, None] * nv + mtri[None]).reshape(-1).astype(np.uint16)
-        for first in range(0, n, per_draw):
-            cnt = min(per_draw, n - first)
-            draws.append((kind, first * nv, cnt * len(mtri) * 3))
     lu = uniform01(seed + 101, nlights * 7).reshape(nlights, 7)
     lights = np.zeros((nlights, 8), np.float32)
     lights[:, 0:3] = lerp(-10.0, 10.0, lu[:, 0:3])

@@ -1,0 +1,318 @@
+"""Learned deferred shader: inputs, gate and fallback, inference, training gain.
+
+Bars:
+  * features (BF16), training targets and per-tile candidate lights: bit-exact
+    against the oracle's restatement (oracle/rsr_oracle.c) on the same G-buffer
+  * every tile forced to the plain fallback: bit-exact with rsrgpu_shade_plain
+  * no fallback: the fused kernel's network output against a CPU forward that
+    rounds where the kernel does (BF16 inputs, weights, hidden activations;
+    FP32 sums), 2e-2 absolute in sqrt(linear RGB)
+  * mixed: fallback tiles bit-exact plain, the others equal to the no-fallback
+    run, and the gate's decision consistent with its estimate
+  * zero output layer: exactly the analytic virtual-light base
+  * training on the GPU: the trained network beats the untrained one (the
+    non-learned virtual-light method on the same inputs) on held-out seeds
+"""
+import numpy as np
+import pytest
+
+from rsr_gb300 import scenes
+
+W, H = 640, 360
+
+
+def _gbuffer_scene(seed, nobj=300_000, width=W, height=H):
+    return scenes.deferred_scene(seed=seed, nobj=nobj, width=width, height=height)
+
+
+def _oracle_gbuffer(sc):
+    import oracle
+    cpu = oracle.CpuRenderer("oracle")
+    return cpu, cpu.render_gbuffer(sc)
+
+
+# ---------------------------------------------------------------- CPU (oracle)
+def test_oracle_feature_properties(built):
+    """Size-independent properties of the feature definition (oracle only)."""
+    sc = _gbuffer_scene(21, nobj=100_000)
+    cpu, g = _oracle_gbuffer(sc)
+    out = cpu.learned_features(g, W, H, sc.ivp, sc.eye, sc.lights)
+    f, cov = out["f32"], g["albedo"] != 0
+    assert cov.any() and (~cov).any()
+    assert not f[~cov].any() and not out["bf16"][~cov].any() and not out["targets"][~cov].any()
+    fc = f[cov]
+    assert np.allclose(np.linalg.norm(fc[:, 0:3], axis=1), 1, atol=1e-5)
+    assert np.allclose(np.linalg.norm(fc[:, 3:6], axis=1), 1, atol=1e-5)
+    wsum = fc[:, 10:13].sum(1)
+    # trace of sum w L L^T is sum w (unit L); |sum w L| <= sum w; cos-weighted sum <= sum w
+    assert np.allclose(fc[:, 16] + fc[:, 19] + fc[:, 21], wsum, rtol=1e-4, atol=1e-6)
+    assert (np.linalg.norm(fc[:, 13:16], axis=1) <= wsum * (1 + 1e-5) + 1e-6).all()
+    assert (fc[:, 22] <= wsum * (1 + 1e-5) + 1e-6).all()
+    assert ((fc[:, 23] >= 0) & (fc[:, 23] < 1)).all()
+    # BF16 columns are the round-to-nearest-even of the FP32 ones
+    import torch
+    want = torch.from_numpy(f).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
+    assert np.array_equal(out["bf16"][:, :24], want) and not out["bf16"][:, 24:].any()
+    # candidates: descending score, distinct, -1 only as padding
+    cand = out["candidates"]
+    for row in cand:
+        valid = row[row >= 0]
+        assert len(set(valid.tolist())) == len(valid)
+        assert (row[len(valid):] == -1).all()
+    assert (cand[:, 0] >= 0).any()
+
+
+def test_oracle_targets_are_residual_of_plain(built):
+    """targets = sqrt(plain) - base, base = sqrt of the virtual-light estimate."""
+    sc = _gbuffer_scene(22, nobj=100_000)
+    cpu, g = _oracle_gbuffer(sc)
+    out = cpu.learned_features(g, W, H, sc.ivp, sc.eye, sc.lights)
+    plain = cpu.shade_plain(g, W, H, sc.ivp, sc.eye, sc.lights)
+    cov = g["albedo"] != 0
+    want = np.sqrt(np.maximum(plain[cov], 0)).astype(np.float32) - out["base"][cov]
+    assert np.array_equal(out["targets"][cov], want)
+    # base against an independent float64 evaluation of the virtual light
+    f = out["f32"][cov].astype(np.float64)
+    n, v, a, E, D = f[:, 0:3], f[:, 3:6], f[:, 6:9], f[:, 10:13], f[:, 13:16]
+    dl = np.linalg.norm(D, axis=1, keepdims=True)
+    l = np.where(dl > 0, D / np.where(dl > 0, dl, 1), 0)
+    h = l + v
+    h /= np.linalg.norm(h, axis=1, keepdims=True)
+    ndl = np.maximum((n * l).sum(1, keepdims=True), 0)
+    sp = np.maximum((n * h).sum(1, keepdims=True), 0) ** 32
+    base = np.sqrt(np.maximum(E * (a * ndl + sp) + 0.03 * a, 0))
+    assert np.allclose(out["base"][cov], base, atol=2e-5, rtol=1e-4)
+    assert not out["base"][~cov].any()
+
+
+# ---------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def gpu(built):
+    from rsr_gb300.gpu import GPU
+    g = GPU(0)
+    g.InstallDefaults()
+    yield g
+    g.close()
+
+
+@pytest.fixture(scope="module")
+def frame(gpu):
+    """A 640x360 deferred frame rendered on the GPU, its host copy and oracle inputs."""
+    from rsr_gb300.learned import DeferredFrame
+    fr = DeferredFrame(gpu, 5, W, H, nobj=300_000)
+    host = {k: v.cpu().numpy() for k, v in fr.gbuf.items()}
+    host = {"depth": host["depth"], "nx": host["nx"].view(np.uint16), "ny": host["ny"].view(np.uint16),
+            "nz": host["nz"].view(np.uint16), "albedo": host["albedo"].view(np.uint32)}
+    import oracle
+    cpu = oracle.CpuRenderer("oracle")
+    ref = cpu.learned_features(host, W, H, fr.ivp, fr.eye, fr.lights_np)
+    ref["plain"] = cpu.shade_plain(host, W, H, fr.ivp, fr.eye, fr.lights_np)
+    return fr, host, ref
+
+
+def _net(seed, zero_output=False):
+    """A network with random weights (the output layer too, unless zero_output)."""
+    from rsr_gb300.learned import LearnedShader, OFFSETS, init_params
+    p = init_params(seed)
+    if not zero_output:
+        rng = np.random.default_rng(seed + 1000)
+        o, _ = OFFSETS["w4"]
+        w4 = np.zeros((16, 64), np.float32); w4[:3] = rng.standard_normal((3, 64)) * 0.125
+        p[o:o + 1024] = w4.reshape(-1)
+        o, _ = OFFSETS["b4"]
+        p[o:o + 3] = rng.standard_normal(3) * 0.05
+    return LearnedShader(params=p)
+
+
+def _shade(gpu, fr, net, thr):
+    import torch
+    n = W * H
+    srgb = torch.zeros(n, dtype=torch.int32, device="cuda")
+    lin = torch.zeros(n, 3, dtype=torch.float32, device="cuda")
+    status = torch.full((fr.ntiles,), 255, dtype=torch.uint8, device="cuda")
+    mse = torch.zeros(fr.ntiles, dtype=torch.float32, device="cuda")
+    fr.shade_learned(gpu, net, thr, srgb, lin, status, mse)
+    gpu.shade_learned_check()
+    return srgb.cpu().numpy().view(np.uint32), lin.cpu().numpy(), status.cpu().numpy(), mse.cpu().numpy()
+
+
+def _plain(gpu, fr):
+    import torch
+    n = W * H
+    srgb = torch.zeros(n, dtype=torch.int32, device="cuda")
+    lin = torch.zeros(n, 3, dtype=torch.float32, device="cuda")
+    fr.shade_plain(gpu, srgb, lin)
+    torch.cuda.synchronize()
+    return srgb.cpu().numpy().view(np.uint32), lin.cpu().numpy()
+
+
+def _tile_of_pixel():
+    y, x = np.divmod(np.arange(W * H), W)
+    return (y // 32) * ((W + 31) // 32) + x // 32
+
+
+@pytest.mark.gpu
+def test_features_targets_candidates_bitexact(gpu, frame):
+    import torch
+    fr, host, ref = frame
+    n = W * H
+    f = torch.zeros(n, 32, dtype=torch.bfloat16, device="cuda")
+    t = torch.zeros(n, 3, dtype=torch.float32, device="cuda")
+    c = torch.zeros(fr.ntiles, 8, dtype=torch.int32, device="cuda")
+    gpu.learned_features(fr.gbuf, W, H, fr.ivp, fr.eye, fr.lights, f, t, c)
+    assert np.array_equal(c.cpu().numpy(), ref["candidates"])
+    got = f.view(torch.int16).cpu().numpy().view(np.uint16)
+    bad = np.nonzero((got != ref["bf16"]).any(1))[0]
+    assert len(bad) == 0, "features differ in %d pixels, first %d" % (len(bad), bad[0])
+    assert np.array_equal(t.cpu().numpy().view(np.uint32), ref["targets"].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_plain_shader_matches_oracle_here(gpu, frame):
+    fr, host, ref = frame
+    _, lin = _plain(gpu, fr)
+    assert np.array_equal(lin.view(np.uint32), ref["plain"].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_all_tiles_fallback_is_plain_bitexact(gpu, frame):
+    fr, host, ref = frame
+    ps, pl = _plain(gpu, fr)
+    s, lin, status, _ = _shade(gpu, fr, _net(1), -1.0)
+    assert np.array_equal(s, ps)
+    assert np.array_equal(lin.view(np.uint32), pl.view(np.uint32))
+    cov_tiles = np.bincount(_tile_of_pixel()[host["albedo"] != 0], minlength=fr.ntiles) > 0
+    assert (status[cov_tiles] == 1).all() and (status[~cov_tiles] == 2).all()
+
+
+def _bf16(x):
+    import torch
+    return torch.as_tensor(x, dtype=torch.float32).to(torch.bfloat16).to(torch.float32)
+
+
+def _reference_forward(params, feat_bf16_bits, base):
+    """CPU forward rounding where the kernel does; returns max(y + base, 0) (sqrt RGB)."""
+    import torch
+    from rsr_gb300.learned import OFFSETS
+    p = torch.from_numpy(params)
+    w = {k: p[o:o + int(np.prod(s))].reshape(s) for k, (o, s) in OFFSETS.items()}
+    h = torch.from_numpy(feat_bf16_bits.view(np.int16)).view(torch.bfloat16).float()
+    for k in ("1", "2", "3"):
+        h = _bf16(torch.relu(h @ _bf16(w["w" + k]).T + w["b" + k]))
+    return torch.relu((h @ _bf16(w["w4"]).T + w["b4"])[:, :3] + torch.from_numpy(base)).numpy()
+
+
+@pytest.mark.gpu
+def test_no_fallback_matches_reference_forward(gpu, frame):
+    fr, host, ref = frame
+    net = _net(2)
+    s, lin, status, _ = _shade(gpu, fr, net, float("inf"))
+    cov = host["albedo"] != 0
+    want = _reference_forward(net.numpy_params(), ref["bf16"][cov], ref["base"][cov])
+    got = np.sqrt(lin[cov])
+    err = np.abs(got - want).max()
+    assert err < 2e-2, "max abs error %g in sqrt(rgb)" % err
+    assert set(np.unique(status).tolist()) <= {0, 2}
+    # uncovered pixels carry the background (0)
+    assert not lin[~cov].any() and not s[~cov].any()
+
+
+@pytest.mark.gpu
+def test_zero_output_layer_is_the_virtual_light_base(gpu, frame):
+    """With a zero output layer the shader computes rgb = base^2 exactly."""
+    fr, host, ref = frame
+    s, lin, status, _ = _shade(gpu, fr, _net(5, zero_output=True), float("inf"))
+    cov = host["albedo"] != 0
+    b = ref["base"][cov]
+    assert np.array_equal(lin[cov].view(np.uint32), (b * b).view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_gate_mixes_learned_and_plain_tiles(gpu, frame):
+    fr, host, ref = frame
+    net = _net(3)
+    ls, ll, _, _ = _shade(gpu, fr, net, float("inf"))
+    ps, pl = _plain(gpu, fr)
+    _, _, _, mse_all = _shade(gpu, fr, net, float("inf"))
+    thr = float(np.median(mse_all[mse_all > 0]))
+    s, lin, status, mse = _shade(gpu, fr, net, thr)
+    assert np.array_equal(mse, mse_all)
+    tile = _tile_of_pixel()
+    fb = status[tile] == 1
+    learned = status[tile] == 0
+    assert fb.any() and learned.any()
+    assert np.array_equal(lin[fb].view(np.uint32), pl[fb].view(np.uint32))
+    assert np.array_equal(lin[learned].view(np.uint32), ll[learned].view(np.uint32))
+    assert ((status == 1) == (mse > thr))[status != 2].all()
+
+
+@pytest.mark.gpu
+def test_gate_estimate_matches_host_recomputation(gpu, frame):
+    """The gate's estimate: mean squared sRGB8 difference over the tile's
+    first min(16, covered) listed pixels (covered grid samples, then the other
+    covered pixels, each in row-major order)."""
+    import torch
+    from rsr_gb300.learned import pack_srgb_torch
+    fr, host, ref = frame
+    net = _net(4)
+    s, lin, status, mse = _shade(gpu, fr, net, float("inf"))
+    from rsr_gb300.learned import srgb8_table
+    lut = torch.from_numpy(srgb8_table())
+    learned_q = pack_srgb_torch(torch.from_numpy(lin), lut).numpy()
+    plain_q = pack_srgb_torch(torch.from_numpy(ref["plain"]), lut).numpy()
+    from rsr_gb300.learned import srgb_channels
+    tx = (W + 31) // 32
+    checked = 0
+    for tile in range(fr.ntiles):
+        x0, y0 = (tile % tx) * 32, (tile // tx) * 32
+        ys, xs = np.mgrid[y0:min(y0 + 32, H), x0:min(x0 + 32, W)]
+        ys, xs = ys.reshape(-1), xs.reshape(-1)
+        pix = ys * W + xs
+        cov = host["albedo"][pix] != 0
+        is_s = ((ys - y0) % 8 == 4) & ((xs - x0) % 8 == 4)
+        order = np.concatenate([pix[cov & is_s], pix[cov & ~is_s]])[:16]
+        if len(order) == 0:
+            assert status[tile] == 2
+            continue
+        d = srgb_channels(learned_q[order]) - srgb_channels(plain_q[order])
+        want = (d ** 2).sum() / (3 * len(order))
+        # the gate's plain reference sums the lights in another order: allow a
+        # one-level sRGB8 flip on one channel of one sample
+        assert abs(mse[tile] - want) <= (2 * np.abs(d).max() + 1) / (3 * len(order)) + 1e-4, (tile, mse[tile], want)
+        checked += 1
+    assert checked > 100
+
+
+@pytest.mark.gpu
+def test_training_gains_over_the_virtual_light_method(gpu):
+    """Trains on sixteen 640x360 frames (seeds 1-16, each with its own 64
+    lights) on the GPU (tcgen05 forward/backward, Adam) and evaluates on two
+    held-out seeds without fallback: the trained network beats the untrained
+    one, whose zero output layer makes the shader the non-learned
+    virtual-light method on the same inputs."""
+    import torch
+    from rsr_gb300 import learned
+    w, h = 640, 360
+    feats, tgts = learned.collect_samples(gpu, list(range(1, 17)), 1 << 16, w, h)
+    net = learned.LearnedShader(seed=0)
+    untrained = learned.LearnedShader(seed=0)
+    losses = learned.train(gpu, net, feats, tgts, steps=10000, batch=8192)
+    assert losses[-1] < 0.5 * losses[0]
+    err = {"trained": 0.0, "virtual": 0.0}
+    count = 0
+    for seed, path in learned.scene_files([100, 101], w, h):
+        fr = learned.DeferredFrame(gpu, seed, w, h, path=path)
+        n = w * h
+        plain = torch.zeros(n, dtype=torch.int32, device="cuda")
+        fr.shade_plain(gpu, plain)
+        p = plain.cpu().numpy()
+        for name, nt in (("trained", net), ("virtual", untrained)):
+            o = torch.zeros(n, dtype=torch.int32, device="cuda")
+            fr.shade_learned(gpu, nt, float("inf"), o)
+            gpu.shade_learned_check()
+            d = learned.srgb_channels(o.cpu().numpy()) - learned.srgb_channels(p)
+            err[name] += float((d.astype(np.float64) ** 2).sum())
+        count += n * 3
+    db = {k: 10 * np.log10(255.0 ** 2 / (v / count)) for k, v in err.items()}
+    print("PSNR vs plain over seeds 100-101 (dB):", db)
+    assert db["trained"] > db["virtual"] + 1.0, db
