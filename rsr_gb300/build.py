@@ -49,7 +49,7 @@ def _stale(target, deps):
 def build_gpu(verbose=False, extra=()):
     os.makedirs(OBJ, exist_ok=True)
     nvcc = _nvcc()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".inc"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     headers.append(os.path.join(REPO, "include", "rsrgpu.h"))
     jobs = []
     objs = []

@@ -44,7 +44,7 @@ cudaError_t launch_learned_features(const rsrgpu_gbuffer& gb, const float ivp[16
 cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
                                  const rsrgpu_light* lights, int nlights, const float background[3], float max_tile_mse,
                                  uint32_t* out_srgb, float* out_linear, uint8_t* tile_status, float* tile_mse,
-                                 const uint8_t* srgb_lut, int* error, int num_sms, cudaStream_t st);
+                                 const uint8_t* srgb_lut, int* error, int* tile_counter, int num_sms, cudaStream_t st);
 
 static const uint32_t kRcpTable[2048] = {
 #include "rcpps_table.inc"
@@ -1073,14 +1073,14 @@ int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gb
         (rc = check_device_output(ctx, tile_status, tiles, 1, "tile status")) ||
         (rc = check_device_output(ctx, tile_mse, tiles * 4, 4, "tile mse")))
         return rc;
-    if (ctx->d_learn_err.p == nullptr) {
-        CK(ctx->d_learn_err.ensure(sizeof(int)), "alloc learned-shader error flag");
-        CK(cudaMemset(ctx->d_learn_err.p, 0, sizeof(int)), "clear learned-shader error flag");
+    if (ctx->d_learn_err.p == nullptr) {   // [0] error flag, [1] tile counter
+        CK(ctx->d_learn_err.ensure(2 * sizeof(int)), "alloc learned-shader flags");
+        CK(cudaMemset(ctx->d_learn_err.p, 0, 2 * sizeof(int)), "clear learned-shader flags");
     }
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
     CK(launch_shade_learned(*mlp, *gbuffer, inv_view_proj, eye, lights, nlights, background, max_tile_mse, out_srgb,
                             out_linear, tile_status, tile_mse, ctx->d_srgb.as<uint8_t>(), ctx->d_learn_err.as<int>(),
-                            ctx->num_sms, st), "shade_learned_kernel");
+                            ctx->d_learn_err.as<int>() + 1, ctx->num_sms, st), "shade_learned_kernel");
     cudaEvent_t& ev = ctx->learn_events[st];
     if (ev == nullptr) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "learned-shader event");
     CK(cudaEventRecord(ev, st), "learned-shader event record");
