@@ -306,6 +306,8 @@ def run_gpu(args):
             "clocks": clocks.summary(local)}
     if not args.no_deferred:
         line["deferred"] = run_deferred(gpu, args, stream, flush)
+    if not args.no_batch:
+        line["batch"] = run_batch(gpu, args, stream, flush)
     print(json.dumps(line))
 
 
@@ -398,6 +400,82 @@ def run_deferred(gpu, args, stream, flush):
     return res
 
 
+def run_batch(gpu, args, stream, flush):
+    """Config 4: 64 independent frames (the plain-raster generator, triangle
+    counts log-uniform in [1k, 1M], resolutions from 320x180 to 3840x2160) in
+    one captured kernel chain, tiling chosen by the autotuner; against the
+    same frames rendered one after another through rsrgpu_run() and against
+    the batch with one fixed tiling."""
+    import torch
+    from rsr_gb300 import scenes
+    from rsr_gb300.gpu import Batch
+    frames = scenes.batch_frames(seed=0, nframes=64, tris=(1_000, 1_000_000))
+    ntris = sum(f.ntris for f in frames)
+    made = []
+    for sc in frames:
+        dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+        col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+        dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+        made.append((dev, col, dep, sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)))
+    b = Batch(0)
+    b.InstallDefaults()
+    sptr = stream.cuda_stream
+    steps = max(5, min(args.steps, 20))
+    t0 = time.perf_counter()
+    choice = b.tune([(m[3], sc.width, sc.height) for sc, m in zip(frames, made)], reps=2)
+    tune_s = time.perf_counter() - t0
+
+    def timed_batch(tilings):
+        b.submit([(m[3], sc.width, sc.height, t, r, c) for (sc, m), (t, r, c) in zip(zip(frames, made), tilings)])
+        for _ in range(3):
+            b.run(sptr)
+            b.wait()
+        ms = []
+        for i in range(steps):
+            flush.fill_(i & 0xff)
+            torch.cuda.synchronize()
+            b.run(sptr)
+            b.wait()
+            ms.append(b.last_ms())
+        return statistics.median(ms)
+
+    tuned_ms = timed_batch(choice)
+    fixed_ms = timed_batch([(32, 32, 0)] * len(frames))
+    # the same frames one after another through the single-frame path (tuned tilings)
+    seq = []
+    for (sc, m), (t, r, c) in zip(zip(frames, made), choice):
+        gpu.Reset(sc.width, sc.height, (t // 8, t // 8))
+        gpu.submit(m[3])
+        gpu.run(sptr)
+        gpu.Wait()
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.fill_(i & 0xff)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for (sc, m), (t, r, c) in zip(zip(frames, made), choice):
+            gpu.Reset(sc.width, sc.height, (t // 8, t // 8))
+            gpu.submit(m[3])
+            gpu.run(sptr)
+            gpu.Wait()
+        seq.append((time.perf_counter() - t0) * 1e3)
+    seq_ms = statistics.median(seq)
+    b.close()
+    hist = {}
+    for t, r, _ in choice:
+        hist["%d/%d" % (t, r)] = hist.get("%d/%d" % (t, r), 0) + 1
+    return {"workload": "64 frames, plain raster (seeded), triangles log-uniform 1k..1M, resolutions 320x180..3840x2160",
+            "frames": len(frames), "triangles": ntris, "steps": steps,
+            "tuned": {"ms": tuned_ms, "frames_per_s": len(frames) / tuned_ms * 1e3,
+                      "mtris_per_s": ntris / tuned_ms / 1e3, "tilings": hist, "tune_seconds": tune_s},
+            "fixed_32px": {"ms": fixed_ms, "frames_per_s": len(frames) / fixed_ms * 1e3,
+                           "mtris_per_s": ntris / fixed_ms / 1e3},
+            "sequential_single_frame": {"ms": seq_ms, "frames_per_s": len(frames) / seq_ms * 1e3,
+                                        "mtris_per_s": ntris / seq_ms / 1e3,
+                                        "note": "wall clock: decode + run + wait per frame"},
+            "gpu_launches_per_batch": "setup 1 + bin 1 + raster 1 per CTA shape (graph)"}
+
+
 def _raster_bytes(gpu, sc):
     """Algorithmic bytes of one raster launch for this frame (see run_gpu)."""
     tiles = gpu.tiles()
@@ -426,6 +504,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-deferred", action="store_true", help="skip the deferred / learned shading figures")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames figures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

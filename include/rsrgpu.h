@@ -340,6 +340,57 @@ int rsrgpu_learned_features(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, cons
                             const float eye[3], const rsrgpu_light* lights, int nlights, uint16_t* features,
                             float* targets, int32_t* candidates, void* stream);
 
+/* ---- batched frames (extension; no counterpart in rsr) ----
+ * Many independent frames rendered by one kernel chain: one launch of the
+ * setup kernel, one of the binning kernel and one raster launch per CTA
+ * shape cover every frame of the batch; the chain, with one upload of all
+ * frames' decoded tables and one read-back of their counters, is captured
+ * once in a CUDA graph and replayed by rsrgpu_batch_run().  Each frame is
+ * rsr's byte stream as for rsrgpu_submit() with its own target size and
+ * tiling; every pointer it holds must be a device pointer.  A frame's
+ * results equal those of rsrgpu_submit()/rsrgpu_run() on a context reset to
+ * the same size and tiling. */
+#define RSRGPU_MAX_BATCH 64
+typedef struct rsrgpu_batch rsrgpu_batch;
+typedef struct rsrgpu_frame_desc {
+    const uint8_t* commands;
+    size_t nbytes;
+    const rsrgpu_glstate* states;
+    int nstates;
+    int width, height;
+    int tile_px;           /* tile edge in pixels: 8, 16, ..., 128 (a multiple of 8) */
+    int region_px;         /* raster CTA region edge: 8, 16 or 32 (0: min(tile, 32)) */
+    uint32_t bin_capacity; /* tile-list entries to reserve (0: default; grows on overflow) */
+} rsrgpu_frame_desc;
+
+int rsrgpu_batch_create(int device, rsrgpu_batch** out);
+int rsrgpu_batch_destroy(rsrgpu_batch* batch);
+/* as rsrgpu_install(), for every frame of the batch */
+int rsrgpu_batch_install(rsrgpu_batch* batch, int program_id, uint32_t state_key, int kind);
+/* decodes up to RSRGPU_MAX_BATCH frames, sizes their scratch and captures the graph */
+int rsrgpu_batch_submit(rsrgpu_batch* batch, const rsrgpu_frame_desc* frames, int nframes);
+/* replays the captured graph on `stream` (NULL: the batch's own stream) */
+int rsrgpu_batch_run(rsrgpu_batch* batch, void* stream);
+/* waits for the run; a frame whose clip staging or tile lists overflowed is
+ * regrown and the batch re-captured and run again (as rsrgpu_wait) */
+int rsrgpu_batch_wait(rsrgpu_batch* batch, int timeout_ms);
+/* device time of the last run (CUDA events around the graph launch) */
+int rsrgpu_batch_last_ms(rsrgpu_batch* batch, float* ms);
+/* the context holding frame i after a run: rsrgpu_get_stats(),
+ * rsrgpu_dump_tiles() and rsrgpu_dump_clipped() read that frame */
+int rsrgpu_batch_frame(rsrgpu_batch* batch, int i, rsrgpu_ctx** ctx);
+/* Autotuner: for each frame, renders it alone with every candidate tiling
+ * (tile 8/16/32/64 px, raster region 8/16/32 px; tilings whose tile lists
+ * exceed the device capacity are skipped) `reps` times, keeps the
+ * fastest median device time, and sizes its tile-list capacity from the
+ * entries the frame used (plus a quarter).  Frames of the same size whose
+ * triangle counts fall in the same power of two reuse a measured tiling
+ * (one run of the frame then sizes its capacity).
+ * Writes tile_px, region_px and bin_capacity into frames[] (the commands
+ * are rendered, so their outputs are written too). */
+int rsrgpu_batch_tune(rsrgpu_batch* batch, rsrgpu_frame_desc* frames, int nframes, int reps);
+int rsrgpu_batch_last_error(rsrgpu_batch* batch, char* buf, size_t len);
+
 /* ---- rendering without any device allocation ----
  * This entry point has no counterpart in the reference.  It is for callers
  * that cannot call cudaMalloc (for example a host framework that owns all

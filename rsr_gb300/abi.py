@@ -123,6 +123,12 @@ class MlpC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("w1", "w2", "w3", "w4", "b1", "b2", "b3", "b4")]
 
 
+class FrameDescC(ctypes.Structure):
+    _fields_ = [("commands", ctypes.c_void_p), ("nbytes", ctypes.c_size_t), ("states", ctypes.c_void_p),
+                ("nstates", ctypes.c_int32), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("tile_px", ctypes.c_int32), ("region_px", ctypes.c_int32), ("bin_capacity", ctypes.c_uint32)]
+
+
 class StatsC(ctypes.Structure):
     _fields_ = [("total_tiles", ctypes.c_int64),
                 ("total_tile_records", ctypes.c_int64),
@@ -168,6 +174,16 @@ SYMBOLS = {
     "rsrgpu_learned_features": ([ctypes.c_void_p, ctypes.POINTER(GBufferC), ctypes.POINTER(ctypes.c_float),
                                  ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_batch_create": ([ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rsrgpu_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_batch_install": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_batch_submit": ([ctypes.c_void_p, ctypes.POINTER(FrameDescC), ctypes.c_int], ctypes.c_int),
+    "rsrgpu_batch_run": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_batch_wait": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_batch_last_ms": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "rsrgpu_batch_frame": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rsrgpu_batch_tune": ([ctypes.c_void_p, ctypes.POINTER(FrameDescC), ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_batch_last_error": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

@@ -29,6 +29,13 @@ namespace rsrgpu {
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
+cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
+cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st);
+int setup_blocks(const FrameView& fv);
+int bin_blocks(const FrameView& fv);
+int raster_blocks(const FrameView& fv);
+int raster_threads(const FrameView& fv);
 cudaError_t launch_mlp_forward(const rsrgpu_mlp& w, const uint16_t* feat, int n, float* out, int* error,
                                int num_sms, cudaStream_t st);
 cudaError_t launch_mlp_train(const rsrgpu_mlp& w, const uint16_t* feat, const float* target, const int32_t* index,
@@ -110,6 +117,7 @@ struct rsrgpu_ctx {
     int* h_mlp_err = nullptr;   // pinned
     uint32_t clip_cap = 1u << 18;
     uint32_t bin_cap = 1u << 22;
+    int region_px = kRegionPx;      // raster CTA region (the autotuner may pick 16)
     FrameCounters* h_counters = nullptr;   // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     FrameView fv{};
@@ -638,19 +646,35 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
 
 namespace {
 
-int prepare_view(rsrgpu_ctx* ctx) {
+// Device tables a batch provides for one of its frames (packed for all frames).
+struct ViewTables {
+    DevState* states;
+    DevDraw* draws;
+    FrameOp* ops;
+    GBufferDesc* gbufs;
+    FrameCounters* counters;
+    int4* super_rect;
+};
+
+// Allocates the frame's scratch and fills ctx->fv; `tables` (batches) points
+// the frame's tables, counters and super-chunk rectangles elsewhere.
+int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     const int ntris = ctx->ntris;
     const int nchunks = (ntris + kChunk - 1) / kChunk;
     const int nsupers = (ntris + kSuper - 1) / kSuper;
     const size_t nt = size_t(std::max(ntris, 1));
-    CK(ctx->d_states.ensure(sizeof(DevState) * ctx->states.size()), "alloc states");
-    CK(ctx->d_draws.ensure(sizeof(DevDraw) * std::max<size_t>(ctx->draws.size(), 1)), "alloc draws");
-    CK(ctx->d_ops.ensure(sizeof(FrameOp) * std::max<size_t>(ctx->ops.size(), 1)), "alloc ops");
+    if (tables == nullptr) {
+        CK(ctx->d_states.ensure(sizeof(DevState) * ctx->states.size()), "alloc states");
+        CK(ctx->d_draws.ensure(sizeof(DevDraw) * std::max<size_t>(ctx->draws.size(), 1)), "alloc draws");
+        CK(ctx->d_ops.ensure(sizeof(FrameOp) * std::max<size_t>(ctx->ops.size(), 1)), "alloc ops");
+        CK(ctx->d_super.ensure(sizeof(int4) * std::max(nsupers, 1)), "alloc super rects");
+        CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
+        CK(ctx->d_gbufs.ensure(sizeof(GBufferDesc) * std::max<size_t>(ctx->gbufs.size(), 1)), "alloc gbuffer table");
+    }
     CK(ctx->d_tris.ensure(sizeof(TriRecord) * nt), "alloc tris");
     CK(ctx->d_bin_rect.ensure(sizeof(uint64_t) * nt), "alloc bin_rect");
     CK(ctx->d_rec16.ensure(sizeof(uint32_t) * 2 * nt), "alloc rec16");
     CK(ctx->d_chunk.ensure(sizeof(int4) * std::max(nchunks, 1)), "alloc chunk rects");
-    CK(ctx->d_super.ensure(sizeof(int4) * std::max(nsupers, 1)), "alloc super rects");
     CK(ctx->d_clip_info.ensure(sizeof(ClipInfo) * nt), "alloc clip info");
     CK(ctx->d_clip_verts.ensure(sizeof(ClipVert) * size_t(ctx->clip_cap)), "alloc clip verts");
     CK(ctx->d_clip_poly.ensure(sizeof(int32_t) * size_t(ctx->clip_cap)), "alloc clip poly");
@@ -658,16 +682,14 @@ int prepare_view(rsrgpu_ctx* ctx) {
     CK(ctx->d_clip_fan.ensure(sizeof(uint64_t) * size_t(ctx->clip_cap)), "alloc clip fans");
     CK(ctx->d_bins.ensure(sizeof(TileBin) * size_t(ctx->ntiles)), "alloc bins");
     CK(ctx->d_pool.ensure(sizeof(uint32_t) * size_t(ctx->bin_cap)), "alloc bin pool");
-    CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
-    CK(ctx->d_gbufs.ensure(sizeof(GBufferDesc) * std::max<size_t>(ctx->gbufs.size(), 1)), "alloc gbuffer table");
     FrameView& fv = ctx->fv;
-    fv.states = ctx->d_states.as<DevState>();
-    fv.draws = ctx->d_draws.as<DevDraw>();
+    fv.states = tables ? tables->states : ctx->d_states.as<DevState>();
+    fv.draws = tables ? tables->draws : ctx->d_draws.as<DevDraw>();
     fv.ndraws = int(ctx->draws.size());
     fv.ntris = ntris;
-    fv.ops = ctx->d_ops.as<FrameOp>();
+    fv.ops = tables ? tables->ops : ctx->d_ops.as<FrameOp>();
     fv.nops = int(ctx->ops.size());
-    fv.gbufs = ctx->d_gbufs.as<GBufferDesc>();
+    fv.gbufs = tables ? tables->gbufs : ctx->d_gbufs.as<GBufferDesc>();
     fv.width = ctx->width; fv.height = ctx->height;
     fv.tile_w = ctx->tile_w; fv.tile_h = ctx->tile_h;
     fv.tiles_x = ctx->tiles_x; fv.tiles_y = ctx->tiles_y; fv.ntiles = ctx->ntiles;
@@ -676,7 +698,7 @@ int prepare_view(rsrgpu_ctx* ctx) {
     fv.bin_rect = ctx->d_bin_rect.as<uint64_t>();
     fv.rec16 = ctx->d_rec16.as<uint32_t>();
     fv.chunk_rect = ctx->d_chunk.as<int4>();
-    fv.super_rect = ctx->d_super.as<int4>();
+    fv.super_rect = tables ? tables->super_rect : ctx->d_super.as<int4>();
     fv.clip_info = ctx->d_clip_info.as<ClipInfo>();
     fv.clip_verts = ctx->d_clip_verts.as<ClipVert>();
     fv.clip_poly = ctx->d_clip_poly.as<int32_t>();
@@ -686,9 +708,10 @@ int prepare_view(rsrgpu_ctx* ctx) {
     fv.bins = ctx->d_bins.as<TileBin>();
     fv.bin_pool = ctx->d_pool.as<uint32_t>();
     fv.bin_cap = ctx->bin_cap;
-    fv.counters = ctx->d_counters.as<FrameCounters>();
+    fv.counters = tables ? tables->counters : ctx->d_counters.as<FrameCounters>();
     fv.rcp_table = ctx->d_rcp.as<uint32_t>();
     fv.srgb_lut = ctx->d_srgb.as<uint8_t>();
+    fv.region_px = std::min(ctx->region_px, std::min(ctx->tile_w, ctx->tile_h));
     return 0;
 }
 
@@ -1118,6 +1141,376 @@ int rsrgpu_learned_features(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, cons
     CK(launch_learned_features(*gbuffer, inv_view_proj, eye, lights, nlights, features, targets, candidates,
                                ctx->num_sms, st), "learned_features_kernel");
     CK(cudaStreamSynchronize(st), "learned features sync");
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// batched frames
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct rsrgpu_batch {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t run_stream = nullptr;
+    std::string err;
+    std::vector<std::tuple<int, uint32_t, int>> installs;
+    std::vector<rsrgpu_ctx*> frames;      // one context per frame slot, reused across submits
+    int nframes = 0;
+    // all frames' tables in one device buffer, staged in pinned memory
+    DevBuf d_tables, d_counters, d_super;
+    uint8_t* h_tables = nullptr;
+    size_t h_tables_cap = 0, tables_bytes = 0, super_count = 0;
+    FrameCounters* h_counters = nullptr;  // pinned, kMaxBatch entries
+    std::vector<size_t> off_states, off_draws, off_ops, off_gbufs, off_super;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool ran = false;
+    std::map<uint64_t, rsrgpu_frame_desc> tuned;   // (w, h, log2 ntris) -> choice
+};
+
+namespace {
+
+int bfail(rsrgpu_batch* b, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    b->err = buf;
+    return code;
+}
+
+#define BCK(call, what)                                                                 \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return bfail(b, RSRGPU_ECUDA, "%s: %s", what, cudaGetErrorString(e_));      \
+    } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int frame_ctx(rsrgpu_batch* b, int i, rsrgpu_ctx** out) {
+    while (int(b->frames.size()) <= i) {
+        rsrgpu_ctx* c = nullptr;
+        int rc = rsrgpu_create(b->device, &c);
+        if (rc) return bfail(b, rc, "frame context: create failed");
+        for (auto& in : b->installs) {
+            rc = rsrgpu_install(c, std::get<0>(in), std::get<1>(in), std::get<2>(in));
+            if (rc) { b->err = c->err; rsrgpu_destroy(c); return rc; }
+        }
+        b->frames.push_back(c);
+    }
+    *out = b->frames[size_t(i)];
+    return 0;
+}
+
+// decodes one frame into context c with the tiling of d
+int decode_into(rsrgpu_batch* b, rsrgpu_ctx* c, const rsrgpu_frame_desc& d) {
+    if (d.tile_px < 8 || d.tile_px > 128 || (d.tile_px & 7))
+        return bfail(b, RSRGPU_EINVAL, "tile_px %d: 8..128, a multiple of 8", d.tile_px);
+    if (d.region_px != 0 && d.region_px != 8 && d.region_px != 16 && d.region_px != 32)
+        return bfail(b, RSRGPU_EINVAL, "region_px %d: 0, 8, 16 or 32", d.region_px);
+    int rc = rsrgpu_reset(c, d.width, d.height, d.tile_px / 8, d.tile_px / 8);
+    if (rc == 0) rc = rsrgpu_submit(c, d.commands, d.nbytes, d.states, d.nstates);
+    if (rc) { b->err = c->err; return rc; }
+    if (!c->host.empty()) return bfail(b, RSRGPU_EINVAL, "batched frames take device pointers only");
+    c->region_px = d.region_px ? d.region_px : std::min(d.tile_px, kRegionPx);
+    if (d.bin_capacity) c->bin_cap = std::max<uint32_t>(d.bin_capacity, 1024u);
+    return 0;
+}
+
+// packs the frames' tables, sizes their scratch and captures the kernel chain
+int build_batch(rsrgpu_batch* b) {
+    const int n = b->nframes;
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    b->off_states.assign(size_t(n), 0); b->off_draws.assign(size_t(n), 0); b->off_ops.assign(size_t(n), 0);
+    b->off_gbufs.assign(size_t(n), 0); b->off_super.assign(size_t(n), 0);
+    size_t bytes = 0, supers = 0;
+    for (int i = 0; i < n; ++i) {
+        rsrgpu_ctx* c = b->frames[size_t(i)];
+        b->off_states[size_t(i)] = bytes; bytes = align256(bytes + sizeof(DevState) * c->states.size());
+        b->off_draws[size_t(i)] = bytes; bytes = align256(bytes + sizeof(DevDraw) * c->draws.size());
+        b->off_ops[size_t(i)] = bytes; bytes = align256(bytes + sizeof(FrameOp) * c->ops.size());
+        b->off_gbufs[size_t(i)] = bytes; bytes = align256(bytes + sizeof(GBufferDesc) * c->gbufs.size());
+        b->off_super[size_t(i)] = supers; supers += size_t((c->ntris + kSuper - 1) / kSuper);
+    }
+    b->tables_bytes = std::max<size_t>(bytes, 256);
+    b->super_count = std::max<size_t>(supers, 1);
+    if (b->h_tables_cap < b->tables_bytes) {
+        if (b->h_tables) cudaFreeHost(b->h_tables);
+        b->h_tables = nullptr;
+        b->h_tables_cap = 0;
+        BCK(cudaHostAlloc(reinterpret_cast<void**>(&b->h_tables), b->tables_bytes, cudaHostAllocDefault), "alloc staging");
+        b->h_tables_cap = b->tables_bytes;
+    }
+    BCK(b->d_tables.ensure(b->tables_bytes), "alloc batch tables");
+    BCK(b->d_super.ensure(sizeof(int4) * b->super_count), "alloc batch super rects");
+    uint8_t* dt = b->d_tables.as<uint8_t>();
+    std::vector<BatchLaunch> setup(1), bin(1);
+    setup[0].nframes = bin[0].nframes = n;
+    int sblocks = 0, bblocks = 0;
+    std::map<int, BatchLaunch> raster;      // by CTA size
+    std::map<int, int> rblocks;
+    for (int i = 0; i < n; ++i) {
+        rsrgpu_ctx* c = b->frames[size_t(i)];
+        std::memcpy(b->h_tables + b->off_states[size_t(i)], c->states.data(), sizeof(DevState) * c->states.size());
+        if (!c->draws.empty()) std::memcpy(b->h_tables + b->off_draws[size_t(i)], c->draws.data(), sizeof(DevDraw) * c->draws.size());
+        if (!c->ops.empty()) std::memcpy(b->h_tables + b->off_ops[size_t(i)], c->ops.data(), sizeof(FrameOp) * c->ops.size());
+        if (!c->gbufs.empty()) std::memcpy(b->h_tables + b->off_gbufs[size_t(i)], c->gbufs.data(), sizeof(GBufferDesc) * c->gbufs.size());
+        ViewTables vt{ reinterpret_cast<DevState*>(dt + b->off_states[size_t(i)]),
+                       reinterpret_cast<DevDraw*>(dt + b->off_draws[size_t(i)]),
+                       reinterpret_cast<FrameOp*>(dt + b->off_ops[size_t(i)]),
+                       reinterpret_cast<GBufferDesc*>(dt + b->off_gbufs[size_t(i)]),
+                       b->d_counters.as<FrameCounters>() + i,
+                       b->d_super.as<int4>() + b->off_super[size_t(i)] };
+        int rc = prepare_view(c, &vt);
+        if (rc) { b->err = c->err; return rc; }
+        const FrameView& fv = c->fv;
+        setup[0].start[i] = sblocks; setup[0].fv[i] = fv; sblocks += setup_blocks(fv);
+        bin[0].start[i] = bblocks; bin[0].fv[i] = fv; bblocks += bin_blocks(fv);
+        const int th = raster_threads(fv);
+        BatchLaunch& rl = raster[th];
+        int& rb = rblocks[th];
+        rl.start[rl.nframes] = rb;
+        rl.fv[rl.nframes] = fv;
+        rl.nframes++;
+        rb += raster_blocks(fv);
+        c->stats.gpu_launches = 0;
+    }
+    setup[0].start[n] = sblocks;
+    bin[0].start[n] = bblocks;
+    for (auto& kv : raster) kv.second.start[kv.second.nframes] = rblocks[kv.first];
+    cudaStream_t st = b->own;
+    BCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int rc = 0;
+    auto step = [&](cudaError_t e, const char* what) {
+        if (rc == 0 && e != cudaSuccess) rc = bfail(b, RSRGPU_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    };
+    step(cudaMemcpyAsync(b->d_tables.p, b->h_tables, b->tables_bytes, cudaMemcpyHostToDevice, st), "H2D tables");
+    step(cudaMemsetAsync(b->d_counters.p, 0, sizeof(FrameCounters) * size_t(n), st), "memset counters");
+    step(cudaMemsetAsync(b->d_super.p, 0x7f, sizeof(int4) * b->super_count, st), "memset super rects");
+    step(launch_setup_batch(setup[0], sblocks, st), "setup_batch_kernel");
+    step(launch_bin_batch(bin[0], bblocks, st), "bin_batch_kernel");
+    for (auto& kv : raster) step(launch_raster_batch(kv.second, rblocks[kv.first], kv.first, st), "raster_batch_kernel");
+    step(cudaMemcpyAsync(b->h_counters, b->d_counters.p, sizeof(FrameCounters) * size_t(n), cudaMemcpyDeviceToHost, st), "D2H counters");
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    BCK(e, "end capture");
+    b->graph = g;
+    BCK(cudaGraphInstantiate(&b->exec, b->graph, 0), "instantiate graph");
+    const int launches = 2 + int(raster.size());
+    for (int i = 0; i < n; ++i) b->frames[size_t(i)]->stats.gpu_launches = launches;
+    return 0;
+}
+
+uint64_t tune_key(const rsrgpu_frame_desc& d, int ntris) {
+    return (uint64_t(uint32_t(d.width)) << 40) | (uint64_t(uint32_t(d.height)) << 16) | uint64_t(ilog2u(unsigned(ntris) | 1u));
+}
+
+}  // namespace
+
+extern "C" {
+
+int rsrgpu_batch_create(int device, rsrgpu_batch** out) {
+    if (out == nullptr) return RSRGPU_EINVAL;
+    *out = nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return RSRGPU_ECUDA;
+    rsrgpu_batch* b = new rsrgpu_batch();
+    b->device = device;
+    if (cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaHostAlloc(reinterpret_cast<void**>(&b->h_counters), sizeof(FrameCounters) * kMaxBatch, cudaHostAllocDefault) != cudaSuccess ||
+        b->d_counters.ensure(sizeof(FrameCounters) * kMaxBatch) != cudaSuccess) {
+        rsrgpu_batch_destroy(b);
+        return RSRGPU_ECUDA;
+    }
+    *out = b;
+    return 0;
+}
+
+int rsrgpu_batch_destroy(rsrgpu_batch* b) {
+    if (b == nullptr) return 0;
+    if (b->own) cudaStreamSynchronize(b->own);
+    if (b->run_stream && b->run_stream != b->own) cudaStreamSynchronize(b->run_stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (rsrgpu_ctx* c : b->frames) rsrgpu_destroy(c);
+    if (b->h_tables) cudaFreeHost(b->h_tables);
+    if (b->h_counters) cudaFreeHost(b->h_counters);
+    b->d_tables.release(); b->d_counters.release(); b->d_super.release();
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->own) cudaStreamDestroy(b->own);
+    delete b;
+    return 0;
+}
+
+int rsrgpu_batch_install(rsrgpu_batch* b, int program_id, uint32_t state_key, int kind) {
+    if (b == nullptr) return RSRGPU_EINVAL;
+    for (rsrgpu_ctx* c : b->frames) {
+        int rc = rsrgpu_install(c, program_id, state_key, kind);
+        if (rc) { b->err = c->err; return rc; }
+    }
+    b->installs.emplace_back(program_id, state_key, kind);
+    return 0;
+}
+
+int rsrgpu_batch_submit(rsrgpu_batch* b, const rsrgpu_frame_desc* frames, int nframes) {
+    if (b == nullptr || frames == nullptr) return RSRGPU_EINVAL;
+    if (nframes < 1 || nframes > kMaxBatch) return bfail(b, RSRGPU_EINVAL, "1..%d frames per batch", kMaxBatch);
+    BCK(cudaSetDevice(b->device), "set device");
+    b->nframes = 0;
+    b->ran = false;
+    for (int i = 0; i < nframes; ++i) {
+        rsrgpu_ctx* c = nullptr;
+        int rc = frame_ctx(b, i, &c);
+        if (rc == 0) rc = decode_into(b, c, frames[i]);
+        if (rc) {
+            std::string m = b->err;
+            return bfail(b, rc, "frame %d: %s", i, m.c_str());
+        }
+    }
+    b->nframes = nframes;
+    return build_batch(b);
+}
+
+int rsrgpu_batch_run(rsrgpu_batch* b, void* stream) {
+    if (b == nullptr) return RSRGPU_EINVAL;
+    if (b->exec == nullptr) return bfail(b, RSRGPU_EINVAL, "nothing submitted");
+    b->run_stream = stream ? static_cast<cudaStream_t>(stream) : b->own;
+    BCK(cudaEventRecord(b->ev0, b->run_stream), "event");
+    BCK(cudaGraphLaunch(b->exec, b->run_stream), "graph launch");
+    BCK(cudaEventRecord(b->ev1, b->run_stream), "event");
+    b->ran = true;
+    for (int i = 0; i < b->nframes; ++i) {
+        b->frames[size_t(i)]->ran = true;
+        b->frames[size_t(i)]->run_stream = b->run_stream;
+    }
+    return 0;
+}
+
+int rsrgpu_batch_wait(rsrgpu_batch* b, int timeout_ms) {
+    if (b == nullptr) return RSRGPU_EINVAL;
+    if (!b->ran) return 0;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        const auto t0 = std::chrono::steady_clock::now();
+        while (true) {
+            cudaError_t q = cudaEventQuery(b->ev1);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) return bfail(b, RSRGPU_ECUDA, "batch run: %s", cudaGetErrorString(q));
+            if (timeout_ms >= 0) {
+                const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+                if (ms > timeout_ms) return bfail(b, RSRGPU_ETIMEOUT, "rsrgpu_batch_wait timed out after %d ms", timeout_ms);
+            }
+            std::this_thread::yield();
+        }
+        bool again = false;
+        for (int i = 0; i < b->nframes; ++i) {
+            const FrameCounters c = b->h_counters[i];
+            rsrgpu_ctx* x = b->frames[size_t(i)];
+            *x->h_counters = c;
+            if (c.overflow == 0) continue;
+            if (c.overflow & 4u) return bfail(b, RSRGPU_EINVAL, "frame %d: a vertex index lies outside its attribute buffer", i);
+            if (c.overflow & 1u) x->clip_cap = std::max<uint32_t>(x->clip_cap * 2, c.clip_verts + c.clip_verts / 4 + 1024);
+            if (c.overflow & 2u) x->bin_cap = std::max<uint32_t>(x->bin_cap * 2, c.bin_used + c.bin_used / 4 + 4096);
+            if (x->clip_cap > (1u << 28) || x->bin_cap > (1u << 30))
+                return bfail(b, RSRGPU_ECAPACITY, "frame %d needs %u clipped vertices and %u tile entries", i, c.clip_verts, c.bin_used);
+            again = true;
+        }
+        if (!again) return 0;
+        int rc = build_batch(b);
+        if (rc == 0) rc = rsrgpu_batch_run(b, b->run_stream);
+        if (rc) return rc;
+    }
+    return bfail(b, RSRGPU_ECAPACITY, "capacity growth did not converge");
+}
+
+int rsrgpu_batch_last_ms(rsrgpu_batch* b, float* ms) {
+    if (b == nullptr || ms == nullptr || !b->ran) return RSRGPU_EINVAL;
+    BCK(cudaEventSynchronize(b->ev1), "sync");
+    BCK(cudaEventElapsedTime(ms, b->ev0, b->ev1), "elapsed");
+    return 0;
+}
+
+int rsrgpu_batch_frame(rsrgpu_batch* b, int i, rsrgpu_ctx** ctx) {
+    if (b == nullptr || ctx == nullptr || i < 0 || i >= b->nframes) return RSRGPU_EINVAL;
+    *ctx = b->frames[size_t(i)];
+    return 0;
+}
+
+int rsrgpu_batch_tune(rsrgpu_batch* b, rsrgpu_frame_desc* frames, int nframes, int reps) {
+    if (b == nullptr || frames == nullptr || nframes < 0) return RSRGPU_EINVAL;
+    if (reps < 1) reps = 1;
+    BCK(cudaSetDevice(b->device), "set device");
+    static const int kCandidates[][2] = { { 8, 8 }, { 16, 16 }, { 16, 8 }, { 32, 32 }, { 32, 16 }, { 64, 32 } };
+    rsrgpu_ctx* c = nullptr;
+    int rc = frame_ctx(b, 0, &c);   // scratch context: frame slot 0 is re-decoded by the next submit
+    if (rc) return rc;
+    for (int i = 0; i < nframes; ++i) {
+        rsrgpu_frame_desc d = frames[i];
+        d.tile_px = 8; d.region_px = 8; d.bin_capacity = 0;
+        rc = decode_into(b, c, d);
+        if (rc) { std::string m = b->err; return bfail(b, rc, "frame %d: %s", i, m.c_str()); }
+        const uint64_t key = tune_key(d, c->ntris);
+        auto hit = b->tuned.find(key);
+        if (hit != b->tuned.end()) {
+            // same size class: keep the measured tiling, size the capacity from one run of this frame
+            d.tile_px = hit->second.tile_px;
+            d.region_px = hit->second.region_px;
+            rc = decode_into(b, c, d);
+            if (rc == 0) rc = rsrgpu_run(c, b->own);
+            if (rc == 0) rc = rsrgpu_wait(c, -1);
+            if (rc) { b->err = c->err; return rc; }
+            const uint32_t used = c->h_counters->bin_used;
+            frames[i].tile_px = d.tile_px;
+            frames[i].region_px = d.region_px;
+            frames[i].bin_capacity = used + used / 4 + 1024;
+            continue;
+        }
+        float best = 1e30f;
+        rsrgpu_frame_desc choice = d;
+        for (const auto& cand : kCandidates) {
+            d.tile_px = cand[0]; d.region_px = cand[1];
+            rc = decode_into(b, c, d);
+            if (rc) { std::string m = b->err; return bfail(b, rc, "frame %d: %s", i, m.c_str()); }
+            std::vector<float> t;
+            uint32_t used = 0;
+            bool fits = true;
+            for (int r = 0; r <= reps && fits; ++r) {
+                rc = rsrgpu_run(c, b->own);
+                if (rc == 0) rc = rsrgpu_wait(c, -1);
+                if (rc == RSRGPU_ECAPACITY) { fits = false; break; }   // this tiling's lists cannot be held
+                if (rc) { b->err = c->err; return rc; }
+                float ms = 0.f;
+                BCK(cudaEventElapsedTime(&ms, c->ev0, c->ev2), "elapsed");
+                if (r > 0) t.push_back(ms);   // the first run warms the scratch up
+                used = c->h_counters->bin_used;
+            }
+            if (!fits || t.empty()) continue;
+            std::sort(t.begin(), t.end());
+            const float med = t[t.size() / 2];
+            if (med < best) {
+                best = med;
+                choice = d;
+                choice.bin_capacity = used + used / 4 + 1024;
+            }
+        }
+        if (best >= 1e30f) return bfail(b, RSRGPU_ECAPACITY, "frame %d: no candidate tiling holds its tile lists", i);
+        b->tuned[key] = choice;
+        frames[i].tile_px = choice.tile_px;
+        frames[i].region_px = choice.region_px;
+        frames[i].bin_capacity = choice.bin_capacity;
+    }
+    return 0;
+}
+
+int rsrgpu_batch_last_error(rsrgpu_batch* b, char* buf, size_t len) {
+    if (b == nullptr || buf == nullptr || len == 0) return RSRGPU_EINVAL;
+    std::snprintf(buf, len, "%s", b->err.c_str());
     return 0;
 }
 

@@ -24,7 +24,9 @@ constexpr int kChunk = 32;        // triangles per chunk (one warp)
 constexpr int kSuper = 1024;      // triangles per super-chunk
 constexpr int kSetupBlock = 256;
 constexpr int kMaxClipVerts = 8;  // 3 + one per clipping plane (5 planes)
-constexpr int kRegionPx = 32;     // raster CTA covers at most 32x32 px of one tile
+constexpr int kRegionPx = 32;     // default raster region: a CTA covers at most 32x32 px of one tile
+constexpr int kBinBlock = 256;    // bin CTA: one warp per tile
+constexpr int kMaxBatch = 64;     // frames per batched launch
 constexpr int kRasterBatch = 256; // triangles set up per shared-memory batch
 
 enum ProgramId : int32_t {
@@ -150,6 +152,15 @@ struct FrameView {
     FrameCounters* counters;
     const uint32_t* rcp_table;
     const uint8_t* srgb_lut;
+    int32_t region_px;        // raster CTA region edge (8, 16 or 32 px; at most the tile)
+};
+
+// One launch of a stage over many frames: block b belongs to frame f when
+// start[f] <= b < start[f + 1]; passed as a __grid_constant__ parameter.
+struct BatchLaunch {
+    int32_t nframes;
+    int32_t start[kMaxBatch + 1];
+    FrameView fv[kMaxBatch];
 };
 
 }  // namespace rsrgpu

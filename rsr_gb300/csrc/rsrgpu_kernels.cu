@@ -269,8 +269,8 @@ __device__ __noinline__ void clip_triangle(const FrameView& fv, const DevState& 
 // ---------------------------------------------------------------------------
 // setup
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kSetupBlock) setup_kernel(FrameView fv) {
-    const int g = blockIdx.x * kSetupBlock + threadIdx.x;
+__device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
+    const int g = block * kSetupBlock + threadIdx.x;
     uint64_t rect = kEmptyRect;
     if (g < fv.ntris) {
         const int d = find_draw(fv.draws, fv.ndraws, g);
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kSetupBlock) setup_kernel(FrameView fv) {
     y0 = __reduce_min_sync(FULL_MASK, y0);
     x1 = __reduce_max_sync(FULL_MASK, x1);
     y1 = __reduce_max_sync(FULL_MASK, y1);
-    const int chunk = (blockIdx.x * kSetupBlock + threadIdx.x) >> 5;
+    const int chunk = (block * kSetupBlock + threadIdx.x) >> 5;
     if ((threadIdx.x & 31) == 0 && chunk < fv.nchunks) {
         fv.chunk_rect[chunk] = make_int4(x0, y0, x1, y1);
         if (x0 <= x1) {
@@ -431,8 +431,8 @@ __device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, in
     }
 }
 
-__global__ void __launch_bounds__(256) bin_kernel(FrameView fv) {
-    const int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__device__ __forceinline__ void bin_body(const FrameView& fv, int block) {
+    const int tile = (block * kBinBlock + int(threadIdx.x)) >> 5;
     const int lane = threadIdx.x & 31;
     if (tile >= fv.ntiles) return;
     if (fv.counters->overflow & 1u) {
@@ -788,21 +788,21 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
     }
 }
 
-__global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
-    __shared__ RasterSmem S;
+__device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
     if (fv.counters->overflow != 0u) return;
 
-    const int sub_x = (fv.tile_w + kRegionPx - 1) / kRegionPx;
-    const int sub_y = (fv.tile_h + kRegionPx - 1) / kRegionPx;
+    const int region = fv.region_px;
+    const int sub_x = (fv.tile_w + region - 1) / region;
+    const int sub_y = (fv.tile_h + region - 1) / region;
     const int subs = sub_x * sub_y;
-    const int tile = blockIdx.x / subs;
-    const int sub = blockIdx.x % subs;
+    const int tile = block / subs;
+    const int sub = block % subs;
     const int ttx = tile % fv.tiles_x, tty = tile / fv.tiles_x;
     int rect[4];   // the tile rectangle (GPU::TileRect, rglv_gpu.hxx:292-299)
     rect[0] = ttx * fv.tile_w; rect[1] = tty * fv.tile_h;
     rect[2] = min(rect[0] + fv.tile_w, fv.width); rect[3] = min(rect[1] + fv.tile_h, fv.height);
-    const int rx0 = rect[0] + (sub % sub_x) * kRegionPx, ry0 = rect[1] + (sub / sub_x) * kRegionPx;
-    const int rx1 = min(rx0 + kRegionPx, rect[2]), ry1 = min(ry0 + kRegionPx, rect[3]);
+    const int rx0 = rect[0] + (sub % sub_x) * region, ry0 = rect[1] + (sub / sub_x) * region;
+    const int rx1 = min(rx0 + region, rect[2]), ry1 = min(ry0 + region, rect[3]);
     if (rx0 >= rx1 || ry0 >= ry1) return;
     const int qw = (rx1 - rx0) >> 1, qh = (ry1 - ry0) >> 1;
     const int tid = threadIdx.x;
@@ -1072,6 +1072,43 @@ __global__ void __launch_bounds__(256) raster_kernel(FrameView fv) {
 }
 
 // ---------------------------------------------------------------------------
+// kernels: one frame, and a batch of frames in one launch per stage
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constant__ FrameView fv) {
+    setup_body(fv, blockIdx.x);
+}
+__global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
+    bin_body(fv, blockIdx.x);
+}
+__global__ void __launch_bounds__(256) raster_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem S;
+    raster_body(fv, blockIdx.x, S);
+}
+
+// frame of a block: the last f with start[f] <= block (start[] ascending)
+__device__ __forceinline__ int batch_frame(const BatchLaunch& b, int block) {
+    int lo = 0, hi = b.nframes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.start[mid] <= block) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+__global__ void __launch_bounds__(kSetupBlock) setup_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    const int f = batch_frame(b, blockIdx.x);
+    setup_body(b.fv[f], blockIdx.x - b.start[f]);
+}
+__global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    const int f = batch_frame(b, blockIdx.x);
+    bin_body(b.fv[f], blockIdx.x - b.start[f]);
+}
+__global__ void __launch_bounds__(256) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ RasterSmem S;
+    const int f = batch_frame(b, blockIdx.x);
+    raster_body(b.fv[f], blockIdx.x - b.start[f], S);
+}
+
+// ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
@@ -1081,21 +1118,43 @@ cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+int setup_blocks(const FrameView& fv) { return (fv.ntris + kSetupBlock - 1) / kSetupBlock; }
+int bin_blocks(const FrameView& fv) { return (fv.ntiles + kBinBlock / 32 - 1) / (kBinBlock / 32); }
+int raster_blocks(const FrameView& fv) {
+    const int sub_x = (fv.tile_w + fv.region_px - 1) / fv.region_px;
+    const int sub_y = (fv.tile_h + fv.region_px - 1) / fv.region_px;
+    return fv.ntiles * sub_x * sub_y;
+}
+// threads of a raster CTA: one per 2x2 quad of a region, in whole warps
+int raster_threads(const FrameView& fv) {
+    const int qx = (fv.tile_w < fv.region_px ? fv.tile_w : fv.region_px) / 2;
+    const int qy = (fv.tile_h < fv.region_px ? fv.tile_h : fv.region_px) / 2;
+    return ((qx * qy + 31) / 32) * 32;
+}
+
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
-    const int warps_per_block = 8;
-    const int blocks = (fv.ntiles + warps_per_block - 1) / warps_per_block;
-    bin_kernel<<<blocks, warps_per_block * 32, 0, st>>>(fv);
+    bin_kernel<<<bin_blocks(fv), kBinBlock, 0, st>>>(fv);
     return cudaGetLastError();
 }
 
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
-    const int sub_x = (fv.tile_w + kRegionPx - 1) / kRegionPx;
-    const int sub_y = (fv.tile_h + kRegionPx - 1) / kRegionPx;
-    const int blocks = fv.ntiles * sub_x * sub_y;
-    const int qx = (fv.tile_w < kRegionPx ? fv.tile_w : kRegionPx) / 2;
-    const int qy = (fv.tile_h < kRegionPx ? fv.tile_h : kRegionPx) / 2;
-    int threads = ((qx * qy + 31) / 32) * 32;
-    raster_kernel<<<blocks, threads, 0, st>>>(fv);
+    raster_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st) {
+    if (blocks == 0) return cudaSuccess;
+    setup_batch_kernel<<<blocks, kSetupBlock, 0, st>>>(b);
+    return cudaGetLastError();
+}
+cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st) {
+    if (blocks == 0) return cudaSuccess;
+    bin_batch_kernel<<<blocks, kBinBlock, 0, st>>>(b);
+    return cudaGetLastError();
+}
+cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st) {
+    if (blocks == 0) return cudaSuccess;
+    raster_batch_kernel<<<blocks, threads, 0, st>>>(b);
     return cudaGetLastError();
 }
 

@@ -199,6 +199,7 @@ int render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* 
     fv.counters = reinterpret_cast<FrameCounters*>(base + kOffCounters);
     fv.rcp_table = reinterpret_cast<const uint32_t*>(base + kOffRcp);
     fv.srgb_lut = reinterpret_cast<const uint8_t*>(base + kOffSrgb);
+    fv.region_px = kRegionPx;
 
 #define CKS(expr) do { cudaError_t e_ = (expr); if (e_ != cudaSuccess) return fail_static(RSRGPU_ECUDA, cudaGetErrorString(e_)); } while (0)
     CKS(cudaMemcpyAsync(base + kOffStates, st.data(), sizeof(DevState) * st.size(), cudaMemcpyHostToDevice, s));

@@ -207,6 +207,103 @@ class GPU:
         return t.value, r.value
 
 
+class FrameContext(GPU):
+    """A batch frame's context (rsrgpu_batch_frame): the inspection calls of
+    GPU (tiles, clipped, stats) on one frame of a batch; owned by the batch."""
+
+    def __init__(self, lib, handle):
+        self.lib = lib
+        self.ctx = handle
+        self._keep = None
+
+    def close(self):
+        self.ctx = None
+
+
+class Batch:
+    """Batched frames (include/rsrgpu.h rsrgpu_batch_*): many independent
+    frames, each rsr's byte stream with its own target size and tiling,
+    rendered by one captured kernel chain.  Frames are GL recordings whose
+    pointers are device tensors."""
+
+    def __init__(self, device=0):
+        self.lib = abi.load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.rsrgpu_batch_create(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise RsrGpuError(rc, "rsrgpu_batch_create failed")
+        self.h = h
+        self._keep = None
+
+    def close(self):
+        if self.h:
+            self.lib.rsrgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.rsrgpu_batch_last_error(self.h, buf, 512)
+            raise RsrGpuError(rc, buf.value.decode(errors="replace"))
+
+    def Install(self, program_id, state_key, kind):
+        self._check(self.lib.rsrgpu_batch_install(self.h, int(program_id), int(state_key), int(kind)))
+
+    def InstallDefaults(self):
+        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY, abi.PROGRAM_GBUFFER):
+            self.Install(pid, 0, abi.KIND_BIN)
+            for key in DRAW_STATE_KEYS:
+                self.Install(pid, key, abi.KIND_DRAW)
+        for pid in (abi.PROGRAM_DEFAULT_POST, abi.PROGRAM_EXPOSURE_POST, abi.PROGRAM_GOURAUD):
+            self.Install(pid, 0, abi.KIND_BLT)
+
+    def _descs(self, frames):
+        """frames: [(gl, width, height, tile_px, region_px, bin_capacity)]"""
+        arr = (abi.FrameDescC * len(frames))()
+        keep = []
+        for i, (gl, w, h, tile, region, cap) in enumerate(frames):
+            cmds = gl.stream()
+            buf = ctypes.create_string_buffer(cmds, max(1, len(cmds)))
+            states = gl.c_states()
+            keep += [buf, states, gl]
+            arr[i] = abi.FrameDescC(ctypes.cast(buf, ctypes.c_void_p), len(cmds), ctypes.cast(states, ctypes.c_void_p),
+                                    len(gl.states), w, h, tile, region, cap)
+        return arr, keep
+
+    def tune(self, frames, reps=3):
+        """Autotuner (rsrgpu_batch_tune): returns [(tile_px, region_px, bin_capacity)] per frame."""
+        arr, keep = self._descs([(gl, w, h, 8, 0, 0) for gl, w, h in frames])
+        self._check(self.lib.rsrgpu_batch_tune(self.h, arr, len(frames), int(reps)))
+        return [(arr[i].tile_px, arr[i].region_px, arr[i].bin_capacity) for i in range(len(frames))]
+
+    def submit(self, frames):
+        arr, keep = self._descs(frames)
+        self._keep = (arr, keep)
+        self._check(self.lib.rsrgpu_batch_submit(self.h, arr, len(frames)))
+
+    def run(self, stream=None):
+        self._check(self.lib.rsrgpu_batch_run(self.h, ctypes.c_void_p(stream) if stream else None))
+
+    def wait(self, timeout_ms=-1):
+        self._check(self.lib.rsrgpu_batch_wait(self.h, int(timeout_ms)))
+
+    def last_ms(self):
+        ms = ctypes.c_float(0)
+        self._check(self.lib.rsrgpu_batch_last_ms(self.h, ctypes.byref(ms)))
+        return ms.value
+
+    def frame(self, i):
+        h = ctypes.c_void_p()
+        self._check(self.lib.rsrgpu_batch_frame(self.h, int(i), ctypes.byref(h)))
+        return FrameContext(self.lib, h)
+
+
 def render_scene(gpu, scene, gamma=True, device_inputs=None, color=None, depth=None):
     """Render a scenes.Scene.  With device_inputs (name -> device tensor) the
     inputs are used in place; otherwise the scene's host arrays are

@@ -118,29 +118,68 @@ def _begin_frame(gl, clear_rgb=(0.0, 0.0, 0.0)):
     gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
 
 
-def plain_raster(seed=0, ntris=10000, width=640, height=360, tile_blocks=(8, 8)):
+def plain_raster(seed=0, ntris=10000, width=640, height=360, tile_blocks=(8, 8), spread=1.0):
     """Random NDC triangles (xyz in [-1,1], w=1), rgb in [0,1], Gouraud, LESS,
-    no culling; one DrawElements of 3*ntris sequential indices."""
+    no culling; DrawElements of sequential indices.  spread < 1 shrinks each
+    triangle about its own centre: centre uniform in [-(1-s), 1-s]^3 and
+    vertices at centre + s * U[-1,1]^3, so positions stay in [-1,1] and the
+    expected screen area scales by s^2 (spread 1 is the unscaled generator)."""
     nverts = 3 * ntris
     u = uniform01(seed, nverts * 6).reshape(ntris, 3, 6)
-    pos = lerp(-1.0, 1.0, u[:, :, 0:3]).reshape(nverts, 3)
+    pos = lerp(-1.0, 1.0, u[:, :, 0:3])
+    if spread < 1.0:
+        c = lerp(-(1.0 - spread), 1.0 - spread, uniform01(seed + 0x5EED, ntris * 3).reshape(ntris, 1, 3))
+        pos = c + spread * pos
+    pos = pos.reshape(nverts, 3)
     rgb = lerp(0.0, 1.0, u[:, :, 3:6]).reshape(nverts, 3)
+    # a draw holds at most 32766 vertices (u16 indices, bit 15 = back-face flag):
+    # larger sets are drawn as consecutive draws of 10922 triangles
+    per_draw = min(ntris, 10922)
     arrays = {
         "px": pad4(pos[:, 0]), "py": pad4(pos[:, 1]), "pz": pad4(pos[:, 2]),
         "cr": pad4(rgb[:, 0]), "cg": pad4(rgb[:, 1]), "cb": pad4(rgb[:, 2]),
-        "idx": np.arange(nverts, dtype=np.uint16),
+        "idx": np.arange(3 * per_draw, dtype=np.uint16),
     }
-    if nverts > 32767:
-        raise ValueError("a draw holds at most 32767 vertices (u16 indices, bit 15 = back-face flag)")
 
     def record(gl, ref):
         _begin_frame(gl)
         gl.UseProgram(abi.PROGRAM_GOURAUD)
-        gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
-        gl.UseBuffer(3, (ref("cr"), ref("cg"), ref("cb")))
-        gl.DrawElements(nverts, ref("idx"), 0)
+        if ntris <= per_draw:
+            gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
+            gl.UseBuffer(3, (ref("cr"), ref("cg"), ref("cb")))
+            gl.DrawElements(nverts, ref("idx"), 0)
+            return
+        for first in range(0, ntris, per_draw):
+            v0 = 3 * first
+            gl.UseBuffer(0, tuple(ref(k)[v0:] for k in ("px", "py", "pz")))
+            gl.UseBuffer(3, tuple(ref(k)[v0:] for k in ("cr", "cg", "cb")))
+            gl.DrawElements(3 * min(per_draw, ntris - first), ref("idx"), 0)
 
     return Scene("plain_raster", width, height, tile_blocks, arrays, record, ntris)
+
+
+BATCH_RESOLUTIONS = ((320, 180), (640, 360), (1280, 720), (1920, 1080), (3840, 2160))
+
+
+def batch_frames(seed=0, nframes=64, tris=(1_000, 1_000_000), resolutions=BATCH_RESOLUTIONS):
+    """Config-4 batch: nframes plain_raster frames (the config-1 generator,
+    frame i seeded seed * 1000 + i), triangle counts log-uniform in
+    [tris[0], tris[1]], resolutions drawn uniformly from `resolutions`.
+    Frames above 10 000 triangles shrink their triangles by sqrt(10 000 / n)
+    (plain_raster spread), which keeps the expected overdraw at that of the
+    10 000-triangle config-1 frame: unscaled, one 1M-triangle 3840x2160 frame
+    needs about 2e9 tile-list entries and 6e11 pixel tests."""
+    u = uniform01(seed + 7_000_001, nframes * 2).reshape(nframes, 2)
+    lo, hi = np.log(tris[0]), np.log(tris[1])
+    counts = np.rint(np.exp(lerp(lo, hi, u[:, 0]))).astype(np.int64)
+    pick = np.minimum((u[:, 1] * len(resolutions)).astype(np.int64), len(resolutions) - 1)
+    out = []
+    for i in range(nframes):
+        w, h = resolutions[int(pick[i])]
+        n = int(counts[i])
+        out.append(plain_raster(seed=seed * 1000 + i, ntris=n, width=w, height=h, tile_blocks=(4, 4),
+                                spread=min(1.0, float(np.sqrt(10_000.0 / n)))))
+    return out
 
 
 # ---- icosphere ----
