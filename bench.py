@@ -331,10 +331,41 @@ def _time_device(fn, steps, stream, flush):
     return statistics.mean(s.elapsed_time(e) for s, e in evs)
 
 
+def _time_graph(fn, steps, flush):
+    """Device time (ms, mean) of fn(stream_ptr) captured once in a CUDA graph
+    and replayed `steps` times; L2 flushed before each replay (untimed).
+    Host-side argument checks run at capture only."""
+    import torch
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        fn(s.cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        fn(s.cuda_stream)
+    torch.cuda.synchronize()
+    evs = []
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            g.replay()
+        for i in range(steps):
+            flush.fill_(i & 0xff)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            g.replay()
+            b.record(s)
+            evs.append((a, b))
+    torch.cuda.synchronize()
+    return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+
 def run_deferred(gpu, args, stream, flush):
     """The 64-light deferred scene (1920x1080, 2M objects, seed 100): G-buffer
     pass, plain shader, learned shader (committed weights) with its per-tile
-    fallback; PSNR / max-abs of the learned image against the plain one."""
+    fallback; PSNR / max-abs of the learned image against the plain one.
+    Shading times ("ms") are device times of CUDA-graph replays of one call
+    (the call's kernels and the gaps between them); "ms_per_api_call" times
+    the C-ABI call itself, host-side argument checks included."""
     import torch
     from rsr_gb300 import learned
     sptr = stream.cuda_stream
@@ -348,11 +379,12 @@ def run_deferred(gpu, args, stream, flush):
     res = {"workload": "deferred_1080p: 2M cubes/icosahedra seed 100, 64 point lights, Blinn-Phong 32",
            "steps": steps}
     gbuf_ms = _time_device(lambda: (gpu.run(sptr), gpu.Wait()), steps, stream, flush)
-    plain_ms = _time_device(lambda: fr.shade_plain(gpu, plain, stream=sptr), steps, stream, flush)
+    plain_call_ms = _time_device(lambda: fr.shade_plain(gpu, plain, stream=sptr), steps, stream, flush)
+    plain_ms = _time_graph(lambda sp: fr.shade_plain(gpu, plain, stream=sp), steps, flush)
     # plain shader bytes: G-buffer read (14 B/px), lights, sRGB8 write (4 B/px)
     plain_bytes = n * 18 + 64 * 32
     res["gbuffer_ms"] = gbuf_ms
-    res["plain"] = {"ms": plain_ms, "frames_per_s_shading": 1e3 / plain_ms,
+    res["plain"] = {"ms": plain_ms, "ms_per_api_call": plain_call_ms, "frames_per_s_shading": 1e3 / plain_ms,
                     "frames_per_s_frame": 1e3 / (gbuf_ms + plain_ms),
                     "roofline": {"kernel": "shade_plain_kernel", "bound": "compute (fp32, IEEE div/sqrt)",
                                  "achieved": plain_bytes / (plain_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -370,18 +402,42 @@ def run_deferred(gpu, args, stream, flush):
     torch.cuda.synchronize()
     db, maxabs = learned.psnr(out.cpu().numpy(), plain.cpu().numpy())
     st = status.cpu().numpy()
-    learned_ms = _time_device(lambda: fr.shade_learned(gpu, net, thr, out, stream=sptr), steps, stream, flush)
+    learned_call_ms = _time_device(lambda: fr.shade_learned(gpu, net, thr, out, stream=sptr), steps, stream, flush)
+    gpu.shade_learned_check()
+    learned_ms = _time_graph(lambda sp: fr.shade_learned(gpu, net, thr, out, stream=sp), steps, flush)
     gpu.shade_learned_check()
     served = float((st == 0).sum() / max(1, (st != 2).sum()))
     covered = int(fr.covered.sum().item())
     mlp_flops = 2 * (24 * 64 + 64 * 64 * 2 + 64 * 3)          # unpadded MACs x 2 per pixel
     tflops = covered * served * mlp_flops / (learned_ms / 1e3) / 1e12
-    res["learned"] = {"ms": learned_ms, "frames_per_s_shading": 1e3 / learned_ms,
+    res["learned"] = {"ms": learned_ms, "ms_per_api_call": learned_call_ms, "frames_per_s_shading": 1e3 / learned_ms,
                       "frames_per_s_frame": 1e3 / (gbuf_ms + learned_ms),
                       "speedup_vs_plain_shading": plain_ms / learned_ms,
                       "psnr_db_vs_plain": db, "max_abs_vs_plain": maxabs, "gate_max_tile_mse": thr,
                       "served_tiles": served, "covered_pixels": covered,
                       "mlp_tflops": tflops, "weights": {k: net.meta.get(k) for k in ("train_seeds", "samples", "steps")}}
+    # more lights on the same G-buffer (positions, colours, radii as the scene's 64)
+    from rsr_gb300 import scenes
+    scaling = []
+    lights64 = fr.lights
+    for nl in (128, 256):
+        lu = scenes.uniform01(100 + 101, nl * 7).reshape(nl, 7)
+        lt = np.zeros((nl, 8), np.float32)
+        lt[:, 0:3] = scenes.lerp(-10.0, 10.0, lu[:, 0:3])
+        lt[:, 3] = scenes.lerp(2.0, 6.0, lu[:, 3])
+        lt[:, 4:7] = scenes.lerp(0.0, 1.0, lu[:, 4:7])
+        fr.lights = torch.from_numpy(lt).cuda()
+        pm = _time_graph(lambda sp: fr.shade_plain(gpu, plain, stream=sp), steps, flush)
+        lm = _time_graph(lambda sp: fr.shade_learned(gpu, net, thr, out, tile_status=status, stream=sp), steps, flush)
+        gpu.shade_learned_check()
+        fr.shade_plain(gpu, plain, stream=sptr)
+        torch.cuda.synchronize()
+        db2, mx2 = learned.psnr(out.cpu().numpy(), plain.cpu().numpy())
+        st2 = status.cpu().numpy()
+        scaling.append({"lights": nl, "plain_ms": pm, "learned_ms": lm, "psnr_db_vs_plain": db2, "max_abs_vs_plain": mx2,
+                        "served_tiles": float((st2 == 0).sum() / max(1, (st2 != 2).sum()))})
+    fr.lights = lights64
+    res["light_scaling"] = scaling
     # end to end: G-buffer pass + shading + sRGB8 image read back to pinned host memory, wall clock
     host = torch.zeros(n, dtype=torch.int32).pin_memory()
     for name, shade in (("plain", lambda: fr.shade_plain(gpu, plain, stream=sptr)),

@@ -318,8 +318,10 @@ int rsrgpu_mlp_adam(rsrgpu_ctx* ctx, float* params, const float* grad, float* m,
  * INFINITY none.  tile_status (optional, one byte per tile in row-major
  * order): 0 learned, 1 plain, 2 nothing covered; tile_mse (optional) the
  * gate's estimate.  All pointers are device pointers; the call is enqueued
- * on `stream` and returns without waiting.  A tensor-core stall is reported
- * by the next rsrgpu_shade_learned_check(). */
+ * on `stream` and returns without waiting (it may be captured into a CUDA
+ * graph).  A tensor-core stall is reported by the next
+ * rsrgpu_shade_learned_check(); after graph replays, synchronise their
+ * stream before that check. */
 #define RSRGPU_SHADE_TILE 32
 int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gbuffer* gbuffer,
                          const float inv_view_proj[16], const float eye[3], const rsrgpu_light* lights, int nlights,

@@ -114,7 +114,8 @@ class CpuRenderer:
     def learned_features(self, gbuf, width, height, ivp, eye, lights, targets=True):
         """The learned shader's per-pixel inputs (oracle restatement): dict with
         'bf16' (H*W, 32) uint16, 'f32' (H*W, 24), 'targets' (H*W, 3) or None
-        (sqrt(plain) - base), 'base' (H*W, 3) and 'candidates' (tiles, 8) int32."""
+        (sqrt(plain) - base), 'base' (H*W, 3), 'candidates' (tiles, 8) int32 and
+        'reach' (H*W,) the candidate lights reaching each pixel."""
         from rsr_gb300 import abi
         if self.which != "oracle":
             raise RuntimeError("only the oracle implements the learned shader's inputs")
@@ -124,13 +125,14 @@ class CpuRenderer:
         tiles = ((width + 31) // 32) * ((height + 31) // 32)
         out = {"bf16": np.zeros((npx, 32), np.uint16), "f32": np.zeros((npx, 24), np.float32),
                "targets": np.zeros((npx, 3), np.float32) if targets else None,
-               "base": np.zeros((npx, 3), np.float32), "candidates": np.zeros((tiles, 8), np.int32)}
+               "base": np.zeros((npx, 3), np.float32), "candidates": np.zeros((tiles, 8), np.int32),
+               "reach": np.zeros(npx, np.uint8)}
         lights = np.ascontiguousarray(lights, np.float32)
         fa = lambda a: (ctypes.c_float * len(a))(*[float(x) for x in a])
         vp = lambda a: a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
         rc = self.lib.rsroracle_learned_features(ctypes.byref(g), fa(ivp), fa(eye), vp(lights), len(lights),
                                                  vp(out["bf16"]), vp(out["f32"]), vp(out["targets"]),
-                                                 vp(out["base"]), vp(out["candidates"]))
+                                                 vp(out["base"]), vp(out["candidates"]), vp(out["reach"]))
         if rc != 0:
             raise RuntimeError("oracle learned_features failed: %d" % rc)
         return out

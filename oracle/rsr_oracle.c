@@ -1324,8 +1324,9 @@ int rsroracle_learned_candidates(const rsrgpu_gbuffer* g, const float ivp[16], c
     return 0;
 }
 
-static void pixel_features(const rsrgpu_gbuffer* g, const float* ivp, const float* eye, const rsrgpu_light* lights,
-                           const int32_t* cand, int x, int y, float f[24]) {
+/* returns the number of candidate lights reaching the pixel */
+static int pixel_features(const rsrgpu_gbuffer* g, const float* ivp, const float* eye, const rsrgpu_light* lights,
+                          const int32_t* cand, int x, int y, float f[24]) {
     const size_t i = (size_t)y * g->width + x;
     float P[3];
     world_pos(g, ivp, x, y, P);
@@ -1341,12 +1342,14 @@ static void pixel_features(const rsrgpu_gbuffer* g, const float* ivp, const floa
     f[9] = vlen / 50.0f;
     for (int k = 10; k < 24; ++k) f[k] = 0.0f;
     float wsum = 0.0f;
+    int reach = 0;
     for (int c = 0; c < NCAND; ++c) {
         if (cand[c] < 0) break;
         const rsrgpu_light* l = &lights[cand[c]];
         float lx = l->position[0] - P[0], ly = l->position[1] - P[1], lz = l->position[2] - P[2];
         const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
         if (!(d < l->radius)) continue;
+        ++reach;
         const float q = d / l->radius;
         const float t = 1.0f - q;
         const float att = t * t;
@@ -1363,6 +1366,7 @@ static void pixel_features(const rsrgpu_gbuffer* g, const float* ivp, const floa
         wsum = wsum + w;
     }
     f[23] = wsum > 0.0f ? f[23] / wsum : 0.0f;
+    return reach;
 }
 
 /* The analytic base the network's output is added to: one virtual light with
@@ -1383,10 +1387,11 @@ static void virtual_light_base(const float* f, float base[3]) {
 
 /* features (bf16 [W*H][32]), features_f32 ([W*H][24], optional), targets
  * ([W*H][3] sqrt(max(plain, 0)) - base, optional), base ([W*H][3], optional),
- * candidates ([tiles][8], optional); uncovered pixels give zero rows */
+ * candidates ([tiles][8], optional), reach ([W*H], optional: candidate lights
+ * reaching the pixel); uncovered pixels give zero rows */
 int rsroracle_learned_features(const rsrgpu_gbuffer* g, const float ivp[16], const float eye[3],
                                const rsrgpu_light* lights, int nlights, uint16_t* features, float* features_f32,
-                               float* targets, float* base, int32_t* candidates) {
+                               float* targets, float* base, int32_t* candidates, uint8_t* reach) {
     const int tiles_x = (g->width + SHADE_TILE - 1) / SHADE_TILE, tiles_y = (g->height + SHADE_TILE - 1) / SHADE_TILE;
     const size_t npx = (size_t)g->width * g->height;
     float* plain = NULL;
@@ -1406,8 +1411,10 @@ int rsroracle_learned_features(const rsrgpu_gbuffer* g, const float ivp[16], con
                 const size_t i = (size_t)y * g->width + x;
                 float f[24];
                 const int covered = g->albedo[i] != 0;
-                if (covered) pixel_features(g, ivp, eye, lights, cand, x, y, f);
+                int nr = 0;
+                if (covered) nr = pixel_features(g, ivp, eye, lights, cand, x, y, f);
                 else for (int k = 0; k < 24; ++k) f[k] = 0.0f;
+                if (reach) reach[i] = (uint8_t)nr;
                 for (int k = 0; k < 32; ++k) features[i * 32 + k] = k < 24 ? bf16_rne(f[k]) : 0;
                 if (features_f32) memcpy(features_f32 + i * 24, f, sizeof(f));
                 float b[3] = { 0.0f, 0.0f, 0.0f };

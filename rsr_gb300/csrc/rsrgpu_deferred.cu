@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(128) learned_features_kernel(FeatParams F) {
     __shared__ rsrgpu_light lights[kMaxLights];
     __shared__ float box[2][4][3];
     __shared__ int cand[kCandidates];
+    __shared__ float scores[kMaxLights];
     const PlainParams& p = F.pl;
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
     for (int i = threadIdx.x; i < nl; i += blockDim.x) lights[i] = p.lights[i];
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(128) learned_features_kernel(FeatParams F) {
                 b1[k] = fmaxf(fmaxf(box[1][0][k], box[1][1][k]), fmaxf(box[1][2][k], box[1][3][k]));
             }
             const bool empty = !(b0[0] <= b1[0]);
-            select_candidates(empty ? 0 : nl, [&](int i) { return light_score(lights[i], b0, b1); }, cand);
+            select_candidates(empty ? 0 : nl, [&](int i) { return light_score(lights[i], b0, b1); }, cand, scores);
             if (lane == 0 && F.candidates)
                 for (int c = 0; c < kCandidates; ++c) F.candidates[tile * kCandidates + c] = cand[c];
         }
@@ -117,9 +118,9 @@ __global__ void __launch_bounds__(128) learned_features_kernel(FeatParams F) {
                 if (F.targets) { F.targets[3 * size_t(pi)] = 0.f; F.targets[3 * size_t(pi) + 1] = 0.f; F.targets[3 * size_t(pi) + 2] = 0.f; }
                 continue;
             }
-            float P[3], f[32];
-            world_pos(p, x, y, p.depth[pi], P);
-            pixel_features(p, lights, cand, P, p.nx[pi], p.ny[pi], p.nz[pi], alb, f);
+            float P[3], f[32], base[3];
+            world_pos_fast(p, x, y, p.depth[pi], P);
+            pixel_features_fast(p, lights, cand, P, p.nx[pi], p.ny[pi], p.nz[pi], alb, f, base);
             for (int q = kFeatures; q < 32; ++q) f[q] = 0.0f;
             uint32_t w[16];
             for (int q = 0; q < 16; ++q)
@@ -127,9 +128,8 @@ __global__ void __launch_bounds__(128) learned_features_kernel(FeatParams F) {
                        (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(f[2 * q + 1]))) << 16);
             for (int q = 0; q < 4; ++q) dst[q] = make_uint4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
             if (F.targets) {
-                float rgb[3], base[3];
+                float rgb[3];
                 plain_pixel(p, lights, nl, x, y, p.depth[pi], p.nx[pi], p.ny[pi], p.nz[pi], alb, rgb);
-                virtual_light_base(f, base);
                 for (int c = 0; c < 3; ++c) F.targets[3 * size_t(pi) + c] = sqrtf(pos0(rgb[c])) - base[c];
             }
         }

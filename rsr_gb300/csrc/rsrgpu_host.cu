@@ -51,7 +51,9 @@ cudaError_t launch_learned_features(const rsrgpu_gbuffer& gb, const float ivp[16
 cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
                                  const rsrgpu_light* lights, int nlights, const float background[3], float max_tile_mse,
                                  uint32_t* out_srgb, float* out_linear, uint8_t* tile_status, float* tile_mse,
-                                 const uint8_t* srgb_lut, int* error, int* tile_counter, int num_sms, cudaStream_t st);
+                                 const uint8_t* srgb_lut, int* error, int* counters, void* scratch,
+                                 int num_sms, cudaStream_t st);
+size_t learned_scratch_bytes(int tiles);
 
 static const uint32_t kRcpTable[2048] = {
 #include "rcpps_table.inc"
@@ -111,7 +113,7 @@ struct rsrgpu_ctx {
     // device memory
     DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
         d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs,
-        d_mlp_err, d_learn_err;
+        d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
     std::map<cudaStream_t, cudaEvent_t> learn_events;   // last learned-shader launch per stream
     int num_sms = 0;
     int* h_mlp_err = nullptr;   // pinned
@@ -365,7 +367,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -1096,17 +1098,28 @@ int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gb
         (rc = check_device_output(ctx, tile_status, tiles, 1, "tile status")) ||
         (rc = check_device_output(ctx, tile_mse, tiles * 4, 4, "tile mse")))
         return rc;
-    if (ctx->d_learn_err.p == nullptr) {   // [0] error flag, [1] tile counter
-        CK(ctx->d_learn_err.ensure(2 * sizeof(int)), "alloc learned-shader flags");
-        CK(cudaMemset(ctx->d_learn_err.p, 0, 2 * sizeof(int)), "clear learned-shader flags");
+    if (ctx->d_learn_err.p == nullptr) {   // [0] error flag, [1..3] work counters
+        CK(ctx->d_learn_err.ensure(4 * sizeof(int)), "alloc learned-shader flags");
+        CK(cudaMemset(ctx->d_learn_err.p, 0, 4 * sizeof(int)), "clear learned-shader flags");
     }
+    if (tile_status == nullptr) {   // the fallback pass reads the gate's decisions
+        CK(ctx->d_learn_status.ensure(tiles), "alloc tile status");
+        tile_status = ctx->d_learn_status.as<uint8_t>();
+    }
+    CK(ctx->d_learn_tiles.ensure(learned_scratch_bytes(int(tiles))), "alloc learned-shader blocks");
+    if (ctx->num_sms == 0)
+        CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
     CK(launch_shade_learned(*mlp, *gbuffer, inv_view_proj, eye, lights, nlights, background, max_tile_mse, out_srgb,
                             out_linear, tile_status, tile_mse, ctx->d_srgb.as<uint8_t>(), ctx->d_learn_err.as<int>(),
-                            ctx->d_learn_err.as<int>() + 1, ctx->num_sms, st), "shade_learned_kernel");
-    cudaEvent_t& ev = ctx->learn_events[st];
-    if (ev == nullptr) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "learned-shader event");
-    CK(cudaEventRecord(ev, st), "learned-shader event record");
+                            ctx->d_learn_err.as<int>() + 1, ctx->d_learn_tiles.p, ctx->num_sms, st), "shade_learned_kernel");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cap), "stream capture status");
+    if (cap == cudaStreamCaptureStatusNone) {   // a captured call is checked after its replays are synchronised
+        cudaEvent_t& ev = ctx->learn_events[st];
+        if (ev == nullptr) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "learned-shader event");
+        CK(cudaEventRecord(ev, st), "learned-shader event record");
+    }
     return 0;
 }
 
@@ -1166,6 +1179,10 @@ struct rsrgpu_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // raster launches of different CTA shapes run as parallel graph branches
+    static constexpr int kBranches = 4;
+    cudaStream_t aux[kBranches] = {};
+    cudaEvent_t fork = nullptr, join[kBranches] = {};
     bool ran = false;
     std::map<uint64_t, rsrgpu_frame_desc> tuned;   // (w, h, log2 ntris) -> choice
 };
@@ -1294,7 +1311,17 @@ int build_batch(rsrgpu_batch* b) {
     step(cudaMemsetAsync(b->d_super.p, 0x7f, sizeof(int4) * b->super_count, st), "memset super rects");
     step(launch_setup_batch(setup[0], sblocks, st), "setup_batch_kernel");
     step(launch_bin_batch(bin[0], bblocks, st), "bin_batch_kernel");
-    for (auto& kv : raster) step(launch_raster_batch(kv.second, rblocks[kv.first], kv.first, st), "raster_batch_kernel");
+    // one branch per CTA shape (the largest on the capture stream), joined before the read-back
+    int branch = 0;
+    if (raster.size() > 1) step(cudaEventRecord(b->fork, st), "fork");
+    for (auto it = raster.rbegin(); it != raster.rend(); ++it, ++branch) {
+        cudaStream_t rs = branch == 0 ? st : b->aux[(branch - 1) % rsrgpu_batch::kBranches];
+        if (branch > 0) step(cudaStreamWaitEvent(rs, b->fork, 0), "fork wait");
+        step(launch_raster_batch(it->second, rblocks[it->first], it->first, rs), "raster_batch_kernel");
+        if (branch > 0) step(cudaEventRecord(b->join[(branch - 1) % rsrgpu_batch::kBranches], rs), "join");
+    }
+    for (int k = 0; k + 1 < branch && k < rsrgpu_batch::kBranches; ++k)
+        step(cudaStreamWaitEvent(st, b->join[k], 0), "join wait");
     step(cudaMemcpyAsync(b->h_counters, b->d_counters.p, sizeof(FrameCounters) * size_t(n), cudaMemcpyDeviceToHost, st), "D2H counters");
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -1324,10 +1351,17 @@ int rsrgpu_batch_create(int device, rsrgpu_batch** out) {
     if (cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
         cudaHostAlloc(reinterpret_cast<void**>(&b->h_counters), sizeof(FrameCounters) * kMaxBatch, cudaHostAllocDefault) != cudaSuccess ||
-        b->d_counters.ensure(sizeof(FrameCounters) * kMaxBatch) != cudaSuccess) {
+        b->d_counters.ensure(sizeof(FrameCounters) * kMaxBatch) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
         rsrgpu_batch_destroy(b);
         return RSRGPU_ECUDA;
     }
+    for (int k = 0; k < rsrgpu_batch::kBranches; ++k)
+        if (cudaStreamCreateWithFlags(&b->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming) != cudaSuccess) {
+            rsrgpu_batch_destroy(b);
+            return RSRGPU_ECUDA;
+        }
     *out = b;
     return 0;
 }
@@ -1344,6 +1378,11 @@ int rsrgpu_batch_destroy(rsrgpu_batch* b) {
     b->d_tables.release(); b->d_counters.release(); b->d_super.release();
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (int k = 0; k < rsrgpu_batch::kBranches; ++k) {
+        if (b->join[k]) cudaEventDestroy(b->join[k]);
+        if (b->aux[k]) cudaStreamDestroy(b->aux[k]);
+    }
     if (b->own) cudaStreamDestroy(b->own);
     delete b;
     return 0;

@@ -1,28 +1,53 @@
-// rsrgpu_learned.cu -- the learned deferred shader as one fused kernel.
+// rsrgpu_learned.cu -- the learned deferred shader: a per-tile SIMT pre-pass,
+// a persistent tensor-core kernel fed by bulk copies, and a fallback pass.
 //
-// Persistent CTAs of four warps take 32x32 shading tiles from a counter:
-//   1. coverage of the tile's pixels, compacted into a list (the tile's 4x4
-//      grid of gate sample pixels first) and the world-space box of the
-//      covered pixels; background pixels are written at once
-//   2. warp 0 picks the tile's candidate lights (rsrgpu_shading.cuh)
-//   3. the gate's reference: the plain shader at the first min(16, covered)
-//      listed pixels, each split over eight threads
-//   4. for each 128 covered pixels: 24 features per pixel into a BF16 A tile
-//      and the analytic base (virtual_light_base, FP32), the MLP's four
-//      layers on tcgen05, output rgb = max(y + base, 0)^2 (the network
-//      predicts the residual of square roots of linear RGB); after the first
-//      128 the gate compares the learned and plain sRGB8 values of the samples
-//      and, when their mean squared error exceeds the threshold, the tile is
-//      shaded by the plain shader instead (bit-exact with rsrgpu_shade_plain),
-//      skipping the remaining MLP work
+// The shader's output is rgb = max(y + base, 0)^2 per channel, base the
+// square root of the analytic virtual-light estimate and y the network's
+// residual.  A pixel reached by at most one of its tile's candidate lights
+// needs no network: its virtual light is that light, so base is its
+// Blinn-Phong shading; only pixels reached by two or more go through the MLP.
 //
-// The biases ride in the MMAs: every A tile carries two columns of ones and
-// every weight tile the bias split into a BF16 high part and a BF16 low part
-// (b - hi), so D = A W^T already holds W a + b to about 2^-16 relative; the
-// epilogue is one cvt.rn.relu.bf16x2 per two activations.  One shared-memory
-// A buffer serves all layers: layer 1 reads it as 128 x 32 (features, ones
-// at 24 and 25), the hidden layers as 128 x 80 (activations, ones at 64 and
-// 65); each MMA group has completed before the epilogue overwrites it.
+// learned_prep_kernel (one CTA of 128 threads per 32x32 shading tile, many
+// resident per SM so that their latency chains overlap): coverage and
+// compaction (the tile's 4x4 grid of gate samples first), the world-space box
+// of the covered pixels, the candidate lights, the plain shader at the gate
+// samples (8 threads per sample), background pixels; then, list entry
+// i * 128 + t per pass, the features and base of every covered pixel: pixels
+// on the exact path are written at once, the others are compacted (ballot,
+// list order) into the tile's blocks of 128 rows -- an 8 KB A tile per block
+// (24 BF16 features and two ones columns per row, in the chunked layout
+// below) and a PipeMeta record (base, pixel index, gate samples) -- and the
+// tile's blocks are appended to a block list.
+//
+// shade_learned_kernel (one CTA per SM): two lanes, each a producer thread
+//   and a consumer warpgroup joined by three pipelines.  The producer takes
+//   blocks from the list and, for each, waits for the next pipeline's slot
+//   to be free and issues two bulk copies (cp.async.bulk) of the block's A
+//   tile and record into it, completed on the pipeline's full barrier by
+//   transaction count.  The consumer visits its pipelines in turn and
+//   advances each by one step: issue layer 1 from a full slot (the block's
+//   record goes to registers), or, when the pipeline's MMAs have completed,
+//   run the epilogue (TMEM -> ReLU -> BF16 into the pipeline's activation
+//   tile) and issue the next layer -- after layer 1 the slot goes back to the
+//   producer, whose copy of the next block overlaps layers 2-4 -- or after
+//   layer 4 write rgb; while one pipeline's MMAs run the warpgroup serves the
+//   other two.
+// The gate: the mean squared difference of learned and plain sRGB8 values
+// over the tile's samples -- those on the exact path are scored in the
+// pre-pass (which decides alone when all are), the others after layer 4 of
+// the tile's first block.  Rejected tiles go to a list; shade_fallback_kernel
+// shades them with the plain shader afterwards (bit-exact with
+// rsrgpu_shade_plain).  The three kernels are chained by programmatic
+// dependent launch.
+//
+// A tiles use a chunked K-major layout: chunk j (8 columns) of all 128 rows
+// is 2 KB, row r at j * 2048 + (r / 8) * 128 + (r % 8) * 16 (descriptor LBO
+// 2048, SBO 128).  Layer 1 reads the 8 KB slot (features, ones at columns
+// 24-25), the hidden layers the pipeline's 20 KB activation tile
+// (activations, ones at 64-65, zeros); the biases ride in the weights as a
+// BF16 high/low pair, so the epilogue is one cvt.rn.relu.bf16x2 per two
+// activations.  Six pipelines x 64 TMEM columns.  Every wait is bounded; on
+// expiry the kernel raises the error flag and winds down.
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -35,35 +60,59 @@ namespace rsrgpu {
 
 constexpr int kTilePx = kShadeTile * kShadeTile;   // 1024
 constexpr int kGateSamples = 16;
-constexpr int kK1 = 32;          // layer-1 K: 24 features, ones at 24/25, zeros
-constexpr int kKH = 80;          // hidden-layer K: 64 activations, ones at 64/65, zeros
+constexpr int kK1 = 32;                 // layer-1 K: 24 features, ones at 24/25, zeros
+constexpr int kKH = 80;                 // hidden-layer K: 64 activations, ones at 64/65, zeros
+constexpr int kLanes = 2;               // producer/consumer pairs per CTA
+constexpr int kPipes = 3;               // pipelines per lane
+constexpr int kChunk = kRows * 16;      // one 8-column chunk of a 128-row tile
+constexpr int kTileBytes = kChunk * (kKH / 8);
+constexpr int kFeatBytes = kChunk * (kK1 / 8);     // the A tile of layer 1: 8 KB
+constexpr int kBlocksPerTile = kTilePx / kRows;    // 8
+constexpr int kThreads = 320;           // 2 consumer warpgroups + 2 producer warps
+
+struct PipeMeta {
+    float base[kRows][3];
+    int32_t pix[kRows];                 // pixel index, -1: row unused
+    uint32_t gate_plain[kGateSamples];  // plain shader at the gate samples among the rows, packed sRGB8
+    int32_t tile;                       // -1: no more work
+    int32_t first;                      // the tile's first block (its first rows are gate samples)
+    int32_t ngate;                      // gate samples among this block's rows
+    int32_t ngate_total;                // the tile's gate samples
+    int32_t gate_err;                   // squared sRGB8 error of the samples shaded in the pre-pass
+    int32_t pad[3];
+};
+static_assert(sizeof(PipeMeta) % 16 == 0, "bulk copies move multiples of 16 bytes");
+
+// tile t's blocks live at t * 8 .. t * 8 + 7 of the block arrays; the
+// pre-pass appends the index of every block it fills to a block list
 
 struct LearnSmem {
-    alignas(128) uint8_t w1[kHid * kK1 * 2];      // 64 x 32
-    alignas(128) uint8_t w2[kHid * kKH * 2];      // 64 x 80
+    alignas(128) uint8_t act[kLanes * kPipes][kTileBytes];     // hidden-layer A tiles
+    alignas(128) uint8_t feat[kLanes * kPipes][kFeatBytes];    // layer-1 A tiles (bulk-copied)
+    alignas(128) uint8_t w1[kHid * kK1 * 2];
+    alignas(128) uint8_t w2[kHid * kKH * 2];
     alignas(128) uint8_t w3[kHid * kKH * 2];
-    alignas(128) uint8_t w4[kOut * kKH * 2];      // 16 x 80
-    alignas(128) uint8_t act[kRows * kKH * 2];    // A operand of every layer
-    uint16_t list[kTilePx];                       // covered pixels (tile-local index y * 32 + x)
-    float box[2][4][3];
-    int scan[4];
-    int cand[kCandidates];
-    float gate_plain[kGateSamples][3];
-    int gate_sum;
-    int tile;
-    uint64_t mbar;
+    alignas(128) uint8_t w4[kOut * kKH * 2];
+    alignas(16) PipeMeta meta[kLanes * kPipes];
+    uint64_t full[kLanes * kPipes], empty[kLanes * kPipes], mma[kLanes * kPipes];
+    int gate_sum[kLanes];
     uint32_t tmem;
-    alignas(16) rsrgpu_light lights[1];           // nlights entries (dynamic shared memory)
+    int abort;
 };
 
 struct LearnParams {
     PlainParams pl;
     rsrgpu_mlp w;
     float max_tile_mse;       // in 8-bit sRGB units squared
-    uint8_t* tile_status;     // [tiles] or null: 0 learned, 1 plain fallback, 2 nothing covered
+    uint8_t* tile_status;     // [tiles]: 0 learned, 1 plain fallback, 2 nothing covered
     float* tile_mse;          // [tiles] or null: the gate's estimate
     int* error;
-    int* tile_counter;        // zero at launch
+    int* counters;            // [0] blocks taken by the producers, [1] blocks listed, [2] tiles
+                              // rejected by the gate; zero at launch
+    int32_t* blocks;          // [tiles * 8] the filled blocks
+    int32_t* rejected;        // [tiles] tiles for the fallback pass
+    uint8_t* feat;            // [tiles * 8][8 KB] A tiles
+    PipeMeta* metas;          // [tiles * 8]
 };
 
 __device__ __forceinline__ void store_pixel(const PlainParams& p, int pi, const float rgb[3]) {
@@ -73,9 +122,226 @@ __device__ __forceinline__ void store_pixel(const PlainParams& p, int pi, const 
 
 __device__ __forceinline__ uint16_t bf16_rn(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
 
+// row r, columns 8j..8j+7 of a chunked 128-row tile
+__device__ __forceinline__ uint4* chunk_row(uint8_t* tile, int j, int r) {
+    return reinterpret_cast<uint4*>(tile + j * kChunk + (r >> 3) * 128 + (r & 7) * 16);
+}
+
+// ---------------------------------------------------------------- pre-pass
+__global__ void __launch_bounds__(128, 8) learned_prep_kernel(LearnParams A) {
+    extern __shared__ rsrgpu_light L[];
+    __shared__ uint16_t list[kTilePx];
+    __shared__ float box[2][4][3];
+    __shared__ int scan[4];
+    __shared__ int cand[kCandidates];
+    __shared__ float scores[kMaxLights];
+    __shared__ uint32_t gate_plain[kGateSamples];
+    __shared__ int gate_err, netsamples;
+    __shared__ int wcount[2][4];
+    const PlainParams& p = A.pl;
+    const int t = threadIdx.x, wl = t & 31, warp = t >> 5;
+    const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
+    for (int i = t; i < nl; i += blockDim.x) L[i] = p.lights[i];
+    const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile;
+    const int tile = blockIdx.x;
+    const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
+    // ---- coverage, compaction (gate samples first), box ----
+    const int ly = t / 4, lx0 = (t % 4) * 8;
+    const int y = y0 + ly;
+    const uint32_t bg = pack_srgb(p.srgb_lut, p.background);
+    uint32_t cov = 0;
+    float zd[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int x = x0 + lx0 + j;
+        zd[j] = 1.0f;
+        if (x >= p.width || y >= p.height) continue;
+        const int pi = y * p.width + x;
+        zd[j] = p.depth[pi];   // loaded with the albedo: one round trip for both
+        if (p.albedo[pi] != 0u) {
+            cov |= 1u << j;
+        } else {
+            if (p.out_srgb) p.out_srgb[pi] = bg;
+            if (p.out_linear) { p.out_linear[3 * size_t(pi)] = p.background[0]; p.out_linear[3 * size_t(pi) + 1] = p.background[1]; p.out_linear[3 * size_t(pi) + 2] = p.background[2]; }
+        }
+    }
+    const uint32_t smp = ((ly & 7) == 4) ? (cov & 0x10u) : 0u;
+    const int mine = (__popc(smp) << 16) | __popc(cov & ~smp);
+    int incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (wl >= o) incl += v;
+    }
+    if (wl == 31) scan[warp] = incl;
+    __syncthreads();
+    int before = incl - mine;
+    for (int w = 0; w < warp; ++w) before += scan[w];
+    const int total = (scan[0] + scan[1]) + (scan[2] + scan[3]);
+    const int nsmp = total >> 16, ncov = nsmp + (total & 0xffff);
+    int sp = before >> 16, op = nsmp + (before & 0xffff);
+    float lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        if (!((cov >> j) & 1u)) continue;
+        const int slot = ((smp >> j) & 1u) ? sp++ : op++;
+        const int x = x0 + lx0 + j;
+        list[slot] = uint16_t(ly * kShadeTile + lx0 + j);
+        float Q[3];
+        world_pos(p, x, y, zd[j], Q);
+        for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], Q[k]); hi[k] = fmaxf(hi[k], Q[k]); }
+    }
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+        if (wl == 0) { box[0][warp][k] = lo[k]; box[1][warp][k] = hi[k]; }
+    }
+    __syncthreads();
+    if (ncov == 0) {
+        if (t == 0) {
+            A.tile_status[tile] = 2;
+            if (A.tile_mse) A.tile_mse[tile] = 0.0f;
+        }
+        return;
+    }
+    // ---- candidate lights (warp 0), gate samples (8 threads each) ----
+    if (warp == 0) {
+        float b0[3], b1[3];
+        for (int k = 0; k < 3; ++k) {
+            b0[k] = fminf(fminf(box[0][0][k], box[0][1][k]), fminf(box[0][2][k], box[0][3][k]));
+            b1[k] = fmaxf(fmaxf(box[1][0][k], box[1][1][k]), fmaxf(box[1][2][k], box[1][3][k]));
+        }
+        select_candidates(nl, [&](int i) { return light_score(L[i], b0, b1); }, cand, scores);
+    }
+    const int ngate = ncov < kGateSamples ? ncov : kGateSamples;
+    {
+        const int sj = t >> 3, g = t & 7;
+        float s[3] = { 0.0f, 0.0f, 0.0f }, a[3] = { 0.0f, 0.0f, 0.0f };
+        if (sj < ngate) {
+            const int li = list[sj];
+            const int x = x0 + li % kShadeTile, yy = y0 + li / kShadeTile;
+            const int pi = yy * p.width + x;
+            float Q[3], n[3], v[3];
+            world_pos_fast(p, x, yy, p.depth[pi], Q);
+            surface_fast(p, Q, p.nx[pi], p.ny[pi], p.nz[pi], n, v);
+            albedo_rgb(p.albedo[pi], a);
+            plain_sum_fast(L, g, 8, nl, Q, n, v, a, s);
+        }
+        for (int o = 1; o < 8; o <<= 1)
+            for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+        if (sj < ngate && g == 0) {
+            const float rgb[3] = { s[0] + 0.03f * a[0], s[1] + 0.03f * a[1], s[2] + 0.03f * a[2] };
+            gate_plain[sj] = pack_srgb(p.srgb_lut, rgb);
+        }
+    }
+    __syncthreads();
+    // ---- features; pixels reached by two or more candidate lights become the
+    // network's rows (in list order, so the gate samples come first), the
+    // others take the analytic base, which is then their Blinn-Phong shading.
+    // Entry i * 128 + t per pass: consecutive threads, consecutive pixels. ----
+    if (t == 0) { gate_err = 0; netsamples = 0; }
+    const uint32_t one2 = uint32_t(bf16_rn(1.0f)) | (uint32_t(bf16_rn(1.0f)) << 16);
+    const uint32_t lt = (1u << wl) - 1u;
+    int nrows = 0;
+    __syncthreads();
+    // G-buffer values of this thread's next list entry, fetched a pass ahead
+    struct Px { int pi; float z; uint16_t hx, hy, hz; uint32_t alb; };
+    auto fetch = [&](int r, Px& q) {
+        if (r >= ncov) return;
+        const int li = list[r];
+        q.pi = (y0 + li / kShadeTile) * p.width + x0 + li % kShadeTile;
+        q.z = p.depth[q.pi]; q.hx = p.nx[q.pi]; q.hy = p.ny[q.pi]; q.hz = p.nz[q.pi]; q.alb = p.albedo[q.pi];
+    };
+    Px nxt{ 0, 0.0f, 0, 0, 0, 0u };
+    fetch(t, nxt);
+    for (int i = 0; i * kRows < ncov; ++i) {
+        const int r = i * kRows + t;
+        const Px cur = nxt;
+        fetch(r + kRows, nxt);
+        bool net = false;
+        const int pi = cur.pi;
+        float f[kFeatures], base[3];
+        if (r < ncov) {
+            const int x = pi % p.width, yy = pi / p.width;
+            float Q[3];
+            world_pos_fast(p, x, yy, cur.z, Q);
+            net = pixel_features_fast(p, L, cand, Q, cur.hx, cur.hy, cur.hz, cur.alb, f, base) >= 2;
+            if (!net) {
+                const float rgb[3] = { base[0] * base[0], base[1] * base[1], base[2] * base[2] };
+                store_pixel(p, pi, rgb);
+                if (r < ngate) {
+                    int err = 0;
+                    for (int c = 0; c < 3; ++c) {
+                        const int d = int(srgb8_lut(p.srgb_lut, rgb[c])) - int((gate_plain[r] >> (16 - 8 * c)) & 255u);
+                        err += d * d;
+                    }
+                    atomicAdd(&gate_err, err);
+                }
+            }
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, net);
+        if (wl == 0) wcount[i & 1][warp] = __popc(bal);
+        __syncthreads();
+        int slot = nrows + __popc(bal & lt);
+        for (int w = 0; w < warp; ++w) slot += wcount[i & 1][w];
+        nrows += (wcount[i & 1][0] + wcount[i & 1][1]) + (wcount[i & 1][2] + wcount[i & 1][3]);
+        if (net) {
+            const int blk = tile * kBlocksPerTile + slot / kRows, row = slot % kRows;
+            uint8_t* ftile = A.feat + size_t(blk) * kFeatBytes;
+            PipeMeta& M = A.metas[blk];
+            uint32_t w[16];
+#pragma unroll
+            for (int q = 0; q < 12; ++q) w[q] = pack_bf16x2(f[2 * q], f[2 * q + 1]);
+            w[12] = one2;
+            w[13] = w[14] = w[15] = 0u;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) *chunk_row(ftile, j, row) = make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
+            M.base[row][0] = base[0]; M.base[row][1] = base[1]; M.base[row][2] = base[2];
+            M.pix[row] = pi;
+            if (r < ngate) { M.gate_plain[slot] = gate_plain[r]; atomicAdd(&netsamples, 1); }
+        }
+    }
+    const int nblocks = (nrows + kRows - 1) / kRows;
+    // rows of the last block past the network's pixels
+    for (int sidx = nrows + t; sidx < nblocks * kRows; sidx += blockDim.x) {
+        const int blk = tile * kBlocksPerTile + sidx / kRows, row = sidx % kRows;
+        uint8_t* ftile = A.feat + size_t(blk) * kFeatBytes;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) *chunk_row(ftile, j, row) = make_uint4(0u, 0u, 0u, 0u);
+        PipeMeta& M = A.metas[blk];
+        M.base[row][0] = M.base[row][1] = M.base[row][2] = 0.0f;
+        M.pix[row] = -1;
+    }
+    __syncthreads();
+    if (t < nblocks) {
+        PipeMeta& M = A.metas[tile * kBlocksPerTile + t];
+        M.tile = tile;
+        M.first = t == 0;
+        M.ngate = t == 0 ? netsamples : 0;
+        M.ngate_total = ngate;
+        M.gate_err = gate_err;
+        M.pad[0] = M.pad[1] = M.pad[2] = 0;
+    }
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (t == 0) {
+        if (nblocks == 0) {   // every sample on the exact path: the gate decides here
+            const float mse = float(gate_err) / float(3 * ngate);
+            const int fb = mse > A.max_tile_mse ? 1 : 0;
+            A.tile_status[tile] = uint8_t(fb);
+            if (A.tile_mse) A.tile_mse[tile] = mse;
+            if (fb) A.rejected[atomicAdd(A.counters + 2, 1)] = tile;
+        } else {
+            const int at = atomicAdd(A.counters + 1, nblocks);
+            for (int b = 0; b < nblocks; ++b) A.blocks[at + b] = tile * kBlocksPerTile + b;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- tensor-core kernel
 // W (the first KSRC columns of a row-major [rows][LD] bf16 matrix) plus the
-// bias as columns KSRC (high) and KSRC+1 (low), zeros to KDIM, into a K-major
-// tile of K = KDIM; 16-byte chunks (8 columns of one row) per thread
+// bias as columns KSRC (high) and KSRC+1 (low), zeros to KDIM, into the
+// row-wise K-major layout (LBO 128, SBO KDIM/8 * 128); 16-byte chunks
 template <int KSRC, int LD, int KDIM>
 __device__ __forceinline__ void load_weights_bias(uint8_t* dst, const uint16_t* __restrict__ W, int rows,
                                                   const float* __restrict__ bias) {
@@ -95,260 +361,251 @@ __device__ __forceinline__ void load_weights_bias(uint8_t* dst, const uint16_t* 
     }
 }
 
-// MMAs of one layer: D[128 x n] = act (128 x kdim) * W (n x kdim)^T, committed to mbar
+// D[128 x n] = A (chunked, K = kdim) * W (n x kdim, row-wise K-major)^T, committed to mbar
 __device__ __forceinline__ void issue(uint32_t d, const uint8_t* a, const uint8_t* w, int kdim, int n, uint64_t* mbar) {
     tc::fence_after_sync();
     const uint32_t sa = tc::smem_addr(a), sw = tc::smem_addr(w);
-    const uint32_t sbo = uint32_t(kdim / 8) * 128u;
+    const uint32_t wsbo = uint32_t(kdim / 8) * 128u;
     for (int ks = 0; ks < kdim / 16; ++ks)
-        tc::mma_bf16(d, tc::smem_desc(sa + ks * 256u, 128u, sbo), tc::smem_desc(sw + ks * 256u, 128u, sbo),
+        tc::mma_bf16(d, tc::smem_desc(sa + ks * 2u * kChunk, kChunk, 128u), tc::smem_desc(sw + ks * 256u, 128u, wsbo),
                      tc::idesc_bf16(kRows, n), ks > 0 ? 1u : 0u);
     tc::mma_commit(mbar);
 }
 
-// TMEM row (64 fp32 columns) -> ReLU -> BF16 activations of row t (K = 80 layout)
-__device__ __forceinline__ void relu_epilogue(uint32_t trow, uint8_t* act, int t) {
-    uint32_t r[64];
-    tc::tmem_ld32_nowait(trow, r);
-    tc::tmem_ld32_nowait(trow + 32, r + 32);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int c = 0; c < 64; c += 8) {
-        uint4 pk;
-        pk.x = tc::relu_bf16x2(r[c], r[c + 1]); pk.y = tc::relu_bf16x2(r[c + 2], r[c + 3]);
-        pk.z = tc::relu_bf16x2(r[c + 4], r[c + 5]); pk.w = tc::relu_bf16x2(r[c + 6], r[c + 7]);
-        *reinterpret_cast<uint4*>(act + tc::kmajor_offset(t, c, kKH)) = pk;
+// bounded wait that also gives up when the CTA is winding down
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
+    for (uint32_t i = 0; i < (1u << 22); ++i) {
+        if (tc::mbar_try_wait(bar, parity)) return true;
+        if ((i & 255u) == 255u && *abort) return false;
+        if (i > 64) __nanosleep(32);
+    }
+    *abort = 1;
+    return false;
+}
+
+// one thread per lane: blocks from the list into the lane's pipelines
+__device__ void produce(LearnSmem& S, const LearnParams& A, int lane) {
+    volatile int* abort = &S.abort;
+    uint32_t eparity = 0xfu;   // per pipeline: the parity to wait for on its empty barrier (fresh: passes)
+    int pipe = 0;
+    const int nblocks = *reinterpret_cast<volatile int*>(A.counters + 1);
+    for (;;) {
+        const int k = atomicAdd(A.counters, 1);
+        if (k >= nblocks || *abort) break;
+        const int blk = A.blocks[k];
+        const int pp = lane * kPipes + pipe;
+        if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort)) break;
+        eparity ^= 1u << pipe;
+        tc::mbar_arrive_expect_tx(&S.full[pp], uint32_t(kFeatBytes + sizeof(PipeMeta)));
+        tc::bulk_g2s(S.feat[pp], A.feat + size_t(blk) * kFeatBytes, kFeatBytes, &S.full[pp]);
+        tc::bulk_g2s(&S.meta[pp], A.metas + blk, uint32_t(sizeof(PipeMeta)), &S.full[pp]);
+        pipe = (pipe + 1) % kPipes;
+    }
+    // end of work: one sentinel per pipeline
+    for (int k = 0; k < kPipes && !*abort; ++k) {
+        const int pp = lane * kPipes + pipe;
+        if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort)) break;
+        eparity ^= 1u << pipe;
+        S.meta[pp].tile = -1;
+        tc::mbar_arrive(&S.full[pp]);
+        pipe = (pipe + 1) % kPipes;
     }
 }
 
-__global__ void __launch_bounds__(128, 4) shade_learned_kernel(LearnParams A) {
+// Per pipeline: wait for a full slot, keep the block's record in registers
+// and issue layer 1 from the slot; when layer 1 has completed the slot is
+// handed back to the producer (it refills it while layers 2-4 run) and the
+// epilogues pass the activations through the pipeline's own A tile.
+struct BlockRegs {
+    int stage;          // 0 wait for a full slot, 1..4 layer in flight, 5 finished
+    int pix, tile, first, ngate, ngate_total, gate_err;
+    float base[3];
+    uint32_t gate;      // thread t < 16: the plain value of sample t
+};
+
+__device__ __forceinline__ void consume_step(LearnSmem& S, const LearnParams& A, int lane, int pipe, BlockRegs& B,
+                                             uint32_t& fparity, uint32_t& mparity, int& done) {
+    const PlainParams& p = A.pl;
+    const int t = threadIdx.x & 127, warp = (threadIdx.x >> 5) & 3;
+    const int bar = 1 + lane;
+    volatile int* abort = &S.abort;
+    const int pp = lane * kPipes + pipe;
+    const uint32_t dcol = S.tmem + uint32_t(64 * pp);
+    const uint32_t trow = dcol + (uint32_t(warp * 32) << 16);
+    uint8_t* tileb = S.act[pp];
+    if (B.stage == 0) {
+        if (!wait_or_abort(&S.full[pp], (fparity >> pipe) & 1u, abort)) return;
+        fparity ^= 1u << pipe;
+        const PipeMeta& M = S.meta[pp];
+        B.tile = M.tile;
+        if (B.tile < 0) { B.stage = 5; ++done; return; }
+        B.pix = M.pix[t];
+        B.base[0] = M.base[t][0]; B.base[1] = M.base[t][1]; B.base[2] = M.base[t][2];
+        B.first = M.first; B.ngate = M.ngate; B.ngate_total = M.ngate_total; B.gate_err = M.gate_err;
+        B.gate = t < kGateSamples ? M.gate_plain[t] : 0u;
+        if (t == 0) issue(dcol, S.feat[pp], S.w1, kK1, kHid, &S.mma[pp]);
+        B.stage = 1;
+        return;
+    }
+    if (!wait_or_abort(&S.mma[pp], (mparity >> pipe) & 1u, abort)) return;
+    mparity ^= 1u << pipe;
+    tc::fence_after_sync();
+    if (B.stage < 4) {
+        uint32_t r[64];
+        tc::tmem_ld32_nowait(trow, r);
+        tc::tmem_ld32_nowait(trow + 32, r + 32);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            *chunk_row(tileb, j, t) = make_uint4(tc::relu_bf16x2(r[8 * j], r[8 * j + 1]), tc::relu_bf16x2(r[8 * j + 2], r[8 * j + 3]),
+                                                 tc::relu_bf16x2(r[8 * j + 4], r[8 * j + 5]), tc::relu_bf16x2(r[8 * j + 6], r[8 * j + 7]));
+        tc::fence_smem_for_mma();
+        tc::fence_before_sync();
+        tc::wg_sync(bar);
+        if (t == 0) {
+            // layer 1 has read the slot and every thread has its record: the producer may refill it
+            if (B.stage == 1) tc::mbar_arrive(&S.empty[pp]);
+            issue(dcol, tileb, B.stage == 1 ? S.w2 : B.stage == 2 ? S.w3 : S.w4, kKH, B.stage == 3 ? kOut : kHid, &S.mma[pp]);
+        }
+        B.stage += 1;
+        return;
+    }
+    // ---- layer 4 done: output ----
+    uint32_t v[32];
+    tc::tmem_ld32_nowait(trow, v);
+    tc::tmem_wait_ld();
+    float rgb[3];
+    for (int c = 0; c < 3; ++c) {
+        const float q = pos0(__uint_as_float(v[c]) + B.base[c]);
+        rgb[c] = q * q;
+    }
+    if (B.first) {
+        if (t == 0) S.gate_sum[lane] = B.gate_err;   // the samples shaded in the pre-pass
+        tc::wg_sync(bar);
+        if (t < B.ngate) {
+            int e = 0;
+            for (int c = 0; c < 3; ++c) {
+                const int d = int(srgb8_lut(p.srgb_lut, rgb[c])) - int((B.gate >> (16 - 8 * c)) & 255u);
+                e += d * d;
+            }
+            atomicAdd(&S.gate_sum[lane], e);
+        }
+        tc::wg_sync(bar);
+        const float mse = float(S.gate_sum[lane]) / float(3 * B.ngate_total);
+        const int fb = mse > A.max_tile_mse ? 1 : 0;
+        if (t == 0) {
+            A.tile_status[B.tile] = uint8_t(fb);
+            if (A.tile_mse) A.tile_mse[B.tile] = mse;
+            if (fb) A.rejected[atomicAdd(A.counters + 2, 1)] = B.tile;
+        }
+    }
+    // pixels of tiles the gate rejects are overwritten by the fallback pass
+    if (B.pix >= 0) store_pixel(p, B.pix, rgb);
+    // every thread's TMEM reads precede the next block's layer 1 in these columns
+    tc::fence_before_sync();
+    tc::wg_sync(bar);
+    B.stage = 0;
+}
+
+__device__ void consume(LearnSmem& S, const LearnParams& A, int lane) {
+    BlockRegs B[kPipes];
+#pragma unroll
+    for (int k = 0; k < kPipes; ++k) B[k].stage = 0;
+    uint32_t fparity = 0, mparity = 0;
+    int done = 0;
+    volatile int* abort = &S.abort;
+    while (done < kPipes && !*abort) {
+#pragma unroll
+        for (int k = 0; k < kPipes; ++k)
+            if (B[k].stage != 5 && !*abort) consume_step(S, A, lane, k, B[k], fparity, mparity, done);
+    }
+    // winding down after an expired wait: let issued MMAs finish before TMEM is released
+    if (*abort) {
+#pragma unroll
+        for (int k = 0; k < kPipes; ++k)
+            if (B[k].stage >= 1 && B[k].stage <= 4)
+                tc::mbar_wait(&S.mma[lane * kPipes + k], (mparity >> k) & 1u, 1u << 20);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) shade_learned_kernel(LearnParams A) {
     extern __shared__ uint8_t smem_raw[];
     LearnSmem& S = *reinterpret_cast<LearnSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const PlainParams& p = A.pl;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
+    const int t = threadIdx.x, warp = t >> 5;
     load_weights_bias<kFeatures, kIn, kK1>(S.w1, A.w.w1, kHid, A.w.b1);
     load_weights_bias<kHid, kHid, kKH>(S.w2, A.w.w2, kHid, A.w.b2);
     load_weights_bias<kHid, kHid, kKH>(S.w3, A.w.w3, kHid, A.w.b3);
     load_weights_bias<kHid, kHid, kKH>(S.w4, A.w.w4, kOut, A.w.b4);
-    for (int i = t; i < nl; i += blockDim.x) S.lights[i] = p.lights[i];
-    if (t == 0) tc::mbar_init(&S.mbar, 1);
-    if (warp == 0) { tc::tmem_alloc(&S.tmem, 64); tc::tmem_relinquish(); }
+    // the constant chunks 8 (ones at columns 64, 65) and 9 (zeros) of every pipeline tile
+    const uint32_t one2 = uint32_t(bf16_rn(1.0f)) | (uint32_t(bf16_rn(1.0f)) << 16);
+    for (int i = t; i < kLanes * kPipes * kRows; i += blockDim.x) {
+        uint8_t* tileb = S.act[i / kRows];
+        *chunk_row(tileb, 8, i % kRows) = make_uint4(one2, 0u, 0u, 0u);
+        *chunk_row(tileb, 9, i % kRows) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (t == 0) {
+        for (int i = 0; i < kLanes * kPipes; ++i) {
+            tc::mbar_init(&S.full[i], 1);
+            tc::mbar_init(&S.empty[i], 1);
+            tc::mbar_init(&S.mma[i], 1);
+        }
+        S.abort = 0;
+    }
+    if (warp == 0) { tc::tmem_alloc(&S.tmem, 512); tc::tmem_relinquish(); }
     tc::fence_smem_for_mma();
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = S.tmem;
-    const uint32_t trow = tmem + (uint32_t(warp * 32) << 16);
-    uint32_t phase = 0;
-    bool aborted = false;
-    // columns 64..79 of a hidden-layer A row: ones at 64 and 65 (the bias columns)
-    const uint32_t one2 = uint32_t(bf16_rn(1.0f)) | (uint32_t(bf16_rn(1.0f)) << 16);
-    const uint4 ones_row = make_uint4(one2, 0u, 0u, 0u);
-
-    const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile, tiles_y = (p.height + kShadeTile - 1) / kShadeTile;
-    const int ntiles = tiles_x * tiles_y;
-    for (;;) {
-        if (t == 0) S.tile = atomicAdd(A.tile_counter, 1);
-        __syncthreads();
-        const int tile = S.tile;
-        if (tile >= ntiles) break;
-        const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
-        // ---- 1. coverage, compaction, box ----
-        const int ly = t / 4, lx0 = (t % 4) * 8;
-        const int y = y0 + ly;
-        uint32_t cov = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int x = x0 + lx0 + j;
-            if (x >= p.width || y >= p.height) continue;
-            const int pi = y * p.width + x;
-            if (p.albedo[pi] != 0u) cov |= 1u << j;
-            else store_pixel(p, pi, p.background);
-        }
-        // the gate samples are the pixels (8i + 4, 8j + 4): j == 4 of rows with ly % 8 == 4
-        const uint32_t smp = ((ly & 7) == 4) ? (cov & 0x10u) : 0u;
-        const uint32_t oth = cov & ~smp;
-        const int mine = (__popc(smp) << 16) | __popc(oth);
-        int incl = mine;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) S.scan[warp] = incl;
-        if (t == 0) S.gate_sum = 0;
-        __syncthreads();
-        int before = incl - mine;
-        for (int w = 0; w < warp; ++w) before += S.scan[w];
-        const int total = (S.scan[0] + S.scan[1]) + (S.scan[2] + S.scan[3]);
-        const int nsmp = total >> 16, ncov = nsmp + (total & 0xffff);
-        int sp = before >> 16, op = nsmp + (before & 0xffff);
-        float lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            if (!((cov >> j) & 1u)) continue;
-            const int slot = ((smp >> j) & 1u) ? sp++ : op++;
-            const int x = x0 + lx0 + j;
-            S.list[slot] = uint16_t(ly * kShadeTile + lx0 + j);
-            float P[3];
-            world_pos(p, x, y, p.depth[y * p.width + x], P);
-            for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], P[k]); hi[k] = fmaxf(hi[k], P[k]); }
-        }
-        for (int k = 0; k < 3; ++k) {
-            for (int o = 16; o > 0; o >>= 1) {
-                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
-                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
-            }
-            if (lane == 0) { S.box[0][warp][k] = lo[k]; S.box[1][warp][k] = hi[k]; }
-        }
-        __syncthreads();
-        if (ncov == 0) {
-            if (t == 0) {
-                if (A.tile_status) A.tile_status[tile] = 2;
-                if (A.tile_mse) A.tile_mse[tile] = 0.0f;
-            }
-            continue;   // every thread has read this tile's shared state
-        }
-        // ---- 2. candidate lights ----
-        if (warp == 0) {
-            float b0[3], b1[3];
-            for (int k = 0; k < 3; ++k) {
-                b0[k] = fminf(fminf(S.box[0][0][k], S.box[0][1][k]), fminf(S.box[0][2][k], S.box[0][3][k]));
-                b1[k] = fmaxf(fmaxf(S.box[1][0][k], S.box[1][1][k]), fmaxf(S.box[1][2][k], S.box[1][3][k]));
-            }
-            select_candidates(nl, [&](int i) { return light_score(S.lights[i], b0, b1); }, S.cand);
-        }
-        // ---- 3. plain shading of the gate samples, 8 threads per sample ----
-        const int ngate = ncov < kGateSamples ? ncov : kGateSamples;
-        {
-            const int sj = t >> 3, g = t & 7;
-            float s[3] = { 0.0f, 0.0f, 0.0f }, a[3] = { 0.0f, 0.0f, 0.0f };
-            if (sj < ngate) {
-                const int li = S.list[sj];
-                const int x = x0 + li % kShadeTile, yy = y0 + li / kShadeTile;
-                const int pi = yy * p.width + x;
-                float P[3], n[3], v[3], vlen;
-                world_pos(p, x, yy, p.depth[pi], P);
-                surface(p, P, p.nx[pi], p.ny[pi], p.nz[pi], n, v, vlen);
-                albedo_rgb(p.albedo[pi], a);
-                plain_sum(S.lights, g, 8, nl, P, n, v, a, s);
-            }
-            for (int o = 1; o < 8; o <<= 1)
-                for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
-            if (sj < ngate && g == 0)
-                for (int c = 0; c < 3; ++c) S.gate_plain[sj][c] = s[c] + 0.03f * a[c];
-        }
-        __syncthreads();
-        // ---- 4. MLP over the covered pixels, 128 at a time ----
-        const int nbatch = (ncov + kRows - 1) / kRows;
-        bool fallback = false;
-        float tile_mse = 0.0f;
-        for (int b = 0; b < nbatch; ++b) {
-            const int r = b * kRows + t;
-            int pi = -1;
-            float base[3] = { 0.0f, 0.0f, 0.0f };
-            {
-                float f[kFeatures];
-                uint32_t w[16];
-                if (r < ncov) {
-                    const int li = S.list[r];
-                    const int x = x0 + li % kShadeTile, yy = y0 + li / kShadeTile;
-                    pi = yy * p.width + x;
-                    float P[3];
-                    world_pos(p, x, yy, p.depth[pi], P);
-                    pixel_features(p, S.lights, S.cand, P, p.nx[pi], p.ny[pi], p.nz[pi], p.albedo[pi], f);
-                    virtual_light_base(f, base);
-#pragma unroll
-                    for (int q = 0; q < 12; ++q) w[q] = pack_bf16x2(f[2 * q], f[2 * q + 1]);
-                    w[12] = one2;
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 13; ++q) w[q] = 0u;
-                }
-                w[13] = w[14] = w[15] = 0u;
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    *reinterpret_cast<uint4*>(S.act + tc::kmajor_offset(t, 8 * j, kK1)) =
-                        make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
-            }
-            float rgb[3] = { 0.0f, 0.0f, 0.0f };
-            for (int layer = 0; layer < 4; ++layer) {
-                tc::fence_smem_for_mma();
-                tc::fence_before_sync();
-                __syncthreads();
-                if (t == 0) {
-                    if (layer == 0) issue(tmem, S.act, S.w1, kK1, kHid, &S.mbar);
-                    else issue(tmem, S.act, layer == 1 ? S.w2 : layer == 2 ? S.w3 : S.w4, kKH,
-                               layer == 3 ? kOut : kHid, &S.mbar);
-                }
-                const bool ok = tc::mbar_wait(&S.mbar, phase);
-                phase ^= 1u;
-                if (__syncthreads_or(!ok)) { aborted = true; break; }
-                tc::fence_after_sync();
-                if (layer < 3) {
-                    relu_epilogue(trow, S.act, t);
-                    if (layer == 0) {
-                        *reinterpret_cast<uint4*>(S.act + tc::kmajor_offset(t, 64, kKH)) = ones_row;
-                        *reinterpret_cast<uint4*>(S.act + tc::kmajor_offset(t, 72, kKH)) = make_uint4(0u, 0u, 0u, 0u);
-                    }
-                } else {
-                    uint32_t v[32];
-                    tc::tmem_ld32_nowait(trow, v);
-                    tc::tmem_wait_ld();
-                    for (int c = 0; c < 3; ++c) {
-                        const float q = pos0(__uint_as_float(v[c]) + base[c]);
-                        rgb[c] = q * q;
-                    }
-                }
-            }
-            if (aborted) break;
-            if (b == 0) {
-                if (t < ngate) {
-                    int e = 0;
-                    for (int c = 0; c < 3; ++c) {
-                        const int d = int(srgb8_lut(p.srgb_lut, rgb[c])) - int(srgb8_lut(p.srgb_lut, S.gate_plain[t][c]));
-                        e += d * d;
-                    }
-                    atomicAdd(&S.gate_sum, e);
-                }
-                __syncthreads();
-                tile_mse = float(S.gate_sum) / float(3 * ngate);
-                if (tile_mse > A.max_tile_mse) { fallback = true; break; }
-            }
-            if (pi >= 0) store_pixel(p, pi, rgb);
-        }
-        if (aborted) break;
-        if (fallback) {
-            for (int r = t; r < ncov; r += blockDim.x) {
-                const int li = S.list[r];
-                const int x = x0 + li % kShadeTile, yy = y0 + li / kShadeTile;
-                const int pi = yy * p.width + x;
-                float rgb[3];
-                plain_pixel(p, S.lights, nl, x, yy, p.depth[pi], p.nx[pi], p.ny[pi], p.nz[pi], p.albedo[pi], rgb);
-                store_pixel(p, pi, rgb);
-            }
-        }
-        if (t == 0) {
-            if (A.tile_status) A.tile_status[tile] = fallback ? 1 : 0;
-            if (A.tile_mse) A.tile_mse[tile] = tile_mse;
-        }
-        __syncthreads();
-    }
-    if (aborted && t == 0) atomicExch(A.error, 1);
+    // the prologue above overlaps the pre-pass's tail; its results are read from here on
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (warp < 4 * kLanes) consume(S, A, warp / 4);
+    else if ((t & 31) == 0) produce(S, A, warp - 4 * kLanes);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    if (t == 0 && S.abort) atomicExch(A.error, 1);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) { tc::fence_after_sync(); tc::tmem_dealloc(tmem, 64); }
+    if (warp == 0) { tc::fence_after_sync(); tc::tmem_dealloc(S.tmem, 512); }
 }
 
-size_t learned_smem_bytes(int nlights) {
-    return sizeof(LearnSmem) + sizeof(rsrgpu_light) * size_t(nlights > 1 ? nlights - 1 : 0) + 128;
+// plain shading of the tiles the gates rejected: work items of 256 pixels
+// (a quarter tile) from the rejected-tile list, one thread per pixel
+__global__ void __launch_bounds__(256) shade_fallback_kernel(PlainParams p, const int32_t* __restrict__ rejected,
+                                                             const int* __restrict__ count) {
+    extern __shared__ rsrgpu_light L[];
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // the gates' decisions are complete
+    const int items = 4 * *count;
+    if (int(blockIdx.x) >= items) return;
+    const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) L[i] = p.lights[i];
+    __syncthreads();
+    const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int tile = rejected[item >> 2];
+        const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
+        const int i = (item & 3) * 256 + threadIdx.x;
+        const int x = x0 + i % kShadeTile, y = y0 + i / kShadeTile;
+        if (x >= p.width || y >= p.height) continue;
+        const int pi = y * p.width + x;
+        const uint32_t alb = p.albedo[pi];
+        if (alb == 0u) continue;
+        float rgb[3];
+        plain_pixel(p, L, nl, x, y, p.depth[pi], p.nx[pi], p.ny[pi], p.nz[pi], alb, rgb);
+        store_pixel(p, pi, rgb);
+    }
+}
+
+size_t learned_scratch_bytes(int tiles) {
+    return 512 + sizeof(int32_t) * size_t(tiles) * (kBlocksPerTile + 1) +
+           size_t(tiles) * kBlocksPerTile * (size_t(kFeatBytes) + sizeof(PipeMeta));
 }
 
 cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
                                  const rsrgpu_light* lights, int nlights, const float background[3], float max_tile_mse,
                                  uint32_t* out_srgb, float* out_linear, uint8_t* tile_status, float* tile_mse,
-                                 const uint8_t* srgb_lut, int* error, int* tile_counter, int num_sms, cudaStream_t st) {
+                                 const uint8_t* srgb_lut, int* error, int* counters, void* scratch,
+                                 int num_sms, cudaStream_t st) {
     LearnParams A{};
     PlainParams& p = A.pl;
     p.depth = gb.depth; p.nx = gb.normal_x; p.ny = gb.normal_y; p.nz = gb.normal_z; p.albedo = gb.albedo;
@@ -356,22 +613,55 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
     for (int i = 0; i < 16; ++i) p.ivp[i] = ivp[i];
     for (int i = 0; i < 3; ++i) { p.eye[i] = eye[i]; p.background[i] = background[i]; }
     p.lights = lights; p.nlights = nlights; p.out_srgb = out_srgb; p.out_linear = out_linear; p.srgb_lut = srgb_lut;
-    A.w = w; A.max_tile_mse = max_tile_mse; A.tile_status = tile_status; A.tile_mse = tile_mse; A.error = error;
-    A.tile_counter = tile_counter;
-    const size_t smem = learned_smem_bytes(nlights);
-    cudaError_t e = cudaFuncSetAttribute(shade_learned_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(tile_counter, 0, sizeof(int), st);
-    if (e != cudaSuccess) return e;
     const int tiles = ((gb.width + kShadeTile - 1) / kShadeTile) * ((gb.height + kShadeTile - 1) / kShadeTile);
-    // CTAs per SM: shared memory (227 KB per SM) and TMEM (512 columns, 64 per CTA)
-    int per_sm = int((227u * 1024u) / (smem + 1024u));
-    if (per_sm > 8) per_sm = 8;
-    if (per_sm < 1) per_sm = 1;
-    int grid = num_sms * per_sm;
-    if (grid > tiles) grid = tiles;
-    shade_learned_kernel<<<grid, 128, smem, st>>>(A);
-    return cudaGetLastError();
+    A.w = w; A.max_tile_mse = max_tile_mse; A.tile_status = tile_status; A.tile_mse = tile_mse; A.error = error;
+    A.counters = counters;
+    uint8_t* base = static_cast<uint8_t*>(scratch);
+    A.blocks = reinterpret_cast<int32_t*>(base);
+    A.rejected = A.blocks + size_t(tiles) * kBlocksPerTile;
+    A.feat = base + ((sizeof(int32_t) * size_t(tiles) * (kBlocksPerTile + 1) + 255) & ~size_t(255));
+    A.metas = reinterpret_cast<PipeMeta*>(A.feat + size_t(tiles) * kBlocksPerTile * kFeatBytes);
+    const size_t smem = sizeof(LearnSmem) + 128;
+    static int smem_set = -1;   // the attribute is per device function: set it once per device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (smem_set != dev) {
+        e = cudaFuncSetAttribute(shade_learned_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+        smem_set = dev;
+    }
+    e = cudaMemsetAsync(counters, 0, 3 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const size_t light_bytes = sizeof(rsrgpu_light) * size_t(nlights > 0 ? nlights : 1);
+    learned_prep_kernel<<<tiles, 128, light_bytes, st>>>(A);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int grid = num_sms;
+    if (grid > (tiles + 1) / 2) grid = (tiles + 1) / 2;
+    if (grid < 1) grid = 1;
+    // the tensor-core kernel and the fallback pass start while their predecessor
+    // drains (programmatic dependent launch); each waits for its inputs
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, shade_learned_kernel, A);
+    if (e != cudaSuccess) return e;
+    int fgrid = num_sms * 4;
+    if (fgrid > tiles * 4) fgrid = tiles * 4;
+    cfg.gridDim = dim3(fgrid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = light_bytes;
+    const int32_t* rej = A.rejected;
+    const int* cnt = counters + 2;
+    return cudaLaunchKernelEx(&cfg, shade_fallback_kernel, p, rej, cnt);
 }
 
 }  // namespace rsrgpu

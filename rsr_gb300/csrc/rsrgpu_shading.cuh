@@ -133,34 +133,26 @@ __device__ __forceinline__ float light_score(const rsrgpu_light& l, const float 
 
 // Warp-wide choice of the tile's candidates: up to kCandidates lights in
 // descending score (ties to the lower index), only scores > 0; -1 pads.
-// score(i) is evaluated for i < nl by the calling warp.
+// score(i) is evaluated for i < nl by the calling warp; `scratch` holds nl
+// floats of shared memory.  Each light's slot is its rank: the number of
+// lights with a higher score, or an equal one and a lower index.
 template <typename Score>
-__device__ __forceinline__ void select_candidates(int nl, Score score, int* cand) {
+__device__ __forceinline__ void select_candidates(int nl, Score score, int* cand, float* scratch) {
     const int lane = threadIdx.x & 31;
-    float s[kMaxLights / 32];
-#pragma unroll
-    for (int j = 0; j < kMaxLights / 32; ++j) {
-        const int i = lane + 32 * j;
-        s[j] = i < nl ? score(i) : -1.0f;
-    }
-    for (int c = 0; c < kCandidates; ++c) {
-        float bs = 0.0f;
-        int bi = -1;
-#pragma unroll
-        for (int j = 0; j < kMaxLights / 32; ++j)
-            if (s[j] > bs) { bs = s[j]; bi = lane + 32 * j; }
-        for (int o = 16; o > 0; o >>= 1) {
-            const float os = __shfl_xor_sync(0xffffffffu, bs, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (oi >= 0 && (bi < 0 || os > bs || (os == bs && oi < bi))) { bs = os; bi = oi; }
+    for (int i = lane; i < nl; i += 32) scratch[i] = score(i);
+    if (lane < kCandidates) cand[lane] = -1;
+    __syncwarp();
+    for (int i = lane; i < nl; i += 32) {
+        const float si = scratch[i];
+        if (!(si > 0.0f)) continue;
+        int rank = 0;
+        for (int j = 0; j < nl && rank < kCandidates; ++j) {
+            const float sj = scratch[j];
+            rank += (sj > si || (sj == si && j < i)) ? 1 : 0;
         }
-        if (lane == 0) cand[c] = bi;
-        if (bi >= 0 && (bi & 31) == lane) {
-#pragma unroll
-            for (int j = 0; j < kMaxLights / 32; ++j)
-                if (lane + 32 * j == bi) s[j] = -1.0f;
-        }
+        if (rank < kCandidates) cand[rank] = i;
     }
+    __syncwarp();
 }
 
 // The 24 input features of one covered pixel:
@@ -203,6 +195,143 @@ __device__ __forceinline__ void pixel_features(const PlainParams& p, const rsrgp
         wsum = wsum + w;
     }
     f[23] = wsum > 0.0f ? f[23] / wsum : 0.0f;
+}
+
+// ---- the learned shader's inputs, in fast arithmetic ----
+// The same definitions as pixel_features / virtual_light_base, evaluated
+// with the SFU's approximate reciprocal and reciprocal square root (about
+// one ulp each) and reciprocals multiplied in; the learned shader's kernels
+// (training data and inference) use these, so training and inference see
+// the same inputs.  Results agree with the exact definitions (the oracle's)
+// to a few ulps.
+__device__ __forceinline__ float frcp(float x) { return __fdividef(1.0f, x); }
+
+__device__ __forceinline__ void world_pos_fast(const PlainParams& p, int x, int y, float z, float P[3]) {
+    const float ndcx = (2.0f * (float(x) + 0.5f)) * frcp(float(p.width)) - 1.0f;
+    const float ndcy = 1.0f - (2.0f * (float(y) + 0.5f)) * frcp(float(p.height));
+    const float* m = p.ivp;
+    const float cx = ((m[0] * ndcx + m[4] * ndcy) + m[8] * z) + m[12];
+    const float cy = ((m[1] * ndcx + m[5] * ndcy) + m[9] * z) + m[13];
+    const float cz = ((m[2] * ndcx + m[6] * ndcy) + m[10] * z) + m[14];
+    const float cw = ((m[3] * ndcx + m[7] * ndcy) + m[11] * z) + m[15];
+    const float iw = frcp(cw);
+    P[0] = cx * iw; P[1] = cy * iw; P[2] = cz * iw;
+}
+
+// the number of candidate lights whose radius reaches P (as pixel_features_fast tests them)
+__device__ __forceinline__ int reaching_lights(const rsrgpu_light* L, const int* cand, const float P[3]) {
+    int k = 0;
+    for (int c = 0; c < kCandidates; ++c) {
+        const int li = cand[c];
+        if (li < 0) break;
+        const rsrgpu_light& l = L[li];
+        const float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
+        const float d2 = dot3(lx, ly, lz, lx, ly, lz);
+        const float d = d2 * rsqrtf(d2);
+        k += (d < l.radius) ? 1 : 0;
+    }
+    return k;
+}
+
+// plain_sum with the SFU's approximate reciprocal square root and reciprocal
+// (for estimates such as the learned shader's gate; the plain shader itself
+// uses plain_sum)
+__device__ __forceinline__ void plain_sum_fast(const rsrgpu_light* L, int first, int step, int nl, const float P[3],
+                                               const float n[3], const float v[3], const float a[3], float s[3]) {
+    for (int i = first; i < nl; i += step) {
+        float lx = L[i].position[0] - P[0], ly = L[i].position[1] - P[1], lz = L[i].position[2] - P[2];
+        const float d2 = dot3(lx, ly, lz, lx, ly, lz);
+        const float id = rsqrtf(d2);
+        const float d = d2 * id;
+        const float r = L[i].radius;
+        if (!(d < r)) continue;
+        lx *= id; ly *= id; lz *= id;
+        const float t = 1.0f - d * frcp(r);
+        const float att = t * t;
+        const float ndl = pos0(dot3(n[0], n[1], n[2], lx, ly, lz));
+        float hx = lx + v[0], hy = ly + v[1], hz = lz + v[2];
+        const float ih = rsqrtf(dot3(hx, hy, hz, hx, hy, hz));
+        hx *= ih; hy *= ih; hz *= ih;
+        float sp = pos0(dot3(n[0], n[1], n[2], hx, hy, hz));
+        sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
+        s[0] = s[0] + (L[i].color[0] * att) * (a[0] * ndl + sp);
+        s[1] = s[1] + (L[i].color[1] * att) * (a[1] * ndl + sp);
+        s[2] = s[2] + (L[i].color[2] * att) * (a[2] * ndl + sp);
+    }
+}
+
+// unit normal, unit view vector (fast arithmetic)
+__device__ __forceinline__ void surface_fast(const PlainParams& p, const float P[3], uint16_t hx, uint16_t hy, uint16_t hz,
+                                             float n[3], float v[3]) {
+    n[0] = __half2float(__ushort_as_half(hx)); n[1] = __half2float(__ushort_as_half(hy)); n[2] = __half2float(__ushort_as_half(hz));
+    const float in = rsqrtf(dot3(n[0], n[1], n[2], n[0], n[1], n[2]));
+    n[0] *= in; n[1] *= in; n[2] *= in;
+    v[0] = p.eye[0] - P[0]; v[1] = p.eye[1] - P[1]; v[2] = p.eye[2] - P[2];
+    const float iv = rsqrtf(dot3(v[0], v[1], v[2], v[0], v[1], v[2]));
+    v[0] *= iv; v[1] *= iv; v[2] *= iv;
+}
+
+// features f[24] and the virtual-light base[3] of one covered pixel; returns
+// the number of candidate lights reaching it (with at most one the base is
+// the pixel's Blinn-Phong shading itself)
+__device__ __forceinline__ int pixel_features_fast(const PlainParams& p, const rsrgpu_light* L, const int* cand,
+                                                   const float P[3], uint16_t hx, uint16_t hy, uint16_t hz,
+                                                   uint32_t alb, float f[kFeatures], float base[3]) {
+    float n[3] = { __half2float(__ushort_as_half(hx)), __half2float(__ushort_as_half(hy)), __half2float(__ushort_as_half(hz)) };
+    const float in = rsqrtf(dot3(n[0], n[1], n[2], n[0], n[1], n[2]));
+    n[0] = n[0] * in; n[1] = n[1] * in; n[2] = n[2] * in;
+    float v[3] = { p.eye[0] - P[0], p.eye[1] - P[1], p.eye[2] - P[2] };
+    const float v2 = dot3(v[0], v[1], v[2], v[0], v[1], v[2]);
+    const float iv = rsqrtf(v2);
+    v[0] = v[0] * iv; v[1] = v[1] * iv; v[2] = v[2] * iv;
+    const float k255 = 1.0f / 255.0f;
+    const float a[3] = { float(alb & 255u) * k255, float((alb >> 8) & 255u) * k255, float((alb >> 16) & 255u) * k255 };
+    for (int k = 0; k < 3; ++k) { f[k] = n[k]; f[3 + k] = v[k]; f[6 + k] = a[k]; }
+    f[9] = (v2 * iv) * 0.02f;
+    for (int k = 10; k < kFeatures; ++k) f[k] = 0.0f;
+    float wsum = 0.0f;
+    int reach = 0;
+    for (int c = 0; c < kCandidates; ++c) {
+        const int li = cand[c];
+        if (li < 0) break;
+        const rsrgpu_light& l = L[li];
+        const float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
+        const float d2 = dot3(lx, ly, lz, lx, ly, lz);
+        const float id = rsqrtf(d2);
+        const float d = d2 * id;
+        if (!(d < l.radius)) continue;
+        ++reach;
+        const float q = d * frcp(l.radius);
+        const float t = 1.0f - q;
+        const float att = t * t;
+        const float cr = l.color[0] * att, cg = l.color[1] * att, cb = l.color[2] * att;
+        const float w = (cr + cg) + cb;
+        const float ux = lx * id, uy = ly * id, uz = lz * id;
+        const float wx = w * ux, wy = w * uy, wz = w * uz;
+        f[10] += cr; f[11] += cg; f[12] += cb;
+        f[13] += wx; f[14] += wy; f[15] += wz;
+        f[16] += wx * ux; f[17] += wx * uy; f[18] += wx * uz;
+        f[19] += wy * uy; f[20] += wy * uz; f[21] += wz * uz;
+        f[22] += w * pos0(dot3(n[0], n[1], n[2], ux, uy, uz));
+        f[23] += w * q;
+        wsum += w;
+    }
+    f[23] = wsum > 0.0f ? f[23] * frcp(wsum) : 0.0f;
+    // virtual light: direction sum w L, colour sum c * att
+    const float D2 = dot3(f[13], f[14], f[15], f[13], f[14], f[15]);
+    float l[3] = { 0.0f, 0.0f, 0.0f };
+    if (D2 > 0.0f) { const float iD = rsqrtf(D2); l[0] = f[13] * iD; l[1] = f[14] * iD; l[2] = f[15] * iD; }
+    float h[3] = { l[0] + v[0], l[1] + v[1], l[2] + v[2] };
+    const float h2 = dot3(h[0], h[1], h[2], h[0], h[1], h[2]);
+    if (h2 > 0.0f) { const float ih = rsqrtf(h2); h[0] *= ih; h[1] *= ih; h[2] *= ih; }
+    const float ndl = pos0(dot3(n[0], n[1], n[2], l[0], l[1], l[2]));
+    float sp = pos0(dot3(n[0], n[1], n[2], h[0], h[1], h[2]));
+    sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
+    for (int c = 0; c < 3; ++c) {
+        const float x = pos0(f[10 + c] * (a[c] * ndl + sp) + 0.03f * a[c]);
+        base[c] = x > 0.0f ? x * rsqrtf(x) : 0.0f;
+    }
+    return reach;
 }
 
 // The learned shader's analytic base, computed from the FP32 features: one

@@ -72,6 +72,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity) {
                  "selp.u32 %0, 1, 0, p;\n\t}" : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" :: "r"(smem_addr(mbar)) : "memory");
+}
+// arrive and add `bytes` to the transaction count the current phase waits for
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                 :: "r"(smem_addr(mbar)), "r"(bytes) : "memory");
+}
+// bulk copy global -> this CTA's shared memory, completing `bytes` on mbar
+// (addresses 16-byte aligned, bytes a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mbar)) : "memory");
+}
+// barrier over the 128 threads of one warpgroup (named barrier `id`, 1..15)
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" :: "r"(id) : "memory"); }
+
 // bounded wait: returns false after `limit` polls
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t limit = 1u << 22) {
     for (uint32_t i = 0; i < limit; ++i) {
