@@ -408,14 +408,13 @@ def run_deferred(gpu, args, stream, flush):
     gpu.shade_learned_check()
     served = float((st == 0).sum() / max(1, (st != 2).sum()))
     covered = int(fr.covered.sum().item())
-    mlp_flops = 2 * (24 * 64 + 64 * 64 * 2 + 64 * 3)          # unpadded MACs x 2 per pixel
-    tflops = covered * served * mlp_flops / (learned_ms / 1e3) / 1e12
     res["learned"] = {"ms": learned_ms, "ms_per_api_call": learned_call_ms, "frames_per_s_shading": 1e3 / learned_ms,
                       "frames_per_s_frame": 1e3 / (gbuf_ms + learned_ms),
                       "speedup_vs_plain_shading": plain_ms / learned_ms,
                       "psnr_db_vs_plain": db, "max_abs_vs_plain": maxabs, "gate_max_tile_mse": thr,
                       "served_tiles": served, "covered_pixels": covered,
-                      "mlp_tflops": tflops, "weights": {k: net.meta.get(k) for k in ("train_seeds", "samples", "steps")}}
+                      "weights": {k: net.meta.get(k) for k in ("train_seeds", "samples", "steps")},
+                      "profile": "profiles/deferred_shading_1080p_64_lights.md (tensor pipe, stalls)"}
     # more lights on the same G-buffer (positions, colours, radii as the scene's 64)
     from rsr_gb300 import scenes
     scaling = []
@@ -542,13 +541,17 @@ def _raster_bytes(gpu, sc):
 
 
 def _ncu_traffic():
-    """DRAM bytes per raster launch from the committed ncu capture, if any."""
-    p = os.path.join(REPO, "profiles", "raster_traffic.json")
+    """DRAM bytes per raster launch from the committed ncu summary (its
+    `traffic_bytes_per_launch:` line), if present."""
+    p = os.path.join(REPO, "profiles", "raster_kernel_textured_sphere_1080p.md")
     try:
         with open(p) as f:
-            return json.load(f)["dram_bytes_per_launch"]
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1])
     except Exception:
-        return None
+        pass
+    return None
 
 
 def main():
