@@ -14,7 +14,7 @@ namespace rsrgpu {
 __global__ void __launch_bounds__(256) shade_plain_kernel(PlainParams p) {
     __shared__ rsrgpu_light L[kMaxLights];
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
-    for (int i = threadIdx.x; i < nl; i += blockDim.x) L[i] = p.lights[i];
+    load_lights(L, p.lights, nl);
     __syncthreads();
     const int n = p.width * p.height;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(128) learned_features_kernel(FeatParams F) {
     __shared__ float scores[kMaxLights];
     const PlainParams& p = F.pl;
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
-    for (int i = threadIdx.x; i < nl; i += blockDim.x) lights[i] = p.lights[i];
+    load_lights(lights, p.lights, nl);
     const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile, tiles_y = (p.height + kShadeTile - 1) / kShadeTile;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {

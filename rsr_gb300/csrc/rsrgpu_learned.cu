@@ -7,12 +7,12 @@
 // needs no network: its virtual light is that light, so base is its
 // Blinn-Phong shading; only pixels reached by two or more go through the MLP.
 //
-// learned_prep_kernel (one CTA of 128 threads per 32x32 shading tile, many
-// resident per SM so that their latency chains overlap): coverage and
+// learned_prep_kernel (four CTAs of 256 threads per SM, so that their latency
+// chains overlap, each taking 32x32 shading tiles in turn): coverage and
 // compaction (the tile's 4x4 grid of gate samples first), the world-space box
 // of the covered pixels, the candidate lights, the plain shader at the gate
 // samples (8 threads per sample), background pixels; then, list entry
-// i * 128 + t per pass, the features and base of every covered pixel: pixels
+// i * 256 + t per pass, the features and base of every covered pixel: pixels
 // on the exact path are written at once, the others are compacted (ballot,
 // list order) into the tile's blocks of 128 rows -- an 8 KB A tile per block
 // (24 BF16 features and two ones columns per row, in the chunked layout
@@ -21,7 +21,8 @@
 //
 // shade_learned_kernel (one CTA per SM): two lanes, each a producer thread
 //   and a consumer warpgroup joined by three pipelines.  The producer takes
-//   blocks from the list and, for each, waits for the next pipeline's slot
+//   its lane's share of the block list (every 2 * gridDim.x-th entry) and,
+//   for each block, waits for the next pipeline's slot
 //   to be free and issues two bulk copies (cp.async.bulk) of the block's A
 //   tile and record into it, completed on the pipeline's full barrier by
 //   transaction count.  The consumer visits its pipelines in turn and
@@ -107,7 +108,7 @@ struct LearnParams {
     uint8_t* tile_status;     // [tiles]: 0 learned, 1 plain fallback, 2 nothing covered
     float* tile_mse;          // [tiles] or null: the gate's estimate
     int* error;
-    int* counters;            // [0] blocks taken by the producers, [1] blocks listed, [2] tiles
+    int* counters;            // [0] tiles taken by the pre-pass, [1] blocks listed, [2] tiles
                               // rejected by the gate; zero at launch
     int32_t* blocks;          // [tiles * 8] the filled blocks
     int32_t* rejected;        // [tiles] tiles for the fallback pass
@@ -128,212 +129,234 @@ __device__ __forceinline__ uint4* chunk_row(uint8_t* tile, int j, int r) {
 }
 
 // ---------------------------------------------------------------- pre-pass
-__global__ void __launch_bounds__(128, 8) learned_prep_kernel(LearnParams A) {
+constexpr int kPrepThreads = 256;   // per 32x32 tile: four pixels of a row per thread
+constexpr int kPrepWarps = kPrepThreads / 32;
+constexpr int kPrepPx = kTilePx / kPrepThreads;
+
+__global__ void __launch_bounds__(kPrepThreads, 4) learned_prep_kernel(LearnParams A) {
     extern __shared__ rsrgpu_light L[];
     __shared__ uint16_t list[kTilePx];
-    __shared__ float box[2][4][3];
-    __shared__ int scan[4];
+    __shared__ float box[2][kPrepWarps][3];
+    __shared__ int scan[kPrepWarps];
     __shared__ int cand[kCandidates];
     __shared__ float scores[kMaxLights];
     __shared__ uint32_t gate_plain[kGateSamples];
     __shared__ int gate_err, netsamples;
-    __shared__ int wcount[2][4];
+    __shared__ int wcount[2][kPrepWarps];
     const PlainParams& p = A.pl;
     const int t = threadIdx.x, wl = t & 31, warp = t >> 5;
+    // the tensor-core kernel may take the SMs this grid's CTAs leave: once
+    // every CTA of this grid has started, its prologue overlaps their work
+    // (it reads nothing of theirs before its griddepcontrol.wait)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
-    for (int i = t; i < nl; i += blockDim.x) L[i] = p.lights[i];
+    load_lights(L, p.lights, nl);
     const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile;
-    const int tile = blockIdx.x;
-    const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
-    // ---- coverage, compaction (gate samples first), box ----
-    const int ly = t / 4, lx0 = (t % 4) * 8;
-    const int y = y0 + ly;
-    const uint32_t bg = pack_srgb(p.srgb_lut, p.background);
-    uint32_t cov = 0;
-    float zd[8];
+    const int ntiles = tiles_x * ((p.height + kShadeTile - 1) / kShadeTile);
+    __shared__ int next_tile;
+    // tiles in turn from a counter: no CTA launch per tile, and the tiles
+    // with nothing covered cost little
+    for (;;) {
+        if (t == 0) next_tile = atomicAdd(A.counters, 1);
+        __syncthreads();   // also: the previous tile's shared state is no longer read
+        const int tile = next_tile;
+        if (tile >= ntiles) break;
+        const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
+        // ---- coverage, compaction (gate samples first), box ----
+        const int ly = t / (kShadeTile / kPrepPx), lx0 = (t % (kShadeTile / kPrepPx)) * kPrepPx;
+        const int y = y0 + ly;
+        const uint32_t bg = pack_srgb(p.srgb_lut, p.background);
+        uint32_t cov = 0;
+        float zd[kPrepPx];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int x = x0 + lx0 + j;
-        zd[j] = 1.0f;
-        if (x >= p.width || y >= p.height) continue;
-        const int pi = y * p.width + x;
-        zd[j] = p.depth[pi];   // loaded with the albedo: one round trip for both
-        if (p.albedo[pi] != 0u) {
-            cov |= 1u << j;
-        } else {
-            if (p.out_srgb) p.out_srgb[pi] = bg;
-            if (p.out_linear) { p.out_linear[3 * size_t(pi)] = p.background[0]; p.out_linear[3 * size_t(pi) + 1] = p.background[1]; p.out_linear[3 * size_t(pi) + 2] = p.background[2]; }
-        }
-    }
-    const uint32_t smp = ((ly & 7) == 4) ? (cov & 0x10u) : 0u;
-    const int mine = (__popc(smp) << 16) | __popc(cov & ~smp);
-    int incl = mine;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (wl >= o) incl += v;
-    }
-    if (wl == 31) scan[warp] = incl;
-    __syncthreads();
-    int before = incl - mine;
-    for (int w = 0; w < warp; ++w) before += scan[w];
-    const int total = (scan[0] + scan[1]) + (scan[2] + scan[3]);
-    const int nsmp = total >> 16, ncov = nsmp + (total & 0xffff);
-    int sp = before >> 16, op = nsmp + (before & 0xffff);
-    float lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        if (!((cov >> j) & 1u)) continue;
-        const int slot = ((smp >> j) & 1u) ? sp++ : op++;
-        const int x = x0 + lx0 + j;
-        list[slot] = uint16_t(ly * kShadeTile + lx0 + j);
-        float Q[3];
-        world_pos(p, x, y, zd[j], Q);
-        for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], Q[k]); hi[k] = fmaxf(hi[k], Q[k]); }
-    }
-    for (int k = 0; k < 3; ++k) {
-        for (int o = 16; o > 0; o >>= 1) {
-            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
-            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
-        }
-        if (wl == 0) { box[0][warp][k] = lo[k]; box[1][warp][k] = hi[k]; }
-    }
-    __syncthreads();
-    if (ncov == 0) {
-        if (t == 0) {
-            A.tile_status[tile] = 2;
-            if (A.tile_mse) A.tile_mse[tile] = 0.0f;
-        }
-        return;
-    }
-    // ---- candidate lights (warp 0), gate samples (8 threads each) ----
-    if (warp == 0) {
-        float b0[3], b1[3];
-        for (int k = 0; k < 3; ++k) {
-            b0[k] = fminf(fminf(box[0][0][k], box[0][1][k]), fminf(box[0][2][k], box[0][3][k]));
-            b1[k] = fmaxf(fmaxf(box[1][0][k], box[1][1][k]), fmaxf(box[1][2][k], box[1][3][k]));
-        }
-        select_candidates(nl, [&](int i) { return light_score(L[i], b0, b1); }, cand, scores);
-    }
-    const int ngate = ncov < kGateSamples ? ncov : kGateSamples;
-    {
-        const int sj = t >> 3, g = t & 7;
-        float s[3] = { 0.0f, 0.0f, 0.0f }, a[3] = { 0.0f, 0.0f, 0.0f };
-        if (sj < ngate) {
-            const int li = list[sj];
-            const int x = x0 + li % kShadeTile, yy = y0 + li / kShadeTile;
-            const int pi = yy * p.width + x;
-            float Q[3], n[3], v[3];
-            world_pos_fast(p, x, yy, p.depth[pi], Q);
-            surface_fast(p, Q, p.nx[pi], p.ny[pi], p.nz[pi], n, v);
-            albedo_rgb(p.albedo[pi], a);
-            plain_sum_fast(L, g, 8, nl, Q, n, v, a, s);
-        }
-        for (int o = 1; o < 8; o <<= 1)
-            for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
-        if (sj < ngate && g == 0) {
-            const float rgb[3] = { s[0] + 0.03f * a[0], s[1] + 0.03f * a[1], s[2] + 0.03f * a[2] };
-            gate_plain[sj] = pack_srgb(p.srgb_lut, rgb);
-        }
-    }
-    __syncthreads();
-    // ---- features; pixels reached by two or more candidate lights become the
-    // network's rows (in list order, so the gate samples come first), the
-    // others take the analytic base, which is then their Blinn-Phong shading.
-    // Entry i * 128 + t per pass: consecutive threads, consecutive pixels. ----
-    if (t == 0) { gate_err = 0; netsamples = 0; }
-    const uint32_t one2 = uint32_t(bf16_rn(1.0f)) | (uint32_t(bf16_rn(1.0f)) << 16);
-    const uint32_t lt = (1u << wl) - 1u;
-    int nrows = 0;
-    __syncthreads();
-    // G-buffer values of this thread's next list entry, fetched a pass ahead
-    struct Px { int pi; float z; uint16_t hx, hy, hz; uint32_t alb; };
-    auto fetch = [&](int r, Px& q) {
-        if (r >= ncov) return;
-        const int li = list[r];
-        q.pi = (y0 + li / kShadeTile) * p.width + x0 + li % kShadeTile;
-        q.z = p.depth[q.pi]; q.hx = p.nx[q.pi]; q.hy = p.ny[q.pi]; q.hz = p.nz[q.pi]; q.alb = p.albedo[q.pi];
-    };
-    Px nxt{ 0, 0.0f, 0, 0, 0, 0u };
-    fetch(t, nxt);
-    for (int i = 0; i * kRows < ncov; ++i) {
-        const int r = i * kRows + t;
-        const Px cur = nxt;
-        fetch(r + kRows, nxt);
-        bool net = false;
-        const int pi = cur.pi;
-        float f[kFeatures], base[3];
-        if (r < ncov) {
-            const int x = pi % p.width, yy = pi / p.width;
-            float Q[3];
-            world_pos_fast(p, x, yy, cur.z, Q);
-            net = pixel_features_fast(p, L, cand, Q, cur.hx, cur.hy, cur.hz, cur.alb, f, base) >= 2;
-            if (!net) {
-                const float rgb[3] = { base[0] * base[0], base[1] * base[1], base[2] * base[2] };
-                store_pixel(p, pi, rgb);
-                if (r < ngate) {
-                    int err = 0;
-                    for (int c = 0; c < 3; ++c) {
-                        const int d = int(srgb8_lut(p.srgb_lut, rgb[c])) - int((gate_plain[r] >> (16 - 8 * c)) & 255u);
-                        err += d * d;
-                    }
-                    atomicAdd(&gate_err, err);
-                }
+        for (int j = 0; j < kPrepPx; ++j) {
+            const int x = x0 + lx0 + j;
+            zd[j] = 1.0f;
+            if (x >= p.width || y >= p.height) continue;
+            const int pi = y * p.width + x;
+            zd[j] = p.depth[pi];   // loaded with the albedo: one round trip for both
+            if (p.albedo[pi] != 0u) {
+                cov |= 1u << j;
+            } else {
+                if (p.out_srgb) p.out_srgb[pi] = bg;
+                if (p.out_linear) { p.out_linear[3 * size_t(pi)] = p.background[0]; p.out_linear[3 * size_t(pi) + 1] = p.background[1]; p.out_linear[3 * size_t(pi) + 2] = p.background[2]; }
             }
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, net);
-        if (wl == 0) wcount[i & 1][warp] = __popc(bal);
-        __syncthreads();
-        int slot = nrows + __popc(bal & lt);
-        for (int w = 0; w < warp; ++w) slot += wcount[i & 1][w];
-        nrows += (wcount[i & 1][0] + wcount[i & 1][1]) + (wcount[i & 1][2] + wcount[i & 1][3]);
-        if (net) {
-            const int blk = tile * kBlocksPerTile + slot / kRows, row = slot % kRows;
-            uint8_t* ftile = A.feat + size_t(blk) * kFeatBytes;
-            PipeMeta& M = A.metas[blk];
-            uint32_t w[16];
-#pragma unroll
-            for (int q = 0; q < 12; ++q) w[q] = pack_bf16x2(f[2 * q], f[2 * q + 1]);
-            w[12] = one2;
-            w[13] = w[14] = w[15] = 0u;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) *chunk_row(ftile, j, row) = make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
-            M.base[row][0] = base[0]; M.base[row][1] = base[1]; M.base[row][2] = base[2];
-            M.pix[row] = pi;
-            if (r < ngate) { M.gate_plain[slot] = gate_plain[r]; atomicAdd(&netsamples, 1); }
+        // gate samples: the pixels (8i + 4, 8j + 4), here the first of every other thread's four
+        const uint32_t smp = ((ly & 7) == 4 && (lx0 & 7) == 4) ? (cov & 1u) : 0u;
+        const int mine = (__popc(smp) << 16) | __popc(cov & ~smp);
+        int incl = mine;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (wl >= o) incl += v;
         }
-    }
-    const int nblocks = (nrows + kRows - 1) / kRows;
-    // rows of the last block past the network's pixels
-    for (int sidx = nrows + t; sidx < nblocks * kRows; sidx += blockDim.x) {
-        const int blk = tile * kBlocksPerTile + sidx / kRows, row = sidx % kRows;
-        uint8_t* ftile = A.feat + size_t(blk) * kFeatBytes;
+        if (wl == 31) scan[warp] = incl;
+        __syncthreads();
+        int before = incl - mine;
+        int total = 0;
+        for (int w = 0; w < kPrepWarps; ++w) {
+            if (w == warp) before += total;
+            total += scan[w];
+        }
+        const int nsmp = total >> 16, ncov = nsmp + (total & 0xffff);
+        int sp = before >> 16, op = nsmp + (before & 0xffff);
+        float lo[3] = { INFINITY, INFINITY, INFINITY }, hi[3] = { -INFINITY, -INFINITY, -INFINITY };
 #pragma unroll
-        for (int j = 0; j < 4; ++j) *chunk_row(ftile, j, row) = make_uint4(0u, 0u, 0u, 0u);
-        PipeMeta& M = A.metas[blk];
-        M.base[row][0] = M.base[row][1] = M.base[row][2] = 0.0f;
-        M.pix[row] = -1;
-    }
-    __syncthreads();
-    if (t < nblocks) {
-        PipeMeta& M = A.metas[tile * kBlocksPerTile + t];
-        M.tile = tile;
-        M.first = t == 0;
-        M.ngate = t == 0 ? netsamples : 0;
-        M.ngate_total = ngate;
-        M.gate_err = gate_err;
-        M.pad[0] = M.pad[1] = M.pad[2] = 0;
-    }
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    if (t == 0) {
-        if (nblocks == 0) {   // every sample on the exact path: the gate decides here
-            const float mse = float(gate_err) / float(3 * ngate);
-            const int fb = mse > A.max_tile_mse ? 1 : 0;
-            A.tile_status[tile] = uint8_t(fb);
-            if (A.tile_mse) A.tile_mse[tile] = mse;
-            if (fb) A.rejected[atomicAdd(A.counters + 2, 1)] = tile;
-        } else {
-            const int at = atomicAdd(A.counters + 1, nblocks);
-            for (int b = 0; b < nblocks; ++b) A.blocks[at + b] = tile * kBlocksPerTile + b;
+        for (int j = 0; j < kPrepPx; ++j) {
+            if (!((cov >> j) & 1u)) continue;
+            const int slot = ((smp >> j) & 1u) ? sp++ : op++;
+            const int x = x0 + lx0 + j;
+            list[slot] = uint16_t(ly * kShadeTile + lx0 + j);
+            float Q[3];
+            world_pos(p, x, y, zd[j], Q);
+            for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], Q[k]); hi[k] = fmaxf(hi[k], Q[k]); }
+        }
+        for (int k = 0; k < 3; ++k) {
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+            }
+            if (wl == 0) { box[0][warp][k] = lo[k]; box[1][warp][k] = hi[k]; }
+        }
+        __syncthreads();
+        if (ncov == 0) {
+            if (t == 0) {
+                A.tile_status[tile] = 2;
+                if (A.tile_mse) A.tile_mse[tile] = 0.0f;
+            }
+            continue;
+        }
+        // ---- candidate lights (warp 0), gate samples (8 threads each) ----
+        if (warp == 0) {
+            float b0[3], b1[3];
+            for (int k = 0; k < 3; ++k) {
+                b0[k] = box[0][0][k]; b1[k] = box[1][0][k];
+                for (int w = 1; w < kPrepWarps; ++w) { b0[k] = fminf(b0[k], box[0][w][k]); b1[k] = fmaxf(b1[k], box[1][w][k]); }
+            }
+            select_candidates(nl, [&](int i) { return light_score(L[i], b0, b1); }, cand, scores);
+        }
+        const int ngate = ncov < kGateSamples ? ncov : kGateSamples;
+        if (t >= 32 && t < 32 + 8 * kGateSamples) {   // warps 1-4, beside warp 0's choice
+            const int sj = (t - 32) >> 3, g = t & 7;
+            float s[3] = { 0.0f, 0.0f, 0.0f }, a[3] = { 0.0f, 0.0f, 0.0f };
+            if (sj < ngate) {
+                const int li = list[sj];
+                const int x = x0 + li % kShadeTile, yy = y0 + li / kShadeTile;
+                const int pi = yy * p.width + x;
+                float Q[3], n[3], v[3];
+                world_pos_fast(p, x, yy, p.depth[pi], Q);
+                surface_fast(p, Q, p.nx[pi], p.ny[pi], p.nz[pi], n, v);
+                albedo_rgb(p.albedo[pi], a);
+                plain_sum_fast(L, g, 8, nl, Q, n, v, a, s);
+            }
+            for (int o = 1; o < 8; o <<= 1)
+                for (int c = 0; c < 3; ++c) s[c] += __shfl_xor_sync(0xffffffffu, s[c], o);
+            if (sj < ngate && g == 0) {
+                const float rgb[3] = { s[0] + 0.03f * a[0], s[1] + 0.03f * a[1], s[2] + 0.03f * a[2] };
+                gate_plain[sj] = pack_srgb(p.srgb_lut, rgb);
+            }
+        }
+        __syncthreads();
+        // ---- features; pixels reached by two or more candidate lights become the
+        // network's rows (in list order, so the gate samples come first), the
+        // others take the analytic base, which is then their Blinn-Phong shading.
+        // Entry i * 256 + t per pass: consecutive threads, consecutive pixels. ----
+        if (t == 0) { gate_err = 0; netsamples = 0; }
+        const uint32_t one2 = uint32_t(bf16_rn(1.0f)) | (uint32_t(bf16_rn(1.0f)) << 16);
+        const uint32_t lt = (1u << wl) - 1u;
+        int nrows = 0;
+        __syncthreads();
+        // G-buffer values of this thread's next list entry, fetched a pass ahead
+        struct Px { int pi; float z; uint16_t hx, hy, hz; uint32_t alb; };
+        auto fetch = [&](int r, Px& q) {
+            if (r >= ncov) return;
+            const int li = list[r];
+            q.pi = (y0 + li / kShadeTile) * p.width + x0 + li % kShadeTile;
+            q.z = p.depth[q.pi]; q.hx = p.nx[q.pi]; q.hy = p.ny[q.pi]; q.hz = p.nz[q.pi]; q.alb = p.albedo[q.pi];
+        };
+        Px nxt{ 0, 0.0f, 0, 0, 0, 0u };
+        fetch(t, nxt);
+        for (int i = 0; i * kPrepThreads < ncov; ++i) {
+            const int r = i * kPrepThreads + t;
+            const Px cur = nxt;
+            fetch(r + kPrepThreads, nxt);
+            bool net = false;
+            const int pi = cur.pi;
+            float f[kFeatures], base[3];
+            if (r < ncov) {
+                const int x = pi % p.width, yy = pi / p.width;
+                float Q[3];
+                world_pos_fast(p, x, yy, cur.z, Q);
+                net = pixel_features_fast(p, L, cand, Q, cur.hx, cur.hy, cur.hz, cur.alb, f, base) >= 2;
+                if (!net) {
+                    const float rgb[3] = { base[0] * base[0], base[1] * base[1], base[2] * base[2] };
+                    store_pixel(p, pi, rgb);
+                    if (r < ngate) {
+                        int err = 0;
+                        for (int c = 0; c < 3; ++c) {
+                            const int d = int(srgb8_lut(p.srgb_lut, rgb[c])) - int((gate_plain[r] >> (16 - 8 * c)) & 255u);
+                            err += d * d;
+                        }
+                        atomicAdd(&gate_err, err);
+                    }
+                }
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, net);
+            if (wl == 0) wcount[i & 1][warp] = __popc(bal);
+            __syncthreads();
+            int slot = nrows + __popc(bal & lt);
+            for (int w = 0; w < kPrepWarps; ++w) {
+                if (w < warp) slot += wcount[i & 1][w];
+                nrows += wcount[i & 1][w];
+            }
+            if (net) {
+                const int blk = tile * kBlocksPerTile + slot / kRows, row = slot % kRows;
+                uint8_t* ftile = A.feat + size_t(blk) * kFeatBytes;
+                PipeMeta& M = A.metas[blk];
+                uint32_t w[16];
+#pragma unroll
+                for (int q = 0; q < 12; ++q) w[q] = pack_bf16x2(f[2 * q], f[2 * q + 1]);
+                w[12] = one2;
+                w[13] = w[14] = w[15] = 0u;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) *chunk_row(ftile, j, row) = make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
+                M.base[row][0] = base[0]; M.base[row][1] = base[1]; M.base[row][2] = base[2];
+                M.pix[row] = pi;
+                if (r < ngate) { M.gate_plain[slot] = gate_plain[r]; atomicAdd(&netsamples, 1); }
+            }
+        }
+        const int nblocks = (nrows + kRows - 1) / kRows;
+        // rows of the last block past the network's pixels
+        for (int sidx = nrows + t; sidx < nblocks * kRows; sidx += blockDim.x) {
+            const int blk = tile * kBlocksPerTile + sidx / kRows, row = sidx % kRows;
+            uint8_t* ftile = A.feat + size_t(blk) * kFeatBytes;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) *chunk_row(ftile, j, row) = make_uint4(0u, 0u, 0u, 0u);
+            PipeMeta& M = A.metas[blk];
+            M.base[row][0] = M.base[row][1] = M.base[row][2] = 0.0f;
+            M.pix[row] = -1;
+        }
+        __syncthreads();
+        if (t < nblocks) {
+            PipeMeta& M = A.metas[tile * kBlocksPerTile + t];
+            M.tile = tile;
+            M.first = t == 0;
+            M.ngate = t == 0 ? netsamples : 0;
+            M.ngate_total = ngate;
+            M.gate_err = gate_err;
+            M.pad[0] = M.pad[1] = M.pad[2] = 0;
+        }
+        if (t == 0) {
+            if (nblocks == 0) {   // every sample on the exact path: the gate decides here
+                const float mse = float(gate_err) / float(3 * ngate);
+                const int fb = mse > A.max_tile_mse ? 1 : 0;
+                A.tile_status[tile] = uint8_t(fb);
+                if (A.tile_mse) A.tile_mse[tile] = mse;
+                if (fb) A.rejected[atomicAdd(A.counters + 2, 1)] = tile;
+            } else {
+                const int at = atomicAdd(A.counters + 1, nblocks);
+                for (int b = 0; b < nblocks; ++b) A.blocks[at + b] = tile * kBlocksPerTile + b;
+            }
         }
     }
 }
@@ -383,15 +406,17 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
     return false;
 }
 
-// one thread per lane: blocks from the list into the lane's pipelines
+// one thread per lane: blocks from the list into the lane's pipelines.  Lane
+// l of CTA c takes list entries c * kLanes + l, + gridDim.x * kLanes, ...: an
+// equal share for every lane, also for CTAs that start late (on SMs the
+// pre-pass still held), where taking blocks first-come would leave them none.
 __device__ void produce(LearnSmem& S, const LearnParams& A, int lane) {
     volatile int* abort = &S.abort;
     uint32_t eparity = 0xfu;   // per pipeline: the parity to wait for on its empty barrier (fresh: passes)
     int pipe = 0;
     const int nblocks = *reinterpret_cast<volatile int*>(A.counters + 1);
-    for (;;) {
-        const int k = atomicAdd(A.counters, 1);
-        if (k >= nblocks || *abort) break;
+    const int stride = int(gridDim.x) * kLanes;
+    for (int k = int(blockIdx.x) * kLanes + lane; k < nblocks && !*abort; k += stride) {
         const int blk = A.blocks[k];
         const int pp = lane * kPipes + pipe;
         if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort)) break;
@@ -558,34 +583,38 @@ __global__ void __launch_bounds__(kThreads, 1) shade_learned_kernel(LearnParams 
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // the prologue above overlaps the pre-pass's tail; its results are read from here on
     asm volatile("griddepcontrol.wait;" ::: "memory");
     if (warp < 4 * kLanes) consume(S, A, warp / 4);
     else if ((t & 31) == 0) produce(S, A, warp - 4 * kLanes);
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (t == 0 && S.abort) atomicExch(A.error, 1);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) { tc::fence_after_sync(); tc::tmem_dealloc(S.tmem, 512); }
 }
 
-// plain shading of the tiles the gates rejected: work items of 256 pixels
-// (a quarter tile) from the rejected-tile list, one thread per pixel
-__global__ void __launch_bounds__(256) shade_fallback_kernel(PlainParams p, const int32_t* __restrict__ rejected,
-                                                             const int* __restrict__ count) {
+// Plain shading of the tiles the gates rejected (bit-exact with the plain
+// shader): one CTA of 1024 threads per rejected tile at a time, one thread
+// per pixel.  The plain shader is issue-bound at this occupancy; smaller
+// CTAs (a quarter tile each, or several threads per pixel with the terms
+// merged in light order) measured slower, their per-pixel chains being
+// latency-bound.
+constexpr int kFbThreads = kTilePx;
+__global__ void __launch_bounds__(kFbThreads, 1) shade_fallback_kernel(PlainParams p, const int32_t* __restrict__ rejected,
+                                                                      const int* __restrict__ count) {
     extern __shared__ rsrgpu_light L[];
     asm volatile("griddepcontrol.wait;" ::: "memory");   // the gates' decisions are complete
-    const int items = 4 * *count;
-    if (int(blockIdx.x) >= items) return;
+    const int ntiles = *count;
+    if (int(blockIdx.x) >= ntiles) return;
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
-    for (int i = threadIdx.x; i < nl; i += blockDim.x) L[i] = p.lights[i];
+    load_lights(L, p.lights, nl);
     __syncthreads();
     const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile;
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
-        const int tile = rejected[item >> 2];
-        const int x0 = (tile % tiles_x) * kShadeTile, y0 = (tile / tiles_x) * kShadeTile;
-        const int i = (item & 3) * 256 + threadIdx.x;
-        const int x = x0 + i % kShadeTile, y = y0 + i / kShadeTile;
+    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        const int tile = rejected[k];
+        const int x = (tile % tiles_x) * kShadeTile + int(threadIdx.x) % kShadeTile;
+        const int y = (tile / tiles_x) * kShadeTile + int(threadIdx.x) / kShadeTile;
         if (x >= p.width || y >= p.height) continue;
         const int pi = y * p.width + x;
         const uint32_t alb = p.albedo[pi];
@@ -634,7 +663,9 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
     e = cudaMemsetAsync(counters, 0, 3 * sizeof(int), st);
     if (e != cudaSuccess) return e;
     const size_t light_bytes = sizeof(rsrgpu_light) * size_t(nlights > 0 ? nlights : 1);
-    learned_prep_kernel<<<tiles, 128, light_bytes, st>>>(A);
+    int pgrid = num_sms * 4;
+    if (pgrid > tiles) pgrid = tiles;
+    learned_prep_kernel<<<pgrid, kPrepThreads, light_bytes, st>>>(A);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     int grid = num_sms;
@@ -654,10 +685,10 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, shade_learned_kernel, A);
     if (e != cudaSuccess) return e;
-    int fgrid = num_sms * 4;
-    if (fgrid > tiles * 4) fgrid = tiles * 4;
+    int fgrid = num_sms;
+    if (fgrid > tiles) fgrid = tiles;
     cfg.gridDim = dim3(fgrid);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(kFbThreads);
     cfg.dynamicSmemBytes = light_bytes;
     const int32_t* rej = A.rejected;
     const int* cnt = counters + 2;

@@ -76,27 +76,65 @@ __device__ __forceinline__ void albedo_rgb(uint32_t alb, float a[3]) {
     a[0] = float(alb & 255u) / 255.0f; a[1] = float((alb >> 8) & 255u) / 255.0f; a[2] = float((alb >> 16) & 255u) / 255.0f;
 }
 
-// Blinn-Phong sum over lights first, first+step, ... < nl:
-// att = (1 - d/r)^2, diffuse max(N.L,0)*albedo, specular max(N.H,0)^32
+// A squared distance at or beyond which a light of radius r is out of reach
+// for certain: for d2 >= reach_bound(r), sqrtf(d2) >= r (the bound is above r^2
+// by far more than the rounding of r * r, sqrtf is correctly rounded and
+// monotonic) and also d2 * rsqrtf(d2) >= r (the approximate reciprocal square
+// root is off by far less than 2^-17).  Radii below 1e-18, whose square would
+// lose precision, and NaN give infinity: such lights are never skipped early.
+__device__ __forceinline__ float reach_bound(float r) {
+    if (!(r >= 1e-18f)) return INFINITY;
+    return (r * r) * 1.0000152587890625f;   // 1 + 2^-16; an overflow gives infinity
+}
+
+// Copies the lights into shared memory with reach_bound(radius) in the
+// reserved field, which the loops below test before any square root.
+__device__ __forceinline__ void load_lights(rsrgpu_light* L, const rsrgpu_light* __restrict__ src, int nl) {
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+        rsrgpu_light l = src[i];
+        l.reserved = reach_bound(l.radius);
+        L[i] = l;
+    }
+}
+
+// The Blinn-Phong term of one light at P: att = (1 - d/r)^2, diffuse
+// max(N.L,0)*albedo, specular max(N.H,0)^32, times the light's colour; false
+// (and no term) when the light does not reach P.  l is a load_lights() copy: a
+// light with d^2 >= its bound is rejected without the square root (sqrtf(d^2)
+// < r would be false), so the outcome is that of testing it with sqrtf.
+__device__ __forceinline__ bool plain_term(const rsrgpu_light& l, const float P[3], const float n[3],
+                                           const float v[3], const float a[3], float term[3]) {
+    float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
+    const float d2 = dot3(lx, ly, lz, lx, ly, lz);
+    if (d2 >= l.reserved) return false;
+    const float d = sqrtf(d2);
+    const float r = l.radius;
+    if (!(d < r)) return false;
+    lx = lx / d; ly = ly / d; lz = lz / d;
+    const float t = 1.0f - d / r;
+    const float att = t * t;
+    const float ndl = pos0(dot3(n[0], n[1], n[2], lx, ly, lz));
+    float hx = lx + v[0], hy = ly + v[1], hz = lz + v[2];
+    const float hlen = sqrtf(dot3(hx, hy, hz, hx, hy, hz));
+    hx = hx / hlen; hy = hy / hlen; hz = hz / hlen;
+    float sp = pos0(dot3(n[0], n[1], n[2], hx, hy, hz));
+    sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
+    term[0] = (l.color[0] * att) * (a[0] * ndl + sp);
+    term[1] = (l.color[1] * att) * (a[1] * ndl + sp);
+    term[2] = (l.color[2] * att) * (a[2] * ndl + sp);
+    return true;
+}
+
+// Blinn-Phong sum over lights first, first+step, ... < nl, added in light
+// order (L: load_lights() copies)
 __device__ __forceinline__ void plain_sum(const rsrgpu_light* L, int first, int step, int nl, const float P[3],
                                           const float n[3], const float v[3], const float a[3], float s[3]) {
     for (int i = first; i < nl; i += step) {
-        float lx = L[i].position[0] - P[0], ly = L[i].position[1] - P[1], lz = L[i].position[2] - P[2];
-        const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
-        const float r = L[i].radius;
-        if (!(d < r)) continue;
-        lx = lx / d; ly = ly / d; lz = lz / d;
-        const float t = 1.0f - d / r;
-        const float att = t * t;
-        const float ndl = pos0(dot3(n[0], n[1], n[2], lx, ly, lz));
-        float hx = lx + v[0], hy = ly + v[1], hz = lz + v[2];
-        const float hlen = sqrtf(dot3(hx, hy, hz, hx, hy, hz));
-        hx = hx / hlen; hy = hy / hlen; hz = hz / hlen;
-        float sp = pos0(dot3(n[0], n[1], n[2], hx, hy, hz));
-        sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
-        s[0] = s[0] + (L[i].color[0] * att) * (a[0] * ndl + sp);
-        s[1] = s[1] + (L[i].color[1] * att) * (a[1] * ndl + sp);
-        s[2] = s[2] + (L[i].color[2] * att) * (a[2] * ndl + sp);
+        float term[3];
+        if (!plain_term(L[i], P, n, v, a, term)) continue;
+        s[0] = s[0] + term[0];
+        s[1] = s[1] + term[1];
+        s[2] = s[2] + term[2];
     }
 }
 
@@ -145,8 +183,10 @@ __device__ __forceinline__ void select_candidates(int nl, Score score, int* cand
     for (int i = lane; i < nl; i += 32) {
         const float si = scratch[i];
         if (!(si > 0.0f)) continue;
+        // every light is compared (no early exit), eight loads in flight at a time
         int rank = 0;
-        for (int j = 0; j < nl && rank < kCandidates; ++j) {
+#pragma unroll 8
+        for (int j = 0; j < nl; ++j) {
             const float sj = scratch[j];
             rank += (sj > si || (sj == si && j < i)) ? 1 : 0;
         }
@@ -227,6 +267,7 @@ __device__ __forceinline__ int reaching_lights(const rsrgpu_light* L, const int*
         const rsrgpu_light& l = L[li];
         const float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
         const float d2 = dot3(lx, ly, lz, lx, ly, lz);
+        if (d2 >= l.reserved) continue;
         const float d = d2 * rsqrtf(d2);
         k += (d < l.radius) ? 1 : 0;
     }
@@ -241,6 +282,7 @@ __device__ __forceinline__ void plain_sum_fast(const rsrgpu_light* L, int first,
     for (int i = first; i < nl; i += step) {
         float lx = L[i].position[0] - P[0], ly = L[i].position[1] - P[1], lz = L[i].position[2] - P[2];
         const float d2 = dot3(lx, ly, lz, lx, ly, lz);
+        if (d2 >= L[i].reserved) continue;
         const float id = rsqrtf(d2);
         const float d = d2 * id;
         const float r = L[i].radius;
@@ -291,10 +333,21 @@ __device__ __forceinline__ int pixel_features_fast(const PlainParams& p, const r
     for (int k = 10; k < kFeatures; ++k) f[k] = 0.0f;
     float wsum = 0.0f;
     int reach = 0;
+    // the candidates within their reach bound first, then the full terms for
+    // those alone (in candidate order): a warp runs the loop body as often as
+    // its busiest pixel needs, not once per candidate
+    uint32_t near = 0u;
     for (int c = 0; c < kCandidates; ++c) {
         const int li = cand[c];
         if (li < 0) break;
         const rsrgpu_light& l = L[li];
+        const float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
+        if (dot3(lx, ly, lz, lx, ly, lz) < l.reserved) near |= 1u << c;
+    }
+    while (near != 0u) {
+        const int c = __ffs(near) - 1;
+        near &= near - 1u;
+        const rsrgpu_light& l = L[cand[c]];
         const float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
         const float d2 = dot3(lx, ly, lz, lx, ly, lz);
         const float id = rsqrtf(d2);
