@@ -11,8 +11,10 @@ Reported (one JSON line from rank 0):
              kernels (CUDA events on the launching stream), L2 flushed with a
              256 MiB write before every timed frame (outside the event pair)
   e2e        the same metric through the C ABI with host (pinned) buffers:
-             every frame copies its inputs to the device and its colour and
-             depth back, inside the timed region
+             every frame moves its inputs to the device (vertex data by one
+             gather kernel, the texture by a copy overlapping setup and
+             binning) and its colour and depth back (written into the host
+             buffers by the raster pass), inside the timed region
   roofline   dominant kernel (raster) against measured HBM bandwidth
   cpu_baseline  the CPU implementation on this machine's cores, bounded sample
 

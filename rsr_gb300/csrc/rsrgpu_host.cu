@@ -29,6 +29,7 @@ namespace rsrgpu {
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_gather(const GatherList& g, cudaStream_t st);
 cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st);
@@ -84,9 +85,17 @@ struct DevBuf {
 struct HostBuffer {
     const uint8_t* host = nullptr;
     size_t bytes = 0;
-    void* dev = nullptr;
-    bool in = false, out = false;
+    void* dev = nullptr;          // device mirror
+    void* mapped = nullptr;       // device address of the host memory itself (pinned and mapped), else null
+    bool in = false, out = false; // this frame reads it through the mirror / writes the mirror
+    bool early = false;           // read by triangle setup (vertices, indices): copied first
+    bool late = false;            // read only by the raster pass (textures): copied while setup and binning run
+    bool direct = false;          // written by this frame straight into host memory (no mirror, no copy back)
 };
+
+// How a frame uses a caller pointer (resolve): kProbe maps without recording
+// a use (entry points that take device pointers only check what they get).
+enum Use { kProbe, kEarlyInput, kLateInput, kOutput };
 
 struct Copy { void* dst; const void* src; size_t bytes; };
 
@@ -122,6 +131,9 @@ struct rsrgpu_ctx {
     int region_px = kRegionPx;      // raster CTA region (the autotuner may pick 16)
     FrameCounters* h_counters = nullptr;   // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    // textures from host buffers are copied on `side` while setup and binning run
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_late = nullptr;
     FrameView fv{};
     rsrgpu_stats stats{};
 };
@@ -208,8 +220,12 @@ void build_srgb_lut(std::vector<uint8_t>& lut) {
 
 // Maps a caller pointer to a device address and the number of bytes that
 // are valid from it (to the end of the registered host buffer, or of the
-// device allocation containing it).
-int resolve(rsrgpu_ctx* ctx, const void* p, bool output, void** out, const char* what, size_t* avail = nullptr) {
+// device allocation containing it).  For a registered host buffer the use
+// decides the address: outputs of pinned, mapped host memory are written in
+// place by the kernels (the transfer overlaps the raster pass instead of
+// following it); other uses go through the device mirror, copied in before
+// the pass that reads it or out after the frame.
+int resolve(rsrgpu_ctx* ctx, const void* p, Use use, void** out, const char* what, size_t* avail = nullptr) {
     *out = nullptr;
     if (avail) *avail = 0;
     if (p == nullptr) return 0;
@@ -219,8 +235,19 @@ int resolve(rsrgpu_ctx* ctx, const void* p, bool output, void** out, const char*
         --it;
         HostBuffer& hb = it->second;
         if (bp >= hb.host && bp < hb.host + hb.bytes) {
-            if (output) hb.out = true; else hb.in = true;
-            *out = static_cast<uint8_t*>(hb.dev) + (bp - hb.host);
+            void* base = hb.dev;
+            if (use == kOutput) {
+                if (hb.mapped != nullptr && !hb.in) { hb.direct = true; base = hb.mapped; }
+                else hb.out = true;
+            } else if (use != kProbe) {
+                if (hb.direct) {
+                    base = hb.mapped;   // this frame writes it in place: read it there too
+                } else {
+                    hb.in = true;
+                    if (use == kLateInput) hb.late = true; else hb.early = true;
+                }
+            }
+            *out = static_cast<uint8_t*>(base) + (bp - hb.host);
             if (avail) *avail = hb.bytes - size_t(bp - hb.host);
             return 0;
         }
@@ -299,7 +326,7 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
     for (int i = 0; i < 16; ++i) {
         void* dp = nullptr;
         size_t avail = 0;
-        int rc = resolve(ctx, s.buffers[i], false, &dp, "vertex buffer", &avail);
+        int rc = resolve(ctx, s.buffers[i], kEarlyInput, &dp, "vertex buffer", &avail);
         if (rc) return rc;
         d.buffers[i] = static_cast<const float*>(dp);
         d.buffer_len[i] = int32_t(std::min<size_t>(avail / sizeof(float), size_t(INT32_MAX)));
@@ -316,7 +343,7 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
             return fail(ctx, RSRGPU_EUNSUPPORTED, "can't make TextureUnit for pow2 size %d", t.width);
         void* dp = nullptr;
         size_t avail = 0;
-        int rc = resolve(ctx, t.ptr, false, &dp, "texture", &avail);
+        int rc = resolve(ctx, t.ptr, kLateInput, &dp, "texture", &avail);
         if (rc) return rc;
         // the mip chain of a square power-of-two texture (2*W*W texels), else H rows of stride texels
         const size_t need = pow2 ? size_t(2) * size_t(t.width) * size_t(t.width) * 16u
@@ -342,6 +369,9 @@ int rsrgpu_create(int device, rsrgpu_ctx** out) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) { delete ctx; return RSRGPU_ECUDA; }
     if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
         cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_counters), sizeof(FrameCounters), cudaHostAllocDefault) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->ev2) != cudaSuccess || cudaEventCreate(&ctx->ev3) != cudaSuccess) {
@@ -373,8 +403,10 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
                        &ctx->d_rcp, &ctx->d_srgb };
     for (DevBuf* b : bufs) b->release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
-    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3 };
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_fork, ctx->ev_late };
     for (cudaEvent_t ev : evs) if (ev) cudaEventDestroy(ev);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
     return 0;
@@ -439,6 +471,12 @@ int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t by
     hb.host = p;
     hb.bytes = bytes;
     CK(cudaMalloc(&hb.dev, bytes), "cudaMalloc(host mirror)");
+    // pinned host memory the device can address (cudaHostAlloc, or registered as mapped)
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer != nullptr)
+        hb.mapped = a.devicePointer;
+    else
+        cudaGetLastError();
     ctx->host[p] = hb;
     return 0;
 }
@@ -456,7 +494,7 @@ int rsrgpu_unregister_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr) {
 int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates) {
     if (ctx == nullptr || (commands == nullptr && nbytes) || nstates < 0) return RSRGPU_EINVAL;
     if (ctx->ntiles == 0) return fail(ctx, RSRGPU_EINVAL, "rsrgpu_reset() has not been called");
-    for (auto& kv : ctx->host) kv.second.in = kv.second.out = false;
+    for (auto& kv : ctx->host) kv.second.in = kv.second.out = kv.second.early = kv.second.late = kv.second.direct = false;
     ctx->states.assign(size_t(nstates), DevState{});
     ctx->state_ordinal.assign(size_t(nstates), -1);
     ctx->draws.clear();
@@ -541,7 +579,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             if (!dd.is_arrays) {
                 void* dp = nullptr;
                 size_t avail = 0;
-                int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(iptr)), false, &dp, "index", &avail);
+                int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(iptr)), kEarlyInput, &dp, "index", &avail);
                 if (rc) return rc;
                 if (dp == nullptr || avail < size_t(dd.ntris) * 3u * sizeof(uint16_t))
                     return fail(ctx, RSRGPU_EINVAL, "index buffer holds %zu bytes, draw needs %zu", avail, size_t(dd.ntris) * 6u);
@@ -568,7 +606,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
                 return fail(ctx, RSRGPU_EINVAL, "TrueColor canvas must match the %dx%d target (even stride)", ctx->width, ctx->height);
             void* dp = nullptr;
             size_t avail = 0;
-            int rc = resolve(ctx, cv->data, true, &dp, "color output", &avail);
+            int rc = resolve(ctx, cv->data, kOutput, &dp, "color output", &avail);
             if (rc) return rc;
             if (dp == nullptr || avail < size_t(cv->stride) * size_t(cv->height) * 4u)
                 return fail(ctx, RSRGPU_EINVAL, "color output holds %zu bytes, needs %zu", avail, size_t(cv->stride) * size_t(cv->height) * 4u);
@@ -588,7 +626,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
                 return fail(ctx, RSRGPU_EUNSUPPORTED, "STORE_DEPTH_FULL_LINEAR_FP not implemented for attachment type %d", states[cur].depth_attachment_type);
             void* dp = nullptr;
             size_t avail = 0;
-            int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(dp64)), true, &dp, "depth output", &avail);
+            int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(dp64)), kOutput, &dp, "depth output", &avail);
             if (rc) return rc;
             if (dp == nullptr || avail < size_t(ctx->width) * size_t(ctx->height) * 4u)
                 return fail(ctx, RSRGPU_EINVAL, "depth output holds %zu bytes, needs %zu", avail, size_t(ctx->width) * size_t(ctx->height) * 4u);
@@ -618,7 +656,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
                                reinterpret_cast<void**>(&gd.ny), reinterpret_cast<void**>(&gd.nz),
                                reinterpret_cast<void**>(&gd.albedo) };
             for (int k = 0; k < 5; ++k) {
-                int rc = resolve(ctx, srcs[k], true, &dp, "G-buffer", &avail);
+                int rc = resolve(ctx, srcs[k], kOutput, &dp, "G-buffer", &avail);
                 if (rc) return rc;
                 if (dp == nullptr || avail < need[k] || (reinterpret_cast<uintptr_t>(dp) & 7))
                     return fail(ctx, RSRGPU_EINVAL, "G-buffer plane %d: need %zu bytes, 8-byte aligned", k, need[k]);
@@ -721,9 +759,35 @@ int enqueue(rsrgpu_ctx* ctx, cudaStream_t st) {
     int rc = prepare_view(ctx);
     if (rc) return rc;
     const FrameView& fv = ctx->fv;
-    // inputs that live in registered host buffers travel with every run
-    for (auto& kv : ctx->host)
-        if (kv.second.in) CK(cudaMemcpyAsync(kv.second.dev, kv.second.host, kv.second.bytes, cudaMemcpyHostToDevice, st), "H2D input");
+    // Inputs that live in registered host buffers travel with every run.  The
+    // ones triangle setup reads come first: from pinned, mapped memory in one
+    // gather kernel (many small arrays cost one launch rather than a copy
+    // each), others by copies.  Textures, which only the raster pass reads,
+    // follow on the side stream while setup and binning run.
+    GatherList gl{};
+    bool any_late = false;
+    for (auto& kv : ctx->host) {
+        HostBuffer& hb = kv.second;
+        if (!hb.in) continue;
+        if (!hb.early) { any_late = true; continue; }
+        if (hb.mapped != nullptr && gl.n < kMaxGather) {
+            gl.src[gl.n] = static_cast<const uint8_t*>(hb.mapped);
+            gl.dst[gl.n] = static_cast<uint8_t*>(hb.dev);
+            gl.bytes[gl.n] = hb.bytes;
+            ++gl.n;
+        } else {
+            CK(cudaMemcpyAsync(hb.dev, hb.host, hb.bytes, cudaMemcpyHostToDevice, st), "H2D input");
+        }
+    }
+    if (gl.n > 0) CK(launch_gather(gl, st), "gather_kernel");
+    if (any_late) {
+        CK(cudaEventRecord(ctx->ev_fork, st), "event");
+        CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0), "stream wait");
+        for (auto& kv : ctx->host)
+            if (kv.second.in && !kv.second.early)
+                CK(cudaMemcpyAsync(kv.second.dev, kv.second.host, kv.second.bytes, cudaMemcpyHostToDevice, ctx->side), "H2D texture");
+        CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
+    }
     CK(cudaMemcpyAsync(ctx->d_states.p, ctx->states.data(), sizeof(DevState) * ctx->states.size(), cudaMemcpyHostToDevice, st), "H2D states");
     if (!ctx->draws.empty())
         CK(cudaMemcpyAsync(ctx->d_draws.p, ctx->draws.data(), sizeof(DevDraw) * ctx->draws.size(), cudaMemcpyHostToDevice, st), "H2D draws");
@@ -736,14 +800,16 @@ int enqueue(rsrgpu_ctx* ctx, cudaStream_t st) {
     CK(cudaEventRecord(ctx->ev0, st), "event");
     CK(launch_setup(fv, st), "setup_kernel");
     CK(launch_bin(fv, st), "bin_kernel");
+    if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
     CK(cudaEventRecord(ctx->ev1, st), "event");
     CK(launch_raster(fv, st), "raster_kernel");
     CK(cudaEventRecord(ctx->ev2, st), "event");
+    // outputs written in place need no copy back
     for (auto& kv : ctx->host)
         if (kv.second.out) CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
     CK(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, st), "D2H counters");
     CK(cudaEventRecord(ctx->ev3, st), "event");
-    ctx->stats.gpu_launches = 3;
+    ctx->stats.gpu_launches = 3 + (gl.n > 0 ? 1 : 0);
     return 0;
 }
 
@@ -928,7 +994,7 @@ int rsrgpu_shade_plain(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const flo
     size_t avail = 0;
     for (int k = 0; k < 6; ++k) {
         if (need[k] == 0) continue;
-        int rc = resolve(ctx, ins[k], false, &dp, "deferred input", &avail);
+        int rc = resolve(ctx, ins[k], kProbe, &dp, "deferred input", &avail);
         if (rc) return rc;
         if (dp == nullptr || avail < need[k]) return fail(ctx, RSRGPU_EINVAL, "deferred input %d holds %zu bytes, needs %zu", k, avail, need[k]);
         if (dp != ins[k]) return fail(ctx, RSRGPU_EINVAL, "rsrgpu_shade_plain takes device pointers");
@@ -937,7 +1003,7 @@ int rsrgpu_shade_plain(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const flo
     const size_t oneed[2] = { npx * 4, npx * 12 };
     for (int k = 0; k < 2; ++k) {
         if (outs[k] == nullptr) continue;
-        int rc = resolve(ctx, outs[k], true, &dp, "deferred output", &avail);
+        int rc = resolve(ctx, outs[k], kProbe, &dp, "deferred output", &avail);
         if (rc) return rc;
         if (dp != outs[k] || avail < oneed[k]) return fail(ctx, RSRGPU_EINVAL, "deferred output %d: device pointer with %zu bytes needed", k, oneed[k]);
     }
@@ -951,7 +1017,7 @@ namespace {
 int check_device_input(rsrgpu_ctx* ctx, const void* p, size_t need, size_t align, const char* what) {
     void* dp = nullptr;
     size_t avail = 0;
-    int rc = resolve(ctx, p, false, &dp, what, &avail);
+    int rc = resolve(ctx, p, kProbe, &dp, what, &avail);
     if (rc) return rc;
     if (dp == nullptr || dp != p || avail < need || (reinterpret_cast<uintptr_t>(p) % align))
         return fail(ctx, RSRGPU_EINVAL, "%s: device pointer with %zu bytes, %zu-byte aligned, needed", what, need, align);
@@ -1070,7 +1136,7 @@ int check_device_output(rsrgpu_ctx* ctx, void* p, size_t need, size_t align, con
     if (p == nullptr) return 0;
     void* dp = nullptr;
     size_t avail = 0;
-    int rc = resolve(ctx, p, true, &dp, what, &avail);
+    int rc = resolve(ctx, p, kProbe, &dp, what, &avail);
     if (rc) return rc;
     if (dp != p || avail < need || (reinterpret_cast<uintptr_t>(p) % align))
         return fail(ctx, RSRGPU_EINVAL, "%s: device pointer with %zu bytes, %zu-byte aligned, needed", what, need, align);

@@ -157,6 +157,16 @@ struct FrameView {
 
 // One launch of a stage over many frames: block b belongs to frame f when
 // start[f] <= b < start[f + 1]; passed as a __grid_constant__ parameter.
+// Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,
+// mapped host memory into their device mirrors).
+constexpr int kMaxGather = 64;
+struct GatherList {
+    int n;
+    const uint8_t* src[kMaxGather];
+    uint8_t* dst[kMaxGather];
+    size_t bytes[kMaxGather];
+};
+
 struct BatchLaunch {
     int32_t nframes;
     int32_t start[kMaxBatch + 1];

@@ -750,6 +750,20 @@ __device__ __forceinline__ void lane_bary(const FrameView& fv, const TriSetup& t
 
 // Shades every pixel of the quad whose last visible fragment is still
 // pending, with the owning triangle's program, and writes the colour.
+// Element l of a four-lane quad array, with constant indices only: the loops
+// over the quad's lanes below stay rolled (their bodies are large), and an
+// array indexed by a variable would live in local memory for the whole kernel.
+template <typename T>
+__device__ __forceinline__ T quad_get(const T a[4], int l) {
+    return l == 0 ? a[0] : l == 1 ? a[1] : l == 2 ? a[2] : a[3];
+}
+__device__ __forceinline__ void quad_put_rgb(float col[4][3], int l, float r, float g, float b) {
+    if (l == 0) { col[0][0] = r; col[0][1] = g; col[0][2] = b; }
+    else if (l == 1) { col[1][0] = r; col[1][1] = g; col[1][2] = b; }
+    else if (l == 2) { col[2][0] = r; col[2][1] = g; col[2][2] = b; }
+    else { col[3][0] = r; col[3][1] = g; col[3][2] = b; }
+}
+
 __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect[4], int qx, int qy,
                                              uint32_t own[4], float col[4][3]) {
     uint32_t cur = kNoOwner;
@@ -758,9 +772,10 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
     int state = 0;
 #pragma unroll 1
     for (int l = 0; l < 4; ++l) {
-        if (own[l] == kNoOwner) continue;
-        if (own[l] != cur) {
-            cur = own[l];
+        const uint32_t ol = quad_get(own, l);
+        if (ol == kNoOwner) continue;
+        if (ol != cur) {
+            cur = ol;
             owner_setup(fv, cur, rect, t, w, vary, state);
         }
         const DevState& s = fv.states[state];
@@ -779,13 +794,16 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
             float o[4];
             const DevTexture tu = s.tu0;
             tex_sample_lane(tu, u0, v0, u1, v1, ul, vl, o);
-            col[l][0] = o[0]; col[l][1] = o[1]; col[l][2] = o[2];
+            quad_put_rgb(col, l, o[0], o[1], o[2]);
         } else {
+            float c[3];
 #pragma unroll
-            for (int q = 0; q < 3; ++q) col[l][q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
+            for (int q = 0; q < 3; ++q) c[q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
+            quad_put_rgb(col, l, c[0], c[1], c[2]);
         }
-        own[l] = kNoOwner;
     }
+#pragma unroll
+    for (int l = 0; l < 4; ++l) own[l] = kNoOwner;
 }
 
 __device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
@@ -1029,25 +1047,33 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         } else if (o.kind == kOpStoreGBuffer) {
             if (active) {
                 const GBufferDesc gb = fv.gbufs[o.arg];
-                uint16_t nx[4], ny[4], nz[4];
-                uint32_t alb[4];
+                // per lane l: normal x/y/z (fp16 bits) and albedo, packed by
+                // constant index (see quad_get)
+                uint32_t nxy[4] = { 0u, 0u, 0u, 0u }, nzl[4] = { 0u, 0u, 0u, 0u }, alb[4] = { 0u, 0u, 0u, 0u };
 #pragma unroll 1
                 for (int l = 0; l < 4; ++l) {
-                    nx[l] = ny[l] = nz[l] = 0;
-                    alb[l] = 0;
-                    if (own[l] == kNoOwner) continue;
+                    const uint32_t ol = quad_get(own, l);
+                    if (ol == kNoOwner) continue;
                     TriSetup t;
                     float w[3], vary[3][kMaxVary];
                     int state;
-                    owner_setup(fv, own[l], rect, t, w, vary, state);
+                    owner_setup(fv, ol, rect, t, w, vary, state);
                     if (fv.states[state].program != kProgGBuffer) continue;
                     float bpx, bpy, bpz;
                     lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
-                    nx[l] = __half_as_ushort(__float2half_rn((bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0]));
-                    ny[l] = __half_as_ushort(__float2half_rn((bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1]));
-                    nz[l] = __half_as_ushort(__float2half_rn((bpx * vary[0][2] + bpy * vary[1][2]) + bpz * vary[2][2]));
-                    alb[l] = uint32_t(vary[0][3]) | 0xff000000u;
+                    const uint32_t hx = __half_as_ushort(__float2half_rn((bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0]));
+                    const uint32_t hy = __half_as_ushort(__float2half_rn((bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1]));
+                    const uint32_t hz = __half_as_ushort(__float2half_rn((bpx * vary[0][2] + bpy * vary[1][2]) + bpz * vary[2][2]));
+                    const uint32_t al = uint32_t(vary[0][3]) | 0xff000000u;
+                    const uint32_t xy = hx | (hy << 16);
+                    if (l == 0) { nxy[0] = xy; nzl[0] = hz; alb[0] = al; }
+                    else if (l == 1) { nxy[1] = xy; nzl[1] = hz; alb[1] = al; }
+                    else if (l == 2) { nxy[2] = xy; nzl[2] = hz; alb[2] = al; }
+                    else { nxy[3] = xy; nzl[3] = hz; alb[3] = al; }
                 }
+                uint16_t nx[4], ny[4], nz[4];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) { nx[l] = uint16_t(nxy[l] & 0xffffu); ny[l] = uint16_t(nxy[l] >> 16); nz[l] = uint16_t(nzl[l]); }
                 const size_t r0 = size_t(qy) * o.stride + qx, r1 = r0 + o.stride;
                 *reinterpret_cast<float2*>(gb.depth + r0) = make_float2(dep[0], dep[1]);
                 *reinterpret_cast<float2*>(gb.depth + r1) = make_float2(dep[2], dep[3]);
@@ -1120,6 +1146,29 @@ cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
 
 int setup_blocks(const FrameView& fv) { return (fv.ntris + kSetupBlock - 1) / kSetupBlock; }
 int bin_blocks(const FrameView& fv) { return (fv.ntiles + kBinBlock / 32 - 1) / (kBinBlock / 32); }
+// One CTA row per range: 16-byte loads and stores where both ends are aligned, bytes otherwise.
+__global__ void __launch_bounds__(256) gather_kernel(const __grid_constant__ GatherList g) {
+    const int r = blockIdx.y;
+    const uint8_t* __restrict__ src = g.src[r];
+    uint8_t* __restrict__ dst = g.dst[r];
+    const size_t n = g.bytes[r];
+    const size_t first = size_t(blockIdx.x) * blockDim.x + threadIdx.x, step = size_t(gridDim.x) * blockDim.x;
+    size_t done = 0;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+        const size_t n16 = n / 16;
+        for (size_t i = first; i < n16; i += step)
+            reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
+        done = n16 * 16;
+    }
+    for (size_t i = done + first; i < n; i += step) dst[i] = src[i];
+}
+
+cudaError_t launch_gather(const GatherList& g, cudaStream_t st) {
+    if (g.n <= 0) return cudaSuccess;
+    gather_kernel<<<dim3(32, unsigned(g.n)), 256, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
 int raster_blocks(const FrameView& fv) {
     const int sub_x = (fv.tile_w + fv.region_px - 1) / fv.region_px;
     const int sub_y = (fv.tile_h + fv.region_px - 1) / fv.region_px;
