@@ -11,25 +11,38 @@
 
 namespace rsrgpu {
 
-__global__ void __launch_bounds__(256) shade_plain_kernel(PlainParams p) {
+// One CTA per 16x16-pixel block: the block's lights are culled against its
+// world-space box once (plain_block_lights), then each pixel sums those.
+__global__ void __launch_bounds__(kPlainThreads) shade_plain_kernel(PlainParams p) {
     __shared__ rsrgpu_light L[kMaxLights];
+    __shared__ PlainBlockShared S;
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
     load_lights(L, p.lights, nl);
-    __syncthreads();
-    const int n = p.width * p.height;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int x = i % p.width, y = i / p.width;
-        const uint32_t alb = p.albedo[i];
-        float rgb[3];
-        if (alb == 0u) {
-            rgb[0] = p.background[0]; rgb[1] = p.background[1]; rgb[2] = p.background[2];
-        } else {
-            plain_pixel(p, L, nl, x, y, p.depth[i], p.nx[i], p.ny[i], p.nz[i], alb, rgb);
-        }
-        if (p.out_linear) { p.out_linear[3 * i] = rgb[0]; p.out_linear[3 * i + 1] = rgb[1]; p.out_linear[3 * i + 2] = rgb[2]; }
-        if (p.out_srgb)
-            p.out_srgb[i] = pack_srgb(p.srgb_lut, rgb);
+    const int bx = (p.width + kPlainBlock - 1) / kPlainBlock;
+    const int x = (int(blockIdx.x) % bx) * kPlainBlock + int(threadIdx.x) % kPlainBlock;
+    const int y = (int(blockIdx.x) / bx) * kPlainBlock + int(threadIdx.x) / kPlainBlock;
+    const bool inside = x < p.width && y < p.height;
+    const int i = y * p.width + x;
+    const uint32_t alb = inside ? p.albedo[i] : 0u;
+    const bool live = alb != 0u;
+    float P[3] = { 0.0f, 0.0f, 0.0f }, n[3], v[3], vlen, a[3];
+    if (live) {
+        world_pos(p, x, y, p.depth[i], P);
+        surface(p, P, p.nx[i], p.ny[i], p.nz[i], n, v, vlen);
+        albedo_rgb(alb, a);
     }
+    __syncthreads();   // the lights are in shared memory
+    const int nkeep = plain_block_lights(L, nl, live, P, S);
+    if (!inside) return;
+    float rgb[3];
+    if (live) {
+        plain_block_pixel(L, S.keep, nkeep, P, n, v, a, rgb);
+    } else {
+        rgb[0] = p.background[0]; rgb[1] = p.background[1]; rgb[2] = p.background[2];
+    }
+    if (p.out_linear) { p.out_linear[3 * i] = rgb[0]; p.out_linear[3 * i + 1] = rgb[1]; p.out_linear[3 * i + 2] = rgb[2]; }
+    if (p.out_srgb)
+        p.out_srgb[i] = pack_srgb(p.srgb_lut, rgb);
 }
 
 cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], const float eye[3],
@@ -41,10 +54,8 @@ cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], co
     for (int i = 0; i < 16; ++i) p.ivp[i] = ivp[i];
     for (int i = 0; i < 3; ++i) { p.eye[i] = eye[i]; p.background[i] = background[i]; }
     p.lights = lights; p.nlights = nlights; p.out_srgb = out_srgb; p.out_linear = out_linear; p.srgb_lut = srgb_lut;
-    const int n = gb.width * gb.height;
-    int blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    shade_plain_kernel<<<blocks, 256, 0, st>>>(p);
+    const int blocks = ((gb.width + kPlainBlock - 1) / kPlainBlock) * ((gb.height + kPlainBlock - 1) / kPlainBlock);
+    shade_plain_kernel<<<blocks, kPlainThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 

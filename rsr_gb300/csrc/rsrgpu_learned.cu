@@ -132,6 +132,7 @@ __device__ __forceinline__ uint4* chunk_row(uint8_t* tile, int j, int r) {
 constexpr int kPrepThreads = 256;   // per 32x32 tile: four pixels of a row per thread
 constexpr int kPrepWarps = kPrepThreads / 32;
 constexpr int kPrepPx = kTilePx / kPrepThreads;
+static_assert(kPrepPx == 4, "the coverage loads move four pixels as one vector");
 
 __global__ void __launch_bounds__(kPrepThreads, 4) learned_prep_kernel(LearnParams A) {
     extern __shared__ rsrgpu_light L[];
@@ -168,16 +169,32 @@ __global__ void __launch_bounds__(kPrepThreads, 4) learned_prep_kernel(LearnPara
         const uint32_t bg = pack_srgb(p.srgb_lut, p.background);
         uint32_t cov = 0;
         float zd[kPrepPx];
+        uint32_t alb[kPrepPx];
+        // every load of the thread's four pixels before any is used: one round
+        // trip to memory (a branch on each albedo would make it four)
+        const int row = y * p.width + x0 + lx0;
+        const bool full = y < p.height && x0 + lx0 + kPrepPx <= p.width && (row % 4) == 0 &&
+                          ((reinterpret_cast<uintptr_t>(p.depth) | reinterpret_cast<uintptr_t>(p.albedo)) & 15u) == 0;
+        if (full) {
+            const float4 z4 = *reinterpret_cast<const float4*>(p.depth + row);
+            const uint4 a4 = *reinterpret_cast<const uint4*>(p.albedo + row);
+            zd[0] = z4.x; zd[1] = z4.y; zd[2] = z4.z; zd[3] = z4.w;
+            alb[0] = a4.x; alb[1] = a4.y; alb[2] = a4.z; alb[3] = a4.w;
+        } else {
+#pragma unroll
+            for (int j = 0; j < kPrepPx; ++j) {
+                const bool in = y < p.height && x0 + lx0 + j < p.width;
+                zd[j] = in ? p.depth[row + j] : 1.0f;
+                alb[j] = in ? p.albedo[row + j] : 0u;
+            }
+        }
 #pragma unroll
         for (int j = 0; j < kPrepPx; ++j) {
-            const int x = x0 + lx0 + j;
-            zd[j] = 1.0f;
-            if (x >= p.width || y >= p.height) continue;
-            const int pi = y * p.width + x;
-            zd[j] = p.depth[pi];   // loaded with the albedo: one round trip for both
-            if (p.albedo[pi] != 0u) {
+            if (y >= p.height || x0 + lx0 + j >= p.width) continue;
+            if (alb[j] != 0u) {
                 cov |= 1u << j;
             } else {
+                const int pi = row + j;
                 if (p.out_srgb) p.out_srgb[pi] = bg;
                 if (p.out_linear) { p.out_linear[3 * size_t(pi)] = p.background[0]; p.out_linear[3 * size_t(pi) + 1] = p.background[1]; p.out_linear[3 * size_t(pi) + 2] = p.background[2]; }
             }
@@ -362,26 +379,52 @@ __global__ void __launch_bounds__(kPrepThreads, 4) learned_prep_kernel(LearnPara
 }
 
 // ---------------------------------------------------------------- tensor-core kernel
-// W (the first KSRC columns of a row-major [rows][LD] bf16 matrix) plus the
-// bias as columns KSRC (high) and KSRC+1 (low), zeros to KDIM, into the
-// row-wise K-major layout (LBO 128, SBO KDIM/8 * 128); 16-byte chunks
-template <int KSRC, int LD, int KDIM>
-__device__ __forceinline__ void load_weights_bias(uint8_t* dst, const uint16_t* __restrict__ W, int rows,
-                                                  const float* __restrict__ bias) {
-    constexpr int kChunks = KDIM / 8, kSrcChunks = KSRC / 8;
-    for (int c = threadIdx.x; c < rows * kChunks; c += blockDim.x) {
-        const int r = c / kChunks, j = c % kChunks;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (j < kSrcChunks) {
-            v = __ldg(reinterpret_cast<const uint4*>(W + r * LD + j * 8));
-        } else if (j == kSrcChunks) {
-            const float b = __ldg(bias + r);
-            const uint16_t hi = bf16_rn(b);
-            const uint16_t lo = bf16_rn(b - __bfloat162float(__ushort_as_bfloat16(hi)));
-            v.x = uint32_t(hi) | (uint32_t(lo) << 16);
-        }
-        *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(r, j * 8, KDIM)) = v;
+// Chunk c (16 bytes) of the four weight matrices, in order w1 | w2 | w3 | w4,
+// each in the row-wise K-major layout (LBO 128, SBO KDIM/8 * 128): columns
+// 8j..8j+7 of W (the first KSRC columns of a row-major [rows][LD] bf16
+// matrix), the bias as columns KSRC (high) and KSRC+1 (low), zeros to KDIM.
+// Returns the chunk and sets its shared-memory destination.
+__device__ __forceinline__ uint4 weight_chunk(const rsrgpu_mlp& w, uint8_t* w1, uint8_t* w2, uint8_t* w3, uint8_t* w4,
+                                              int c, uint8_t*& dst) {
+    constexpr int c1 = kHid * (kK1 / 8), c2 = kHid * (kKH / 8);
+    const uint16_t* W;
+    const float* B;
+    int kdim, ksrc, ld;
+    if (c < c1) { W = w.w1; B = w.b1; dst = w1; kdim = kK1; ksrc = kFeatures; ld = kIn; }
+    else if (c < c1 + c2) { c -= c1; W = w.w2; B = w.b2; dst = w2; kdim = kKH; ksrc = kHid; ld = kHid; }
+    else if (c < c1 + 2 * c2) { c -= c1 + c2; W = w.w3; B = w.b3; dst = w3; kdim = kKH; ksrc = kHid; ld = kHid; }
+    else { c -= c1 + 2 * c2; W = w.w4; B = w.b4; dst = w4; kdim = kKH; ksrc = kHid; ld = kHid; }
+    const int r = c / (kdim / 8), j = c % (kdim / 8);
+    dst += tc::kmajor_offset(r, j * 8, kdim);
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (j < ksrc / 8) {
+        v = __ldg(reinterpret_cast<const uint4*>(W + r * ld + j * 8));
+    } else if (j == ksrc / 8) {
+        const float b = __ldg(B + r);
+        const uint16_t hi = bf16_rn(b);
+        const uint16_t lo = bf16_rn(b - __bfloat162float(__ushort_as_bfloat16(hi)));
+        v.x = uint32_t(hi) | (uint32_t(lo) << 16);
     }
+    return v;
+}
+
+// All four weight matrices into shared memory: every thread issues its loads
+// (at most kPer chunks) before it stores any, so the prologue waits for one
+// round trip to memory rather than one per chunk.
+__device__ __forceinline__ void load_weights(const rsrgpu_mlp& w, uint8_t* w1, uint8_t* w2, uint8_t* w3, uint8_t* w4) {
+    constexpr int total = kHid * (kK1 / 8) + 2 * kHid * (kKH / 8) + kOut * (kKH / 8);
+    constexpr int kPer = (total + kThreads - 1) / kThreads;
+    uint4 v[kPer];
+    uint8_t* dst[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const int c = int(threadIdx.x) + k * kThreads;
+        dst[k] = nullptr;
+        if (c < total) v[k] = weight_chunk(w, w1, w2, w3, w4, c, dst[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+        if (dst[k] != nullptr) *reinterpret_cast<uint4*>(dst[k]) = v[k];
 }
 
 // D[128 x n] = A (chunked, K = kdim) * W (n x kdim, row-wise K-major)^T, committed to mbar
@@ -558,10 +601,7 @@ __global__ void __launch_bounds__(kThreads, 1) shade_learned_kernel(LearnParams 
     LearnSmem& S = *reinterpret_cast<LearnSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     const PlainParams& p = A.pl;
     const int t = threadIdx.x, warp = t >> 5;
-    load_weights_bias<kFeatures, kIn, kK1>(S.w1, A.w.w1, kHid, A.w.b1);
-    load_weights_bias<kHid, kHid, kKH>(S.w2, A.w.w2, kHid, A.w.b2);
-    load_weights_bias<kHid, kHid, kKH>(S.w3, A.w.w3, kHid, A.w.b3);
-    load_weights_bias<kHid, kHid, kKH>(S.w4, A.w.w4, kOut, A.w.b4);
+    load_weights(A.w, S.w1, S.w2, S.w3, S.w4);
     // the constant chunks 8 (ones at columns 64, 65) and 9 (zeros) of every pipeline tile
     const uint32_t one2 = uint32_t(bf16_rn(1.0f)) | (uint32_t(bf16_rn(1.0f)) << 16);
     for (int i = t; i < kLanes * kPipes * kRows; i += blockDim.x) {
@@ -594,34 +634,42 @@ __global__ void __launch_bounds__(kThreads, 1) shade_learned_kernel(LearnParams 
     if (warp == 0) { tc::fence_after_sync(); tc::tmem_dealloc(S.tmem, 512); }
 }
 
-// Plain shading of the tiles the gates rejected (bit-exact with the plain
-// shader): one CTA of 1024 threads per rejected tile at a time, one thread
-// per pixel.  The plain shader is issue-bound at this occupancy; smaller
-// CTAs (a quarter tile each, or several threads per pixel with the terms
-// merged in light order) measured slower, their per-pixel chains being
-// latency-bound.
-constexpr int kFbThreads = kTilePx;
-__global__ void __launch_bounds__(kFbThreads, 1) shade_fallback_kernel(PlainParams p, const int32_t* __restrict__ rejected,
-                                                                      const int* __restrict__ count) {
-    extern __shared__ rsrgpu_light L[];
+// Plain shading of the tiles the gates rejected, bit-exact with the plain
+// shader: work items of 16x16 pixels (four per tile), each culling the lights
+// against its box and summing the rest (plain_block_lights / _pixel), one
+// thread per pixel.  The CTAs are small enough to sit beside the tensor-core
+// kernel's CTA on an SM, so one per SM is resident and waiting when it ends.
+constexpr int kFbItems = (kShadeTile / kPlainBlock) * (kShadeTile / kPlainBlock);   // per tile
+__global__ void __launch_bounds__(kPlainThreads, 6) shade_fallback_kernel(PlainParams p, const int32_t* __restrict__ rejected,
+                                                                       const int* __restrict__ count) {
+    __shared__ rsrgpu_light L[kMaxLights];
+    __shared__ PlainBlockShared S;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // the gates' decisions are complete
-    const int ntiles = *count;
-    if (int(blockIdx.x) >= ntiles) return;
+    const int items = kFbItems * *count;
+    if (int(blockIdx.x) >= items) return;
     const int nl = p.nlights < kMaxLights ? p.nlights : kMaxLights;
     load_lights(L, p.lights, nl);
-    __syncthreads();
     const int tiles_x = (p.width + kShadeTile - 1) / kShadeTile;
-    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
-        const int tile = rejected[k];
-        const int x = (tile % tiles_x) * kShadeTile + int(threadIdx.x) % kShadeTile;
-        const int y = (tile / tiles_x) * kShadeTile + int(threadIdx.x) / kShadeTile;
-        if (x >= p.width || y >= p.height) continue;
+    constexpr int per_row = kShadeTile / kPlainBlock;
+    for (int k = blockIdx.x; k < items; k += gridDim.x) {
+        const int tile = rejected[k / kFbItems], b = k % kFbItems;
+        const int x = (tile % tiles_x) * kShadeTile + (b % per_row) * kPlainBlock + int(threadIdx.x) % kPlainBlock;
+        const int y = (tile / tiles_x) * kShadeTile + (b / per_row) * kPlainBlock + int(threadIdx.x) / kPlainBlock;
         const int pi = y * p.width + x;
-        const uint32_t alb = p.albedo[pi];
-        if (alb == 0u) continue;
-        float rgb[3];
-        plain_pixel(p, L, nl, x, y, p.depth[pi], p.nx[pi], p.ny[pi], p.nz[pi], alb, rgb);
-        store_pixel(p, pi, rgb);
+        const bool live = x < p.width && y < p.height && p.albedo[pi] != 0u;
+        float P[3] = { 0.0f, 0.0f, 0.0f }, n[3], v[3], vlen, a[3];
+        if (live) {
+            world_pos(p, x, y, p.depth[pi], P);
+            surface(p, P, p.nx[pi], p.ny[pi], p.nz[pi], n, v, vlen);
+            albedo_rgb(p.albedo[pi], a);
+        }
+        __syncthreads();   // lights loaded; the previous item's light list read
+        const int nkeep = plain_block_lights(L, nl, live, P, S);
+        if (live) {
+            float rgb[3];
+            plain_block_pixel(L, S.keep, nkeep, P, n, v, a, rgb);
+            store_pixel(p, pi, rgb);
+        }
     }
 }
 
@@ -685,11 +733,11 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
     cfg.numAttrs = 1;
     e = cudaLaunchKernelEx(&cfg, shade_learned_kernel, A);
     if (e != cudaSuccess) return e;
-    int fgrid = num_sms;
-    if (fgrid > tiles) fgrid = tiles;
+    int fgrid = num_sms * 4;
+    if (fgrid > tiles * kFbItems) fgrid = tiles * kFbItems;
     cfg.gridDim = dim3(fgrid);
-    cfg.blockDim = dim3(kFbThreads);
-    cfg.dynamicSmemBytes = light_bytes;
+    cfg.blockDim = dim3(kPlainThreads);
+    cfg.dynamicSmemBytes = 0;
     const int32_t* rej = A.rejected;
     const int* cnt = counters + 2;
     return cudaLaunchKernelEx(&cfg, shade_fallback_kernel, p, rej, cnt);

@@ -153,6 +153,81 @@ __device__ __forceinline__ void plain_pixel(const PlainParams& p, const rsrgpu_l
     rgb[2] = s[2] + 0.03f * a[2];
 }
 
+// ---- the plain shader over a block of pixels ----
+// kPlainBlock x kPlainBlock pixels, one per thread of a 256-thread CTA.  The
+// lights that can reach the world-space box of the block's covered pixels
+// are gathered once, in light order, and every pixel sums only those.  A
+// light is dropped only if its squared distance to the box is at least
+// (1 + 2^-12) times its reach bound: the distance to the box is a lower
+// bound of the distance to every pixel of the block, and the few ulps by
+// which the two computed values can disagree are far below that margin, so
+// every dropped light fails plain_term for every pixel of the block and the
+// sum is that of plain_sum over all lights, bit for bit.
+constexpr int kPlainBlock = 16;
+constexpr int kPlainThreads = kPlainBlock * kPlainBlock;
+
+struct PlainBlockShared {
+    float lo[kPlainThreads / 32][3], hi[kPlainThreads / 32][3];
+    int count[kPlainThreads / 32];
+    uint16_t keep[kMaxLights];
+};
+
+// The block's lights (all threads of the CTA call it; L: load_lights()
+// copies, nl <= kMaxLights); returns how many were kept, in S.keep.
+__device__ __forceinline__ int plain_block_lights(const rsrgpu_light* L, int nl, bool live, const float P[3],
+                                                  PlainBlockShared& S) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = live ? P[k] : INFINITY;
+        hi[k] = live ? P[k] : -INFINITY;
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+        if (lane == 0) { S.lo[warp][k] = lo[k]; S.hi[warp][k] = hi[k]; }
+    }
+    __syncthreads();
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = S.lo[0][k]; hi[k] = S.hi[0][k];
+        for (int w = 1; w < kPlainThreads / 32; ++w) { lo[k] = fminf(lo[k], S.lo[w][k]); hi[k] = fmaxf(hi[k], S.hi[w][k]); }
+    }
+    bool keep = false;
+    if (t < nl) {
+        const rsrgpu_light& l = L[t];
+        float e[3];
+        for (int k = 0; k < 3; ++k) e[k] = l.position[k] - fminf(fmaxf(l.position[k], lo[k]), hi[k]);
+        keep = dot3(e[0], e[1], e[2], e[0], e[1], e[2]) < l.reserved * 1.000244140625f;
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) S.count[warp] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < kPlainThreads / 32; ++w) {
+        if (w == warp) before = total;
+        total += S.count[w];
+    }
+    if (keep) S.keep[before + __popc(bal & ((1u << lane) - 1u))] = uint16_t(t);
+    __syncthreads();
+    return total;
+}
+
+// Blinn-Phong sum over the kept lights, in light order, plus ambient.
+__device__ __forceinline__ void plain_block_pixel(const rsrgpu_light* L, const uint16_t* keep, int nkeep, const float P[3],
+                                                  const float n[3], const float v[3], const float a[3], float rgb[3]) {
+    float s[3] = { 0.0f, 0.0f, 0.0f };
+    for (int k = 0; k < nkeep; ++k) {
+        float term[3];
+        if (!plain_term(L[keep[k]], P, n, v, a, term)) continue;
+        s[0] = s[0] + term[0];
+        s[1] = s[1] + term[1];
+        s[2] = s[2] + term[2];
+    }
+    rgb[0] = s[0] + 0.03f * a[0];
+    rgb[1] = s[1] + 0.03f * a[1];
+    rgb[2] = s[2] + 0.03f * a[2];
+}
+
 // ---- learned shader inputs ----
 // Candidate score of a light for a shading tile whose covered pixels span the
 // world-space box [b0, b1]: (1 - d/r)^2 * (r + g + b) at the box point nearest
