@@ -1106,7 +1106,7 @@ __global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constan
 __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
     bin_body(fv, blockIdx.x);
 }
-__global__ void __launch_bounds__(256) raster_kernel(const __grid_constant__ FrameView fv) {
+__global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
     raster_body(fv, blockIdx.x, S);
 }
@@ -1128,7 +1128,7 @@ __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_const
     const int f = batch_frame(b, blockIdx.x);
     bin_body(b.fv[f], blockIdx.x - b.start[f]);
 }
-__global__ void __launch_bounds__(256) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
+__global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ RasterSmem S;
     const int f = batch_frame(b, blockIdx.x);
     raster_body(b.fv[f], blockIdx.x - b.start[f], S);
