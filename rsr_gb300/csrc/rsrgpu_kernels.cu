@@ -366,66 +366,128 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
 // ---------------------------------------------------------------------------
 // binning
 // ---------------------------------------------------------------------------
+// Which of the super-chunks g0 * 32 .. (g0 + 32) * 32 - 1 overlap tile (tx, ty):
+// lane j returns the mask of group g0 + j (32 super-chunks).  Eight groups'
+// rectangles are in flight per lane at a time.
+__device__ __forceinline__ uint32_t super_masks(const FrameView& fv, int tx, int ty, int lane, int g0) {
+    const int ngroups = min((fv.nsupers + 31) / 32 - g0, 32);
+    uint32_t gm = 0u;
+    for (int gg = 0; gg < ngroups; gg += 8) {
+        bool hs[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int sidx = (g0 + gg + k) * 32 + lane;
+            hs[k] = false;
+            if (gg + k < ngroups && sidx < fv.nsupers) {
+                const int4 r = fv.super_rect[sidx];
+                hs[k] = r.x <= tx && tx <= -r.z && r.y <= ty && ty <= -r.w;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t m = __ballot_sync(FULL_MASK, hs[k]);
+            if (lane == gg + k) gm = m;
+        }
+    }
+    return gm;
+}
+
+// The tile's entries from super-chunk groups g0 .. g0 + 31 (gm: super_masks),
+// in triangle order: counted, or written from inl_out / clip_out on.
 template <bool WRITE>
-__device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, int lane,
+__device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, int lane, uint32_t gm, int g0,
                                          uint32_t& ninl, uint32_t& nclip,
                                          uint32_t* __restrict__ inl_out, uint32_t* __restrict__ clip_out) {
     const uint32_t lt = (1u << lane) - 1u;
-    for (int sb = 0; sb < fv.nsupers; sb += 32) {
-        const int sidx = sb + lane;
-        bool hs = false;
-        if (sidx < fv.nsupers) {
-            const int4 r = fv.super_rect[sidx];
-            hs = r.x <= tx && tx <= -r.z && r.y <= ty && ty <= -r.w;
-        }
-        uint32_t ms = __ballot_sync(FULL_MASK, hs);
+    const int ngroups = min((fv.nsupers + 31) / 32 - g0, 32);
+    for (int gi = 0; gi < ngroups; ++gi) {
+        const int sb = (g0 + gi) * 32;
+        uint32_t ms = __shfl_sync(FULL_MASK, gm, gi);
+        // likewise the chunk rectangles of up to kSuperAhead overlapping super-chunks
+        constexpr int kSuperAhead = 4;
+        int4 sahead[kSuperAhead];
+        int snahead = 0, staken = 0;
         while (ms) {
             const int s2 = sb + __ffs(ms) - 1;
-            ms &= ms - 1;
-            const int c = s2 * 32 + lane;
-            bool hc = false;
-            if (c < fv.nchunks) {
-                const int4 r = fv.chunk_rect[c];
-                hc = r.x <= tx && tx <= r.z && r.y <= ty && ty <= r.w;
-            }
-            uint32_t mc = __ballot_sync(FULL_MASK, hc);
-            while (mc) {
-                const int c2 = s2 * 32 + __ffs(mc) - 1;
-                mc &= mc - 1;
-                const int g = c2 * 32 + lane;
-                bool inl = false;
-                int cnt = 0;
-                uint64_t br = kEmptyRect;
-                if (g < fv.ntris) {
-                    br = fv.bin_rect[g];
-                    if (rect_has(br, tx, ty)) {
-                        if ((br >> 63) == 0) {
-                            inl = true;
-                        } else {
-                            const ClipInfo ci = fv.clip_info[g];
-                            for (int vi = 1; vi < ci.nverts - 1; ++vi)
-                                cnt += rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty) ? 1 : 0;
-                        }
+            if (staken == snahead) {
+                uint32_t mm = ms;
+                snahead = 0;
+#pragma unroll
+                for (int k = 0; k < kSuperAhead; ++k) {
+                    sahead[k] = make_int4(1, 1, 0, 0);   // empty: x > z
+                    if (mm) {
+                        const int ck = (sb + __ffs(mm) - 1) * 32 + lane;
+                        mm &= mm - 1;
+                        if (ck < fv.nchunks) sahead[k] = fv.chunk_rect[ck];
+                        ++snahead;
                     }
                 }
-                const uint32_t mi = __ballot_sync(FULL_MASK, inl);
-                if (WRITE && inl) inl_out[ninl + __popc(mi & lt)] = uint32_t(g);
-                ninl += __popc(mi);
-                // clipped fans: warp exclusive scan of per-lane counts
-                int incl = cnt;
+                staken = 0;
+            }
+            int4 r = sahead[0];
 #pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int v = __shfl_up_sync(FULL_MASK, incl, o);
-                    if (lane >= o) incl += v;
+            for (int k = 1; k < kSuperAhead; ++k) if (staken == k) r = sahead[k];
+            ++staken;
+            ms &= ms - 1;
+            const int c = s2 * 32 + lane;
+            const bool hc = c < fv.nchunks && r.x <= tx && tx <= r.z && r.y <= ty && ty <= r.w;
+            uint32_t mc = __ballot_sync(FULL_MASK, hc);
+            // the tile's overlapping chunks of this super-chunk, up to
+            // kBinStep at a time: their rectangles are loaded and tested
+            // together (independent chains), then appended in chunk order
+            constexpr int kBinStep = 4;
+            while (mc) {
+                int g[kBinStep];
+                uint64_t br[kBinStep];
+#pragma unroll
+                for (int k = 0; k < kBinStep; ++k) {
+                    g[k] = -1;
+                    br[k] = kEmptyRect;
+                    if (mc) {
+                        g[k] = (s2 * 32 + __ffs(mc) - 1) * 32 + lane;
+                        mc &= mc - 1;
+                        if (g[k] < fv.ntris) br[k] = fv.bin_rect[g[k]];
+                    }
                 }
-                const int total = __shfl_sync(FULL_MASK, incl, 31);
-                if (WRITE && cnt) {
-                    const ClipInfo ci = fv.clip_info[g];
-                    uint32_t pos = nclip + uint32_t(incl - cnt);
-                    for (int vi = 1; vi < ci.nverts - 1; ++vi)
-                        if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
+                bool inl[kBinStep], clp[kBinStep];
+                uint32_t mi[kBinStep];
+                bool anyclip = false;
+#pragma unroll
+                for (int k = 0; k < kBinStep; ++k) {
+                    const bool has = g[k] >= 0 && g[k] < fv.ntris && rect_has(br[k], tx, ty);
+                    inl[k] = has && (br[k] >> 63) == 0;
+                    clp[k] = has && (br[k] >> 63) != 0;
+                    mi[k] = __ballot_sync(FULL_MASK, inl[k]);
+                    anyclip |= clp[k];
                 }
-                nclip += uint32_t(total);
+                anyclip = __any_sync(FULL_MASK, anyclip);
+#pragma unroll
+                for (int k = 0; k < kBinStep; ++k) {
+                    if (WRITE && inl[k]) inl_out[ninl + __popc(mi[k] & lt)] = uint32_t(g[k]);
+                    ninl += __popc(mi[k]);
+                    if (!anyclip) continue;
+                    // clipped fans: warp exclusive scan of per-lane counts
+                    int cnt = 0;
+                    if (clp[k]) {
+                        const ClipInfo ci = fv.clip_info[g[k]];
+                        for (int vi = 1; vi < ci.nverts - 1; ++vi)
+                            cnt += rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty) ? 1 : 0;
+                    }
+                    int incl = cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(FULL_MASK, incl, o);
+                        if (lane >= o) incl += v;
+                    }
+                    const int total = __shfl_sync(FULL_MASK, incl, 31);
+                    if (WRITE && cnt) {
+                        const ClipInfo ci = fv.clip_info[g[k]];
+                        uint32_t pos = nclip + uint32_t(incl - cnt);
+                        for (int vi = 1; vi < ci.nverts - 1; ++vi)
+                            if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
+                    }
+                    nclip += uint32_t(total);
+                }
             }
         }
     }
@@ -440,8 +502,12 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int block) {
         return;
     }
     const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
+    const int ngroups = (fv.nsupers + 31) / 32;
     uint32_t ninl = 0, nclip = 0;
-    bin_walk<false>(fv, tx, ty, lane, ninl, nclip, nullptr, nullptr);
+    // up to 1024 super-chunks (1M triangles) the masks are found once for both passes
+    const uint32_t gm0 = super_masks(fv, tx, ty, lane, 0);
+    for (int g0 = 0; g0 < ngroups; g0 += 32)
+        bin_walk<false>(fv, tx, ty, lane, g0 == 0 ? gm0 : super_masks(fv, tx, ty, lane, g0), g0, ninl, nclip, nullptr, nullptr);
     uint32_t off = 0;
     if (lane == 0) {
         off = atomicAdd(&fv.counters->bin_used, ninl + nclip);
@@ -456,7 +522,9 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int block) {
     off = __shfl_sync(FULL_MASK, off, 0);
     if (off == 0xffffffffu) return;
     uint32_t w_inl = 0, w_clip = 0;
-    bin_walk<true>(fv, tx, ty, lane, w_inl, w_clip, fv.bin_pool + off, fv.bin_pool + off + ninl);
+    for (int g0 = 0; g0 < ngroups; g0 += 32)
+        bin_walk<true>(fv, tx, ty, lane, g0 == 0 ? gm0 : super_masks(fv, tx, ty, lane, g0), g0, w_inl, w_clip,
+                       fv.bin_pool + off, fv.bin_pool + off + ninl);
 }
 
 // ---------------------------------------------------------------------------
