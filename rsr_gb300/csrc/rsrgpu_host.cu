@@ -129,6 +129,7 @@ struct rsrgpu_ctx {
     uint32_t clip_cap = 1u << 18;
     uint32_t bin_cap = 1u << 22;
     int region_px = kRegionPx;      // raster CTA region (the autotuner may pick 16)
+    int vis_keys = 0;               // FrameView::vis_keys of the submitted frame
     FrameCounters* h_counters = nullptr;   // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     // textures from host buffers are copied on `side` while setup and binning run
@@ -680,6 +681,26 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
                 return fail(ctx, RSRGPU_EINVAL, "a frame with CMD_STORE_GBUFFER draws only with the G-buffer program");
     }
     if (nstates == 0) ctx->states.assign(1, DevState{});
+    // visibility by (depth, order) keys in the raster pass: every draw opaque
+    // with depth test and write on and one depth function (LESS or LEQUAL),
+    // clears before the first draw, stores after the last, at most 4096 draws
+    {
+        int func = -1;
+        bool ok = !ctx->draws.empty() && ctx->draws.size() <= 4096, drawn = false, stored = false;
+        for (const FrameOp& o : ctx->ops) {
+            if (o.kind == kOpClear && drawn) ok = false;
+            if (o.kind == kOpStoreTC || o.kind == kOpStoreDepth || o.kind == kOpStoreGBuffer) stored = true;
+            if (o.kind != kOpDraw) continue;
+            if (stored) ok = false;
+            drawn = true;
+            const DevState& st = ctx->states[size_t(ctx->draws[size_t(o.arg)].state)];
+            if (st.blend || !st.depth_test || !st.depth_write || !st.color_write || st.depth_func < 0 || st.depth_func > 1 ||
+                (func >= 0 && st.depth_func != func))
+                ok = false;
+            func = st.depth_func;
+        }
+        ctx->vis_keys = ok ? 1 + func : 0;
+    }
     ctx->submitted = true;
     return 0;
 }
@@ -752,6 +773,7 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.rcp_table = ctx->d_rcp.as<uint32_t>();
     fv.srgb_lut = ctx->d_srgb.as<uint8_t>();
     fv.region_px = std::min(ctx->region_px, std::min(ctx->tile_w, ctx->tile_h));
+    fv.vis_keys = ctx->vis_keys;
     return 0;
 }
 

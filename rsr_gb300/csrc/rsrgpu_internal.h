@@ -153,10 +153,10 @@ struct FrameView {
     const uint32_t* rcp_table;
     const uint8_t* srgb_lut;
     int32_t region_px;        // raster CTA region edge (8, 16 or 32 px; at most the tile)
+    int32_t vis_keys;         // 0, or 1 + the depth function (LESS / LEQUAL) of a frame whose draws
+                              // are all opaque with depth test and write on (see raster_body)
 };
 
-// One launch of a stage over many frames: block b belongs to frame f when
-// start[f] <= b < start[f + 1]; passed as a __grid_constant__ parameter.
 // Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,
 // mapped host memory into their device mirrors).
 constexpr int kMaxGather = 64;
@@ -167,6 +167,8 @@ struct GatherList {
     size_t bytes[kMaxGather];
 };
 
+// One launch of a stage over many frames: block b belongs to frame f when
+// start[f] <= b < start[f + 1]; passed as a __grid_constant__ parameter.
 struct BatchLaunch {
     int32_t nframes;
     int32_t start[kMaxBatch + 1];

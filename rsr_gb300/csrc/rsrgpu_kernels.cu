@@ -550,6 +550,8 @@ struct RasterSmem {
     float z[3][kRasterBatch], w[3][kRasterBatch];
     float vary[3][kMaxVary][kRasterBatch];
     uint32_t code[kRasterBatch];   // fragment owner: triangle id, or clipped fan id | bit 31
+    uint8_t big[kRasterBatch];     // visibility by keys: the triangle covers many quads of the region
+    int qsum;                      // visibility by keys: the batch's boxes, in quads of the region
 };
 
 // VTriangleRasterizer setup for one lane (rglv_triangle.hxx:209-240), int32 wrap
@@ -874,6 +876,134 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
     for (int l = 0; l < 4; ++l) own[l] = kNoOwner;
 }
 
+// ---- visibility by (depth, order) keys ----
+// In a frame whose draws are all opaque (no blending) with depth test and
+// depth write on and one depth function, LESS or LEQUAL, and whose clears
+// all come before its first draw and stores after its last, the fragment
+// that ends up owning a pixel is the one with the least depth, ties going to
+// the earliest (LESS) or latest (LEQUAL) in drawing order, among those that
+// pass against the cleared depth.  That is a minimum over 64-bit keys
+// (depth rank, order rank), so the fragments of a batch can be taken in any
+// order -- one triangle per lane -- with shared-memory atomicMin, and the
+// owners and depths are those of drawing them one after another.
+//   depth rank: an order-preserving map of the float bits (-0 ranks with +0,
+//     as the comparison treats them; NaN depths never pass and are skipped);
+//   order rank: draw index (12 bits), inline / clipped pass (1 bit),
+//     position in the tile's list (19 bits) -- the drawing order within a tile.
+constexpr uint32_t kKeyPosBits = 19;
+constexpr int kKeySmallQuads = 8;   // triangles covering at most this many quads of the region go one per lane,
+constexpr int kKeyTinyQuads = 2;    // or this many where the batch's boxes cover the region more than
+constexpr int kKeyCrowded = 6;      // kKeyCrowded times over
+
+__device__ __forceinline__ uint32_t depth_rank(float z) {
+    uint32_t b = __float_as_uint(z);
+    if ((b & 0x7fffffffu) == 0u) b = 0u;
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float rank_depth(uint32_t r) {   // inverse of depth_rank (+0 for the zero rank)
+    return __uint_as_float((r & 0x80000000u) ? (r & 0x7fffffffu) : ~r);
+}
+__device__ __forceinline__ unsigned long long frag_key(float z, uint32_t order, bool leq) {
+    return (static_cast<unsigned long long>(depth_rank(z)) << 32) | (leq ? 0xfffffffeu - order : order + 1u);
+}
+__device__ __forceinline__ unsigned long long clear_key(float z, bool leq) {
+    return (static_cast<unsigned long long>(depth_rank(z)) << 32) | (leq ? 0xffffffffu : 0u);
+}
+
+// Quads of the region [rx0, rx1) x [ry0, ry1) in batch triangle i's box.
+__device__ __forceinline__ int region_quads(const RasterSmem& S, int i, int rx0, int ry0, int rx1, int ry1) {
+    const int x0 = max(S.minx[i], rx0), x1 = min(S.maxx[i], rx1);
+    const int y0 = max(S.miny[i], ry0), y1 = min(S.maxy[i], ry1);
+    return x0 < x1 && y0 < y1 ? ((x1 - x0 + 1) >> 1) * ((y1 - y0 + 1) >> 1) : 0;
+}
+
+// Coverage and depth of the pixels of quad (qx, qy) for batch triangle i,
+// with the arithmetic of the lockstep loop in raster_body; false (and no
+// depths) when the triangle covers none of them.
+__device__ __forceinline__ bool batch_quad(const RasterSmem& S, int i, int qx, int qy, bool inside[4], float fz[4]) {
+    const int32_t kx = qx - S.minx[i], ky = qy - S.miny[i];
+    const int32_t dy12 = S.dy12[i], dx12 = S.dx12[i];
+    const int32_t dy23 = S.dy23[i], dx23 = S.dx23[i];
+    const int32_t dy31 = S.dy31[i], dx31 = S.dx31[i];
+    const int32_t e1 = wadd(wadd(S.c1[i], wmul(kx, dy12)), wmul(ky, dx12));
+    const int32_t e2 = wadd(wadd(S.c2[i], wmul(kx, dy23)), wmul(ky, dx23));
+    const int32_t e3 = wadd(wadd(S.c3[i], wmul(kx, dy31)), wmul(ky, dx31));
+    int32_t l1[4], l2[4], l3[4];
+    l1[0] = e1; l1[1] = wadd(e1, dy12); l1[2] = wadd(e1, dx12); l1[3] = wadd(wadd(e1, dx12), dy12);
+    l2[0] = e2; l2[1] = wadd(e2, dy23); l2[2] = wadd(e2, dx23); l2[3] = wadd(wadd(e2, dx23), dy23);
+    l3[0] = e3; l3[1] = wadd(e3, dy31); l3[2] = wadd(e3, dx31); l3[3] = wadd(wadd(e3, dx31), dy31);
+    bool any = false;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) { inside[l] = (l1[l] | l2[l] | l3[l]) >= 0; any |= inside[l]; }
+    if (!any) return false;
+    const float scale = S.scale[i];
+    const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        const float bx = itof(l2[l]) * scale;
+        const float bz = itof(l1[l]) * scale;
+        const float by = (1.0f - bx) - bz;
+        fz[l] = (bx * z0 + by * z1) + bz * z2;
+    }
+    return true;
+}
+
+// The keys of quad (qx, qy) for batch triangle i, by atomicMin: other lanes
+// may update the same pixels.
+__device__ __forceinline__ void key_quad(const RasterSmem& S, unsigned long long* keys, int rx0, int ry0, int rw,
+                                         int i, int qx, int qy, uint32_t order, bool leq) {
+    bool inside[4];
+    float fz[4];
+    if (!batch_quad(S, i, qx, qy, inside, fz)) return;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        if (!inside[l] || fz[l] != fz[l]) continue;
+        unsigned long long* k = keys + (qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1));
+        const unsigned long long key = frag_key(fz[l], order, leq);
+        if (key < *k) atomicMin(k, key);
+    }
+}
+
+// The same for the lane's own quad, whose keys it holds in registers.
+__device__ __forceinline__ void key_quad_own(const RasterSmem& S, unsigned long long kq[4], int i, int qx, int qy,
+                                             uint32_t order, bool leq) {
+    bool inside[4];
+    float fz[4];
+    if (!batch_quad(S, i, qx, qy, inside, fz)) return;
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        if (!inside[l] || fz[l] != fz[l]) continue;
+        const unsigned long long key = frag_key(fz[l], order, leq);
+        kq[l] = key < kq[l] ? key : kq[l];
+    }
+}
+
+// The depth the owner of pixel l of quad (qx, qy) gave it (for owners whose
+// depth rank is that of zero, whose sign the key does not keep).
+__device__ __noinline__ float owner_depth(const FrameView& fv, uint32_t code, const int rect[4], int qx, int qy, int l) {
+    TriSetup t;
+    float z[3];
+    if (code & kClippedBit) {
+        const uint32_t e = code & ~kClippedBit;
+        const int pbase = fv.clip_poly[e];
+        const ClipVert v0 = fv.clip_verts[pbase], v1 = fv.clip_verts[e], v2 = fv.clip_verts[e + 1];
+        setup_scalar(t, rect,
+                     __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
+                     __float2int_rz(v0.coord[1] * 16.0f), __float2int_rz(v1.coord[1] * 16.0f), __float2int_rz(v2.coord[1] * 16.0f));
+        z[0] = v0.coord[2]; z[1] = v1.coord[2]; z[2] = v2.coord[2];
+    } else {
+        const TriRecord& r = fv.tris[code];
+        setup_vector(t, rect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
+        z[0] = r.z[0]; z[1] = r.z[1]; z[2] = r.z[2];
+    }
+    int32_t e1, e2, e3;
+    lane_edges(t, qx, qy, l, e1, e2, e3);
+    const float bx = itof(e2) * t.scale;
+    const float bz = itof(e1) * t.scale;
+    const float by = (1.0f - bx) - bz;
+    return (bx * z[0] + by * z[1]) + bz * z[2];
+}
+
 __device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
     if (fv.counters->overflow != 0u) return;
 
@@ -912,6 +1042,12 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
     int cur_state = 0;
     FragState fs;
     load_frag_state(fv.states[0], fs);
+    // visibility by keys (see frag_key): decided at the first draw, resolved
+    // into own / dep before the first store
+    __shared__ unsigned long long keys[32 * 32];
+    const int rw = rx1 - rx0;
+    const bool leq = fv.vis_keys == 2;
+    int key_state = 0;   // 0 not decided, 1 keys in use, 2 not used, 3 resolved
 
     for (int op = 0; op < fv.nops; ++op) {
         const FrameOp o = fv.ops[op];
@@ -919,6 +1055,25 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             cur_state = o.arg;
             load_frag_state(fv.states[cur_state], fs);
             continue;
+        }
+        if (key_state == 1 && o.kind != kOpDraw && o.kind != kOpState) {
+            // owners and depths from the keys
+            __syncthreads();
+            if (active) {
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const unsigned long long k = keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))];
+                    const uint32_t low = uint32_t(k), rank = uint32_t(k >> 32);
+                    if (low == (leq ? 0xffffffffu : 0u)) continue;   // no fragment passed
+                    const uint32_t order = leq ? 0xfffffffeu - low : low - 1u;
+                    const uint32_t pos = order & ((1u << kKeyPosBits) - 1u);
+                    const uint32_t code = ((order >> kKeyPosBits) & 1u) ? (fv.bin_pool[bin.clip_off + pos] | kClippedBit)
+                                                                        : fv.bin_pool[bin.inl_off + pos];
+                    own[l] = code;
+                    dep[l] = rank == depth_rank(0.0f) ? owner_depth(fv, code, rect, qx, qy, l) : rank_depth(rank);
+                }
+            }
+            key_state = 3;
         }
         // Without blending the colour of a pixel is that of the last fragment
         // that passed the depth test, so draws without blending only track
@@ -944,6 +1099,18 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             const DevDraw dr = fv.draws[o.arg];
             const int end_tri = dr.first_tri + dr.ntris;
             if (visibility) pending = true;
+            if (key_state == 0) {
+                bool ok = fv.vis_keys != 0 && bin.inl_cnt < (1u << kKeyPosBits) && bin.clip_cnt < (1u << kKeyPosBits);
+                if (active) {
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) if (dep[l] != dep[l]) ok = false;   // a NaN clear depth: nothing passes
+                }
+                key_state = __syncthreads_and(ok) ? 1 : 2;
+                if (key_state == 1 && active) {
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))] = clear_key(dep[l], leq);
+                }
+            }
             // inline triangles of this draw, then its clipped fans (rglv_gpu_impl.hxx:506-508)
             for (int pass = 0; pass < 2; ++pass) {
                 const uint32_t base = pass == 0 ? bin.inl_off : bin.clip_off;
@@ -951,6 +1118,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                 uint32_t& cur = pass == 0 ? inl_cur : clip_cur;
                 while (true) {
                     __syncthreads();
+                    if (tid == 0) S.qsum = 0;
                     bool valid = false;
                     uint32_t e = 0;
                     if (cur + uint32_t(tid) < cnt) {
@@ -992,8 +1160,64 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             S.code[tid] = e | kClippedBit;
                         }
                         put_setup(S, tid, t);
+                        if (key_state == 1) atomicAdd(&S.qsum, region_quads(S, tid, rx0, ry0, rx1, ry1));
                     }
                     __syncthreads();
+                    if (key_state == 1) {
+                        const uint32_t order0 = (uint32_t(o.arg) << (kKeyPosBits + 1)) | (uint32_t(pass) << kKeyPosBits) | cur;
+                        // small triangles: one per lane, over its quads in the region.
+                        // Where the batch covers the region many times over, lanes
+                        // would contend for the same keys: then only the smallest go
+                        // one per lane.
+                        const int small_max = S.qsum > kKeyCrowded * qw * qh ? kKeyTinyQuads : kKeySmallQuads;
+                        bool big = false;
+                        if (tid < n) {
+                            const int x0 = max(S.minx[tid], rx0), x1 = min(S.maxx[tid], rx1);
+                            const int y0 = max(S.miny[tid], ry0), y1 = min(S.maxy[tid], ry1);
+                            const int nq = x0 < x1 && y0 < y1 ? ((x1 - x0 + 1) >> 1) * ((y1 - y0 + 1) >> 1) : 0;
+                            big = nq > small_max;
+                            if (!big) {
+                                for (int qyy = y0; qyy < y1; qyy += 2)
+                                    for (int qxx = x0; qxx < x1; qxx += 2)
+                                        key_quad(S, keys, rx0, ry0, rw, tid, qxx, qyy, order0 + uint32_t(tid), leq);
+                            }
+                        }
+                        // larger ones: every lane its own quad, a triangle at a time,
+                        // with the quad's keys in registers (after the small ones:
+                        // each pixel then has one writer)
+                        S.big[tid] = big ? 1 : 0;
+                        if (!__syncthreads_or(big)) {
+                            cur += uint32_t(n);
+                            if (n < int(blockDim.x)) break;
+                            continue;
+                        }
+                        unsigned long long kq[4];
+                        if (active) {
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) kq[l] = keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))];
+                        }
+                        for (int b0 = 0; b0 < n; b0 += 32) {
+                            bool hit = false;
+                            if (b0 + lane < n && S.big[b0 + lane]) {
+                                const int j = b0 + lane;
+                                hit = !(S.maxx[j] <= wx0 || S.minx[j] > wx1 || S.maxy[j] <= wy0 || S.miny[j] > wy1);
+                            }
+                            uint32_t m = __ballot_sync(FULL_MASK, hit);
+                            while (m) {
+                                const int i = b0 + __ffs(m) - 1;
+                                m &= m - 1;
+                                if (!active || qx < S.minx[i] || qx >= S.maxx[i] || qy < S.miny[i] || qy >= S.maxy[i]) continue;
+                                key_quad_own(S, kq, i, qx, qy, order0 + uint32_t(i), leq);
+                            }
+                        }
+                        if (active) {
+#pragma unroll
+                            for (int l = 0; l < 4; ++l) keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))] = kq[l];
+                        }
+                        cur += uint32_t(n);
+                        if (n < int(blockDim.x)) break;
+                        continue;
+                    }
                     // triangles of the batch in list order; a warp visits only
                     // those whose box meets its quads (ballot over 32 at a time)
                     for (int b0 = 0; b0 < n; b0 += 32) {
