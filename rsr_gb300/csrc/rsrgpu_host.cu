@@ -130,6 +130,14 @@ struct rsrgpu_ctx {
     uint32_t bin_cap = 1u << 22;
     int region_px = kRegionPx;      // raster CTA region (the autotuner may pick 16)
     int vis_keys = 0;               // FrameView::vis_keys of the submitted frame
+    DevBuf d_vis;                   // owners and depths between the two launches of a split raster pass
+    // the run's work captured once per submission and replayed by every run
+    // (one launch instead of a dozen API calls); dropped when anything it
+    // holds changes (submit, reset, host buffers, capacity growth)
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    bool tables_uploaded = false;   // states, draws, ops and G-buffer tables of this submission
+    cudaGraphExec_t gexec = nullptr;
     FrameCounters* h_counters = nullptr;   // pinned
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     // textures from host buffers are copied on `side` while setup and binning run
@@ -362,6 +370,13 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
 
 extern "C" {
 
+namespace {
+void drop_graph(rsrgpu_ctx* ctx) {
+    if (ctx->gexec) { cudaGraphExecDestroy(ctx->gexec); ctx->gexec = nullptr; }
+    if (ctx->graph) { cudaGraphDestroy(ctx->graph); ctx->graph = nullptr; }
+}
+}  // namespace
+
 int rsrgpu_create(int device, rsrgpu_ctx** out) {
     if (out == nullptr) return RSRGPU_EINVAL;
     *out = nullptr;
@@ -371,6 +386,7 @@ int rsrgpu_create(int device, rsrgpu_ctx** out) {
     if (e != cudaSuccess) { delete ctx; return RSRGPU_ECUDA; }
     if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
         cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_counters), sizeof(FrameCounters), cudaHostAllocDefault) != cudaSuccess ||
@@ -398,13 +414,15 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
     for (DevBuf* b : bufs) b->release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
+    drop_graph(ctx);
+    if (ctx->cap) cudaStreamDestroy(ctx->cap);
     cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_fork, ctx->ev_late };
     for (cudaEvent_t ev : evs) if (ev) cudaEventDestroy(ev);
     if (ctx->side) cudaStreamDestroy(ctx->side);
@@ -450,6 +468,7 @@ int rsrgpu_reset(rsrgpu_ctx* ctx, int width, int height, int tile_blocks_x, int 
 }
 
 int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t bytes) {
+    if (ctx != nullptr) drop_graph(ctx);
     if (ctx == nullptr || host_ptr == nullptr || bytes == 0) return RSRGPU_EINVAL;
     const uint8_t* p = static_cast<const uint8_t*>(host_ptr);
     auto it = ctx->host.find(p);
@@ -484,6 +503,7 @@ int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t by
 
 int rsrgpu_unregister_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr) {
     if (ctx == nullptr) return RSRGPU_EINVAL;
+    drop_graph(ctx);
     auto it = ctx->host.find(static_cast<const uint8_t*>(host_ptr));
     if (it == ctx->host.end()) return fail(ctx, RSRGPU_EINVAL, "buffer %p is not registered", host_ptr);
     cudaStreamSynchronize(ctx->own);
@@ -504,6 +524,8 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
     ctx->ntris = 0;
     bool gbuffer_frame = false, other_op_since_draw = false, any_draw = false;
     ctx->submitted = false;
+    ctx->tables_uploaded = false;
+    drop_graph(ctx);
     std::vector<bool> decoded(size_t(nstates), false);
     int ordinals = 0;
     int cur = -1;
@@ -774,18 +796,50 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.srgb_lut = ctx->d_srgb.as<uint8_t>();
     fv.region_px = std::min(ctx->region_px, std::min(ctx->tile_w, ctx->tile_h));
     fv.vis_keys = ctx->vis_keys;
+    fv.raster_phase = 0;
+    fv.vis_own = nullptr;
+    fv.vis_dep = nullptr;
     return 0;
 }
 
-int enqueue(rsrgpu_ctx* ctx, cudaStream_t st) {
+// whether a registered host buffer only the raster pass reads comes with the run
+bool late_inputs(const rsrgpu_ctx* ctx) {
+    for (const auto& kv : ctx->host)
+        if (kv.second.in && !kv.second.early) return true;
+    return false;
+}
+
+// allocations of a run, and the frame's tables, which change only with a
+// submission (before the run's own stream work, which may be captured)
+int prepare_run(rsrgpu_ctx* ctx, cudaStream_t st) {
     int rc = prepare_view(ctx);
     if (rc) return rc;
+    if (!ctx->tables_uploaded) {
+        CK(cudaMemcpyAsync(ctx->d_states.p, ctx->states.data(), sizeof(DevState) * ctx->states.size(), cudaMemcpyHostToDevice, st), "H2D states");
+        if (!ctx->draws.empty())
+            CK(cudaMemcpyAsync(ctx->d_draws.p, ctx->draws.data(), sizeof(DevDraw) * ctx->draws.size(), cudaMemcpyHostToDevice, st), "H2D draws");
+        if (!ctx->ops.empty())
+            CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
+        if (!ctx->gbufs.empty())
+            CK(cudaMemcpyAsync(ctx->d_gbufs.p, ctx->gbufs.data(), sizeof(GBufferDesc) * ctx->gbufs.size(), cudaMemcpyHostToDevice, st), "H2D gbuffers");
+        ctx->tables_uploaded = true;
+    }
+    if (ctx->fv.vis_keys != 0 && late_inputs(ctx))
+        CK(ctx->d_vis.ensure(size_t(ctx->fv.width) * size_t(ctx->fv.height) * 8u), "alloc visibility hand-over");
+    return 0;
+}
+
+// the stream work of a run; `captured`: into a graph, whose timing and
+// completion events must then be recorded as external event nodes
+int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
     const FrameView& fv = ctx->fv;
+    const unsigned evflags = captured ? cudaEventRecordExternal : cudaEventRecordDefault;
     // Inputs that live in registered host buffers travel with every run.  The
     // ones triangle setup reads come first: from pinned, mapped memory in one
     // gather kernel (many small arrays cost one launch rather than a copy
     // each), others by copies.  Textures, which only the raster pass reads,
-    // follow on the side stream while setup and binning run.
+    // follow on the side stream while setup, binning and the visibility half
+    // of a split raster pass run.
     GatherList gl{};
     bool any_late = false;
     for (auto& kv : ctx->host) {
@@ -810,38 +864,79 @@ int enqueue(rsrgpu_ctx* ctx, cudaStream_t st) {
                 CK(cudaMemcpyAsync(kv.second.dev, kv.second.host, kv.second.bytes, cudaMemcpyHostToDevice, ctx->side), "H2D texture");
         CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
     }
-    CK(cudaMemcpyAsync(ctx->d_states.p, ctx->states.data(), sizeof(DevState) * ctx->states.size(), cudaMemcpyHostToDevice, st), "H2D states");
-    if (!ctx->draws.empty())
-        CK(cudaMemcpyAsync(ctx->d_draws.p, ctx->draws.data(), sizeof(DevDraw) * ctx->draws.size(), cudaMemcpyHostToDevice, st), "H2D draws");
-    if (!ctx->ops.empty())
-        CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
-    if (!ctx->gbufs.empty())
-        CK(cudaMemcpyAsync(ctx->d_gbufs.p, ctx->gbufs.data(), sizeof(GBufferDesc) * ctx->gbufs.size(), cudaMemcpyHostToDevice, st), "H2D gbuffers");
     CK(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(FrameCounters), st), "memset counters");
     if (fv.nsupers > 0) CK(cudaMemsetAsync(ctx->d_super.p, 0x7f, sizeof(int4) * size_t(fv.nsupers), st), "memset super rects");
-    CK(cudaEventRecord(ctx->ev0, st), "event");
+    CK(cudaEventRecordWithFlags(ctx->ev0, st, evflags), "event");
     CK(launch_setup(fv, st), "setup_kernel");
     CK(launch_bin(fv, st), "bin_kernel");
-    if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
-    CK(cudaEventRecord(ctx->ev1, st), "event");
-    CK(launch_raster(fv, st), "raster_kernel");
-    CK(cudaEventRecord(ctx->ev2, st), "event");
+    // With textures still on their way, a frame whose visibility is resolved
+    // by keys rasterises first (the visibility launch needs no texture) and
+    // shades after the copy.
+    const bool split = any_late && fv.vis_keys != 0;
+    CK(cudaEventRecordWithFlags(ctx->ev1, st, evflags), "event");
+    if (split) {
+        FrameView f = fv;
+        f.vis_own = ctx->d_vis.as<uint32_t>();
+        f.vis_dep = reinterpret_cast<float*>(f.vis_own + size_t(fv.width) * size_t(fv.height));
+        f.raster_phase = 1;
+        CK(launch_raster(f, st), "raster_kernel");
+        CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
+        f.raster_phase = 2;
+        CK(launch_raster(f, st), "raster_kernel");
+    } else {
+        if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
+        CK(launch_raster(fv, st), "raster_kernel");
+    }
+    CK(cudaEventRecordWithFlags(ctx->ev2, st, evflags), "event");
     // outputs written in place need no copy back
     for (auto& kv : ctx->host)
         if (kv.second.out) CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
     CK(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, st), "D2H counters");
-    CK(cudaEventRecord(ctx->ev3, st), "event");
-    ctx->stats.gpu_launches = 3 + (gl.n > 0 ? 1 : 0);
+    CK(cudaEventRecordWithFlags(ctx->ev3, st, evflags), "event");
+    ctx->stats.gpu_launches = 3 + (gl.n > 0 ? 1 : 0) + (split ? 1 : 0);
     return 0;
 }
 
+}  // namespace
+
+namespace {
+// One run on ctx->run_stream.  Unless the stream is being captured by the
+// caller, or pageable host memory has to be copied, the work is captured
+// once into a CUDA graph and replayed.
+int run_frame(rsrgpu_ctx* ctx) {
+    cudaStream_t st = ctx->run_stream;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cs), "stream capture status");
+    bool graph = cs == cudaStreamCaptureStatusNone;
+    for (const auto& kv : ctx->host)
+        if ((kv.second.in || kv.second.out) && kv.second.mapped == nullptr) graph = false;
+    if (!graph) {
+        int rc = prepare_run(ctx, st);
+        return rc ? rc : record_run(ctx, st, false);
+    }
+    if (ctx->gexec == nullptr) {
+        int rc = prepare_run(ctx, st);
+        if (rc) return rc;
+        CK(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+        rc = record_run(ctx, ctx->cap, true);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->cap, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        CK(e, "end capture");
+        ctx->graph = g;
+        const cudaError_t ie = cudaGraphInstantiate(&ctx->gexec, g, 0);
+        if (ie != cudaSuccess) { drop_graph(ctx); return cuda_fail(ctx, ie, "graph instantiate"); }
+    }
+    CK(cudaGraphLaunch(ctx->gexec, st), "graph launch");
+    return 0;
+}
 }  // namespace
 
 int rsrgpu_run(rsrgpu_ctx* ctx, void* stream) {
     if (ctx == nullptr) return RSRGPU_EINVAL;
     if (!ctx->submitted) return fail(ctx, RSRGPU_EINVAL, "nothing submitted");
     ctx->run_stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
-    int rc = enqueue(ctx, ctx->run_stream);
+    int rc = run_frame(ctx);
     if (rc) return rc;
     ctx->ran = true;
     return 0;
@@ -870,7 +965,8 @@ int rsrgpu_wait(rsrgpu_ctx* ctx, int timeout_ms) {
         if (c.overflow & 2u) ctx->bin_cap = std::max<uint32_t>(ctx->bin_cap * 2, c.bin_used + c.bin_used / 4 + 4096);
         if (ctx->clip_cap > (1u << 28) || ctx->bin_cap > (1u << 30))
             return fail(ctx, RSRGPU_ECAPACITY, "frame needs %u clipped vertices and %u tile entries", c.clip_verts, c.bin_used);
-        int rc = enqueue(ctx, ctx->run_stream);
+        drop_graph(ctx);   // its scratch pointers and capacities change
+        int rc = run_frame(ctx);
         if (rc) return rc;
     }
     return fail(ctx, RSRGPU_ECAPACITY, "capacity growth did not converge");

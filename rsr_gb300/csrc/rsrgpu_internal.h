@@ -155,6 +155,10 @@ struct FrameView {
     int32_t region_px;        // raster CTA region edge (8, 16 or 32 px; at most the tile)
     int32_t vis_keys;         // 0, or 1 + the depth function (LESS / LEQUAL) of a frame whose draws
                               // are all opaque with depth test and write on (see raster_body)
+    int32_t raster_phase;     // 0 the whole raster pass; for vis_keys frames split in two launches:
+                              // 1 visibility (owners and depths into vis_own / vis_dep), 2 the rest
+    uint32_t* vis_own;        // [height * width] per pixel, phases 1 and 2
+    float* vis_dep;
 };
 
 // Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,

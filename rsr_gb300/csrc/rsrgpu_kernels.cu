@@ -1048,6 +1048,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
     const int rw = rx1 - rx0;
     const bool leq = fv.vis_keys == 2;
     int key_state = 0;   // 0 not decided, 1 keys in use, 2 not used, 3 resolved
+    bool phase_pending = true;   // second launch of a split pass: the hand-over is still to take
 
     for (int op = 0; op < fv.nops; ++op) {
         const FrameOp o = fv.ops[op];
@@ -1075,12 +1076,33 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             }
             key_state = 3;
         }
+        // A pass split in two launches (raster_phase): the first draws, stores
+        // depth and hands over the owners and depths at its end; the second
+        // replays states and clears, skips the draws and depth stores, takes
+        // the owners and depths at the first store and shades.
+        if (fv.raster_phase != 0 && (o.kind == kOpStoreTC || o.kind == kOpStoreDepth || o.kind == kOpStoreGBuffer)) {
+            if (fv.raster_phase == 1 && o.kind != kOpStoreDepth) continue;
+            if (fv.raster_phase == 2) {
+                if (phase_pending) {
+                    if (active) {
+#pragma unroll
+                        for (int l = 0; l < 4; ++l) {
+                            const size_t i = size_t(qy + (l >> 1)) * size_t(fv.width) + size_t(qx + (l & 1));
+                            own[l] = fv.vis_own[i];
+                            dep[l] = fv.vis_dep[i];
+                        }
+                    }
+                    phase_pending = false;
+                }
+                if (o.kind == kOpStoreDepth) continue;
+            }
+        }
         // Without blending the colour of a pixel is that of the last fragment
         // that passed the depth test, so draws without blending only track
         // that fragment's owner and shade it once; anything that reads or
         // replaces colour first resolves the pending pixels.
         const bool visibility = o.kind == kOpDraw && !fs.blend;
-        if (!visibility && o.kind != kOpStoreGBuffer && pending) {
+        if (!visibility && o.kind != kOpStoreGBuffer && pending && fv.raster_phase != 1) {
             if (active) resolve_quad(fv, rect, qx, qy, own, col);
             pending = false;
         }
@@ -1099,6 +1121,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             const DevDraw dr = fv.draws[o.arg];
             const int end_tri = dr.first_tri + dr.ntris;
             if (visibility) pending = true;
+            if (fv.raster_phase == 2) continue;   // drawn by the first launch
             if (key_state == 0) {
                 bool ok = fv.vis_keys != 0 && bin.inl_cnt < (1u << kKeyPosBits) && bin.clip_cnt < (1u << kKeyPosBits);
                 if (active) {
@@ -1385,6 +1408,14 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                 *reinterpret_cast<float2*>(dst + size_t(qy) * o.stride + qx) = make_float2(dep[0], dep[1]);
                 *reinterpret_cast<float2*>(dst + size_t(qy + 1) * o.stride + qx) = make_float2(dep[2], dep[3]);
             }
+        }
+    }
+    if (fv.raster_phase == 1 && active) {   // the hand-over to the second launch
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const size_t i = size_t(qy + (l >> 1)) * size_t(fv.width) + size_t(qx + (l & 1));
+            fv.vis_own[i] = own[l];
+            fv.vis_dep[i] = dep[l];
         }
     }
 }
