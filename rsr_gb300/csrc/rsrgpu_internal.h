@@ -25,7 +25,7 @@ constexpr int kSuper = 1024;      // triangles per super-chunk
 constexpr int kSetupBlock = 256;
 constexpr int kMaxClipVerts = 8;  // 3 + one per clipping plane (5 planes)
 constexpr int kRegionPx = 32;     // default raster region: a CTA covers at most 32x32 px of one tile
-constexpr int kBinBlock = 256;    // bin CTA: one warp per tile
+constexpr int kBinBlock = 256;    // bin CTA: one tile, eight warps
 constexpr int kMaxBatch = 64;     // frames per batched launch
 constexpr int kRasterBatch = 256; // triangles set up per shared-memory batch
 

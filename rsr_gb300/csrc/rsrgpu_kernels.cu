@@ -493,15 +493,9 @@ __device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, in
     }
 }
 
-__device__ __forceinline__ void bin_body(const FrameView& fv, int block) {
-    const int tile = (block * kBinBlock + int(threadIdx.x)) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (tile >= fv.ntiles) return;
-    if (fv.counters->overflow & 1u) {
-        if (lane == 0) fv.bins[tile] = TileBin{0, 0, 0, 0};
-        return;
-    }
-    const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
+// The tile's entries by one warp (lane order within a warp): count, take
+// pool space, write.  The fallback of bin_body for tiles beyond its limits.
+__device__ __forceinline__ void bin_tile_warp(const FrameView& fv, int tile, int tx, int ty, int lane) {
     const int ngroups = (fv.nsupers + 31) / 32;
     uint32_t ninl = 0, nclip = 0;
     // up to 1024 super-chunks (1M triangles) the masks are found once for both passes
@@ -525,6 +519,239 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int block) {
     for (int g0 = 0; g0 < ngroups; g0 += 32)
         bin_walk<true>(fv, tx, ty, lane, g0 == 0 ? gm0 : super_masks(fv, tx, ty, lane, g0), g0, w_inl, w_clip,
                        fv.bin_pool + off, fv.bin_pool + off + ninl);
+}
+
+// ---- binning: one CTA of kBinBlock threads per tile ----
+// The tile's overlapping chunks are listed in triangle order (super-chunk
+// masks, then chunk masks of the overlapping super-chunks, then a prefix),
+// the warps count the chunks' entries in parallel (chunk k: warp k % 8), a
+// prefix over the counts gives every chunk its place, and the warps write.
+// Chunks are taken in windows of up to kBinChunks (consecutive overlapping
+// super-chunks), counted in one pass and written in a second.  The lists
+// equal the one-warp walk's (order within a chunk: lane order; clipped fans:
+// lane order, then fan order).  Frames of more than 1024 super-chunks take
+// the one-warp walk.
+constexpr int kBinWarps = kBinBlock / 32;
+constexpr int kBinChunks = 1024;
+struct BinShared {
+    uint32_t gm[32];                 // overlap masks of super-chunk groups
+    uint32_t cm[1024];               // overlap masks of the chunks of the listed super-chunks
+    int32_t sup[1024];               // overlapping super-chunks, in order
+    int32_t pre[1024];               // exclusive prefix of their overlapping chunks
+    int32_t chunk[kBinChunks];       // the window's overlapping chunks, in order
+    uint32_t imask[kBinChunks];      // per chunk: lanes with an inline entry
+    int32_t ninl[kBinChunks];        // per chunk: inline entries, then their prefix
+    int32_t ncl[kBinChunks];         // per chunk: clipped fan entries, then their prefix
+    int32_t wsum[kBinWarps];
+    int nsup;
+    uint32_t base;
+};
+
+// Exclusive prefix of v[0 .. n) in place (n <= 4 * kBinBlock), total returned
+// (all threads of the CTA call it).
+__device__ __forceinline__ int bin_scan(int32_t* v, int n, BinShared& S) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    int x[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { const int i = 4 * t + k; x[k] = i < n ? v[i] : 0; sum += x[k]; }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL_MASK, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) S.wsum[warp] = incl;
+    __syncthreads();
+    int before = incl - sum, total = 0;
+    for (int w = 0; w < kBinWarps; ++w) {
+        if (w < warp) before += S.wsum[w];
+        total += S.wsum[w];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { const int i = 4 * t + k; if (i < n) v[i] = before; before += x[k]; }
+    __syncthreads();
+    return total;
+}
+
+// Entries of chunk c (32 triangles) for tile (tx, ty): the inline lanes, and
+// this lane's clipped fan entries.
+__device__ __forceinline__ void chunk_entries(const FrameView& fv, int c, int tx, int ty, int lane, bool& inl, int& fans) {
+    const int g = c * 32 + lane;
+    inl = false;
+    fans = 0;
+    if (g >= fv.ntris) return;
+    const uint64_t br = fv.bin_rect[g];
+    if (!rect_has(br, tx, ty)) return;
+    if ((br >> 63) == 0) { inl = true; return; }
+    const ClipInfo ci = fv.clip_info[g];
+    for (int vi = 1; vi < ci.nverts - 1; ++vi) fans += rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty) ? 1 : 0;
+}
+
+// The window of overlapping super-chunks from k0: up to kBinChunks chunks
+// (a super-chunk has at most 32, so a window holds at least one).
+__device__ __forceinline__ int bin_window_end(const BinShared& S, int k0, int nsup) {
+    int lo = k0 + 1, hi = nsup;   // the last k1 in [k0 + 1, nsup] with pre[k1] - pre[k0] <= kBinChunks
+    const int limit = S.pre[k0] + kBinChunks;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int pm = mid < nsup ? S.pre[mid] : S.pre[nsup - 1] + __popc(S.cm[nsup - 1]);
+        if (pm <= limit) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The window's chunks into S.chunk, counted into S.imask / S.ninl / S.ncl;
+// returns how many.
+__device__ __forceinline__ int bin_window_count(const FrameView& fv, BinShared& S, int k0, int k1, int tx, int ty) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int p0 = S.pre[k0];
+    for (int k = k0 + t; k < k1; k += kBinBlock) {
+        int at = S.pre[k] - p0;
+        for (uint32_t mm = S.cm[k]; mm; mm &= mm - 1) S.chunk[at++] = S.sup[k] * 32 + __ffs(mm) - 1;
+    }
+    __syncthreads();
+    const int nc = (k1 < S.nsup ? S.pre[k1] : S.pre[S.nsup - 1] + __popc(S.cm[S.nsup - 1])) - p0;
+    for (int k = warp; k < nc; k += kBinWarps) {
+        bool inl;
+        int fans;
+        chunk_entries(fv, S.chunk[k], tx, ty, lane, inl, fans);
+        const uint32_t mi = __ballot_sync(FULL_MASK, inl);
+        const int tf = __reduce_add_sync(FULL_MASK, fans);
+        if (lane == 0) { S.imask[k] = mi; S.ninl[k] = __popc(mi); S.ncl[k] = tf; }
+    }
+    __syncthreads();
+    return nc;
+}
+
+__device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShared& S) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (tile >= fv.ntiles) return;
+    if (fv.counters->overflow & 1u) {
+        if (t == 0) fv.bins[tile] = TileBin{0, 0, 0, 0};
+        return;
+    }
+    const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
+    const int ngroups = (fv.nsupers + 31) / 32;
+    if (ngroups > 32) {
+        if (warp == 0) bin_tile_warp(fv, tile, tx, ty, lane);
+        return;
+    }
+    // super-chunk group masks: group g by warp g % 8
+    for (int g = warp; g < ngroups; g += kBinWarps) {
+        const int sidx = g * 32 + lane;
+        bool hs = false;
+        if (sidx < fv.nsupers) {
+            const int4 r = fv.super_rect[sidx];
+            hs = r.x <= tx && tx <= -r.z && r.y <= ty && ty <= -r.w;
+        }
+        const uint32_t m = __ballot_sync(FULL_MASK, hs);
+        if (lane == 0) S.gm[g] = m;
+    }
+    __syncthreads();
+    // the overlapping super-chunks in order (warp 0: lane g lists group g)
+    if (warp == 0) {
+        const uint32_t m = lane < ngroups ? S.gm[lane] : 0u;
+        const int c = __popc(m);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL_MASK, incl, o);
+            if (lane >= o) incl += y;
+        }
+        int at = incl - c;
+        for (uint32_t mm = m; mm; mm &= mm - 1) S.sup[at++] = lane * 32 + __ffs(mm) - 1;
+        if (lane == 31) S.nsup = incl;
+    }
+    __syncthreads();
+    const int nsup = S.nsup;
+    // their chunk masks: super-chunk k by warp k % 8, and the prefix of their counts
+    for (int k = warp; k < nsup; k += kBinWarps) {
+        const int c = S.sup[k] * 32 + lane;
+        bool hc = false;
+        if (c < fv.nchunks) {
+            const int4 r = fv.chunk_rect[c];
+            hc = r.x <= tx && tx <= r.z && r.y <= ty && ty <= r.w;
+        }
+        const uint32_t m = __ballot_sync(FULL_MASK, hc);
+        if (lane == 0) { S.cm[k] = m; S.pre[k] = __popc(m); }
+    }
+    __syncthreads();
+    bin_scan(S.pre, nsup, S);
+    // count, window by window
+    int tinl = 0, tcl = 0;
+    for (int k0 = 0; k0 < nsup;) {
+        const int k1 = bin_window_end(S, k0, nsup);
+        const int nc = bin_window_count(fv, S, k0, k1, tx, ty);
+        tinl += bin_scan(S.ninl, nc, S);
+        tcl += bin_scan(S.ncl, nc, S);
+        k0 = k1;
+    }
+    if (t == 0) {
+        uint32_t off = 0;
+        if (tinl + tcl > 0) off = atomicAdd(&fv.counters->bin_used, uint32_t(tinl + tcl));
+        if (off + uint32_t(tinl + tcl) > fv.bin_cap) {
+            atomicOr(&fv.counters->overflow, 2u);
+            fv.bins[tile] = TileBin{0, 0, 0, 0};
+            off = 0xffffffffu;
+        } else {
+            fv.bins[tile] = TileBin{off, uint32_t(tinl), off + uint32_t(tinl), uint32_t(tcl)};
+        }
+        S.base = off;
+    }
+    __syncthreads();
+    const uint32_t base = S.base;
+    if (base == 0xffffffffu) return;
+    uint32_t* inl_out = fv.bin_pool + base;
+    uint32_t* clip_out = fv.bin_pool + base + tinl;
+    const uint32_t lt = (1u << lane) - 1u;
+    // write, window by window (the first window's counts are recounted
+    // unless it was the only one)
+    int winl = 0, wcl = 0;
+    for (int k0 = 0; k0 < nsup;) {
+        const int k1 = bin_window_end(S, k0, nsup);
+        int nc;
+        if (k0 == 0 && k1 == nsup) {
+            nc = S.pre[nsup - 1] + __popc(S.cm[nsup - 1]);   // still in place from the count
+        } else {
+            nc = bin_window_count(fv, S, k0, k1, tx, ty);
+            bin_scan(S.ninl, nc, S);
+            bin_scan(S.ncl, nc, S);
+        }
+        for (int k = warp; k < nc; k += kBinWarps) {
+            const int c = S.chunk[k];
+            const uint32_t mi = S.imask[k];
+            if (mi & (1u << lane)) inl_out[winl + S.ninl[k] + __popc(mi & lt)] = uint32_t(c * 32 + lane);
+            bool inl;
+            int fans;
+            const bool has_fans = k + 1 < nc ? S.ncl[k + 1] != S.ncl[k] : true;
+            if (!has_fans) continue;
+            chunk_entries(fv, c, tx, ty, lane, inl, fans);
+            if (!__any_sync(FULL_MASK, fans != 0)) continue;
+            int incl = fans;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (fans) {
+                const ClipInfo ci = fv.clip_info[c * 32 + lane];
+                uint32_t pos = uint32_t(wcl + S.ncl[k] + incl - fans);
+                for (int vi = 1; vi < ci.nverts - 1; ++vi)
+                    if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
+            }
+        }
+        // the window's totals (from the last chunk's prefix and count)
+        if (nc > 0) {
+            winl += S.ninl[nc - 1] + __popc(S.imask[nc - 1]);
+            // clip total: recount the last chunk's fans (cheap; rarely any)
+            bool inl;
+            int fans;
+            chunk_entries(fv, S.chunk[nc - 1], tx, ty, lane, inl, fans);
+            wcl += S.ncl[nc - 1] + __reduce_add_sync(FULL_MASK, fans);
+        }
+        __syncthreads();
+        k0 = k1;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1427,7 +1654,8 @@ __global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constan
     setup_body(fv, blockIdx.x);
 }
 __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
-    bin_body(fv, blockIdx.x);
+    __shared__ BinShared S;
+    bin_body(fv, blockIdx.x, S);
 }
 __global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
@@ -1448,8 +1676,9 @@ __global__ void __launch_bounds__(kSetupBlock) setup_batch_kernel(const __grid_c
     setup_body(b.fv[f], blockIdx.x - b.start[f]);
 }
 __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ BinShared S;
     const int f = batch_frame(b, blockIdx.x);
-    bin_body(b.fv[f], blockIdx.x - b.start[f]);
+    bin_body(b.fv[f], blockIdx.x - b.start[f], S);
 }
 __global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ RasterSmem S;
@@ -1468,7 +1697,7 @@ cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
 }
 
 int setup_blocks(const FrameView& fv) { return (fv.ntris + kSetupBlock - 1) / kSetupBlock; }
-int bin_blocks(const FrameView& fv) { return (fv.ntiles + kBinBlock / 32 - 1) / (kBinBlock / 32); }
+int bin_blocks(const FrameView& fv) { return fv.ntiles; }
 // One CTA row per range: 16-byte loads and stores where both ends are aligned, bytes otherwise.
 __global__ void __launch_bounds__(256) gather_kernel(const __grid_constant__ GatherList g) {
     const int r = blockIdx.y;
