@@ -183,14 +183,23 @@ __device__ __forceinline__ uint64_t fan_rect(const FrameView& fv, const int sc[4
     return pack_rect(vminx / fv.tile_w, vminy / fv.tile_h, vmaxx / fv.tile_w, vmaxy / fv.tile_h);
 }
 
-__device__ __noinline__ void clip_triangle(const FrameView& fv, const DevState& s, int g,
-                                           const float pos[3][4], const float vary[3][kMaxVary],
-                                           uint64_t& rect_union) {
+// The three transformed vertices of a triangle, passed by value to the
+// clipper: the setup keeps them in registers (a pointer would put them in
+// local memory for every triangle, clipped or not).
+struct TriVerts {
+    float pos[3][4];
+    float vary[3][kMaxVary];
+};
+
+// Returns the tile rectangle of the triangle's fans (bit 63 set), or rect_union
+// when no fan survives.
+__device__ __noinline__ uint64_t clip_triangle(const FrameView& fv, const DevState& s, int g, const TriVerts tv,
+                                               uint64_t rect_union) {
     CV A[kMaxClipVerts + 1], B[kMaxClipVerts + 1];
     int na = 3;
     for (int i = 0; i < 3; ++i) {
-        for (int k = 0; k < 4; ++k) A[i].c[k] = pos[i][k];
-        for (int k = 0; k < kMaxVary; ++k) A[i].d[k] = vary[i][k];
+        for (int k = 0; k < 4; ++k) A[i].c[k] = tv.pos[i][k];
+        for (int k = 0; k < kMaxVary; ++k) A[i].d[k] = tv.vary[i][k];
     }
     const int nv = s.nvary;
     for (int plane = 0; plane < 5 && na > 0; ++plane) {   // clipping_panes order L,B,N,R,T
@@ -264,6 +273,7 @@ __device__ __noinline__ void clip_triangle(const FrameView& fv, const DevState& 
         }
     }
     fv.clip_info[g] = info;
+    return rect_union;
 }
 
 // ---------------------------------------------------------------------------
@@ -280,17 +290,17 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
         int idx[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) idx[k] = dr.is_arrays ? 3 * t + k : int(__ldg(dr.indices + 3 * t + k));
-        float pos[3][4], vary[3][kMaxVary];
+        TriVerts tv;
         float dx[3], dy[3], zz[3], ww[3];
         uint32_t cf[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            shade_vertex(s, idx[k], pos[k], vary[k], fv.counters);
-            cf[k] = frustum_test(s.guard, pos[k]);
-            const float iw = oneover(fv.rcp_table, pos[k][3]);
-            dx[k] = (pos[k][0] * iw) * s.DS[0] + s.DO[0];
-            dy[k] = (pos[k][1] * iw) * s.DS[1] + s.DO[1];
-            zz[k] = pos[k][2] * iw;
+            shade_vertex(s, idx[k], tv.pos[k], tv.vary[k], fv.counters);
+            cf[k] = frustum_test(s.guard, tv.pos[k]);
+            const float iw = oneover(fv.rcp_table, tv.pos[k][3]);
+            dx[k] = (tv.pos[k][0] * iw) * s.DS[0] + s.DO[0];
+            dy[k] = (tv.pos[k][1] * iw) * s.DS[1] + s.DO[1];
+            zz[k] = tv.pos[k][2] * iw;
             ww[k] = iw;
         }
         // BinTriangles1P (rglv_gpu_impl.hxx:605-661)
@@ -311,30 +321,33 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
         notCulled = notCulled && !pointsOutside;
         const bool accept = notCulled && vmaxx > vminx && vmaxy > vminy;
         if (accept) {
-            const int o0 = front ? 0 : 2, o2 = front ? 2 : 0;
-            const int ord[3] = { o0, 1, o2 };
-            TriRecord r;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int v = ord[k];
-                r.fx[k] = ftoi(16.0f * dx[v]);
-                r.fy[k] = ftoi(16.0f * dy[v]);
-                r.z[k] = zz[v];
-                r.w[k] = ww[v];
-#pragma unroll
-                for (int q = 0; q < kMaxVary; ++q) r.vary[k][q] = vary[v][q];
-            }
-            const float4* src = reinterpret_cast<const float4*>(&r);
+            // vertices in record order: back faces swap the first and last
+            // (by selects: a variable index would put the arrays in local memory)
+            auto sel = [front](float a0, float a2) { return front ? a0 : a2; };
+            const float x0 = sel(dx[0], dx[2]), x2 = sel(dx[2], dx[0]);
+            const float y0 = sel(dy[0], dy[2]), y2 = sel(dy[2], dy[0]);
+            float4 q[6];   // TriRecord: fx[3], fy[3], z[3], w[3], vary[3][4]
+            q[0] = make_float4(__int_as_float(ftoi(16.0f * x0)), __int_as_float(ftoi(16.0f * dx[1])),
+                               __int_as_float(ftoi(16.0f * x2)), __int_as_float(ftoi(16.0f * y0)));
+            q[1] = make_float4(__int_as_float(ftoi(16.0f * dy[1])), __int_as_float(ftoi(16.0f * y2)),
+                               sel(zz[0], zz[2]), zz[1]);
+            q[2] = make_float4(sel(zz[2], zz[0]), sel(ww[0], ww[2]), ww[1], sel(ww[2], ww[0]));
+            q[3] = make_float4(sel(tv.vary[0][0], tv.vary[2][0]), sel(tv.vary[0][1], tv.vary[2][1]),
+                               sel(tv.vary[0][2], tv.vary[2][2]), sel(tv.vary[0][3], tv.vary[2][3]));
+            q[4] = make_float4(tv.vary[1][0], tv.vary[1][1], tv.vary[1][2], tv.vary[1][3]);
+            q[5] = make_float4(sel(tv.vary[2][0], tv.vary[0][0]), sel(tv.vary[2][1], tv.vary[0][1]),
+                               sel(tv.vary[2][2], tv.vary[0][2]), sel(tv.vary[2][3], tv.vary[0][3]));
             float4* dst = reinterpret_cast<float4*>(fv.tris + g);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) dst[q] = src[q];
-            const uint32_t ni0 = uint32_t(uint16_t(idx[o0])) | (front ? 0u : 0x8000u);
+            for (int k = 0; k < 6; ++k) dst[k] = q[k];
+            const int i0 = front ? idx[0] : idx[2], i2 = front ? idx[2] : idx[0];
+            const uint32_t ni0 = uint32_t(uint16_t(i0)) | (front ? 0u : 0x8000u);
             fv.rec16[2 * g] = (ni0 & 0xffffu) | (uint32_t(uint16_t(idx[1])) << 16);
-            fv.rec16[2 * g + 1] = uint32_t(uint16_t(idx[o2]));
+            fv.rec16[2 * g + 1] = uint32_t(uint16_t(i2));
             rect = pack_rect(vminx / fv.tile_w, vminy / fv.tile_h, vmaxx / fv.tile_w, vmaxy / fv.tile_h);
         }
         if (needClip) {
-            clip_triangle(fv, s, g, pos, vary, rect);
+            rect = clip_triangle(fv, s, g, tv, rect);
         } else {
             fv.clip_info[g] = ClipInfo{0, 0, 0, 0};
         }
