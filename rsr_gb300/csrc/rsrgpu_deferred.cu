@@ -64,7 +64,7 @@ cudaError_t launch_shade_plain(const rsrgpu_gbuffer& gb, const float ivp[16], co
 // Pass 1: the world-space box of the tile's covered pixels; warp 0 picks the
 // tile's candidate lights; pass 2: features (BF16, 32 columns,
 // 24..31 zero) and the network's targets sqrt(max(plain, 0)) - base per pixel
-// (base: virtual_light_base of the FP32 features).  Uncovered pixels
+// (base: the analytic virtual-light estimate, see rsrgpu_shading.cuh).  Uncovered pixels
 // (albedo 0) get zero rows.
 struct FeatParams {
     PlainParams pl;

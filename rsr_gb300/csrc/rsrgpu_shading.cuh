@@ -270,55 +270,23 @@ __device__ __forceinline__ void select_candidates(int nl, Score score, int* cand
     __syncwarp();
 }
 
+// ---- the learned shader's inputs ----
 // The 24 input features of one covered pixel:
 //   0-2 unit normal, 3-5 unit view vector, 6-8 albedo, 9 eye distance / 50,
-//   and a summary of the candidate lights that reach the pixel, each with
-//   colour c * att (att = (1 - d/r)^2), weight w = c.r + c.g + c.b (of c * att)
-//   and unit direction L:
+//   and a summary of the tile's candidate lights that reach the pixel, each
+//   with colour c * att (att = (1 - d/r)^2), weight w = c.r + c.g + c.b (of
+//   c * att) and unit direction L:
 //   10-12 sum c*att, 13-15 sum w L, 16-21 sum w L L^T (xx xy xz yy yz zz),
-//   22 sum w max(N.L, 0), 23 sum w (d/r) / sum w (0 without lights)
-__device__ __forceinline__ void pixel_features(const PlainParams& p, const rsrgpu_light* L, const int* cand,
-                                               const float P[3], uint16_t hx, uint16_t hy, uint16_t hz,
-                                               uint32_t alb, float f[kFeatures]) {
-    float n[3], v[3], vlen, a[3];
-    surface(p, P, hx, hy, hz, n, v, vlen);
-    albedo_rgb(alb, a);
-    for (int k = 0; k < 3; ++k) { f[k] = n[k]; f[3 + k] = v[k]; f[6 + k] = a[k]; }
-    f[9] = vlen / 50.0f;
-    for (int k = 10; k < kFeatures; ++k) f[k] = 0.0f;
-    float wsum = 0.0f;
-    for (int c = 0; c < kCandidates; ++c) {
-        const int li = cand[c];
-        if (li < 0) break;
-        const rsrgpu_light& l = L[li];
-        float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
-        const float d = sqrtf(dot3(lx, ly, lz, lx, ly, lz));
-        if (!(d < l.radius)) continue;
-        const float q = d / l.radius;
-        const float t = 1.0f - q;
-        const float att = t * t;
-        const float cr = l.color[0] * att, cg = l.color[1] * att, cb = l.color[2] * att;
-        const float w = (cr + cg) + cb;
-        lx = lx / d; ly = ly / d; lz = lz / d;
-        const float wx = w * lx, wy = w * ly, wz = w * lz;
-        f[10] = f[10] + cr; f[11] = f[11] + cg; f[12] = f[12] + cb;
-        f[13] = f[13] + wx; f[14] = f[14] + wy; f[15] = f[15] + wz;
-        f[16] = f[16] + wx * lx; f[17] = f[17] + wx * ly; f[18] = f[18] + wx * lz;
-        f[19] = f[19] + wy * ly; f[20] = f[20] + wy * lz; f[21] = f[21] + wz * lz;
-        f[22] = f[22] + w * pos0(dot3(n[0], n[1], n[2], lx, ly, lz));
-        f[23] = f[23] + w * q;
-        wsum = wsum + w;
-    }
-    f[23] = wsum > 0.0f ? f[23] / wsum : 0.0f;
-}
-
-// ---- the learned shader's inputs, in fast arithmetic ----
-// The same definitions as pixel_features / virtual_light_base, evaluated
-// with the SFU's approximate reciprocal and reciprocal square root (about
-// one ulp each) and reciprocals multiplied in; the learned shader's kernels
-// (training data and inference) use these, so training and inference see
-// the same inputs.  Results agree with the exact definitions (the oracle's)
-// to a few ulps.
+//   22 sum w max(N.L, 0), 23 sum w (d/r) / sum w (0 without lights).
+// The analytic base: one virtual light with direction sum w L (normalised)
+// and colour sum c * att, Blinn-Phong (exponent 32) plus ambient 0.03 *
+// albedo; base = its square root per channel.  The network adds its output
+// to base, so it learns the residual sqrt(plain) - base.
+// The oracle restates these exactly (oracle/rsr_oracle.c).  The kernels
+// evaluate them with the SFU's approximate reciprocal and reciprocal square
+// root (about one ulp each) and reciprocals multiplied in; the training data
+// and the inference kernels use the same functions, so both see the same
+// inputs, within a few ulps of the exact definitions.
 __device__ __forceinline__ float frcp(float x) { return __fdividef(1.0f, x); }
 
 __device__ __forceinline__ void world_pos_fast(const PlainParams& p, int x, int y, float z, float P[3]) {
@@ -331,22 +299,6 @@ __device__ __forceinline__ void world_pos_fast(const PlainParams& p, int x, int 
     const float cw = ((m[3] * ndcx + m[7] * ndcy) + m[11] * z) + m[15];
     const float iw = frcp(cw);
     P[0] = cx * iw; P[1] = cy * iw; P[2] = cz * iw;
-}
-
-// the number of candidate lights whose radius reaches P (as pixel_features_fast tests them)
-__device__ __forceinline__ int reaching_lights(const rsrgpu_light* L, const int* cand, const float P[3]) {
-    int k = 0;
-    for (int c = 0; c < kCandidates; ++c) {
-        const int li = cand[c];
-        if (li < 0) break;
-        const rsrgpu_light& l = L[li];
-        const float lx = l.position[0] - P[0], ly = l.position[1] - P[1], lz = l.position[2] - P[2];
-        const float d2 = dot3(lx, ly, lz, lx, ly, lz);
-        if (d2 >= l.reserved) continue;
-        const float d = d2 * rsqrtf(d2);
-        k += (d < l.radius) ? 1 : 0;
-    }
-    return k;
 }
 
 // plain_sum with the SFU's approximate reciprocal square root and reciprocal
@@ -460,24 +412,6 @@ __device__ __forceinline__ int pixel_features_fast(const PlainParams& p, const r
         base[c] = x > 0.0f ? x * rsqrtf(x) : 0.0f;
     }
     return reach;
-}
-
-// The learned shader's analytic base, computed from the FP32 features: one
-// virtual light with direction sum w L (normalised) and colour sum c * att,
-// Blinn-Phong (exponent 32) plus ambient 0.03 * albedo; base = its square
-// root per channel.  The network adds its output to base, so it learns the
-// residual sqrt(plain) - base.
-__device__ __forceinline__ void virtual_light_base(const float f[kFeatures], float base[3]) {
-    const float dlen = sqrtf(dot3(f[13], f[14], f[15], f[13], f[14], f[15]));
-    float l[3] = { 0.0f, 0.0f, 0.0f };
-    if (dlen > 0.0f) { l[0] = f[13] / dlen; l[1] = f[14] / dlen; l[2] = f[15] / dlen; }
-    float h[3] = { l[0] + f[3], l[1] + f[4], l[2] + f[5] };
-    const float hlen = sqrtf(dot3(h[0], h[1], h[2], h[0], h[1], h[2]));
-    if (hlen > 0.0f) { h[0] = h[0] / hlen; h[1] = h[1] / hlen; h[2] = h[2] / hlen; }
-    const float ndl = pos0(dot3(f[0], f[1], f[2], l[0], l[1], l[2]));
-    float sp = pos0(dot3(f[0], f[1], f[2], h[0], h[1], h[2]));
-    sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp; sp = sp * sp;   // ^32
-    for (int c = 0; c < 3; ++c) base[c] = sqrtf(pos0(f[10 + c] * (f[6 + c] * ndl + sp) + 0.03f * f[6 + c]));
 }
 
 }  // namespace rsrgpu
