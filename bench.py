@@ -114,15 +114,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def dist_setup():
+def dist_setup(backend="nccl"):
+    """One rank per GPU from the torchrun environment (RANK, LOCAL_RANK,
+    WORLD_SIZE, MASTER_*).  Frames are independent, so ranks only meet for the
+    barriers around the timed region and the max of their times; `backend`
+    "gloo" runs the same on CPU (tests)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        import torch
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl", init_method="env://")
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend, init_method="env://")
     return world, rank, local
 
 
@@ -137,7 +142,8 @@ def max_over_ranks(world, x):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
