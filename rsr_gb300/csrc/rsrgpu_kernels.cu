@@ -1131,7 +1131,7 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
 //   order rank: draw index (12 bits), inline / clipped pass (1 bit),
 //     position in the tile's list (19 bits) -- the drawing order within a tile.
 constexpr uint32_t kKeyPosBits = 19;
-constexpr int kKeySmallQuads = 8;   // triangles covering at most this many quads of the region go one per lane,
+constexpr int kKeySmallQuads = 16;  // triangles covering at most this many quads of the region go one per lane,
 constexpr int kKeyTinyQuads = 2;    // or this many where the batch's boxes cover the region more than
 constexpr int kKeyCrowded = 6;      // kKeyCrowded times over
 
