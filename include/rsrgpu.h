@@ -26,9 +26,12 @@
  * ------
  * Pointers in the stream and in the state snapshots may be device pointers
  * (used in place) or host pointers previously declared with
- * rsrgpu_register_host_buffer(); host inputs are copied to the device and
- * host outputs copied back inside every rsrgpu_run(), so the caller's buffers
- * keep the reference's meaning of "read when the frame runs".
+ * rsrgpu_register_host_buffer().  Host inputs reach the device and host
+ * outputs come back inside every rsrgpu_run(), so the caller's buffers keep
+ * the reference's meaning of "read when the frame runs".  Pageable memory
+ * goes through device mirrors and copies.  Pinned, mapped memory
+ * (cudaHostAlloc) is read by a gather kernel, textures are copied while
+ * setup and binning run, and outputs are written in place by the kernels.
  *
  * Errors
  * ------
@@ -228,7 +231,12 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes,
                   const rsrgpu_glstate* states, int nstates);
 
 /* GPU::Run() -- rglv_gpu.hxx:167, rglv_gpu.cxx:90-116.  Enqueues the frame on
- * `stream` (a cudaStream_t; NULL = the context's own stream). */
+ * `stream` (a cudaStream_t; NULL = the context's own stream).  The first run
+ * after a submission captures the run's work into a CUDA graph; later runs
+ * replay it (inputs are still read when each run executes).  The graph is
+ * dropped by rsrgpu_submit(), rsrgpu_reset(), host-buffer (un)registration
+ * and capacity growth.  A run on a stream the caller is capturing, or one
+ * that copies pageable host memory, is enqueued directly. */
 int rsrgpu_run(rsrgpu_ctx* ctx, void* stream);
 
 /* Wait for the last run; timeout_ms < 0 waits without limit. */
