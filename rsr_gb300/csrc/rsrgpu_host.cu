@@ -1665,11 +1665,33 @@ int rsrgpu_batch_frame(rsrgpu_batch* b, int i, rsrgpu_ctx** ctx) {
     return 0;
 }
 
+namespace {
+// median device time of the batch over `reps` runs after one warm-up run
+int time_batch(rsrgpu_batch* b, const rsrgpu_frame_desc* frames, int nframes, int reps, float* ms) {
+    int rc = rsrgpu_batch_submit(b, frames, nframes);
+    if (rc) return rc;
+    std::vector<float> t;
+    for (int r = 0; r <= reps; ++r) {
+        rc = rsrgpu_batch_run(b, nullptr);
+        if (rc == 0) rc = rsrgpu_batch_wait(b, -1);
+        if (rc) return rc;
+        float x = 0.f;
+        rc = rsrgpu_batch_last_ms(b, &x);
+        if (rc) return rc;
+        if (r > 0) t.push_back(x);
+    }
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return 0;
+}
+}  // namespace
+
 int rsrgpu_batch_tune(rsrgpu_batch* b, rsrgpu_frame_desc* frames, int nframes, int reps) {
     if (b == nullptr || frames == nullptr || nframes < 0) return RSRGPU_EINVAL;
     if (reps < 1) reps = 1;
     BCK(cudaSetDevice(b->device), "set device");
     static const int kCandidates[][2] = { { 8, 8 }, { 16, 16 }, { 16, 8 }, { 32, 32 }, { 32, 16 }, { 64, 32 } };
+    static const int kTuneDefault[2] = { 32, 32 };
     rsrgpu_ctx* c = nullptr;
     int rc = frame_ctx(b, 0, &c);   // scratch context: frame slot 0 is re-decoded by the next submit
     if (rc) return rc;
@@ -1694,8 +1716,8 @@ int rsrgpu_batch_tune(rsrgpu_batch* b, rsrgpu_frame_desc* frames, int nframes, i
             frames[i].bin_capacity = used + used / 4 + 1024;
             continue;
         }
-        float best = 1e30f;
-        rsrgpu_frame_desc choice = d;
+        float best = 1e30f, base = 1e30f;
+        rsrgpu_frame_desc choice = d, base_choice = d;
         for (const auto& cand : kCandidates) {
             d.tile_px = cand[0]; d.region_px = cand[1];
             rc = decode_into(b, c, d);
@@ -1721,12 +1743,49 @@ int rsrgpu_batch_tune(rsrgpu_batch* b, rsrgpu_frame_desc* frames, int nframes, i
                 choice = d;
                 choice.bin_capacity = used + used / 4 + 1024;
             }
+            if (cand[0] == kTuneDefault[0] && cand[1] == kTuneDefault[1]) {
+                base = med;
+                base_choice = d;
+                base_choice.bin_capacity = used + used / 4 + 1024;
+            }
         }
         if (best >= 1e30f) return bfail(b, RSRGPU_ECAPACITY, "frame %d: no candidate tiling holds its tile lists", i);
+        (void)base;
+        (void)base_choice;
         b->tuned[key] = choice;
         frames[i].tile_px = choice.tile_px;
         frames[i].region_px = choice.region_px;
         frames[i].bin_capacity = choice.bin_capacity;
+    }
+    // Timed alone, a small frame is mostly launch latency, while in the batch
+    // it shares the launches (and another region size adds a raster launch):
+    // the tuned tilings are kept only if the whole batch runs faster with them
+    // than with the default tiling everywhere.
+    if (nframes > 1) {
+        std::vector<rsrgpu_frame_desc> deflt(frames, frames + nframes);
+        bool differs = false;
+        for (auto& f : deflt) {
+            if (f.tile_px != kTuneDefault[0] || f.region_px != kTuneDefault[1]) {
+                differs = true;
+                f.tile_px = kTuneDefault[0];
+                f.region_px = kTuneDefault[1];
+                f.bin_capacity = 0;
+            }
+        }
+        if (differs) {
+            float t_tuned = 0.f, t_default = 0.f;
+            rc = time_batch(b, frames, nframes, reps, &t_tuned);
+            if (rc == 0) rc = time_batch(b, deflt.data(), nframes, reps, &t_default);
+            if (rc) return rc;
+            if (t_default < t_tuned) {
+                // capacities from the entries each frame used in those runs
+                for (int i = 0; i < nframes; ++i) {
+                    const uint32_t used = b->frames[size_t(i)]->h_counters->bin_used;
+                    frames[i] = deflt[size_t(i)];
+                    frames[i].bin_capacity = used + used / 4 + 1024;
+                }
+            }
+        }
     }
     return 0;
 }
