@@ -237,8 +237,11 @@ def run_gpu(args):
         gpu.Wait()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     raster_ms = []
-    clocks = ClockSampler(os.path.join(REPO, "gpurun_out", "bench_clocks_%d.csv" % rank)
-                          if os.path.isdir(os.path.join(REPO, "gpurun_out")) else "/tmp/bench_clocks_%d.csv" % rank)
+    # the raw samples go to RSR_BENCH_CLOCKS_DIR (default: the temp directory);
+    # the line carries their summary
+    import tempfile
+    clocks = ClockSampler(os.path.join(os.environ.get("RSR_BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                                       "bench_clocks_%d.csv" % rank))
     barrier(world)
     torch.cuda.synchronize()
     with clocks, torch.cuda.stream(stream):
