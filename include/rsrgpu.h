@@ -20,6 +20,9 @@
  *   CMD_CLEAR           op u8, bits u8
  *   CMD_STORE_COLOR_FULL_LINEAR_TC  op u8, gamma u8, rsrgpu_truecolor_canvas*
  *   CMD_STORE_DEPTH_FULL_LINEAR_FP  op u8, float* (width*height, row-major)
+ *   CMD_STORE_COLOR_FULL_LINEAR_FP  op u8, rsrgpu_fp_canvas* (width x height)
+ *   CMD_STORE_COLOR_HALF_LINEAR_FP  op u8, rsrgpu_fp_canvas* (width/2 x height/2)
+ *   CMD_STORE_COLOR_FULL_QUADS_FP   op u8, rsrgpu_qfloat4_canvas* (width x height)
  *   CMD_EOF (optional; the stream may simply end)
  *
  * Memory
@@ -164,6 +167,41 @@ typedef struct rsrgpu_truecolor_canvas {
     int32_t stride;   /* in pixels */
     int32_t reserved;
 } rsrgpu_truecolor_canvas;
+
+/* Target of CMD_STORE_COLOR_FULL_LINEAR_FP and CMD_STORE_COLOR_HALF_LINEAR_FP,
+ * mirrors rglr::FloatingPointCanvas (src/rgl/rglr/rglr_canvas.hxx:488-529):
+ * RGBA float pixels (PixelToaster::FloatingPointPixel), row-major, stride in
+ * pixels.  The full store writes (r, g, b, 0) per pixel as
+ * Copy(QFloat3Canvas|QFloat4Canvas -> FloatingPointCanvas) does
+ * (src/rgl/rglr/rglr_algorithm.cxx:192-225,247-280); the half store writes
+ * one pixel per 2x2 quad, (((p0 + p1) + p2) + p3) * 0.25 per channel, as
+ * Downsample does (rglr_algorithm.cxx:118-168).  The tile interpreter's
+ * cases are src/rgl/rglv/rglv_gpu.cxx:345-383.  For the full store the
+ * canvas is width x height, for the half store width/2 x height/2; data must
+ * be 16-byte aligned. */
+typedef struct rsrgpu_fp_canvas {
+    float* data;      /* 4 floats per pixel */
+    int32_t width;
+    int32_t height;
+    int32_t stride;   /* in pixels */
+    int32_t reserved;
+} rsrgpu_fp_canvas;
+
+/* Target of CMD_STORE_COLOR_FULL_QUADS_FP, mirrors rglr::QFloat4Canvas
+ * (src/rgl/rglr/rglr_canvas.hxx:228-320): one 64-byte qfloat4 per 2x2 quad,
+ * laid out x[4] y[4] z[4] w[4] over the quad's lanes (x,y) (x+1,y) (x,y+1)
+ * (x+1,y+1); quads row-major, stride in quads.  x, y, z are the colour; w is
+ * 1 for an RB_RGBF32 colour buffer and the depth for RB_COLOR_DEPTH, as
+ * Copy(QFloat3Canvas|QFloat4Canvas -> QFloat4Canvas) writes them
+ * (src/rgl/rglr/rglr_algorithm.cxx:320-372).  width x height in pixels
+ * (the target's size); data must be 16-byte aligned. */
+typedef struct rsrgpu_qfloat4_canvas {
+    float* data;      /* 16 floats per quad */
+    int32_t width;
+    int32_t height;
+    int32_t stride;   /* in quads */
+    int32_t reserved;
+} rsrgpu_qfloat4_canvas;
 
 /* G-buffer written by RSRGPU_CMD_STORE_GBUFFER: fp32 NDC depth, the normal
  * as three fp16 planes (IEEE binary16 bits, round to nearest even), and
@@ -377,7 +415,9 @@ int rsrgpu_batch_create(int device, rsrgpu_batch** out);
 int rsrgpu_batch_destroy(rsrgpu_batch* batch);
 /* as rsrgpu_install(), for every frame of the batch */
 int rsrgpu_batch_install(rsrgpu_batch* batch, int program_id, uint32_t state_key, int kind);
-/* decodes up to RSRGPU_MAX_BATCH frames, sizes their scratch and captures the graph */
+/* decodes up to RSRGPU_MAX_BATCH frames, sizes their scratch and captures the
+ * graph; a frame with a float colour store (CMD_STORE_COLOR_*_FP) fails with
+ * RSRGPU_EUNSUPPORTED (render it with rsrgpu_run) */
 int rsrgpu_batch_submit(rsrgpu_batch* batch, const rsrgpu_frame_desc* frames, int nframes);
 /* replays the captured graph on `stream` (NULL: the batch's own stream) */
 int rsrgpu_batch_run(rsrgpu_batch* batch, void* stream);

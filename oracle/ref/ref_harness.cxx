@@ -170,10 +170,17 @@ T Read(const uint8_t*& p) {
 	T v; std::memcpy(&v, p, sizeof(T)); p += sizeof(T); return v; }
 
 
-// Replays the caller's stream into the reference's GL recorder.  Canvases are
-// created per store command and kept alive until the frame completes.
+// Output canvases of one frame, created per store command and kept alive
+// until the frame completes.
+struct Canvases {
+	std::vector<std::unique_ptr<rglr::TrueColorCanvas>> tc;
+	std::vector<std::unique_ptr<rglr::FloatingPointCanvas>> fp;
+	std::vector<std::unique_ptr<rglr::QFloat4Canvas>> quads; };
+
+
+// Replays the caller's stream into the reference's GL recorder.
 int Replay(rglv::GL& gl, const uint8_t* cmds, size_t n, const rsrgpu_glstate* states, int nstates,
-           std::vector<std::unique_ptr<rglr::TrueColorCanvas>>& canvases) {
+           Canvases& canvases) {
 	using namespace rglv;
 	const uint8_t* p = cmds;
 	const uint8_t* end = cmds + n;
@@ -204,9 +211,22 @@ int Replay(rglv::GL& gl, const uint8_t* cmds, size_t n, const rsrgpu_glstate* st
 		case CMD_STORE_COLOR_FULL_LINEAR_TC: {
 			auto gamma = Read<uint8_t>(p);
 			auto* c = Read<const rsrgpu_truecolor_canvas*>(p);
-			canvases.emplace_back(std::make_unique<rglr::TrueColorCanvas>(
+			canvases.tc.emplace_back(std::make_unique<rglr::TrueColorCanvas>(
 				reinterpret_cast<PixelToaster::TrueColorPixel*>(c->data), c->width, c->height, c->stride));
-			gl.StoreColor(canvases.back().get(), gamma != 0); }
+			gl.StoreColor(canvases.tc.back().get(), gamma != 0); }
+			break;
+		case CMD_STORE_COLOR_FULL_LINEAR_FP:
+		case CMD_STORE_COLOR_HALF_LINEAR_FP: {
+			auto* c = Read<const rsrgpu_fp_canvas*>(p);
+			canvases.fp.emplace_back(std::make_unique<rglr::FloatingPointCanvas>(
+				reinterpret_cast<PixelToaster::FloatingPointPixel*>(c->data), c->width, c->height, c->stride));
+			gl.StoreColor(canvases.fp.back().get(), op == CMD_STORE_COLOR_HALF_LINEAR_FP); }
+			break;
+		case CMD_STORE_COLOR_FULL_QUADS_FP: {
+			auto* c = Read<const rsrgpu_qfloat4_canvas*>(p);
+			canvases.quads.emplace_back(std::make_unique<rglr::QFloat4Canvas>(
+				c->width, c->height, reinterpret_cast<rmlv::qfloat4*>(c->data), c->stride));
+			gl.StoreColor(canvases.quads.back().get()); }
 			break;
 		case CMD_STORE_DEPTH_FULL_LINEAR_FP:
 			gl.StoreDepth(Read<float*>(p));
@@ -306,7 +326,7 @@ int rsrref_render(const uint8_t* cmds, size_t n, const rsrgpu_glstate* states, i
 	auto& gpu = *s->gpu;
 	jobsys::reset();
 	gpu.Reset(rmlv::ivec2{ width, height }, rmlv::ivec2{ tile_blocks_x, tile_blocks_y });
-	std::vector<std::unique_ptr<rglr::TrueColorCanvas>> canvases;
+	harness::Canvases canvases;
 	if (harness::Replay(gpu.IC(), cmds, n, states, nstates, canvases) != 0) return -1;
 	auto* done = jobsys::make_job(jobsys::noop);
 	auto* run = gpu.Run();

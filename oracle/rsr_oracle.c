@@ -554,6 +554,9 @@ static int bin_frame(Frame* f, const uint8_t* cmds, size_t n) {
             for (int t = 0; t < f->ntiles; ++t) { bb_u8(&f->tiles[t], op); bb_u8(&f->tiles[t], gamma); bb_u64(&f->tiles[t], ptr); }
         } break;
         case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP:
+        case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP:   /* GPU::BinImpl, rglv_gpu.cxx:156-176 */
+        case RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP:
+        case RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP:
         case RSRGPU_CMD_STORE_GBUFFER: {
             RD(uint64_t, ptr);
             for (int t = 0; t < f->ntiles; ++t) { bb_u8(&f->tiles[t], op); bb_u64(&f->tiles[t], ptr); }
@@ -969,6 +972,54 @@ static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8
                 }
             }
         } break;
+        case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP:
+        case RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP:
+        case RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP: {
+            /* GPU::DrawImpl, rglv_gpu.cxx:345-383: the tile's RGB colour
+               (an RB_RGBF32 QFloat3 buffer or the rgb of RB_COLOR_DEPTH's
+               QFloat4 buffer, whose w is the depth) copied out as float */
+            uint64_t cp;
+            memcpy(&cp, p, 8); p += 8;
+            const int c0 = tc.s->color0_attachment_type;
+            if (c0 != RSRGPU_RB_RGBF32 && c0 != RSRGPU_RB_COLOR_DEPTH) return RSRGPU_EUNSUPPORTED;
+            const rsrgpu_fp_canvas* cv = (const rsrgpu_fp_canvas*)(uintptr_t)cp;
+            for (int y = tc.rect[1]; y < tc.rect[3]; y += 2) {
+                for (int x = tc.rect[0]; x < tc.rect[2]; x += 2) {
+                    /* the quad's lanes: (x,y) (x+1,y) (x,y+1) (x+1,y+1) */
+                    const float* px[4];
+                    float dq[4];
+                    for (int l = 0; l < 4; ++l) {
+                        const int li = (y + (l >> 1) - tc.rect[1]) * f->tile_w + (x + (l & 1) - tc.rect[0]);
+                        px[l] = &color[li * 4];
+                        dq[l] = depth[li];
+                    }
+                    if (op == RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP) {
+                        /* Copy(QFloat3Canvas|QFloat4Canvas -> FloatingPointCanvas),
+                           rglr_algorithm.cxx:192-225,247-280: the transpose of
+                           (r, g, b, zero) quads gives (r, g, b, 0) pixels */
+                        for (int l = 0; l < 4; ++l) {
+                            float* d = cv->data + ((size_t)(y + (l >> 1)) * cv->stride + (x + (l & 1))) * 4;
+                            d[0] = px[l][0]; d[1] = px[l][1]; d[2] = px[l][2]; d[3] = 0.0f;
+                        }
+                    } else if (op == RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP) {
+                        /* Downsample, rglr_algorithm.cxx:118-168: the four
+                           (r, g, b, 0) pixels added in lane order, times 0.25 */
+                        float* d = cv->data + ((size_t)(y / 2) * cv->stride + x / 2) * 4;
+                        for (int c = 0; c < 3; ++c) d[c] = (((px[0][c] + px[1][c]) + px[2][c]) + px[3][c]) * 0.25f;
+                        d[3] = (((0.0f + 0.0f) + 0.0f) + 0.0f) * 0.25f;
+                    } else {
+                        /* Copy(QFloat3Canvas -> QFloat4Canvas) sets w to 1,
+                           Copy(QFloat4Canvas -> QFloat4Canvas) keeps it (the
+                           depth of RB_COLOR_DEPTH), rglr_algorithm.cxx:320-372 */
+                        float* q = cv->data + ((size_t)(y / 2) * cv->stride + x / 2) * 16;
+                        for (int l = 0; l < 4; ++l) {
+                            q[l] = px[l][0]; q[4 + l] = px[l][1]; q[8 + l] = px[l][2];
+                            q[12 + l] = c0 == RSRGPU_RB_COLOR_DEPTH ? dq[l] : 1.0f;
+                        }
+                    }
+                }
+            }
+        } break;
         case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: {
             uint64_t dp;
             memcpy(&dp, p, 8); p += 8;
@@ -1092,6 +1143,9 @@ int rsroracle_dump_tiles(uint8_t* out, size_t capacity, size_t* needed) {
             case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC: bb_u8(&one, *p++); p += 8; break;
             case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: p += 8; break;
             case RSRGPU_CMD_STORE_GBUFFER: p += 8; break;
+            case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP:
+            case RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP:
+            case RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP: p += 8; break;
             case RSRGPU_CMD_DRAW_INLINE:
                 while (1) {
                     uint16_t w; p = rd_u16(p, &w); bb_u16(&one, w);

@@ -17,7 +17,10 @@ CMD_CLEAR = 10
 CMD_DRAW_ELEMENTS = 11
 CMD_DRAW_ARRAYS = 12
 CMD_DRAW_INLINE = 15
+CMD_STORE_COLOR_FULL_LINEAR_FP = 20
+CMD_STORE_COLOR_HALF_LINEAR_FP = 21
 CMD_STORE_COLOR_FULL_LINEAR_TC = 22
+CMD_STORE_COLOR_FULL_QUADS_FP = 23
 CMD_STORE_DEPTH_FULL_LINEAR_FP = 25
 CMD_CLIPPED_TRI = 100
 CMD_STORE_GBUFFER = 40
@@ -99,6 +102,13 @@ class GLStateC(ctypes.Structure):
 
 
 class TrueColorCanvasC(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("stride", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class FloatCanvasC(ctypes.Structure):
+    """rsrgpu_fp_canvas and rsrgpu_qfloat4_canvas (same layout)."""
     _fields_ = [("data", ctypes.c_void_p), ("width", ctypes.c_int32),
                 ("height", ctypes.c_int32), ("stride", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]

@@ -641,6 +641,43 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             fo.width = cv->width; fo.height = cv->height; fo.stride = cv->stride;
             ctx->ops.push_back(fo);
         } break;
+        case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP:
+        case RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP:
+        case RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP: {
+            // rglv_gpu.cxx:345-383: Copy / Downsample of the tile's colour
+            // buffer into a float canvas (RB_RGBF32 or RB_COLOR_DEPTH)
+            uint64_t cp;
+            if (!rd(p, end, cp)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_STORE_COLOR_*_FP");
+            if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "store before any state");
+            const int ct = states[cur].color0_attachment_type;
+            if (ct != RSRGPU_RB_RGBF32 && ct != RSRGPU_RB_COLOR_DEPTH)
+                return fail(ctx, RSRGPU_EUNSUPPORTED, "CMD_STORE_COLOR_*_FP not implemented for attachment type %d", ct);
+            const bool half = op == RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP;
+            const bool quads = op == RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP;
+            // both canvas mirrors share the layout {data, width, height, stride}
+            const auto* cv = reinterpret_cast<const rsrgpu_fp_canvas*>(uintptr_t(cp));
+            const int want_w = half ? ctx->width / 2 : ctx->width;
+            const int want_h = half ? ctx->height / 2 : ctx->height;
+            const int min_stride = quads ? ctx->width / 2 : want_w;
+            if (cv == nullptr || cv->width != want_w || cv->height != want_h || cv->stride < min_stride)
+                return fail(ctx, RSRGPU_EINVAL, "float canvas must be %dx%d with stride >= %d", want_w, want_h, min_stride);
+            // bytes from the canvas base to the end of its last written row
+            const size_t rows = quads ? size_t(ctx->height / 2) : size_t(want_h);
+            const size_t unit = quads ? 64u : 16u;
+            const size_t need = ((rows - 1) * size_t(cv->stride) + size_t(min_stride)) * unit;
+            void* dp = nullptr;
+            size_t avail = 0;
+            int rc = resolve(ctx, cv->data, kOutput, &dp, "float color output", &avail);
+            if (rc) return rc;
+            if (dp == nullptr || avail < need)
+                return fail(ctx, RSRGPU_EINVAL, "float color output holds %zu bytes, needs %zu", avail, need);
+            if (reinterpret_cast<uintptr_t>(dp) & 15) return fail(ctx, RSRGPU_EINVAL, "float color output must be 16-byte aligned");
+            other_op_since_draw = true;
+            fo.kind = half ? kOpStoreHalfFP : quads ? kOpStoreQuadsFP : kOpStoreFP;
+            fo.ptr = dp;
+            fo.width = cv->width; fo.height = cv->height; fo.stride = cv->stride;
+            ctx->ops.push_back(fo);
+        } break;
         case RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP: {
             uint64_t dp64;
             if (!rd(p, end, dp64)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_STORE_DEPTH_FULL_LINEAR_FP");
@@ -711,7 +748,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
         bool ok = !ctx->draws.empty() && ctx->draws.size() <= 4096, drawn = false, stored = false;
         for (const FrameOp& o : ctx->ops) {
             if (o.kind == kOpClear && drawn) ok = false;
-            if (o.kind == kOpStoreTC || o.kind == kOpStoreDepth || o.kind == kOpStoreGBuffer) stored = true;
+            if (op_is_store(o.kind)) stored = true;
             if (o.kind != kOpDraw) continue;
             if (stored) ok = false;
             drawn = true;
@@ -799,6 +836,9 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.raster_phase = 0;
     fv.vis_own = nullptr;
     fv.vis_dep = nullptr;
+    fv.fp_stores = 0;
+    for (const FrameOp& o : ctx->ops)
+        if (o.kind >= kOpStoreFP) fv.fp_stores = 1;
     return 0;
 }
 
@@ -1030,6 +1070,9 @@ int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* ne
             else if (o.kind == kOpStoreTC) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC); put8(one, uint8_t(o.arg)); }
             else if (o.kind == kOpStoreDepth) { put8(one, RSRGPU_CMD_STORE_DEPTH_FULL_LINEAR_FP); }
             else if (o.kind == kOpStoreGBuffer) { put8(one, RSRGPU_CMD_STORE_GBUFFER); }
+            else if (o.kind == kOpStoreFP) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_FP); }
+            else if (o.kind == kOpStoreHalfFP) { put8(one, RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP); }
+            else if (o.kind == kOpStoreQuadsFP) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP); }
             else if (o.kind == kOpDraw) {
                 const DevDraw& d = ctx->draws[size_t(o.arg)];
                 const uint32_t endg = uint32_t(d.first_tri + d.ntris);
@@ -1417,6 +1460,9 @@ int decode_into(rsrgpu_batch* b, rsrgpu_ctx* c, const rsrgpu_frame_desc& d) {
     if (rc == 0) rc = rsrgpu_submit(c, d.commands, d.nbytes, d.states, d.nstates);
     if (rc) { b->err = c->err; return rc; }
     if (!c->host.empty()) return bfail(b, RSRGPU_EINVAL, "batched frames take device pointers only");
+    for (const FrameOp& o : c->ops)
+        if (o.kind >= kOpStoreFP)
+            return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no float colour stores (CMD_STORE_COLOR_*_FP); render them with rsrgpu_run");
     c->region_px = d.region_px ? d.region_px : std::min(d.tile_px, kRegionPx);
     if (d.bin_capacity) c->bin_cap = std::max<uint32_t>(d.bin_capacity, 1024u);
     return 0;

@@ -73,7 +73,13 @@ struct DevDraw {
     const uint16_t* indices;
 };
 
-enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4, kOpStoreGBuffer = 5 };
+// Every kind from kOpStoreTC on is a store; all but kOpStoreDepth read colour.
+// The FP stores: rsr's CMD_STORE_COLOR_FULL_LINEAR_FP (kOpStoreFP),
+// CMD_STORE_COLOR_HALF_LINEAR_FP (kOpStoreHalfFP) and
+// CMD_STORE_COLOR_FULL_QUADS_FP (kOpStoreQuadsFP).
+enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4, kOpStoreGBuffer = 5,
+                        kOpStoreFP = 6, kOpStoreHalfFP = 7, kOpStoreQuadsFP = 8 };
+__host__ __device__ inline bool op_is_store(int32_t kind) { return kind >= kOpStoreTC; }
 
 // device addresses of one G-buffer target (RSRGPU_CMD_STORE_GBUFFER)
 struct GBufferDesc {
@@ -159,6 +165,8 @@ struct FrameView {
                               // 1 visibility (owners and depths into vis_own / vis_dep), 2 the rest
     uint32_t* vis_own;        // [height * width] per pixel, phases 1 and 2
     float* vis_dep;
+    int32_t fp_stores;        // the op list has float colour stores (raster_fp_kernel runs it)
+    int32_t pad_fp;
 };
 
 // Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,

@@ -1244,6 +1244,9 @@ __device__ __noinline__ float owner_depth(const FrameView& fv, uint32_t code, co
     return (bx * z[0] + by * z[1]) + bz * z[2];
 }
 
+// kFPStores: the frame has float colour stores (rsr's CMD_STORE_COLOR_*_FP);
+// frames without them run the instantiation that has no code for them.
+template <bool kFPStores>
 __device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
     if (fv.counters->overflow != 0u) return;
 
@@ -1320,7 +1323,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         // depth and hands over the owners and depths at its end; the second
         // replays states and clears, skips the draws and depth stores, takes
         // the owners and depths at the first store and shades.
-        if (fv.raster_phase != 0 && (o.kind == kOpStoreTC || o.kind == kOpStoreDepth || o.kind == kOpStoreGBuffer)) {
+        if (fv.raster_phase != 0 && op_is_store(o.kind)) {
             if (fv.raster_phase == 1 && o.kind != kOpStoreDepth) continue;
             if (fv.raster_phase == 2) {
                 if (phase_pending) {
@@ -1648,6 +1651,36 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                 *reinterpret_cast<float2*>(dst + size_t(qy) * o.stride + qx) = make_float2(dep[0], dep[1]);
                 *reinterpret_cast<float2*>(dst + size_t(qy + 1) * o.stride + qx) = make_float2(dep[2], dep[3]);
             }
+        } else if (kFPStores && o.kind >= kOpStoreFP) {
+            // rsr's CMD_STORE_COLOR_{FULL_LINEAR,HALF_LINEAR,FULL_QUADS}_FP
+            // (rglv_gpu.cxx:345-383); four float4 writes at most
+            if (active) {
+                float4* base = static_cast<float4*>(o.ptr);
+                const size_t qoff = size_t(qy >> 1) * o.stride + (qx >> 1);
+                if (o.kind == kOpStoreHalfFP) {
+                    // Downsample (rglr_algorithm.cxx:118-168): the quad's four
+                    // pixels (r, g, b, 0) summed in lane order, times 0.25
+                    base[qoff] = make_float4((((col[0][0] + col[1][0]) + col[2][0]) + col[3][0]) * 0.25f,
+                                             (((col[0][1] + col[1][1]) + col[2][1]) + col[3][1]) * 0.25f,
+                                             (((col[0][2] + col[1][2]) + col[2][2]) + col[3][2]) * 0.25f, 0.0f);
+                } else if (o.kind == kOpStoreFP) {
+                    // Copy(QFloat3Canvas|QFloat4Canvas -> FloatingPointCanvas)
+                    // (rglr_algorithm.cxx:192-225,247-280): (r, g, b, 0) per pixel
+                    float4* p0 = base + size_t(qy) * o.stride + qx;
+#pragma unroll
+                    for (int l = 0; l < 4; ++l)
+                        p0[(l >> 1) * o.stride + (l & 1)] = make_float4(col[l][0], col[l][1], col[l][2], 0.0f);
+                } else {
+                    // Copy(QFloat3Canvas|QFloat4Canvas -> QFloat4Canvas)
+                    // (rglr_algorithm.cxx:320-372): x, y, z the colour lanes, w 1
+                    // for RB_RGBF32 and the packed depth for RB_COLOR_DEPTH
+                    float4* q = base + qoff * 4;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) q[c] = make_float4(col[0][c], col[1][c], col[2][c], col[3][c]);
+                    const bool packed = fv.states[cur_state].color_type == 0;
+                    q[3] = packed ? make_float4(dep[0], dep[1], dep[2], dep[3]) : make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+                }
+            }
         }
     }
     if (fv.raster_phase == 1 && active) {   // the hand-over to the second launch
@@ -1672,7 +1705,11 @@ __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ 
 }
 __global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
-    raster_body(fv, blockIdx.x, S);
+    raster_body<false>(fv, blockIdx.x, S);
+}
+__global__ void __launch_bounds__(256, 2) raster_fp_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem S;
+    raster_body<true>(fv, blockIdx.x, S);
 }
 
 // frame of a block: the last f with start[f] <= block (start[] ascending)
@@ -1696,7 +1733,7 @@ __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_const
 __global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ RasterSmem S;
     const int f = batch_frame(b, blockIdx.x);
-    raster_body(b.fv[f], blockIdx.x - b.start[f], S);
+    raster_body<false>(b.fv[f], blockIdx.x - b.start[f], S);
 }
 
 // ---------------------------------------------------------------------------
@@ -1752,7 +1789,8 @@ cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
 }
 
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
-    raster_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
+    if (fv.fp_stores) raster_fp_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
+    else raster_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
     return cudaGetLastError();
 }
 

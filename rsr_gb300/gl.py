@@ -260,6 +260,24 @@ class GL:
         self.commands += struct.pack("<BBQ", abi.CMD_STORE_COLOR_FULL_LINEAR_TC,
                                      1 if gamma else 0, ctypes.addressof(c))
 
+    def StoreColorFP(self, data, width, height, downsample=False, stride=None):
+        """StoreColor(FloatingPointCanvas*, downsample) (rglv_gl.cxx:64-70):
+        RGBA float pixels, the full target (width x height) or, downsampled,
+        one pixel per 2x2 quad (width/2 x height/2 -- pass the canvas size)."""
+        self._maybe_update_state()
+        c = abi.FloatCanvasC(_addr(data), width, height, stride or width, 0)
+        self._keep.append(c)
+        op = abi.CMD_STORE_COLOR_HALF_LINEAR_FP if downsample else abi.CMD_STORE_COLOR_FULL_LINEAR_FP
+        self.commands += struct.pack("<BQ", op, ctypes.addressof(c))
+
+    def StoreColorQuads(self, data, width, height, stride=None):
+        """StoreColor(QFloat4Canvas*) (rglv_gl.cxx:73-77): one 64-byte qfloat4
+        per 2x2 quad, stride in quads (default width/2)."""
+        self._maybe_update_state()
+        c = abi.FloatCanvasC(_addr(data), width, height, stride or width // 2, 0)
+        self._keep.append(c)
+        self.commands += struct.pack("<BQ", abi.CMD_STORE_COLOR_FULL_QUADS_FP, ctypes.addressof(c))
+
     def StoreDepth(self, data):
         self._maybe_update_state()
         self.commands += struct.pack("<BQ", abi.CMD_STORE_DEPTH_FULL_LINEAR_FP, _addr(data))

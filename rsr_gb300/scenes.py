@@ -571,3 +571,75 @@ class DeferredScene(Scene):
         self._record(gl, ref)
         gl.StoreGBuffer(g["depth"], g["nx"], g["ny"], g["nz"], g["albedo"], self.width, self.height)
         return gl
+
+
+class FloatStoreScene(Scene):
+    """A frame whose colour also leaves through rsr's float stores:
+    StoreColor(FloatingPointCanvas*, downsample) and StoreColor(QFloat4Canvas*).
+    record(ref, outputs=...) takes the output arrays by name ("tc", "depth",
+    "full", "half", "quads", and "full_mid", "quads_mid" when stores come
+    between the draws); self.outputs holds host arrays of the right sizes."""
+
+    def __init__(self, *a, color_depth=False, mid=False, **kw):
+        super().__init__(*a, **kw)
+        w, h = self.width, self.height
+        self.color_depth = color_depth
+        self.mid = mid
+        self.outputs = {"tc": np.zeros(w * h, np.uint32), "full": np.zeros(w * h * 4, np.float32),
+                        "half": np.zeros((w // 2) * (h // 2) * 4, np.float32),
+                        "quads": np.zeros((w // 2) * (h // 2) * 16, np.float32)}
+        if not color_depth:
+            self.outputs["depth"] = np.zeros(w * h, np.float32)
+        if mid:
+            self.outputs["full_mid"] = np.zeros(w * h * 4, np.float32)
+            self.outputs["quads_mid"] = np.zeros((w // 2) * (h // 2) * 16, np.float32)
+
+    def record(self, ref=None, outputs=None, gamma=True, **_):
+        gl = GL()
+        ref = ref or (lambda k: self.arrays[k])
+        out = outputs or self.outputs
+        w, h = self.width, self.height
+        self._record(gl, ref, out)
+        gl.StoreColorFP(out["full"], w, h)
+        gl.StoreColorFP(out["half"], w // 2, h // 2, downsample=True)
+        gl.StoreColorQuads(out["quads"], w, h)
+        gl.UseProgram(abi.PROGRAM_DEFAULT_POST)
+        gl.StoreColor(out["tc"], w, h, gamma)
+        if not self.color_depth:
+            gl.StoreDepth(out["depth"])
+        return gl
+
+
+def float_store_frame(seed=21, ntris=6000, width=320, height=180, tile_blocks=(4, 4), color_depth=False, mid=False,
+                      spread=0.35):
+    """Random Gouraud triangles (the config-1 generator, shrunk by `spread`)
+    drawn in two halves; the colour buffer is RB_RGBF32 with RB_F32 depth, or
+    RB_COLOR_DEPTH (depth in the colour's w).  With mid=True the full float
+    and quad stores are also taken between the two halves (stores between
+    draws keep the raster pass in its sequential walk)."""
+    base = plain_raster(seed=seed, ntris=ntris, width=width, height=height, tile_blocks=tile_blocks, spread=spread)
+    arrays = base.arrays
+    half = (ntris // 2) * 3
+
+    def record(gl, ref, out):
+        if color_depth:
+            gl.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, abi.RB_COLOR_DEPTH)
+            gl.RenderbufferType(abi.GL_DEPTH_ATTACHMENT, abi.RB_COLOR_DEPTH)
+            gl.ClearColor((0.05, 0.1, 0.15))
+            gl.ClearDepth(1.0)
+            gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
+        else:
+            _begin_frame(gl, (0.05, 0.1, 0.15))
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
+        gl.UseBuffer(3, (ref("cr"), ref("cg"), ref("cb")))
+        gl.DrawElements(half, ref("idx"), 0)
+        if mid:
+            gl.StoreColorFP(out["full_mid"], width, height)
+            gl.StoreColorQuads(out["quads_mid"], width, height)
+        gl.UseBuffer(0, tuple(ref(k)[half:] for k in ("px", "py", "pz")))
+        gl.UseBuffer(3, tuple(ref(k)[half:] for k in ("cr", "cg", "cb")))
+        gl.DrawElements(3 * ntris - half, ref("idx"), 0)
+
+    name = "float_store_%s%s" % ("color_depth" if color_depth else "rgbf32", "_mid" if mid else "")
+    return FloatStoreScene(name, width, height, tile_blocks, arrays, record, ntris, color_depth=color_depth, mid=mid)

@@ -39,6 +39,26 @@ GOLDEN_SCENES = {
 }
 
 
+# frames with rsr's float colour stores (StoreColor to FloatingPointCanvas,
+# downsampled or not, and to QFloat4Canvas): name -> float_store_frame kwargs
+FLOAT_STORE_SCENES = {
+    "float_store_rgbf32": {},
+    "float_store_rgbf32_mid": dict(mid=True),
+    "float_store_color_depth": dict(color_depth=True),
+    "float_store_color_depth_mid": dict(color_depth=True, mid=True),
+}
+
+
+def render_float_store(renderer, sc, gamma):
+    """Renders a scenes.FloatStoreScene; returns {output: digest} plus the tile streams' digest."""
+    for v in sc.outputs.values():
+        v[:] = 0
+    renderer.render_gl(sc.record(gamma=gamma), sc.width, sc.height, sc.tile_blocks)
+    out = {k: digest(np.ascontiguousarray(v).view(np.uint32).tobytes()) for k, v in sc.outputs.items()}
+    out["tiles"] = digest(b"".join(len(t).to_bytes(4, "little") + t for t in renderer.tiles()))
+    return out
+
+
 def make_scene(name):
     fn, kw, _ = GOLDEN_SCENES[name]
     kw = dict(kw)
@@ -74,6 +94,11 @@ def main():
             c, d = ref.render(sc, gamma)
             out["%s/gamma%d" % (name, int(gamma))] = frame_digests(c, d, ref.tiles(), ref.clipped(), nvary)
             print(name, gamma, out["%s/gamma%d" % (name, int(gamma))]["covered"])
+    for name, kw in FLOAT_STORE_SCENES.items():
+        sc = scenes.float_store_frame(**kw)
+        for gamma in (False, True):
+            out["%s/gamma%d" % (name, int(gamma))] = render_float_store(ref, sc, gamma)
+            print(name, gamma)
     with open(os.path.join(HERE, "frames.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
 

@@ -51,8 +51,10 @@ def test_top_left_fill_rule_kat(orc):
 
 
 def _golden():
+    # frames of the scenes this test renders (the float-store frames have
+    # their own test, tests/test_float_stores.py)
     with open(os.path.join(HERE, "golden", "frames.json")) as f:
-        return json.load(f)
+        return {k: v for k, v in json.load(f).items() if not k.startswith("float_store")}
 
 
 GOLDEN = _golden()
