@@ -294,6 +294,38 @@ int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms);
 
 int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
 
+/* ---- texture upload and mip chain on the device ----
+ * rglr::Texture's layout (src/rgl/rglr/rglr_texture.hxx:10-33): RGBA float
+ * texels (16 bytes, PixelToaster::FloatingPointPixel), row-major with stride
+ * width.  A square power-of-two texture of edge w <= 4096 gets the mip chain
+ * Texture::maybe_make_mipmap builds (src/rgl/rglr/rglr_texture.cxx:33-80):
+ * w*w*2 texels, level k (edge w >> k) in rows [2w - 2(w >> k), 2w - (w >> k))
+ * and columns [0, w >> k), every other texel of rows [w, 2w) zero; a level-k
+ * texel is (((a + b) + c) + d) / 4 of its 2x2 parents in level k-1, in
+ * row-major order.  Other sizes get no chain (power -1), as in the
+ * reference.  All pointers are device pointers; the work is enqueued on
+ * `stream` (NULL = the context's stream) and the call returns without
+ * waiting. */
+#define RSRGPU_TEXTURE_MAX_EDGE 4096
+
+/* PNGToTexture's conversion of decoded RGBA8 pixels
+ * (src/rgl/rglr/rglr_texture_load.cxx:40-63): r, g, b through
+ * ryg::srgb8_to_float, alpha / 255, rgb multiplied by alpha when
+ * `premultiply`; then the mip chain above.  rgba8: width*height*4 bytes,
+ * 4-byte aligned.  texels: 16-byte aligned, room for 2*width*height texels
+ * when a chain is built, else width*height.  *power (may be NULL) receives
+ * Texture::pow: log2(width), or -1 without a chain. */
+int rsrgpu_texture_from_rgba8(rsrgpu_ctx* ctx, const uint8_t* rgba8, int width, int height, int premultiply,
+                              float* texels, size_t texel_capacity, int* power, void* stream);
+
+/* Texture::maybe_make_mipmap on a float texture already on the device (level
+ * 0 in texels[0 .. width*height)), for example a frame stored there by
+ * CMD_STORE_COLOR_FULL_LINEAR_FP as rsr's render-to-texture node does
+ * (src/viewer/node/rendertotexture.cxx:64-95).  Without a chain (power -1)
+ * nothing is written. */
+int rsrgpu_texture_mipmap(rsrgpu_ctx* ctx, float* texels, int width, int height, size_t texel_capacity,
+                          int* power, void* stream);
+
 /* ---- deferred shading (extension; no counterpart in rsr) ----
  * Plain multi-light Blinn-Phong over a G-buffer: for each pixel with albedo
  * != 0, world position from depth through inv_view_proj (column-major), then

@@ -24,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "librsrref.so")
 ORACLE_LIB = os.path.join(HERE, "librsroracle.so")
 SRGB_LUT = os.path.join(os.path.dirname(HERE), "tests", "golden", "srgb8_lut.bin")
+SRGB_DECODE = os.path.join(os.path.dirname(HERE), "tests", "golden", "srgb8_to_float.bin")
 
 _ref = None
 _oracle = None
@@ -136,6 +137,39 @@ class CpuRenderer:
         if rc != 0:
             raise RuntimeError("oracle learned_features failed: %d" % rc)
         return out
+
+    def texture_from_rgba8(self, rgba8, width, height, premultiply=False):
+        """PNGToTexture's conversion + Texture::maybe_make_mipmap; returns
+        (texels float32 (n, 4), power).  The oracle decodes with the reference
+        decoder's golden table (tests/golden/srgb8_to_float.bin)."""
+        rgba8 = np.ascontiguousarray(rgba8, np.uint8)
+        n = width * height
+        out = np.zeros((2 * n, 4), np.float32)
+        power = ctypes.c_int(0)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        if self.which == "ref":
+            rc = self.lib.rsrref_texture_from_rgba8(vp(rgba8), width, height, int(premultiply), vp(out),
+                                                    ctypes.c_size_t(2 * n), ctypes.byref(power))
+        else:
+            lut = np.fromfile(SRGB_DECODE, np.float32)
+            rc = self.lib.rsroracle_texture_from_rgba8(vp(rgba8), width, height, int(premultiply), vp(lut), vp(out),
+                                                       ctypes.c_size_t(2 * n), ctypes.byref(power))
+        if rc != 0:
+            raise RuntimeError("%s texture build failed: %d" % (self.which, rc))
+        return out[:2 * n if power.value >= 0 else n].copy(), power.value
+
+    def texture_mipmap(self, texels, width, height):
+        """Texture::maybe_make_mipmap on float texels (level 0 in the first
+        width*height rows of texels (n, 4)); returns (texels, power)."""
+        n = width * height
+        out = np.zeros((2 * n, 4), np.float32)
+        out[:n] = texels[:n]
+        power = ctypes.c_int(0)
+        fn = getattr(self.lib, self.prefix + "_texture_mipmap")
+        rc = fn(out.ctypes.data_as(ctypes.c_void_p), width, height, ctypes.c_size_t(2 * n), ctypes.byref(power))
+        if rc != 0:
+            raise RuntimeError("%s mipmap failed: %d" % (self.which, rc))
+        return out[:2 * n if power.value >= 0 else n].copy(), power.value
 
     def tiles(self):
         need = ctypes.c_size_t(0)

@@ -20,6 +20,7 @@
 #include "src/rcl/rclmt/rclmt_jobsys.hxx"
 #include "src/rgl/rglr/rglr_canvas.hxx"
 #include "src/rgl/rglr/rglr_fragmentcursor.hxx"
+#include "src/rgl/rglr/rglr_texture.hxx"
 #include "src/rgl/rglv/rglv_gl.hxx"
 #include "src/rgl/rglv/rglv_gpu.hxx"
 #include "src/rgl/rglv/rglv_gpu_impl.hxx"
@@ -27,6 +28,7 @@
 #include "src/viewer/shaders.hxx"
 
 #include "include/rsrgpu.h"
+#include "3rdparty/ryg-srgb/ryg-srgb.h"
 
 namespace rqdq {
 namespace harness {
@@ -362,6 +364,44 @@ int rsrref_dump_clipped(rsrgpu_clipped_vertex* out, int capacity, int* count) {
 		out[i].coord[0] = cv[i].coord.x; out[i].coord[1] = cv[i].coord.y;
 		out[i].coord[2] = cv[i].coord.z; out[i].coord[3] = cv[i].coord.w;
 		std::memcpy(out[i].data, cv[i].data, sizeof(out[i].data)); }
+	return 0; }
+
+// A texture built the way rsr's image loader builds one: PNGToTexture's
+// per-pixel conversion with the reference's ryg::srgb8_to_float
+// (src/rgl/rglr/rglr_texture_load.cxx:40-63; the loop is restated here, it
+// sits in an unnamed namespace behind the PNG decoder), then the reference's
+// own rglr::Texture::maybe_make_mipmap (src/rgl/rglr/rglr_texture.cxx:33-80).
+// out receives buf (texels * 4 floats); returns -1 if cap (texels) is short.
+int rsrref_texture_from_rgba8(const uint8_t* rgba8, int w, int h, int premultiply, float* out, size_t cap,
+                              int* power) {
+	rcls::vector<PixelToaster::FloatingPointPixel> pc(size_t(w) * size_t(h));
+	const uint8_t* ic = rgba8;
+	for (auto& dst : pc) {
+		dst.r = ryg::srgb8_to_float(*(ic++));
+		dst.g = ryg::srgb8_to_float(*(ic++));
+		dst.b = ryg::srgb8_to_float(*(ic++));
+		dst.a = *(ic++) / 255.0F;
+		if (premultiply) {
+			dst.r *= dst.a;
+			dst.g *= dst.a;
+			dst.b *= dst.a; }}
+	rglr::Texture tex{ pc, w, h, w, "oracle", -1, false };
+	tex.maybe_make_mipmap();
+	if (cap < tex.buf.size()) return -1;
+	std::memcpy(out, tex.buf.data(), tex.buf.size() * sizeof(PixelToaster::FloatingPointPixel));
+	*power = tex.pow;
+	return 0; }
+
+// rglr::Texture::maybe_make_mipmap on float texels (level 0 in texels).
+int rsrref_texture_mipmap(float* texels, int w, int h, size_t cap, int* power) {
+	rcls::vector<PixelToaster::FloatingPointPixel> pc(size_t(w) * size_t(h));
+	std::memcpy(pc.data(), texels, pc.size() * sizeof(PixelToaster::FloatingPointPixel));
+	rglr::Texture tex{ pc, w, h, w, "oracle", -1, false };
+	tex.maybe_make_mipmap();
+	*power = tex.pow;
+	if (!tex.mipmap) return 0;
+	if (cap < tex.buf.size()) return -1;
+	std::memcpy(texels, tex.buf.data(), tex.buf.size() * sizeof(PixelToaster::FloatingPointPixel));
 	return 0; }
 
 }  // extern "C"

@@ -1481,3 +1481,71 @@ int rsroracle_learned_features(const rsrgpu_gbuffer* g, const float ivp[16], con
     free(plain);
     return 0;
 }
+
+
+/* ======================================================================
+ * texture upload and mip chain (test infrastructure: the oracle of
+ * rsrgpu_texture_from_rgba8 / rsrgpu_texture_mipmap)
+ * ====================================================================== */
+
+/* Texture::maybe_make_mipmap's size test (src/rgl/rglr/rglr_texture.cxx:35-50) */
+static int texture_power(int w, int h) {
+    if (w != h || w <= 0 || (w & (w - 1)) != 0) return -1;
+    const int p = ilog2u((unsigned)w);
+    return p > 12 ? -1 : p;
+}
+
+/* Texture::maybe_make_mipmap (rglr_texture.cxx:33-80): the buffer grows to
+   w*w*2 zeroed texels past level 0, then each level is written below the
+   previous one with the level-0 row stride, texel = (((a + b) + c) + d) / 4 */
+static void make_mipmap(float* buf, int w, int p) {
+    memset(buf + (size_t)w * w * 4, 0, sizeof(float) * 4 * (size_t)w * w);
+    int src_size = w;
+    size_t src = 0, dst = (size_t)w * w;
+    for (int level = p - 1; level >= 0; --level) {
+        for (int sy = 0; sy < src_size; sy += 2) {
+            size_t drow = dst;
+            for (int sx = 0; sx < src_size; sx += 2) {
+                const float* a = buf + (src + (size_t)sy * w + sx) * 4;
+                const float* c = buf + (src + (size_t)(sy + 1) * w + sx) * 4;
+                float* d = buf + drow * 4;
+                for (int k = 0; k < 4; ++k) d[k] = (((a[k] + a[4 + k]) + c[k]) + c[4 + k]) / 4.0f;
+                ++drow;
+            }
+            dst += (size_t)w;
+        }
+        src += (size_t)src_size * w;
+        src_size >>= 1;
+    }
+}
+
+/* PNGToTexture's per-pixel conversion (src/rgl/rglr/rglr_texture_load.cxx:
+   40-63) with the reference decoder's table (lut: ryg::srgb8_to_float of
+   every byte), then the chain.  Returns 0, or -1 if cap (texels) is short. */
+int rsroracle_texture_from_rgba8(const uint8_t* rgba8, int w, int h, int premultiply, const float* lut,
+                                 float* out, size_t cap, int* power) {
+    const int p = texture_power(w, h);
+    const size_t n = (size_t)w * h;
+    if (cap < (p >= 0 ? 2 * n : n)) return -1;
+    for (size_t i = 0; i < n; ++i) {
+        const uint8_t* c = rgba8 + 4 * i;
+        float* d = out + 4 * i;
+        d[0] = lut[c[0]];
+        d[1] = lut[c[1]];
+        d[2] = lut[c[2]];
+        d[3] = (float)c[3] / 255.0f;
+        if (premultiply) { d[0] *= d[3]; d[1] *= d[3]; d[2] *= d[3]; }
+    }
+    if (p >= 0) make_mipmap(out, w, p);
+    if (power) *power = p;
+    return 0;
+}
+
+int rsroracle_texture_mipmap(float* texels, int w, int h, size_t cap, int* power) {
+    const int p = texture_power(w, h);
+    if (power) *power = p;
+    if (p < 0) return 0;
+    if (cap < 2 * (size_t)w * h) return -1;
+    make_mipmap(texels, w, p);
+    return 0;
+}

@@ -170,6 +170,11 @@ SYMBOLS = {
                             ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_int,
                             ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
                            ctypes.c_int),
+    "rsrgpu_texture_from_rgba8": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p],
+                                  ctypes.c_int),
+    "rsrgpu_texture_mipmap": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_size_t,
+                               ctypes.POINTER(ctypes.c_int), ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_mlp_forward": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                             ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_mlp_grad": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,

@@ -55,6 +55,10 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
                                  const uint8_t* srgb_lut, int* error, int* counters, void* scratch,
                                  int num_sms, cudaStream_t st);
 size_t learned_scratch_bytes(int tiles);
+int texture_power(int width, int height);
+cudaError_t launch_texture_chain(float* tex, const uint8_t* rgba8, int w, int premultiply, cudaStream_t st);
+cudaError_t launch_rgba8_to_float(const uint8_t* rgba8, float* out, size_t n, int premultiply, int num_sms,
+                                  cudaStream_t st);
 
 static const uint32_t kRcpTable[2048] = {
 #include "rcpps_table.inc"
@@ -1185,6 +1189,42 @@ int check_device_input(rsrgpu_ctx* ctx, const void* p, size_t need, size_t align
     return 0;
 }
 }  // namespace
+
+int rsrgpu_texture_from_rgba8(rsrgpu_ctx* ctx, const uint8_t* rgba8, int width, int height, int premultiply,
+                              float* texels, size_t texel_capacity, int* power, void* stream) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (width <= 0 || height <= 0) return fail(ctx, RSRGPU_EINVAL, "texture of %dx%d pixels", width, height);
+    const int p = texture_power(width, height);
+    const size_t npx = size_t(width) * size_t(height);
+    const size_t need = p >= 0 ? 2 * npx : npx;
+    if (texel_capacity < need) return fail(ctx, RSRGPU_EINVAL, "texture needs %zu texels, room for %zu", need, texel_capacity);
+    int rc = check_device_input(ctx, rgba8, npx * 4, 4, "RGBA8 pixels");
+    if (rc == 0) rc = check_device_input(ctx, texels, need * 16, 16, "texels");
+    if (rc) return rc;
+    if (ctx->num_sms == 0)
+        CK(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    if (p >= 0) CK(launch_texture_chain(texels, rgba8, width, premultiply, st), "mip_block_kernel");
+    else CK(launch_rgba8_to_float(rgba8, texels, npx, premultiply, ctx->num_sms, st), "rgba8_to_float_kernel");
+    if (power) *power = p;
+    return 0;
+}
+
+int rsrgpu_texture_mipmap(rsrgpu_ctx* ctx, float* texels, int width, int height, size_t texel_capacity,
+                          int* power, void* stream) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (width <= 0 || height <= 0) return fail(ctx, RSRGPU_EINVAL, "texture of %dx%d pixels", width, height);
+    const int p = texture_power(width, height);
+    if (power) *power = p;
+    if (p < 0) return 0;   // no chain: the texture stays as it is
+    const size_t need = 2 * size_t(width) * size_t(height);
+    if (texel_capacity < need) return fail(ctx, RSRGPU_EINVAL, "the mip chain needs %zu texels, room for %zu", need, texel_capacity);
+    int rc = check_device_input(ctx, texels, need * 16, 16, "texels");
+    if (rc) return rc;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_texture_chain(texels, nullptr, width, 0, st), "mip_block_kernel");
+    return 0;
+}
 
 int rsrgpu_mlp_forward(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const uint16_t* features, int n,
                        float* out, void* stream) {

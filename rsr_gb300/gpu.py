@@ -130,6 +130,25 @@ class GPU:
                                      shape=(max(1, n.value) * 20,))
         return flat[:n.value * 20].reshape(n.value, 20).copy()
 
+    def texture_from_rgba8(self, rgba8, width, height, texels, premultiply=False, stream=None):
+        """rsrgpu_texture_from_rgba8: device RGBA8 pixels -> device float texels
+        (with rsr's mip chain when square, a power of two and at most 4096);
+        returns Texture::pow.  texels: a device tensor of float32."""
+        p = ctypes.c_int(0)
+        self._check(self.lib.rsrgpu_texture_from_rgba8(self.ctx, ctypes.c_void_p(rgba8.data_ptr()), int(width),
+                                                       int(height), 1 if premultiply else 0,
+                                                       ctypes.c_void_p(texels.data_ptr()), texels.numel() // 4,
+                                                       ctypes.byref(p), ctypes.c_void_p(stream) if stream else None))
+        return p.value
+
+    def texture_mipmap(self, texels, width, height, stream=None):
+        """rsrgpu_texture_mipmap on a device float texture; returns Texture::pow."""
+        p = ctypes.c_int(0)
+        self._check(self.lib.rsrgpu_texture_mipmap(self.ctx, ctypes.c_void_p(texels.data_ptr()), int(width), int(height),
+                                                   texels.numel() // 4, ctypes.byref(p),
+                                                   ctypes.c_void_p(stream) if stream else None))
+        return p.value
+
     def shade_plain(self, gbuf, width, height, ivp, eye, lights, background=(0.0, 0.0, 0.0),
                     out_srgb=None, out_linear=None, stream=None):
         """Deferred plain shading (include/rsrgpu.h rsrgpu_shade_plain); device tensors."""

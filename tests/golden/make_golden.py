@@ -1,11 +1,15 @@
-"""Generates tests/golden/frames.json from rsr's own CPU rasteriser.
+"""Generates tests/golden/frames.json and tests/golden/textures.json from
+rsr's own CPU code.
 
 Runs oracle/_ref/librsrref.so (rsr's sources built by oracle/ref/Makefile,
 x86-64 only) on the seeded scenes of GOLDEN_SCENES and records, per scene
 and gamma setting, SHA-256 digests of the sRGB8/linear colour buffer, the fp32
 depth buffer, the canonical per-tile command streams, and the clipped vertex
-buffer (coordinates + the program's varyings).  The oracle is checked
-against these digests on every machine, including ones without the
+buffer (coordinates + the program's varyings); the frames with float colour
+stores (FLOAT_STORE_SCENES) record every output.  textures.json holds the
+digests of textures built by rsr's image-loader path (TEXTURE_CASES: the
+sRGB8 decode of PNGToTexture and Texture::maybe_make_mipmap).  The oracle is
+checked against these digests on every machine, including ones without the
 reference.
 
     python tests/golden/make_golden.py
@@ -59,6 +63,30 @@ def render_float_store(renderer, sc, gamma):
     return out
 
 
+# textures built the way rsr's image loader builds them (PNGToTexture's
+# conversion, Texture::maybe_make_mipmap): name -> (edge x, edge y, premultiply, seed)
+TEXTURE_CASES = {
+    "tex_1": (1, 1, 0, 1),
+    "tex_2_premul": (2, 2, 1, 2),
+    "tex_32": (32, 32, 0, 3),
+    "tex_64_premul": (64, 64, 1, 4),
+    "tex_512": (512, 512, 0, 5),
+    "tex_128x64_nochain": (128, 64, 1, 6),
+    "tex_48_nochain": (48, 48, 0, 7),
+}
+
+
+def texture_bytes(w, h, seed):
+    """Seeded RGBA8 pixels (splitmix64 uniforms scaled to bytes)."""
+    u = scenes.uniform01(seed * 7 + 1000, w * h * 4)
+    return np.minimum((u * np.float32(256.0)).astype(np.int32), 255).astype(np.uint8)
+
+
+def texture_digest(texels, power):
+    return {"texels": digest(np.ascontiguousarray(texels).view(np.uint32).tobytes()), "power": int(power),
+            "count": int(texels.shape[0])}
+
+
 def make_scene(name):
     fn, kw, _ = GOLDEN_SCENES[name]
     kw = dict(kw)
@@ -101,6 +129,13 @@ def main():
             print(name, gamma)
     with open(os.path.join(HERE, "frames.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
+    tex = {}
+    for name, (w, h, pm, seed) in TEXTURE_CASES.items():
+        texels, power = ref.texture_from_rgba8(texture_bytes(w, h, seed), w, h, pm)
+        tex[name] = texture_digest(texels, power)
+        print(name, power)
+    with open(os.path.join(HERE, "textures.json"), "w") as f:
+        json.dump(tex, f, indent=1, sort_keys=True)
 
 
 if __name__ == "__main__":

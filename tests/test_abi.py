@@ -36,7 +36,8 @@ def test_struct_layouts_match_header(tmp_path):
     """ctypes mirrors agree with the C compiler on sizes and field offsets."""
     import subprocess
     structs = {"rsrgpu_texture_state": abi.TextureState, "rsrgpu_glstate": abi.GLStateC,
-               "rsrgpu_truecolor_canvas": abi.TrueColorCanvasC,
+               "rsrgpu_truecolor_canvas": abi.TrueColorCanvasC, "rsrgpu_fp_canvas": abi.FloatCanvasC,
+               "rsrgpu_qfloat4_canvas": abi.FloatCanvasC,
                "rsrgpu_clipped_vertex": abi.ClippedVertexC, "rsrgpu_stats": abi.StatsC}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rsrgpu.h"', "int main(void) {"]
     for cname, py in structs.items():
