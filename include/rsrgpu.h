@@ -326,6 +326,38 @@ int rsrgpu_texture_from_rgba8(rsrgpu_ctx* ctx, const uint8_t* rgba8, int width, 
 int rsrgpu_texture_mipmap(rsrgpu_ctx* ctx, float* texels, int width, int height, size_t texel_capacity,
                           int* power, void* stream);
 
+/* ---- post-processing of float canvases (rsr's $kawase and $glow nodes) ----
+ * Device pointers; enqueued on `stream` (NULL = the context's stream).
+ *
+ * KawaseBlurFilter (src/rgl/rglr/rglr_kawase.cxx:22-84) over the whole
+ * canvas: dst(x, y) = (((+0 + S(x-d-1, y-d-1)) + S(x+d, y-d-1)) + S(x-d-1, y+d))
+ * + S(x+d, y+d), times 1/16, per channel (RGBA), where S(u, v) is the box sum
+ * ((p(u,v) + p(u+1,v)) + p(u,v+1)) + p(u+1,v+1) of source pixels with
+ * coordinates clamped to the source.  src and dst are float canvases of the
+ * same size (16-byte aligned, stride >= width) that do not overlap. */
+int rsrgpu_kawase_blur(rsrgpu_ctx* ctx, const rsrgpu_fp_canvas* src, const rsrgpu_fp_canvas* dst, int dist,
+                       void* stream);
+
+/* The $kawase node's chain (src/viewer/node/kawase.cxx:79-117): `intensity`
+ * passes with distances 0, 1, ..., the first from src into tmp_a, then
+ * alternating tmp_a -> tmp_b -> tmp_a ...  *result (may be NULL) names the
+ * canvas holding the result: 0 src (intensity 0), 1 tmp_a, 2 tmp_b. */
+int rsrgpu_kawase_chain(rsrgpu_ctx* ctx, const rsrgpu_fp_canvas* src, const rsrgpu_fp_canvas* tmp_a,
+                        const rsrgpu_fp_canvas* tmp_b, int intensity, int* result, void* stream);
+
+/* The $glow node's resolve, rglr::Filter<GlowShader, sRGB|LinearColor>
+ * (src/rgl/rglr/rglr_algorithm.hxx:107-144, shader src/viewer/node/
+ * glow.cxx:24-36): per output pixel (image + blur * 0.7) * 0.5 per channel,
+ * image the pixel's lane of the full-size quads canvas (x, y, z), blur the
+ * half-size canvas pixel under its quad; packed to 0x00RRGGBB with the
+ * sRGB8 encoder of the TrueColor stores (srgb != 0: within 1/255 of rsr's
+ * table encoder) or to_tc_basic's truncation (srgb == 0: bit-exact).  The
+ * image is width x height (width a multiple of 4, height of 2), the blur
+ * canvas at least width/2 x height/2, the output width x height with an
+ * even stride. */
+int rsrgpu_glow(rsrgpu_ctx* ctx, const rsrgpu_qfloat4_canvas* image, const rsrgpu_fp_canvas* blur,
+                const rsrgpu_truecolor_canvas* out, int srgb, void* stream);
+
 /* ---- deferred shading (extension; no counterpart in rsr) ----
  * Plain multi-light Blinn-Phong over a G-buffer: for each pixel with albedo
  * != 0, world position from depth through inv_view_proj (column-major), then

@@ -171,6 +171,36 @@ class CpuRenderer:
             raise RuntimeError("%s mipmap failed: %d" % (self.which, rc))
         return out[:2 * n if power.value >= 0 else n].copy(), power.value
 
+    def kawase(self, src, d, out=None):
+        """KawaseBlurFilter over a whole RGBA float canvas src (h, w, 4);
+        returns the blurred canvas (same size)."""
+        src = np.ascontiguousarray(src, np.float32)
+        h, w = src.shape[:2]
+        dst = np.zeros_like(src) if out is None else out
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        rc = getattr(self.lib, self.prefix + "_kawase")(vp(src), w, h, w, vp(dst), w, h, w, int(d))
+        if rc != 0:
+            raise RuntimeError("%s kawase failed: %d" % (self.which, rc))
+        return dst
+
+    def glow(self, quads, blur, width, height, srgb):
+        """Filter<GlowShader> of a full-size quads canvas ((h/2, w/2, 16)
+        floats) and a half-size RGBA blur canvas ((h/2, w/2, 4)); returns the
+        0x00RRGGBB pixels (h*w,) uint32."""
+        quads = np.ascontiguousarray(quads, np.float32)
+        blur = np.ascontiguousarray(blur, np.float32)
+        out = np.zeros(width * height, np.uint32)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        bh, bw = blur.shape[:2]
+        if self.which == "ref":
+            rc = self.lib.rsrref_glow(vp(quads), width // 2, vp(blur), bw, bh, bw, vp(out), width, width, height,
+                                      int(srgb))
+        else:
+            rc = self.lib.rsroracle_glow(vp(quads), width // 2, vp(blur), bw, vp(out), width, width, height, int(srgb))
+        if rc != 0:
+            raise RuntimeError("%s glow failed: %d" % (self.which, rc))
+        return out
+
     def tiles(self):
         need = ctypes.c_size_t(0)
         fn = getattr(self.lib, self.prefix + "_dump_tiles")

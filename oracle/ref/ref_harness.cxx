@@ -21,6 +21,9 @@
 #include "src/rgl/rglr/rglr_canvas.hxx"
 #include "src/rgl/rglr/rglr_fragmentcursor.hxx"
 #include "src/rgl/rglr/rglr_texture.hxx"
+#include "src/rgl/rglr/rglr_algorithm.hxx"
+#include "src/rgl/rglr/rglr_canvas_util.hxx"
+#include "src/rgl/rglr/rglr_kawase.hxx"
 #include "src/rgl/rglv/rglv_gl.hxx"
 #include "src/rgl/rglv/rglv_gpu.hxx"
 #include "src/rgl/rglv/rglv_gpu_impl.hxx"
@@ -92,6 +95,19 @@ struct GouraudProgram final : public rglv::BaseProgram {
 
 	static rmlv::qfloat3 ShadeCanvas(const UniformsMD&, const rmlv::qfloat2, const rmlv::qfloat3 source) {
 		return source; } };
+
+
+// The $glow node's shader (src/viewer/node/glow.cxx:24-36), which rsr keeps
+// in an unnamed namespace of the viewer: (image + blur * 0.7) * 0.5.
+struct GlowShader {
+	static rmlv::qfloat3 ShadeCanvas(rmlv::qfloat2, rmlv::qfloat3 c1, rmlv::qfloat3 c2) {
+		auto& image = c1;
+		auto& blur = c2;
+		const rmlv::qfloat blurAmt{ 0.700F };
+		const rmlv::qfloat brightness{ 0.5F };
+		rmlv::qfloat3 out;
+		out = (image + blur*blurAmt) * brightness;
+		return out; } };
 
 
 // Subclass that exposes the protected tile streams and clipped vertices of
@@ -402,6 +418,27 @@ int rsrref_texture_mipmap(float* texels, int w, int h, size_t cap, int* power) {
 	if (!tex.mipmap) return 0;
 	if (cap < tex.buf.size()) return -1;
 	std::memcpy(texels, tex.buf.data(), tex.buf.size() * sizeof(PixelToaster::FloatingPointPixel));
+	return 0; }
+
+// rsr's own KawaseBlurFilter over the whole destination (one job's rows).
+int rsrref_kawase(const float* src, int sw, int sh, int sstride, float* dst, int dw, int dh, int dstride, int d) {
+	using PT = PixelToaster::FloatingPointPixel;
+	const rglr::FloatingPointCanvas s(reinterpret_cast<PT*>(const_cast<float*>(src)), sw, sh, sstride);
+	rglr::FloatingPointCanvas o(reinterpret_cast<PT*>(dst), dw, dh, dstride);
+	rglr::KawaseBlurFilter(s, o, d, 0, dh);
+	return 0; }
+
+// rsr's own rglr::Filter template with the $glow node's shader (restated as
+// harness::GlowShader; the node's copy sits in an unnamed namespace).
+int rsrref_glow(const float* image, int istride, const float* blur, int bw, int bh, int bstride, uint32_t* out,
+                int ostride, int w, int h, int srgb) {
+	using PT = PixelToaster::FloatingPointPixel;
+	const rglr::QFloat4Canvas src1(w, h, reinterpret_cast<rmlv::qfloat4*>(const_cast<float*>(image)), istride);
+	const rglr::FloatingPointCanvas src2(reinterpret_cast<PT*>(const_cast<float*>(blur)), bw, bh, bstride);
+	rglr::TrueColorCanvas dst(reinterpret_cast<PixelToaster::TrueColorPixel*>(out), w, h, ostride);
+	const rmlg::irect rect{ { 0, 0 }, { w, h } };
+	if (srgb) rglr::Filter<harness::GlowShader, rglr::sRGB>(src1, src2, dst, rect);
+	else rglr::Filter<harness::GlowShader, rglr::LinearColor>(src1, src2, dst, rect);
 	return 0; }
 
 }  // extern "C"

@@ -1549,3 +1549,62 @@ int rsroracle_texture_mipmap(float* texels, int w, int h, size_t cap, int* power
     make_mipmap(texels, w, p);
     return 0;
 }
+
+
+/* ======================================================================
+ * post-processing of float canvases (test infrastructure: the oracle of
+ * rsrgpu_kawase_blur / rsrgpu_glow)
+ * ====================================================================== */
+
+/* KawaseBlurFilter (src/rgl/rglr/rglr_kawase.cxx:22-84): per output pixel the
+   four 2x2 boxes at offsets (-d-1,-d-1) (d,-d-1) (-d-1,d) (d,d), each summed
+   ((p00 + p10) + p01) + p11 with clamped coordinates, added in that order onto
+   a zero accumulator, times 1/16.  Canvases are RGBA float, strides in pixels. */
+int rsroracle_kawase(const float* src, int sw, int sh, int sstride, float* dst, int dw, int dh, int dstride, int d) {
+    const int ox[4] = { -d - 1, d, -d - 1, d };
+    const int oy[4] = { -d - 1, -d - 1, d, d };
+    for (int y = 0; y < dh; ++y) {
+        for (int x = 0; x < dw; ++x) {
+            float ax[4] = { 0.0f, 0.0f, 0.0f, 0.0f };
+            for (int k = 0; k < 4; ++k) {
+                const int bx = x + ox[k], by = y + oy[k];
+                const int x0 = iclamp(bx, 0, sw - 1), x1 = iclamp(bx + 1, 0, sw - 1);
+                const int y0 = iclamp(by, 0, sh - 1), y1 = iclamp(by + 1, 0, sh - 1);
+                const float* p00 = src + ((size_t)y0 * sstride + x0) * 4;
+                const float* p10 = src + ((size_t)y0 * sstride + x1) * 4;
+                const float* p01 = src + ((size_t)y1 * sstride + x0) * 4;
+                const float* p11 = src + ((size_t)y1 * sstride + x1) * 4;
+                for (int c = 0; c < 4; ++c) ax[c] = ax[c] + (((p00[c] + p10[c]) + p01[c]) + p11[c]);
+            }
+            float* o = dst + ((size_t)y * dstride + x) * 4;
+            for (int c = 0; c < 4; ++c) o[c] = ax[c] * (1.0f / 16.0f);
+        }
+    }
+    return 0;
+}
+
+/* rglr::Filter<GlowShader, sRGB|LinearColor> (src/rgl/rglr/rglr_algorithm.hxx:
+   107-144) with the $glow node's shader (src/viewer/node/glow.cxx:24-36):
+   (image + blur * 0.7) * 0.5 per channel; image = the pixel's lane of the
+   full-size quads canvas (16 floats per quad: x[4] y[4] z[4] w[4]), blur = the
+   half-size RGBA pixel under the quad; packed like the TrueColor store
+   (srgb: the reference encoder's golden table, else to_tc_basic). */
+int rsroracle_glow(const float* image, int istride, const float* blur, int bstride, uint32_t* out, int ostride,
+                   int w, int h, int srgb) {
+    if (srgb && !g_session.srgb_lut) return RSRGPU_EINVAL;
+    for (int y = 0; y < h; y += 2) {
+        for (int x = 0; x < w; x += 2) {
+            const float* q = image + ((size_t)(y / 2) * istride + x / 2) * 16;
+            const float* b = blur + ((size_t)(y / 2) * bstride + x / 2) * 4;
+            for (int l = 0; l < 4; ++l) {
+                float c[3];
+                for (int k = 0; k < 3; ++k) c[k] = (q[4 * k + l] + b[k] * 0.700f) * 0.5f;
+                uint32_t px;
+                if (srgb) px = ((uint32_t)srgb8(g_session.srgb_lut, c[0]) << 16) | ((uint32_t)srgb8(g_session.srgb_lut, c[1]) << 8) | srgb8(g_session.srgb_lut, c[2]);
+                else px = ((uint32_t)basic8(c[0]) << 16) | ((uint32_t)basic8(c[1]) << 8) | (uint32_t)basic8(c[2]);
+                out[(size_t)(y + (l >> 1)) * ostride + x + (l & 1)] = px;
+            }
+        }
+    }
+    return 0;
+}

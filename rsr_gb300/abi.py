@@ -175,6 +175,13 @@ SYMBOLS = {
                                   ctypes.c_int),
     "rsrgpu_texture_mipmap": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_size_t,
                                ctypes.POINTER(ctypes.c_int), ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_kawase_blur": ([ctypes.c_void_p, ctypes.POINTER(FloatCanvasC), ctypes.POINTER(FloatCanvasC), ctypes.c_int,
+                            ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_kawase_chain": ([ctypes.c_void_p, ctypes.POINTER(FloatCanvasC), ctypes.POINTER(FloatCanvasC),
+                             ctypes.POINTER(FloatCanvasC), ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p],
+                            ctypes.c_int),
+    "rsrgpu_glow": ([ctypes.c_void_p, ctypes.POINTER(FloatCanvasC), ctypes.POINTER(FloatCanvasC),
+                     ctypes.POINTER(TrueColorCanvasC), ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_mlp_forward": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                             ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_mlp_grad": ([ctypes.c_void_p, ctypes.POINTER(MlpC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,

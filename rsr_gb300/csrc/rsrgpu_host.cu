@@ -56,6 +56,13 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
                                  int num_sms, cudaStream_t st);
 size_t learned_scratch_bytes(int tiles);
 int texture_power(int width, int height);
+struct FloatCanvasView {
+    float4* data;
+    int width, height, stride;
+};
+cudaError_t launch_kawase(const FloatCanvasView& src, const FloatCanvasView& dst, int dist, cudaStream_t st);
+cudaError_t launch_glow(const FloatCanvasView& image, const FloatCanvasView& blur, uint32_t* out, int ostride,
+                        int width, int height, const uint8_t* srgb_lut, cudaStream_t st);
 cudaError_t launch_texture_chain(float* tex, const uint8_t* rgba8, int w, int premultiply, cudaStream_t st);
 cudaError_t launch_rgba8_to_float(const uint8_t* rgba8, float* out, size_t n, int premultiply, int num_sms,
                                   cudaStream_t st);
@@ -1223,6 +1230,86 @@ int rsrgpu_texture_mipmap(rsrgpu_ctx* ctx, float* texels, int width, int height,
     if (rc) return rc;
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
     CK(launch_texture_chain(texels, nullptr, width, 0, st), "mip_block_kernel");
+    return 0;
+}
+
+namespace {
+// a float canvas of device memory: width x height pixels of `unit` bytes,
+// stride >= width, 16-byte aligned
+int float_canvas(rsrgpu_ctx* ctx, const rsrgpu_fp_canvas* c, size_t unit, const char* what, FloatCanvasView& v) {
+    if (c == nullptr || c->data == nullptr || c->width <= 0 || c->height <= 0 || c->stride < c->width)
+        return fail(ctx, RSRGPU_EINVAL, "%s: canvas needs data, a positive size and stride >= width", what);
+    const size_t bytes = ((size_t(c->height) - 1) * size_t(c->stride) + size_t(c->width)) * unit;
+    int rc = check_device_input(ctx, c->data, bytes, 16, what);
+    if (rc) return rc;
+    v.data = reinterpret_cast<float4*>(c->data);
+    v.width = c->width; v.height = c->height; v.stride = c->stride;
+    return 0;
+}
+size_t canvas_end(const FloatCanvasView& v, size_t unit) {
+    return reinterpret_cast<uintptr_t>(v.data) + ((size_t(v.height) - 1) * size_t(v.stride) + size_t(v.width)) * unit;
+}
+bool canvases_overlap(const FloatCanvasView& a, const FloatCanvasView& b) {
+    return reinterpret_cast<uintptr_t>(a.data) < canvas_end(b, 16) && reinterpret_cast<uintptr_t>(b.data) < canvas_end(a, 16);
+}
+}  // namespace
+
+int rsrgpu_kawase_blur(rsrgpu_ctx* ctx, const rsrgpu_fp_canvas* src, const rsrgpu_fp_canvas* dst, int dist, void* stream) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (dist < 0 || dist > (1 << 20)) return fail(ctx, RSRGPU_EINVAL, "kawase distance %d: 0 .. 2^20", dist);
+    FloatCanvasView s{}, d{};
+    int rc = float_canvas(ctx, src, 16, "kawase source", s);
+    if (rc == 0) rc = float_canvas(ctx, dst, 16, "kawase destination", d);
+    if (rc) return rc;
+    if (s.width != d.width || s.height != d.height)
+        return fail(ctx, RSRGPU_EINVAL, "kawase canvases differ in size (%dx%d, %dx%d)", s.width, s.height, d.width, d.height);
+    if (canvases_overlap(s, d)) return fail(ctx, RSRGPU_EINVAL, "kawase source and destination overlap");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_kawase(s, d, dist, st), "kawase_kernel");
+    return 0;
+}
+
+int rsrgpu_kawase_chain(rsrgpu_ctx* ctx, const rsrgpu_fp_canvas* src, const rsrgpu_fp_canvas* tmp_a,
+                        const rsrgpu_fp_canvas* tmp_b, int intensity, int* result, void* stream) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (intensity < 0 || intensity > 64) return fail(ctx, RSRGPU_EINVAL, "kawase intensity %d: 0 .. 64", intensity);
+    if (result) *result = 0;
+    if (intensity == 0) return 0;
+    // pass k blurs with distance k: src -> a, a -> b, b -> a, ...
+    const rsrgpu_fp_canvas* from = src;
+    const rsrgpu_fp_canvas* to = tmp_a;
+    for (int k = 0; k < intensity; ++k) {
+        int rc = rsrgpu_kawase_blur(ctx, from, to, k, stream);
+        if (rc) return rc;
+        from = to;
+        to = (to == tmp_a) ? tmp_b : tmp_a;
+    }
+    if (result) *result = (from == tmp_a) ? 1 : 2;
+    return 0;
+}
+
+int rsrgpu_glow(rsrgpu_ctx* ctx, const rsrgpu_qfloat4_canvas* image, const rsrgpu_fp_canvas* blur,
+                const rsrgpu_truecolor_canvas* out, int srgb, void* stream) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (image == nullptr || out == nullptr) return fail(ctx, RSRGPU_EINVAL, "glow needs an image and an output");
+    const int w = image->width, h = image->height;
+    if (w <= 0 || h <= 0 || (w & 3) || (h & 1))
+        return fail(ctx, RSRGPU_EINVAL, "glow image %dx%d: width a multiple of 4, height of 2", w, h);
+    // the quads canvas: (h/2) rows of (w/2) 64-byte quads
+    rsrgpu_fp_canvas iq{ image->data, w / 2, h / 2, image->stride, 0 };
+    FloatCanvasView iv{}, bv{};
+    int rc = float_canvas(ctx, &iq, 64, "glow image", iv);
+    if (rc == 0) rc = float_canvas(ctx, blur, 16, "glow blur", bv);
+    if (rc) return rc;
+    if (bv.width < w / 2 || bv.height < h / 2)
+        return fail(ctx, RSRGPU_EINVAL, "glow blur canvas %dx%d is smaller than %dx%d", bv.width, bv.height, w / 2, h / 2);
+    if (out->width != w || out->height != h || out->stride < w || (out->stride & 1))
+        return fail(ctx, RSRGPU_EINVAL, "glow output must be %dx%d with an even stride >= width", w, h);
+    const size_t obytes = ((size_t(h) - 1) * size_t(out->stride) + size_t(w)) * 4;
+    rc = check_device_input(ctx, out->data, obytes, 8, "glow output");
+    if (rc) return rc;
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    CK(launch_glow(iv, bv, out->data, out->stride, w, h, srgb ? ctx->d_srgb.as<uint8_t>() : nullptr, st), "glow_kernel");
     return 0;
 }
 

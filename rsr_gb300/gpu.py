@@ -149,6 +149,36 @@ class GPU:
                                                    ctypes.c_void_p(stream) if stream else None))
         return p.value
 
+    @staticmethod
+    def _canvas(t, width, height, stride=None):
+        return abi.FloatCanvasC(t.data_ptr(), int(width), int(height), int(stride or width), 0)
+
+    def kawase_blur(self, src, dst, width, height, dist, stream=None):
+        """rsrgpu_kawase_blur: one KawaseBlurFilter pass between two device RGBA
+        float canvases (tensors of width*height*4 float32)."""
+        a, b = self._canvas(src, width, height), self._canvas(dst, width, height)
+        self._check(self.lib.rsrgpu_kawase_blur(self.ctx, ctypes.byref(a), ctypes.byref(b), int(dist),
+                                                ctypes.c_void_p(stream) if stream else None))
+
+    def kawase_chain(self, src, tmp_a, tmp_b, width, height, intensity, stream=None):
+        """rsrgpu_kawase_chain (the $kawase node); returns the tensor holding the result."""
+        cs = [self._canvas(t, width, height) for t in (src, tmp_a, tmp_b)]
+        r = ctypes.c_int(-1)
+        self._check(self.lib.rsrgpu_kawase_chain(self.ctx, ctypes.byref(cs[0]), ctypes.byref(cs[1]), ctypes.byref(cs[2]),
+                                                 int(intensity), ctypes.byref(r),
+                                                 ctypes.c_void_p(stream) if stream else None))
+        return (src, tmp_a, tmp_b)[r.value]
+
+    def glow(self, quads, blur, out, width, height, srgb=True, blur_size=None, stream=None):
+        """rsrgpu_glow: full-size quads canvas + half-size blur canvas -> 0x00RRGGBB
+        (device tensors; blur_size (w, h) defaults to half the image)."""
+        bw, bh = blur_size or (width // 2, height // 2)
+        q = self._canvas(quads, width, height, width // 2)
+        b = self._canvas(blur, bw, bh)
+        o = abi.TrueColorCanvasC(out.data_ptr(), int(width), int(height), int(width), 0)
+        self._check(self.lib.rsrgpu_glow(self.ctx, ctypes.byref(q), ctypes.byref(b), ctypes.byref(o), 1 if srgb else 0,
+                                         ctypes.c_void_p(stream) if stream else None))
+
     def shade_plain(self, gbuf, width, height, ivp, eye, lights, background=(0.0, 0.0, 0.0),
                     out_srgb=None, out_linear=None, stream=None):
         """Deferred plain shading (include/rsrgpu.h rsrgpu_shade_plain); device tensors."""

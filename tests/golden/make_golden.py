@@ -1,4 +1,4 @@
-"""Generates tests/golden/frames.json and tests/golden/textures.json from
+"""Generates tests/golden/frames.json, textures.json and postfx.json from
 rsr's own CPU code.
 
 Runs oracle/_ref/librsrref.so (rsr's sources built by oracle/ref/Makefile,
@@ -8,7 +8,9 @@ depth buffer, the canonical per-tile command streams, and the clipped vertex
 buffer (coordinates + the program's varyings); the frames with float colour
 stores (FLOAT_STORE_SCENES) record every output.  textures.json holds the
 digests of textures built by rsr's image-loader path (TEXTURE_CASES: the
-sRGB8 decode of PNGToTexture and Texture::maybe_make_mipmap).  The oracle is
+sRGB8 decode of PNGToTexture and Texture::maybe_make_mipmap), postfx.json
+those of KawaseBlurFilter and Filter<GlowShader> on seeded canvases
+(POSTFX_CASES).  The oracle is
 checked against these digests on every machine, including ones without the
 reference.
 
@@ -87,6 +89,36 @@ def texture_digest(texels, power):
             "count": int(texels.shape[0])}
 
 
+# post-processing of seeded float canvases by rsr's KawaseBlurFilter and
+# Filter<GlowShader>: name -> (kind, width, height, distance or sRGB flag, seed)
+POSTFX_CASES = {
+    "kawase_2x2_d0": ("kawase", 2, 2, 0, 1),
+    "kawase_61x37_d1": ("kawase", 61, 37, 1, 2),
+    "kawase_160x90_d3": ("kawase", 160, 90, 3, 3),
+    "kawase_96x54_d30": ("kawase", 96, 54, 30, 4),
+    "glow_64x36_linear": ("glow", 64, 36, 0, 5),
+    "glow_320x180_srgb": ("glow", 320, 180, 1, 6),
+}
+
+
+def postfx_inputs(kind, w, h, seed):
+    """Seeded canvases: kawase an RGBA float (h, w, 4) source in [-1, 3);
+    glow a quads canvas (h/2, w/2, 16) in [0, 1.5) and a blur (h/2, w/2, 4) in [0, 1.2)."""
+    if kind == "kawase":
+        return (scenes.uniform01(seed * 11 + 2000, h * w * 4).reshape(h, w, 4) * np.float32(4.0) - np.float32(1.0),)
+    q = scenes.uniform01(seed * 11 + 3000, (h // 2) * (w // 2) * 16).reshape(h // 2, w // 2, 16) * np.float32(1.5)
+    b = scenes.uniform01(seed * 11 + 4000, (h // 2) * (w // 2) * 4).reshape(h // 2, w // 2, 4) * np.float32(1.2)
+    return q, b
+
+
+def run_postfx(renderer, name):
+    kind, w, h, arg, seed = POSTFX_CASES[name]
+    ins = postfx_inputs(kind, w, h, seed)
+    if kind == "kawase":
+        return renderer.kawase(ins[0], arg)
+    return renderer.glow(ins[0], ins[1], w, h, arg)
+
+
 def make_scene(name):
     fn, kw, _ = GOLDEN_SCENES[name]
     kw = dict(kw)
@@ -136,6 +168,10 @@ def main():
         print(name, power)
     with open(os.path.join(HERE, "textures.json"), "w") as f:
         json.dump(tex, f, indent=1, sort_keys=True)
+    post = {name: digest(np.ascontiguousarray(run_postfx(ref, name)).view(np.uint32).tobytes())
+            for name in POSTFX_CASES}
+    with open(os.path.join(HERE, "postfx.json"), "w") as f:
+        json.dump(post, f, indent=1, sort_keys=True)
 
 
 if __name__ == "__main__":
