@@ -315,6 +315,11 @@ def run_gpu(args):
             "frames_per_s": 1e3 / ms_per_step, "e2e_frames_per_s": 1e3 * args.steps / e2e_ms,
             "gpu_launches": 3 * args.steps, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks.summary(local)}
+    if not args.no_post:
+        try:
+            line["post"] = run_post(gpu, args, stream, flush, sc, dev)
+        except Exception as e:   # the headline line is printed whatever happens here
+            line["post"] = {"error": "%s: %s" % (type(e).__name__, e)}
     if not args.no_deferred:
         line["deferred"] = run_deferred(gpu, args, stream, flush)
     if not args.no_batch:
@@ -368,6 +373,79 @@ def _time_graph(fn, steps, flush):
             evs.append((a, b))
     torch.cuda.synchronize()
     return statistics.mean(a.elapsed_time(b) for a, b in evs)
+
+
+def run_post(gpu, args, stream, flush, sc, dev):
+    """rsr's post-processing and texture paths on the device.
+      texture_upload  rsrgpu_texture_from_rgba8: RGBA8 -> linear float + rsr's
+                      stacked mip chain (1024^2 and 4096^2, seeded bytes);
+                      algorithmic bytes = the RGBA8 read + the 2*w*w float
+                      texels written
+      glow_frame      the headline frame with two more stores (full-size
+                      quads and the half-size float canvas: rsr's
+                      StoreColor(QFloat4Canvas*) and StoreColor(FloatingPointCanvas*,
+                      downsample)), then 4 Kawase passes on the 960x540 canvas
+                      and the glow resolve to sRGB8 -- the $kawase / $glow chain
+                      of rsr's viewer
+    Device times: CUDA-graph replays (post kernels) or CUDA events around a
+    run (frames), L2 flushed by a 256 MiB write before each (untimed)."""
+    import torch
+    peak, peak_kind = hbm_peak()
+    steps = max(5, min(args.steps, 20))
+    sptr = stream.cuda_stream
+    res = {"steps": steps, "peak_gbs": peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1234)
+    cases = []
+    for w in (1024, 4096):
+        px = torch.randint(0, 256, (w * w * 4,), dtype=torch.uint8, device="cuda", generator=g)
+        out = torch.empty(2 * w * w * 4, dtype=torch.float32, device="cuda")
+        ms = _time_graph(lambda sp: gpu.texture_from_rgba8(px, w, w, out, stream=sp), steps, flush)
+        nbytes = w * w * 4 + 2 * w * w * 16
+        cases.append({"edge": w, "ms": ms, "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / ms / 1e6,
+                      "frac": nbytes / ms / 1e6 / peak, "gtexels_per_s": w * w / ms / 1e6})
+        del px, out
+    res["texture_upload"] = {"kernel": "mip_block_kernel", "bound": "hbm", "cases": cases}
+    # glow frame
+    W, H = sc.width, sc.height
+    nq = (H // 2) * (W // 2)
+    col = torch.zeros(W * H, dtype=torch.int32, device="cuda")
+    dep = torch.zeros(W * H, dtype=torch.float32, device="cuda")
+    quads = torch.zeros(nq * 16, dtype=torch.float32, device="cuda")
+    half = torch.zeros(nq * 4, dtype=torch.float32, device="cuda")
+    ta = torch.zeros(nq * 4, dtype=torch.float32, device="cuda")
+    tb = torch.zeros(nq * 4, dtype=torch.float32, device="cuda")
+    out = torch.zeros(W * H, dtype=torch.int32, device="cuda")
+    gpu.Reset(W, H, sc.tile_blocks)
+    gl = sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)
+    gl.StoreColorQuads(quads, W, H)
+    gl.StoreColorFP(half, W // 2, H // 2, downsample=True)
+    gpu.submit(gl)
+    for _ in range(3):
+        gpu.run(sptr)
+        gpu.Wait()
+    frame_ms = _time_device(lambda: (gpu.run(sptr), gpu.Wait()), steps, stream, flush)
+    intensity = 4
+
+    def post(sp):
+        r = gpu.kawase_chain(half, ta, tb, W // 2, H // 2, intensity, stream=sp)
+        gpu.glow(quads, r, out, W, H, srgb=True, stream=sp)
+
+    post_ms = _time_graph(post, steps, flush)
+    kawase_ms = _time_graph(lambda sp: gpu.kawase_blur(half, ta, W // 2, H // 2, 3, stream=sp), steps, flush)
+    glow_ms = _time_graph(lambda sp: gpu.glow(quads, ta, out, W, H, srgb=True, stream=sp), steps, flush)
+    kawase_bytes = nq * 32                      # each source pixel read once, each output written once
+    glow_bytes = nq * (48 + 16) + W * H * 4     # quad colour lanes + blur pixel read, sRGB8 written
+    res["glow_frame"] = {
+        "workload": "headline frame + quads and half-size float stores, %d Kawase passes (960x540), glow to sRGB8"
+                    % intensity,
+        "frame_ms": frame_ms, "post_ms": post_ms, "frames_per_s": 1e3 / (frame_ms + post_ms),
+        "kawase": {"kernel": "kawase_kernel", "ms_per_pass": kawase_ms, "algorithmic_bytes": kawase_bytes,
+                   "achieved_gbs": kawase_bytes / kawase_ms / 1e6, "frac": kawase_bytes / kawase_ms / 1e6 / peak,
+                   "bound": "L1/L2 (16 pixel reads per output, the canvas is L2-resident)"},
+        "glow": {"kernel": "glow_kernel", "ms": glow_ms, "algorithmic_bytes": glow_bytes,
+                 "achieved_gbs": glow_bytes / glow_ms / 1e6, "frac": glow_bytes / glow_ms / 1e6 / peak, "bound": "hbm"}}
+    return res
 
 
 def run_deferred(gpu, args, stream, flush):
@@ -575,6 +653,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-deferred", action="store_true", help="skip the deferred / learned shading figures")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames figures")
+    ap.add_argument("--no-post", action="store_true", help="skip the texture-upload and glow-chain figures")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
