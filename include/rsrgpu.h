@@ -17,6 +17,12 @@
  * Every other pointer field is an address supplied by the caller:
  *   CMD_DRAW_ELEMENTS   op u8, 0x14 u8, hint u8, count i32, indices u16*
  *   CMD_DRAW_ARRAYS     op u8, count i32
+ *   CMD_DRAW_ELEMENTS_INSTANCED  op u8, 0x14 u8, count i32, indices u16*, instances i32
+ *   CMD_DRAW_ARRAYS_INSTANCED    op u8, count i32, instances i32
+ *     (the draw's triangles once per instance, instance ids 0 .. instances-1,
+ *     at most 65536; ManyProgram reads instance i's column-major mat4 from
+ *     buffer 15 at floats [16i, 16i+16) and is drawn only this way; frames with
+ *     instanced draws are not taken by batches or rsrgpu_render_static)
  *   CMD_CLEAR           op u8, bits u8
  *   CMD_STORE_COLOR_FULL_LINEAR_TC  op u8, gamma u8, rsrgpu_truecolor_canvas*
  *   CMD_STORE_DEPTH_FULL_LINEAR_FP  op u8, float* (width*height, row-major)
@@ -97,6 +103,9 @@ extern "C" {
 #define RSRGPU_PROGRAM_DEFAULT_POST  1   /* DefaultPostProgram, shaders.hxx:32 */
 #define RSRGPU_PROGRAM_EXPOSURE_POST 2   /* ExposurePostProgram, shaders.hxx:40 */
 #define RSRGPU_PROGRAM_AMY           4   /* AmyProgram (textured), shaders.hxx:69 */
+#define RSRGPU_PROGRAM_MANY          6   /* ManyProgram (instanced: per-instance matrix in buffer 15,
+                                            position 0-2, uv 9-10; colour (u, v, uniform 0)),
+                                            shaders.hxx:482-585 */
 #define RSRGPU_PROGRAM_OBJ1          7   /* OBJ1Program (lit Gouraud), shaders.hxx:586 */
 #define RSRGPU_PROGRAM_GOURAUD       90  /* test program: per-vertex rgb, no lighting */
 #define RSRGPU_PROGRAM_GBUFFER       91  /* G-buffer program: position 0-2, normal 3-5,

@@ -226,6 +226,18 @@ int Replay(rglv::GL& gl, const uint8_t* cmds, size_t n, const rsrgpu_glstate* st
 			auto count = Read<int32_t>(p);
 			gl.DrawArrays(GL_TRIANGLES, 0, count); }
 			break;
+		case CMD_DRAW_ELEMENTS_INSTANCED: {
+			Read<uint8_t>(p);  // 0x14
+			auto count = Read<int32_t>(p);
+			auto ptr = Read<const uint16_t*>(p);
+			auto ninst = Read<int32_t>(p);
+			gl.DrawElementsInstanced(GL_TRIANGLES, count, GL_UNSIGNED_SHORT, ptr, ninst); }
+			break;
+		case CMD_DRAW_ARRAYS_INSTANCED: {
+			auto count = Read<int32_t>(p);
+			auto ninst = Read<int32_t>(p);
+			gl.DrawArraysInstanced(GL_TRIANGLES, 0, count, ninst); }
+			break;
 		case CMD_STORE_COLOR_FULL_LINEAR_TC: {
 			auto gamma = Read<uint8_t>(p);
 			auto* c = Read<const rsrgpu_truecolor_canvas*>(p);
@@ -292,10 +304,12 @@ void Canonical(const uint8_t* s, std::map<const void*, uint32_t>& ordinals, std:
 			Read<const void*>(p);
 			break;
 		case CMD_DRAW_INLINE:
+		case CMD_DRAW_INLINE_INSTANCED:
 			while (true) {
 				auto w = Read<uint16_t>(p);
 				put16(w);
 				if (w == 0xffff) break;
+				if (op == CMD_DRAW_INLINE_INSTANCED) put16(Read<uint16_t>(p));
 				put16(Read<uint16_t>(p));
 				put16(Read<uint16_t>(p)); }
 			break;
@@ -328,6 +342,7 @@ int rsrref_init(int threads) {
 	harness::InstallDrawStates<harness::GouraudProgram>(gpu);
 	harness::InstallDrawStates<rqv::AmyProgram>(gpu);
 	harness::InstallDrawStates<rqv::OBJ1Program>(gpu);
+	harness::InstallDrawStates<rqv::ManyProgram>(gpu);
 	gpu.Install(harness::GouraudProgram::id, 0, rglv::GPUBltImpl<harness::GouraudProgram>::MakeBltProgramPtrs());
 	gpu.Install(rqv::DefaultPostProgram::id, 0, rglv::GPUBltImpl<rqv::DefaultPostProgram>::MakeBltProgramPtrs());
 	gpu.Install(rqv::ExposurePostProgram::id, 0, rglv::GPUBltImpl<rqv::ExposurePostProgram>::MakeBltProgramPtrs());

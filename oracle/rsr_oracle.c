@@ -108,6 +108,7 @@ static int program_nvary(int pid) {
     switch (pid) {
     case RSRGPU_PROGRAM_GOURAUD: return 3;
     case RSRGPU_PROGRAM_AMY: return 2;
+    case RSRGPU_PROGRAM_MANY: return 2;
     case RSRGPU_PROGRAM_GBUFFER: return 4;
     default: return -1;
     }
@@ -116,16 +117,26 @@ static int program_nvary(int pid) {
 /* SHADER::ShadeVertex for one vertex: gl_Position = vpm * (pos, 1) and the
  * VertexOutputSD (GouraudProgram: rgb from buffers 3-5; AmyProgram
  * shaders.hxx:127-135: uv from buffers 9-10, zero when unbound). */
-static void shade_vertex(const rsrgpu_glstate* s, const float* vpm, int idx, float pos[4], float vary[MAX_VARY]) {
+static void shade_vertex_inst(const rsrgpu_glstate* s, const float* vpm, int iid, int idx, float pos[4],
+                              float vary[MAX_VARY]) {
     float in[4];
     if (s->buffers[0]) { in[0] = s->buffers[0][idx]; in[1] = s->buffers[1][idx]; in[2] = s->buffers[2][idx]; }
     else { in[0] = in[1] = in[2] = 0.0f; }
     in[3] = 1.0f;
-    qmat_mul(vpm, in, pos);
+    if (s->program_id == RSRGPU_PROGRAM_MANY) {
+        /* ManyProgram::ShadeVertex (shaders.hxx:555-562): p1 = imat * (pos, 1),
+           gl_Position = vpm * p1; imat = instance iid's mat4 from buffer 15
+           (Loader::LoadInstance, :505-506) */
+        float p1[4];
+        qmat_mul(s->buffers[15] + (size_t)iid * 16, in, p1);
+        qmat_mul(vpm, p1, pos);
+    } else {
+        qmat_mul(vpm, in, pos);
+    }
     memset(vary, 0, sizeof(float) * MAX_VARY);
     if (s->program_id == RSRGPU_PROGRAM_GOURAUD) {
         vary[0] = s->buffers[3][idx]; vary[1] = s->buffers[4][idx]; vary[2] = s->buffers[5][idx];
-    } else if (s->program_id == RSRGPU_PROGRAM_AMY) {
+    } else if (s->program_id == RSRGPU_PROGRAM_AMY || s->program_id == RSRGPU_PROGRAM_MANY) {
         vary[0] = s->buffers[9] ? s->buffers[9][idx] : 0.0f;
         vary[1] = s->buffers[10] ? s->buffers[10][idx] : 0.0f;
     } else if (s->program_id == RSRGPU_PROGRAM_GBUFFER) {
@@ -133,6 +144,10 @@ static void shade_vertex(const rsrgpu_glstate* s, const float* vpm, int idx, flo
         vary[0] = s->buffers[3][idx]; vary[1] = s->buffers[4][idx]; vary[2] = s->buffers[5][idx];
         vary[3] = s->buffers[6][idx];
     }
+}
+
+static void shade_vertex(const rsrgpu_glstate* s, const float* vpm, int idx, float pos[4], float vary[MAX_VARY]) {
+    shade_vertex_inst(s, vpm, 0, idx, pos, vary);
 }
 
 /* ---- texture units (src/rgl/rglr/rglr_texture_sampler.cxx) ---- */
@@ -329,13 +344,19 @@ static void make_vpm(const rsrgpu_glstate* s, float vpm[16]) {  /* MakeMatrices 
 /* ======================================================================
  * binning: GPUBinImpl::BinTriangles1P/2P (rglv_gpu_impl.hxx:315-675)
  * ====================================================================== */
-typedef struct ClipEntry { int i0, i1, i2; } ClipEntry;
+typedef struct ClipEntry { int iid, i0, i1, i2; } ClipEntry;
 
 static int clip_triangles(Frame* f, const rsrgpu_glstate* s, const ClipEntry* q, int nq);
 
-static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices, int cmd_is_arrays) {
+/* BinTriangles1P/2P (rglv_gpu_impl.hxx:315-675) for `ninst` instances
+ * (instanced: CMD_DRAW_INLINE_INSTANCED records start with the instance id) */
+static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices, int cmd_is_arrays, int ninst,
+                    int instanced) {
     const rsrgpu_glstate* s = &f->states[state_idx];
     if (program_nvary(s->program_id) < 0) return RSRGPU_ENODISPATCH;
+    /* ManyProgram's vertex input includes the instance matrix, which only
+       instanced draws load (rglv_gpu_impl.hxx:364-366,561-564) */
+    if (s->program_id == RSRGPU_PROGRAM_MANY && (!instanced || !s->buffers[15])) return RSRGPU_EUNSUPPORTED;
     float vpm[16];
     make_vpm(s, vpm);
     const float factor = guard_band_factor(f->width, f->height);
@@ -358,21 +379,21 @@ static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices,
     uint32_t* cf = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)nv);
     float* dx = (float*)malloc(sizeof(float) * (size_t)nv);
     float* dy = (float*)malloc(sizeof(float) * (size_t)nv);
-    ClipEntry* q = (ClipEntry*)malloc(sizeof(ClipEntry) * (size_t)(count / 3 + 1));
+    ClipEntry* q = (ClipEntry*)malloc(sizeof(ClipEntry) * ((size_t)(count / 3) * (size_t)(ninst > 0 ? ninst : 1) + 1));
     int nq = 0;
     if (!cf || !dx || !dy || !q) { free(cf); free(dx); free(dy); free(q); return RSRGPU_EINVAL; }
+    for (int t = 0; t < f->ntiles; ++t) {
+        bb_u8(&f->tiles[t], instanced ? RSRGPU_CMD_DRAW_INLINE_INSTANCED : RSRGPU_CMD_DRAW_INLINE);
+        f->mark[t] = f->tiles[t].n;
+    }
+    for (int iid = 0; iid < ninst; ++iid) {
     for (int v = 0; v < nv; ++v) {
         float pos[4], vary[MAX_VARY];
-        shade_vertex(s, vpm, v, pos, vary);
+        shade_vertex_inst(s, vpm, iid, v, pos, vary);
         cf[v] = frustum_test(factor, pos);
         float iw = oneover(pos[3]);                       /* pdiv (rglv_math.hxx:19-23) */
         dx[v] = (pos[0] * iw) * DS[0] + DO[0];
         dy[v] = (pos[1] * iw) * DS[1] + DO[1];
-    }
-
-    for (int t = 0; t < f->ntiles; ++t) {
-        bb_u8(&f->tiles[t], RSRGPU_CMD_DRAW_INLINE);
-        f->mark[t] = f->tiles[t].n;
     }
     const int numPrims = count / 3;
     for (int pi = 0; pi < numPrims; ++pi) {
@@ -382,7 +403,7 @@ static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices,
         uint32_t c0 = cf[i0], c1 = cf[i1], c2 = cf[i2];
         int pointsOutside = (int32_t)(c0 | c1 | c2) > 0;
         int primsOutside = (int32_t)(c0 & c1 & c2) > 0;
-        if (!primsOutside && pointsOutside) { q[nq].i0 = i0; q[nq].i1 = i1; q[nq].i2 = i2; ++nq; }
+        if (!primsOutside && pointsOutside) { q[nq].iid = iid; q[nq].i0 = i0; q[nq].i1 = i1; q[nq].i2 = i2; ++nq; }
         /* rmlg::Area (rmlg_triangle.hxx:17-21) */
         float d31x = dx[i2] - dx[i0], d31y = dy[i2] - dy[i0];
         float d21x = dx[i1] - dx[i0], d21y = dy[i1] - dy[i0];
@@ -406,10 +427,12 @@ static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices,
         for (int ty = ty0; ty <= ty1; ++ty) {
             for (int tx = tx0; tx <= tx1; ++tx) {
                 ByteBuf* b = &f->tiles[ty * f->tiles_x + tx];
+                if (instanced) bb_u16(b, (uint16_t)iid);
                 bb_u16(b, (uint16_t)ni0); bb_u16(b, (uint16_t)ni1); bb_u16(b, (uint16_t)ni2);
             }
         }
     }
+    }   /* instance loop */
     for (int t = 0; t < f->ntiles; ++t) {
         if (f->tiles[t].n != f->mark[t]) bb_u16(&f->tiles[t], 0xffff);
         else f->tiles[t].n -= 1;   /* Unappend the opcode (rglv_gpu_impl.hxx:665-671) */
@@ -446,7 +469,7 @@ static int clip_triangles(Frame* f, const rsrgpu_glstate* s, const ClipEntry* q,
         const int idx[3] = { q[e].i0, q[e].i1, q[e].i2 };
         for (int i = 0; i < 3; ++i) {
             memset(&A[na], 0, sizeof(CV));
-            shade_vertex(s, vpm, idx[i], A[na].c, A[na].d);
+            shade_vertex_inst(s, vpm, q[e].iid, idx[i], A[na].c, A[na].d);
             ++na;
         }
         for (int pl = 0; pl < 5 && na > 0; ++pl) {
@@ -567,13 +590,29 @@ static int bin_frame(Frame* f, const uint8_t* cmds, size_t n) {
             RD(int32_t, count);
             RD(uint64_t, ptr);
             if (state < 0) return RSRGPU_EINVAL;
-            rc = bin_draw(f, state, count, (const uint16_t*)(uintptr_t)ptr, 0);
+            rc = bin_draw(f, state, count, (const uint16_t*)(uintptr_t)ptr, 0, 1, 0);
             if (rc) return rc;
         } break;
         case RSRGPU_CMD_DRAW_ARRAYS: {
             RD(int32_t, count);
             if (state < 0) return RSRGPU_EINVAL;
-            rc = bin_draw(f, state, count, NULL, 1);
+            rc = bin_draw(f, state, count, NULL, 1, 1, 0);
+            if (rc) return rc;
+        } break;
+        case RSRGPU_CMD_DRAW_ELEMENTS_INSTANCED: {   /* GPU::BinImpl, rglv_gpu.cxx:230-242 */
+            RD(uint8_t, flags); (void)flags;
+            RD(int32_t, count);
+            RD(uint64_t, ptr);
+            RD(int32_t, ninst);
+            if (state < 0 || ninst < 0 || ninst > 65536) return RSRGPU_EINVAL;
+            rc = bin_draw(f, state, count, (const uint16_t*)(uintptr_t)ptr, 0, ninst, 1);
+            if (rc) return rc;
+        } break;
+        case RSRGPU_CMD_DRAW_ARRAYS_INSTANCED: {     /* rglv_gpu.cxx:204-215 */
+            RD(int32_t, count);
+            RD(int32_t, ninst);
+            if (state < 0 || ninst < 0 || ninst > 65536) return RSRGPU_EINVAL;
+            rc = bin_draw(f, state, count, NULL, 1, ninst, 1);
             if (rc) return rc;
         } break;
         default:
@@ -668,6 +707,9 @@ static void render_quad(TileCtx* tc, const TriSetup* tri, int qx, int qy, const 
         float uv[4][2];
         for (int l = 0; l < 4; ++l) { uv[l][0] = attr[l][0]; uv[l][1] = attr[l][1]; }
         tex_sample(&tc->tu0, uv, frag);
+    } else if (s->program_id == RSRGPU_PROGRAM_MANY) {
+        /* ManyProgram::ShadeFragment (shaders.hxx:567-582): (u, v, magic, 1) */
+        for (int l = 0; l < 4; ++l) { frag[l][0] = attr[l][0]; frag[l][1] = attr[l][1]; frag[l][2] = s->uniforms[0]; frag[l][3] = 1.0f; }
     } else if (s->program_id == RSRGPU_PROGRAM_GBUFFER) {
         /* colour = interpolated normal, alpha = flat albedo of the record's first vertex */
         for (int l = 0; l < 4; ++l) { frag[l][0] = attr[l][0]; frag[l][1] = attr[l][1]; frag[l][2] = attr[l][2]; frag[l][3] = tri->vary[0][3]; }
@@ -787,12 +829,14 @@ static void raster_scalar(TileCtx* tc, const TriSetup* tri, int x1, int x2, int 
 
 static const uint8_t* rd_u16(const uint8_t* p, uint16_t* v) { memcpy(v, p, 2); return p + 2; }
 
-/* GPUTileImpl::DrawTriangles (rglv_gpu_impl.hxx:841-947) */
-static const uint8_t* draw_inline(TileCtx* tc, const uint8_t* p) {
+/* GPUTileImpl::DrawTriangles<INSTANCED> (rglv_gpu_impl.hxx:841-947): an
+ * instanced record is (iid, i0|bf, i1, i2) and is shaded with its instance */
+static const uint8_t* draw_inline(TileCtx* tc, const uint8_t* p, int instanced) {
     while (1) {
-        uint16_t w0, i1, i2;
+        uint16_t w0, i1, i2, iid = 0;
         p = rd_u16(p, &w0);
         if (w0 == 0xffff) break;
+        if (instanced) { iid = w0; p = rd_u16(p, &w0); }
         p = rd_u16(p, &i1);
         p = rd_u16(p, &i2);
         const int idx[3] = { w0 & 0x7fff, i1, i2 };
@@ -800,7 +844,7 @@ static const uint8_t* draw_inline(TileCtx* tc, const uint8_t* p) {
         int32_t fx[3], fy[3];
         for (int i = 0; i < 3; ++i) {
             float pos[4];
-            shade_vertex(tc->s, tc->vpm, idx[i], pos, tri.vary[i]);
+            shade_vertex_inst(tc->s, tc->vpm, iid, idx[i], pos, tri.vary[i]);
             float iw = oneover(pos[3]);
             float dvx = pos[0] * iw, dvy = pos[1] * iw;
             tri.z[i] = pos[2] * iw;
@@ -921,8 +965,9 @@ static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8
             }
         } break;
         case RSRGPU_CMD_DRAW_INLINE:
+        case RSRGPU_CMD_DRAW_INLINE_INSTANCED:
             if (!draw_dispatch_ok(tc.s)) return RSRGPU_ENODISPATCH;
-            p = draw_inline(&tc, p);
+            p = draw_inline(&tc, p, op == RSRGPU_CMD_DRAW_INLINE_INSTANCED);
             break;
         case RSRGPU_CMD_CLIPPED_TRI:
             if (!draw_dispatch_ok(tc.s)) return RSRGPU_ENODISPATCH;
@@ -1147,9 +1192,11 @@ int rsroracle_dump_tiles(uint8_t* out, size_t capacity, size_t* needed) {
             case RSRGPU_CMD_STORE_COLOR_HALF_LINEAR_FP:
             case RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP: p += 8; break;
             case RSRGPU_CMD_DRAW_INLINE:
+            case RSRGPU_CMD_DRAW_INLINE_INSTANCED:
                 while (1) {
                     uint16_t w; p = rd_u16(p, &w); bb_u16(&one, w);
                     if (w == 0xffff) break;
+                    if (op == RSRGPU_CMD_DRAW_INLINE_INSTANCED) { p = rd_u16(p, &w); bb_u16(&one, w); }
                     p = rd_u16(p, &w); bb_u16(&one, w);
                     p = rd_u16(p, &w); bb_u16(&one, w);
                 }

@@ -16,7 +16,10 @@ CMD_STATE = 1
 CMD_CLEAR = 10
 CMD_DRAW_ELEMENTS = 11
 CMD_DRAW_ARRAYS = 12
+CMD_DRAW_ELEMENTS_INSTANCED = 13
+CMD_DRAW_ARRAYS_INSTANCED = 14
 CMD_DRAW_INLINE = 15
+CMD_DRAW_INLINE_INSTANCED = 16
 CMD_STORE_COLOR_FULL_LINEAR_FP = 20
 CMD_STORE_COLOR_HALF_LINEAR_FP = 21
 CMD_STORE_COLOR_FULL_LINEAR_TC = 22
@@ -51,6 +54,7 @@ GL_LINEAR_MIPMAP_NEAREST = 1
 PROGRAM_DEFAULT_POST = 1
 PROGRAM_EXPOSURE_POST = 2
 PROGRAM_AMY = 4
+PROGRAM_MANY = 6
 PROGRAM_OBJ1 = 7
 PROGRAM_GOURAUD = 90
 PROGRAM_GBUFFER = 91

@@ -127,13 +127,15 @@ struct rsrgpu_ctx {
     std::vector<DevDraw> draws;
     std::vector<FrameOp> ops;
     std::vector<GBufferDesc> gbufs;
+    std::vector<DevInst> inst;      // per draw; uploaded when a draw is instanced
+    bool any_inst = false;
     int ntris = 0;
     bool submitted = false;
     bool ran = false;
     // device memory
     DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
         d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs,
-        d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
+        d_inst, d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
     std::map<cudaStream_t, cudaEvent_t> learn_events;   // last learned-shader launch per stream
     int num_sms = 0;
     int* h_mlp_err = nullptr;   // pinned
@@ -205,7 +207,7 @@ uint32_t fragment_state_key(const rsrgpu_glstate& s) {   // GLState::FragmentSta
     return key;
 }
 
-bool draw_program_supported(int pid) { return pid == kProgGouraud || pid == kProgAmy || pid == kProgGBuffer; }
+bool draw_program_supported(int pid) { return pid == kProgGouraud || pid == kProgAmy || pid == kProgGBuffer || pid == kProgMany; }
 bool blt_program_supported(int pid) { return pid == kProgDefaultPost || pid == kProgExposurePost || pid == kProgGouraud; }
 
 // the fragment state keys this device implementation covers: no scissor, depth
@@ -328,7 +330,7 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
         d.scissor[0] = left; d.scissor[1] = top; d.scissor[2] = right; d.scissor[3] = bottom;
     }
     d.program = s.program_id;
-    d.nvary = s.program_id == kProgGouraud ? 3 : (s.program_id == kProgAmy ? 2 : (s.program_id == kProgGBuffer ? 4 : 0));
+    d.nvary = s.program_id == kProgGouraud ? 3 : (s.program_id == kProgAmy || s.program_id == kProgMany ? 2 : (s.program_id == kProgGBuffer ? 4 : 0));
     d.keep_backs = !(s.culling_enabled && s.cull_face == RSRGPU_GL_BACK);
     d.keep_fronts = !(s.culling_enabled && s.cull_face == RSRGPU_GL_FRONT);
     d.cull_enabled = s.culling_enabled != 0;
@@ -425,7 +427,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_inst, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -532,6 +534,8 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
     ctx->draws.clear();
     ctx->ops.clear();
     ctx->gbufs.clear();
+    ctx->inst.clear();
+    ctx->any_inst = false;
     ctx->ntris = 0;
     bool gbuffer_frame = false, other_op_since_draw = false, any_draw = false;
     ctx->submitted = false;
@@ -577,17 +581,30 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             other_op_since_draw = true;
         } break;
         case RSRGPU_CMD_DRAW_ELEMENTS:
-        case RSRGPU_CMD_DRAW_ARRAYS: {
-            int32_t count = 0;
+        case RSRGPU_CMD_DRAW_ARRAYS:
+        case RSRGPU_CMD_DRAW_ELEMENTS_INSTANCED:
+        case RSRGPU_CMD_DRAW_ARRAYS_INSTANCED: {
+            int32_t count = 0, ninst = 1;
             uint64_t iptr = 0;
+            const bool instanced = op == RSRGPU_CMD_DRAW_ELEMENTS_INSTANCED || op == RSRGPU_CMD_DRAW_ARRAYS_INSTANCED;
             if (op == RSRGPU_CMD_DRAW_ELEMENTS) {
                 uint8_t flags, hint;
                 if (!rd(p, end, flags) || !rd(p, end, hint) || !rd(p, end, count) || !rd(p, end, iptr))
                     return fail(ctx, RSRGPU_EINVAL, "truncated CMD_DRAW_ELEMENTS");
                 if (flags != 0x14) return fail(ctx, RSRGPU_EINVAL, "CMD_DRAW_ELEMENTS flags must be 0x14");
+            } else if (op == RSRGPU_CMD_DRAW_ELEMENTS_INSTANCED) {
+                // GL::DrawElementsInstanced (rglv_gl.cxx:46-55): no hint byte
+                uint8_t flags;
+                if (!rd(p, end, flags) || !rd(p, end, count) || !rd(p, end, iptr) || !rd(p, end, ninst))
+                    return fail(ctx, RSRGPU_EINVAL, "truncated CMD_DRAW_ELEMENTS_INSTANCED");
+                if (flags != 0x14) return fail(ctx, RSRGPU_EINVAL, "CMD_DRAW_ELEMENTS_INSTANCED flags must be 0x14");
+            } else if (op == RSRGPU_CMD_DRAW_ARRAYS_INSTANCED) {
+                if (!rd(p, end, count) || !rd(p, end, ninst)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_DRAW_ARRAYS_INSTANCED");
             } else {
                 if (!rd(p, end, count)) return fail(ctx, RSRGPU_EINVAL, "truncated CMD_DRAW_ARRAYS");
             }
+            // the tile records carry the instance id as a u16 (rglv_gpu_impl.hxx:490,657)
+            if (ninst < 0 || ninst > 65536) return fail(ctx, RSRGPU_EINVAL, "instance count %d: 0 .. 65536", ninst);
             if (cur < 0) return fail(ctx, RSRGPU_EINVAL, "draw before any state");
             const auto& s = states[cur];
             const uint32_t vkey = (uint32_t(s.program_id) & 0xff) << 24;
@@ -603,20 +620,39 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
                 return fail(ctx, RSRGPU_EINVAL, "G-buffer program needs buffers 0-6");
             if (s.program_id == kProgGBuffer && s.blending_enabled)
                 return fail(ctx, RSRGPU_EUNSUPPORTED, "the G-buffer program does not blend");
+            if (s.program_id == kProgMany && !instanced)
+                return fail(ctx, RSRGPU_EUNSUPPORTED, "ManyProgram draws take instance matrices: use an instanced draw");
+            if (s.program_id == kProgMany && s.blending_enabled)
+                return fail(ctx, RSRGPU_EUNSUPPORTED, "ManyProgram is not drawn with blending on the device");
+            if (s.program_id == kProgMany && ninst > 0 &&
+                (ctx->states[size_t(cur)].buffers[15] == nullptr ||
+                 int64_t(ctx->states[size_t(cur)].buffer_len[15]) < int64_t(ninst) * 16))
+                return fail(ctx, RSRGPU_EINVAL, "ManyProgram: buffer 15 must hold %d instance matrices", ninst);
             any_draw = true;
             other_op_since_draw = false;
             DevDraw dd{};
             dd.state = cur;
             dd.first_tri = ctx->ntris;
             dd.ntris = count / 3;
-            dd.is_arrays = op == RSRGPU_CMD_DRAW_ARRAYS;
+            dd.is_arrays = op == RSRGPU_CMD_DRAW_ARRAYS || op == RSRGPU_CMD_DRAW_ARRAYS_INSTANCED;
+            DevInst di{};
+            if (instanced) {
+                di.per_inst = dd.ntris;
+                di.ninst = ninst;
+                di.matrices = s.program_id == kProgMany ? ctx->states[size_t(cur)].buffers[15] : nullptr;
+                if (int64_t(dd.ntris) * ninst > (int64_t(1) << 30)) return fail(ctx, RSRGPU_ECAPACITY, "too many triangles");
+                dd.ntris *= ninst;
+                ctx->any_inst = true;
+            }
             if (!dd.is_arrays) {
+                // the indices of one instance (every instance reads the same ones)
+                const size_t tris = size_t(instanced ? di.per_inst : dd.ntris);
                 void* dp = nullptr;
                 size_t avail = 0;
                 int rc = resolve(ctx, reinterpret_cast<const void*>(uintptr_t(iptr)), kEarlyInput, &dp, "index", &avail);
                 if (rc) return rc;
-                if (dp == nullptr || avail < size_t(dd.ntris) * 3u * sizeof(uint16_t))
-                    return fail(ctx, RSRGPU_EINVAL, "index buffer holds %zu bytes, draw needs %zu", avail, size_t(dd.ntris) * 6u);
+                if (dp == nullptr || avail < tris * 3u * sizeof(uint16_t))
+                    return fail(ctx, RSRGPU_EINVAL, "index buffer holds %zu bytes, draw needs %zu", avail, tris * 6u);
                 dd.indices = static_cast<const uint16_t*>(dp);
             }
             if (int64_t(ctx->ntris) + dd.ntris > (int64_t(1) << 30)) return fail(ctx, RSRGPU_ECAPACITY, "too many triangles");
@@ -624,6 +660,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             fo.kind = kOpDraw;
             fo.arg = int(ctx->draws.size());
             ctx->draws.push_back(dd);
+            ctx->inst.push_back(di);
             ctx->ops.push_back(fo);
         } break;
         case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC: {
@@ -801,6 +838,7 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
         CK(ctx->d_super.ensure(sizeof(int4) * std::max(nsupers, 1)), "alloc super rects");
         CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
         CK(ctx->d_gbufs.ensure(sizeof(GBufferDesc) * std::max<size_t>(ctx->gbufs.size(), 1)), "alloc gbuffer table");
+        if (ctx->any_inst) CK(ctx->d_inst.ensure(sizeof(DevInst) * ctx->inst.size()), "alloc instance table");
     }
     CK(ctx->d_tris.ensure(sizeof(TriRecord) * nt), "alloc tris");
     CK(ctx->d_bin_rect.ensure(sizeof(uint64_t) * nt), "alloc bin_rect");
@@ -847,9 +885,12 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.raster_phase = 0;
     fv.vis_own = nullptr;
     fv.vis_dep = nullptr;
-    fv.fp_stores = 0;
+    fv.ext = 0;
     for (const FrameOp& o : ctx->ops)
-        if (o.kind >= kOpStoreFP) fv.fp_stores = 1;
+        if (o.kind >= kOpStoreFP) fv.ext = 1;
+    for (const DevDraw& d : ctx->draws)
+        if (ctx->states[size_t(d.state)].program == kProgMany) fv.ext = 1;
+    fv.inst = (ctx->any_inst && tables == nullptr) ? ctx->d_inst.as<DevInst>() : nullptr;
     return 0;
 }
 
@@ -873,6 +914,8 @@ int prepare_run(rsrgpu_ctx* ctx, cudaStream_t st) {
             CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
         if (!ctx->gbufs.empty())
             CK(cudaMemcpyAsync(ctx->d_gbufs.p, ctx->gbufs.data(), sizeof(GBufferDesc) * ctx->gbufs.size(), cudaMemcpyHostToDevice, st), "H2D gbuffers");
+        if (ctx->any_inst)
+            CK(cudaMemcpyAsync(ctx->d_inst.p, ctx->inst.data(), sizeof(DevInst) * ctx->inst.size(), cudaMemcpyHostToDevice, st), "H2D instances");
         ctx->tables_uploaded = true;
     }
     if (ctx->fv.vis_keys != 0 && late_inputs(ctx))
@@ -1086,11 +1129,17 @@ int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* ne
             else if (o.kind == kOpStoreQuadsFP) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP); }
             else if (o.kind == kOpDraw) {
                 const DevDraw& d = ctx->draws[size_t(o.arg)];
+                const DevInst& di = ctx->inst[size_t(o.arg)];
                 const uint32_t endg = uint32_t(d.first_tri + d.ntris);
                 bool opened = false;
                 while (ic < b.inl_cnt && pool[b.inl_off + ic] < endg) {
                     const uint32_t g = pool[b.inl_off + ic++];
-                    if (!opened) { put8(one, RSRGPU_CMD_DRAW_INLINE); opened = true; }
+                    if (!opened) {
+                        put8(one, di.per_inst > 0 ? RSRGPU_CMD_DRAW_INLINE_INSTANCED : RSRGPU_CMD_DRAW_INLINE);
+                        opened = true;
+                    }
+                    // an instanced record starts with its instance id (rglv_gpu_impl.hxx:488-494)
+                    if (di.per_inst > 0) put16(one, uint16_t((g - uint32_t(d.first_tri)) / uint32_t(di.per_inst)));
                     put16(one, uint16_t(rec16[2 * g] & 0xffff));
                     put16(one, uint16_t(rec16[2 * g] >> 16));
                     put16(one, uint16_t(rec16[2 * g + 1]));
@@ -1590,6 +1639,8 @@ int decode_into(rsrgpu_batch* b, rsrgpu_ctx* c, const rsrgpu_frame_desc& d) {
     for (const FrameOp& o : c->ops)
         if (o.kind >= kOpStoreFP)
             return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no float colour stores (CMD_STORE_COLOR_*_FP); render them with rsrgpu_run");
+    if (c->any_inst)
+        return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no instanced draws; render them with rsrgpu_run");
     c->region_px = d.region_px ? d.region_px : std::min(d.tile_px, kRegionPx);
     if (d.bin_capacity) c->bin_cap = std::max<uint32_t>(d.bin_capacity, 1024u);
     return 0;
@@ -2007,6 +2058,10 @@ int decode_frame_without_context(int width, int height, int tile_blocks_x, int t
     }
     if (!tmp.gbufs.empty()) {
         err = "CMD_STORE_GBUFFER is not available without a context";
+        return RSRGPU_EUNSUPPORTED;
+    }
+    if (tmp.any_inst) {
+        err = "instanced draws are not available without a context";
         return RSRGPU_EUNSUPPORTED;
     }
     out_states = std::move(tmp.states);

@@ -33,6 +33,7 @@ enum ProgramId : int32_t {
     kProgDefaultPost = 1,
     kProgExposurePost = 2,
     kProgAmy = 4,
+    kProgMany = 6,        // ManyProgram (src/viewer/shaders.hxx:482-585): per-instance matrix, uv, magic
     kProgOBJ1 = 7,
     kProgGouraud = 90,
     kProgGBuffer = 91,
@@ -77,6 +78,14 @@ struct DevDraw {
 // The FP stores: rsr's CMD_STORE_COLOR_FULL_LINEAR_FP (kOpStoreFP),
 // CMD_STORE_COLOR_HALF_LINEAR_FP (kOpStoreHalfFP) and
 // CMD_STORE_COLOR_FULL_QUADS_FP (kOpStoreQuadsFP).
+// Per draw of a frame with instanced draws (CMD_DRAW_*_INSTANCED): its
+// triangles are numbered instance by instance, g = first_tri + iid * per_inst + t.
+struct DevInst {
+    const float* matrices;   // buffers[15]: one column-major mat4 per instance (ManyProgram)
+    int32_t per_inst;        // triangles per instance; 0: not instanced
+    int32_t ninst;
+};
+
 enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4, kOpStoreGBuffer = 5,
                         kOpStoreFP = 6, kOpStoreHalfFP = 7, kOpStoreQuadsFP = 8 };
 __host__ __device__ inline bool op_is_store(int32_t kind) { return kind >= kOpStoreTC; }
@@ -165,8 +174,9 @@ struct FrameView {
                               // 1 visibility (owners and depths into vis_own / vis_dep), 2 the rest
     uint32_t* vis_own;        // [height * width] per pixel, phases 1 and 2
     float* vis_dep;
-    int32_t fp_stores;        // the op list has float colour stores (raster_fp_kernel runs it)
-    int32_t pad_fp;
+    int32_t ext;              // float colour stores or ManyProgram draws: raster_ext_kernel runs the frame
+    int32_t pad_ext;
+    const DevInst* inst;      // per draw, for frames with instanced draws (setup_inst_kernel); else null
 };
 
 // Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,

@@ -113,6 +113,32 @@ __device__ __forceinline__ void shade_vertex(const DevState& s, int idx, float p
     }
 }
 
+// ManyProgram::ShadeVertex (src/viewer/shaders.hxx:555-562): the instance's
+// matrix times (position, 1), then vpm times that; uv from buffers 9-10 (its
+// Loader, :500-535: missing position or uv buffers read as 0)
+__device__ __forceinline__ void shade_vertex_many(const DevState& s, const float* __restrict__ imat, int idx,
+                                                  float pos[4], float vary[kMaxVary], FrameCounters* ctr) {
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (s.buffers[0] != nullptr && s.buffers[1] != nullptr && s.buffers[2] != nullptr) {
+        x = fetch(s, 0, idx, ctr);
+        y = fetch(s, 1, idx, ctr);
+        z = fetch(s, 2, idx, ctr);
+    }
+    float m[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) m[i] = __ldg(imat + i);
+    float p1[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) p1[r] = ((m[r] * x + m[4 + r] * y) + m[8 + r] * z) + m[12 + r] * 1.0f;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        pos[r] = ((s.vpm[r] * p1[0] + s.vpm[4 + r] * p1[1]) + s.vpm[8 + r] * p1[2]) + s.vpm[12 + r] * p1[3];
+#pragma unroll
+    for (int k = 0; k < kMaxVary; ++k) vary[k] = 0.f;
+    vary[0] = s.buffers[9] ? fetch(s, 9, idx, ctr) : 0.f;
+    vary[1] = s.buffers[10] ? fetch(s, 10, idx, ctr) : 0.f;
+}
+
 // ViewFrustum::Test, SIMD version (rglv_view_frustum.hxx:60-73)
 __device__ __forceinline__ uint32_t frustum_test(float factor, const float p[4]) {
     const float w = p[3] * factor;
@@ -279,6 +305,10 @@ __device__ __noinline__ uint64_t clip_triangle(const FrameView& fv, const DevSta
 // ---------------------------------------------------------------------------
 // setup
 // ---------------------------------------------------------------------------
+// kInst: the frame has instanced draws (fv.inst): a draw's triangles are its
+// instances' triangles in instance order (BinTriangles1P/2P's instance loop,
+// rglv_gpu_impl.hxx:364,554), ManyProgram vertices take their instance's matrix.
+template <bool kInst>
 __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
     const int g = block * kSetupBlock + threadIdx.x;
     uint64_t rect = kEmptyRect;
@@ -286,7 +316,16 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
         const int d = find_draw(fv.draws, fv.ndraws, g);
         const DevDraw dr = fv.draws[d];
         const DevState& s = fv.states[dr.state];
-        const int t = g - dr.first_tri;
+        int t = g - dr.first_tri;
+        const float* imat = nullptr;
+        if (kInst) {
+            const DevInst in = fv.inst[d];
+            if (in.per_inst > 0) {
+                const int iid = t / in.per_inst;
+                t -= iid * in.per_inst;
+                if (s.program == kProgMany) imat = in.matrices + size_t(iid) * 16;
+            }
+        }
         int idx[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) idx[k] = dr.is_arrays ? 3 * t + k : int(__ldg(dr.indices + 3 * t + k));
@@ -295,7 +334,8 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
         uint32_t cf[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            shade_vertex(s, idx[k], tv.pos[k], tv.vary[k], fv.counters);
+            if (kInst && imat != nullptr) shade_vertex_many(s, imat, idx[k], tv.pos[k], tv.vary[k], fv.counters);
+            else shade_vertex(s, idx[k], tv.pos[k], tv.vary[k], fv.counters);
             cf[k] = frustum_test(s.guard, tv.pos[k]);
             const float iw = oneover(fv.rcp_table, tv.pos[k][3]);
             dx[k] = (tv.pos[k][0] * iw) * s.DS[0] + s.DO[0];
@@ -1074,6 +1114,7 @@ __device__ __forceinline__ void quad_put_rgb(float col[4][3], int l, float r, fl
     else { col[3][0] = r; col[3][1] = g; col[3][2] = b; }
 }
 
+template <bool kExt>
 __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect[4], int qx, int qy,
                                              uint32_t own[4], float col[4][3]) {
     uint32_t cur = kNoOwner;
@@ -1109,6 +1150,8 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
             float c[3];
 #pragma unroll
             for (int q = 0; q < 3; ++q) c[q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
+            // ManyProgram::ShadeFragment (shaders.hxx:567-582): (u, v, magic, 1)
+            if (kExt && s.program == kProgMany) c[2] = s.uniforms[0];
             quad_put_rgb(col, l, c[0], c[1], c[2]);
         }
     }
@@ -1244,9 +1287,10 @@ __device__ __noinline__ float owner_depth(const FrameView& fv, uint32_t code, co
     return (bx * z[0] + by * z[1]) + bz * z[2];
 }
 
-// kFPStores: the frame has float colour stores (rsr's CMD_STORE_COLOR_*_FP);
-// frames without them run the instantiation that has no code for them.
-template <bool kFPStores>
+// kExt: the frame has float colour stores (rsr's CMD_STORE_COLOR_*_FP) or
+// ManyProgram draws; frames without them run the instantiation that has no
+// code for them.
+template <bool kExt>
 __device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
     if (fv.counters->overflow != 0u) return;
 
@@ -1346,7 +1390,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         // replaces colour first resolves the pending pixels.
         const bool visibility = o.kind == kOpDraw && !fs.blend;
         if (!visibility && o.kind != kOpStoreGBuffer && pending && fv.raster_phase != 1) {
-            if (active) resolve_quad(fv, rect, qx, qy, own, col);
+            if (active) resolve_quad<kExt>(fv, rect, qx, qy, own, col);
             pending = false;
         }
         if (o.kind == kOpClear) {
@@ -1651,7 +1695,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                 *reinterpret_cast<float2*>(dst + size_t(qy) * o.stride + qx) = make_float2(dep[0], dep[1]);
                 *reinterpret_cast<float2*>(dst + size_t(qy + 1) * o.stride + qx) = make_float2(dep[2], dep[3]);
             }
-        } else if (kFPStores && o.kind >= kOpStoreFP) {
+        } else if (kExt && o.kind >= kOpStoreFP) {
             // rsr's CMD_STORE_COLOR_{FULL_LINEAR,HALF_LINEAR,FULL_QUADS}_FP
             // (rglv_gpu.cxx:345-383); four float4 writes at most
             if (active) {
@@ -1697,7 +1741,10 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 // kernels: one frame, and a batch of frames in one launch per stage
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constant__ FrameView fv) {
-    setup_body(fv, blockIdx.x);
+    setup_body<false>(fv, blockIdx.x);
+}
+__global__ void __launch_bounds__(kSetupBlock) setup_inst_kernel(const __grid_constant__ FrameView fv) {
+    setup_body<true>(fv, blockIdx.x);
 }
 __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
     __shared__ BinShared S;
@@ -1707,7 +1754,7 @@ __global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ 
     __shared__ RasterSmem S;
     raster_body<false>(fv, blockIdx.x, S);
 }
-__global__ void __launch_bounds__(256, 2) raster_fp_kernel(const __grid_constant__ FrameView fv) {
+__global__ void __launch_bounds__(256, 2) raster_ext_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
     raster_body<true>(fv, blockIdx.x, S);
 }
@@ -1723,7 +1770,7 @@ __device__ __forceinline__ int batch_frame(const BatchLaunch& b, int block) {
 }
 __global__ void __launch_bounds__(kSetupBlock) setup_batch_kernel(const __grid_constant__ BatchLaunch b) {
     const int f = batch_frame(b, blockIdx.x);
-    setup_body(b.fv[f], blockIdx.x - b.start[f]);
+    setup_body<false>(b.fv[f], blockIdx.x - b.start[f]);
 }
 __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ BinShared S;
@@ -1742,7 +1789,8 @@ __global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_const
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
     const int blocks = (fv.ntris + kSetupBlock - 1) / kSetupBlock;
     if (blocks == 0) return cudaSuccess;
-    setup_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
+    if (fv.inst != nullptr) setup_inst_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
+    else setup_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
     return cudaGetLastError();
 }
 
@@ -1789,7 +1837,7 @@ cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
 }
 
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
-    if (fv.fp_stores) raster_fp_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
+    if (fv.ext) raster_ext_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
     else raster_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
     return cudaGetLastError();
 }

@@ -201,7 +201,7 @@ int render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* 
     fv.srgb_lut = reinterpret_cast<const uint8_t*>(base + kOffSrgb);
     fv.region_px = kRegionPx;
     for (const FrameOp& o : ops)
-        if (o.kind >= kOpStoreFP) fv.fp_stores = 1;
+        if (o.kind >= kOpStoreFP) fv.ext = 1;
 
 #define CKS(expr) do { cudaError_t e_ = (expr); if (e_ != cudaSuccess) return fail_static(RSRGPU_ECUDA, cudaGetErrorString(e_)); } while (0)
     CKS(cudaMemcpyAsync(base + kOffStates, st.data(), sizeof(DevState) * st.size(), cudaMemcpyHostToDevice, s));

@@ -248,6 +248,17 @@ class GL:
         self._maybe_update_state()
         self.commands += struct.pack("<Bi", abi.CMD_DRAW_ARRAYS, int(count))
 
+    def DrawElementsInstanced(self, count, indices, instances):
+        """GL::DrawElementsInstanced (rglv_gl.cxx:46-55): no hint byte."""
+        self._maybe_update_state()
+        self.commands += struct.pack("<BBiQi", abi.CMD_DRAW_ELEMENTS_INSTANCED, 0x14, int(count),
+                                     _addr(indices), int(instances))
+
+    def DrawArraysInstanced(self, count, instances):
+        """GL::DrawArraysInstanced (rglv_gl.cxx:23-31)."""
+        self._maybe_update_state()
+        self.commands += struct.pack("<Bii", abi.CMD_DRAW_ARRAYS_INSTANCED, int(count), int(instances))
+
     def Clear(self, bits):
         self._maybe_update_state()
         self.commands += struct.pack("<BB", abi.CMD_CLEAR, bits)

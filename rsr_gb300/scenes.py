@@ -643,3 +643,65 @@ def float_store_frame(seed=21, ntris=6000, width=320, height=180, tile_blocks=(4
 
     name = "float_store_%s%s" % ("color_depth" if color_depth else "rgbf32", "_mid" if mid else "")
     return FloatStoreScene(name, width, height, tile_blocks, arrays, record, ntris, color_depth=color_depth, mid=mid)
+
+
+def instanced_scene(seed=41, ninst=2000, width=640, height=360, tile_blocks=(4, 4), cull=True, near_share=0.004,
+                    magic=0.625):
+    """Instanced draws: ninst unit cubes drawn by one DrawElementsInstanced
+    with ManyProgram (per-instance column-major mat4 in buffer 15: random
+    rotation, size 0.3-0.8, centre in [-4,4]^2 x [-6,2]; a near_share of them
+    around the near plane of the camera at (0,0,8), so some are clipped; uv
+    per face corner; fragment colour (u, v, magic)), then 200 random Gouraud
+    triangles drawn three times by one DrawArraysInstanced (instances of a
+    program without instance data are copies).  Back faces culled for the
+    cubes when `cull`."""
+    pos, _, tri = _cube_mesh()
+    uv = np.array([[(su + 1) / 2, (sv + 1) / 2] for _ in range(6) for (su, sv) in ((-1, -1), (1, -1), (1, 1), (-1, 1))])
+    u = uniform01(seed * 131 + 7, ninst * 8).reshape(ninst, 8).astype(np.float64)
+    rot = _random_rotations(u[:, 0:3])
+    size = 0.3 + 0.5 * u[:, 3]
+    centre = np.stack([-4 + 8 * u[:, 4], -4 + 8 * u[:, 5], -6 + 8 * u[:, 6]], 1)
+    near = u[:, 7] < near_share
+    centre[near] = np.stack([-1.5 + 3.0 * u[near, 4], -0.9 + 1.8 * u[near, 5], 7.4 + 1.2 * u[near, 6]], 1)
+    m = np.zeros((ninst, 4, 4))
+    m[:, :3, :3] = rot * size[:, None, None]
+    m[:, :3, 3] = centre
+    m[:, 3, 3] = 1.0
+    imat = np.ascontiguousarray(m.transpose(0, 2, 1).reshape(-1), np.float32)   # column-major per instance
+    gt = plain_raster(seed=seed + 1, ntris=200, width=width, height=height, tile_blocks=tile_blocks, spread=0.5)
+    arrays = {"cx": pad4(pos[:, 0]), "cy": pad4(pos[:, 1]), "cz": pad4(pos[:, 2]),
+              "cu": pad4(uv[:, 0]), "cv": pad4(uv[:, 1]), "cidx": np.ascontiguousarray(tri.reshape(-1), np.uint16),
+              "imat": imat}
+    for k in ("px", "py", "pz", "cr", "cg", "cb"):
+        arrays["g" + k] = gt.arrays[k]
+    view = look_at((0.0, 0.0, 8.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0))
+    proj = perspective(60.0, width / height, 0.1, 100.0)
+    ident = np.eye(4, dtype=np.float32)
+
+    def record(gl, ref):
+        _begin_frame(gl, (0.02, 0.03, 0.05))
+        gl.UseProgram(abi.PROGRAM_MANY)
+        gl.UseUniforms([magic])
+        if cull:
+            gl.Enable(abi.GL_CULL_FACE)
+            gl.CullFace(abi.GL_BACK)
+        gl.ViewMatrix(view)
+        gl.ProjectionMatrix(proj)
+        gl.UseBuffer(0, (ref("cx"), ref("cy"), ref("cz")))
+        gl.UseBuffer(9, ref("cu"))
+        gl.UseBuffer(10, ref("cv"))
+        gl.UseBuffer(15, ref("imat"))
+        gl.DrawElementsInstanced(len(tri) * 3, ref("cidx"), ninst)
+        gl.Disable(abi.GL_CULL_FACE)
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        gl.UseUniforms([0.0])
+        gl.ViewMatrix(ident)
+        gl.ProjectionMatrix(ident)
+        gl.UseBuffer(0, (ref("gpx"), ref("gpy"), ref("gpz")))
+        gl.UseBuffer(3, (ref("gcr"), ref("gcg"), ref("gcb")))
+        gl.UseBuffer(9, None)
+        gl.UseBuffer(10, None)
+        gl.UseBuffer(15, None)
+        gl.DrawArraysInstanced(3 * 200, 3)
+
+    return Scene("instanced_%d" % ninst, width, height, tile_blocks, arrays, record, ninst * len(tri) + 600)

@@ -42,6 +42,12 @@ GOLDEN_SCENES = {
     # geometry of the deferred (G-buffer) scene drawn with the Gouraud program:
     # pins the G-buffer pass's depth to rsr
     "deferred_gouraud_640": ("deferred_scene", dict(nobj=20000, width=640, height=360, gouraud=True), 3),
+    # instanced draws: ManyProgram cubes (per-instance matrices, some clipped)
+    # and an instanced Gouraud DrawArraysInstanced
+    "instanced_640_t32": ("instanced_scene", {}, 2),
+    "instanced_320_t8_nocull": ("instanced_scene", dict(cull=False, seed=42, ninst=500, width=320, height=180,
+                                                         tile_blocks=(1, 1)), 2),
+    "instanced_720_t64": ("instanced_scene", dict(seed=43, ninst=3000, width=1280, height=720, tile_blocks=(8, 8)), 2),
 }
 
 

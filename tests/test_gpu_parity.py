@@ -30,6 +30,12 @@ SCENES = {
     # 1250 chunks of 32 large triangles, nearly all overlapping every 8x8 tile:
     # binning takes its windows of 1024 chunks; four draws
     "plain_320_t8_windows": lambda: scenes.plain_raster(seed=31, ntris=40000, width=320, height=180, tile_blocks=(1, 1)),
+    # instanced draws (ManyProgram with per-instance matrices, clipped
+    # instances, and an instanced Gouraud draw)
+    "instanced_640_t32": lambda: scenes.instanced_scene(),
+    "instanced_320_t8_nocull": lambda: scenes.instanced_scene(cull=False, seed=42, ninst=500, width=320, height=180,
+                                                              tile_blocks=(1, 1)),
+    "instanced_720_t64": lambda: scenes.instanced_scene(seed=43, ninst=3000, width=1280, height=720, tile_blocks=(8, 8)),
 }
 
 
