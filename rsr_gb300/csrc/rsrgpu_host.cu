@@ -2041,7 +2041,7 @@ int decode_frame_without_context(int width, int height, int tile_blocks_x, int t
                                  std::vector<FrameOp>& out_ops, int& ntris, int& ntiles, std::string& err) {
     rsrgpu_ctx tmp;
     int rc = rsrgpu_reset(&tmp, width, height, tile_blocks_x, tile_blocks_y);
-    const int programs[] = { kProgGouraud, kProgAmy };
+    const int programs[] = { kProgGouraud, kProgAmy, kProgMany };
     const uint32_t keys[] = { 0x6e2, 0x6e6, 0x6ea, 0x6f2, 0x6f6, 0x6c2, 0x6c6, 0x62, 0x66, 0x72, 0x42, 0x6a };
     for (int pid : programs) {
         if (rc == 0) rc = rsrgpu_install(&tmp, pid, 0, 0);
