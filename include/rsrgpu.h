@@ -106,7 +106,9 @@ extern "C" {
 #define RSRGPU_PROGRAM_MANY          6   /* ManyProgram (instanced: per-instance matrix in buffer 15,
                                             position 0-2, uv 9-10; colour (u, v, uniform 0)),
                                             shaders.hxx:482-585 */
-#define RSRGPU_PROGRAM_OBJ1          7   /* OBJ1Program (lit Gouraud), shaders.hxx:586 */
+#define RSRGPU_PROGRAM_OBJ1          7   /* OBJ1Program (Gouraud kd lit per vertex by a light at the eye;
+                                            position 0-2, normal 3-5, kd 6-8), shaders.hxx:586-699;
+                                            not taken by batches */
 #define RSRGPU_PROGRAM_GOURAUD       90  /* test program: per-vertex rgb, no lighting */
 #define RSRGPU_PROGRAM_GBUFFER       91  /* G-buffer program: position 0-2, normal 3-5,
                                             RGBA8 albedo bits (as float) in 6 */

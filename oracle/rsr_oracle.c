@@ -53,6 +53,22 @@ static float rcpps(float x) {
     return u2f(s | ((uint32_t)er << 23) | (t & 0x7fffffu));
 }
 
+/* _mm_rsqrt_ps, modelled by the measured table (see gen_rsqrtps_table.c):
+   the parity of the exponent and the top 11 mantissa bits index it */
+static const uint32_t RSQRTPS_TABLE[4096] = {
+#include "../rsr_gb300/csrc/rsqrtps_table.inc"
+};
+static float rsqrtps(float x) {
+    uint32_t b = f2u(x), s = b & 0x80000000u, e = (b >> 23) & 255u, m = b & 0x7fffffu;
+    if (e == 255u) return u2f(m ? (b | 0x00400000u) : (s ? 0xffc00000u : 0u));
+    if (e == 0u) return u2f(s | 0x7f800000u);
+    if (s) return u2f(0xffc00000u);
+    int k = (int)e - 127, p = k & 1;
+    uint32_t t = RSQRTPS_TABLE[(uint32_t)p * 2048u + (m >> 12)];
+    int er = (int)((t >> 23) & 255u) - (k - p) / 2;
+    return u2f(((uint32_t)er << 23) | (t & 0x7fffffu));
+}
+
 /* rmlv::oneover: rcpps + one Newton step (rmlv_mvec4.hxx:631-651) */
 static float oneover(float a) {
     float r = rcpps(a);
@@ -109,6 +125,7 @@ static int program_nvary(int pid) {
     case RSRGPU_PROGRAM_GOURAUD: return 3;
     case RSRGPU_PROGRAM_AMY: return 2;
     case RSRGPU_PROGRAM_MANY: return 2;
+    case RSRGPU_PROGRAM_OBJ1: return 3;
     case RSRGPU_PROGRAM_GBUFFER: return 4;
     default: return -1;
     }
@@ -117,12 +134,54 @@ static int program_nvary(int pid) {
 /* SHADER::ShadeVertex for one vertex: gl_Position = vpm * (pos, 1) and the
  * VertexOutputSD (GouraudProgram: rgb from buffers 3-5; AmyProgram
  * shaders.hxx:127-135: uv from buffers 9-10, zero when unbound). */
+/* OBJ1Program::ShadeVertex (src/viewer/shaders.hxx:656-676) for one vertex:
+ * view-space point light at the eye,
+ *   mvv = vm*(p,1), mvn = vm*(n,0), d = (0,0,0,1) - mvv with rmlv's qfloat4
+ *   operator- taking w as 1 - mvv.z (src/rml/rmlv/rmlv_soa.hxx:163),
+ *   distance = sqrt(dot(d,d)) (rmlv::length, :220-223),
+ *   L = d * rsqrtps(dot(d,d)) (rmlv::normalize, :242-248),
+ *   diffuse = maxps(dot(mvn, L), 0.1) * (100 / distance),
+ *   kd_out = kd * diffuse, gl_Position = vpm*(p,1). */
+static void obj1_vertex(const float* vm, const float* vpm, const float p[3], const float n[3], const float kd[3],
+                        float pos[4], float kd_out[3]) {
+    const float in[4] = { p[0], p[1], p[2], 1.0f }, nrm[4] = { n[0], n[1], n[2], 0.0f };
+    float mvv[4], mvn[4];
+    qmat_mul(vm, in, mvv);
+    qmat_mul(vm, nrm, mvn);
+    const float d[4] = { 0.0f - mvv[0], 0.0f - mvv[1], 0.0f - mvv[2], 1.0f - mvv[2] };
+    const float dd = ((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) + d[3] * d[3];
+    const float distance = sqrtf(dd);
+    const float sc = rsqrtps(dd);
+    const float L[4] = { d[0] * sc, d[1] * sc, d[2] * sc, d[3] * sc };
+    float diffuse = sse_max(((mvn[0] * L[0] + mvn[1] * L[1]) + mvn[2] * L[2]) + mvn[3] * L[3], 0.1f);
+    diffuse = diffuse * (100.0f / distance);
+    for (int c = 0; c < 3; ++c) kd_out[c] = kd[c] * diffuse;
+    qmat_mul(vpm, in, pos);
+}
+
+/* exported for the check of the device shading source (tests/test_obj1.py) */
+int rsroracle_obj1_vertices(const float* vm, const float* vpm, const float* p, const float* n, const float* kd, int count,
+                            float* pos, float* kd_out) {
+    for (int i = 0; i < count; ++i) obj1_vertex(vm, vpm, p + 3 * i, n + 3 * i, kd + 3 * i, pos + 4 * i, kd_out + 3 * i);
+    return 0;
+}
+
 static void shade_vertex_inst(const rsrgpu_glstate* s, const float* vpm, int iid, int idx, float pos[4],
                               float vary[MAX_VARY]) {
     float in[4];
     if (s->buffers[0]) { in[0] = s->buffers[0][idx]; in[1] = s->buffers[1][idx]; in[2] = s->buffers[2][idx]; }
     else { in[0] = in[1] = in[2] = 0.0f; }
     in[3] = 1.0f;
+    if (s->program_id == RSRGPU_PROGRAM_OBJ1) {
+        /* OBJ1Program's Loader::LoadLane (shaders.hxx:623-636): position 0,
+           normal (0,0,1), kd (1,1,1) when unbound */
+        float nrm[3] = { 0.0f, 0.0f, 1.0f }, kd[3] = { 1.0f, 1.0f, 1.0f };
+        if (s->buffers[3]) { nrm[0] = s->buffers[3][idx]; nrm[1] = s->buffers[4][idx]; nrm[2] = s->buffers[5][idx]; }
+        if (s->buffers[6]) { kd[0] = s->buffers[6][idx]; kd[1] = s->buffers[7][idx]; kd[2] = s->buffers[8][idx]; }
+        memset(vary, 0, sizeof(float) * MAX_VARY);
+        obj1_vertex(s->view_matrix, vpm, in, nrm, kd, pos, vary);
+        return;
+    }
     if (s->program_id == RSRGPU_PROGRAM_MANY) {
         /* ManyProgram::ShadeVertex (shaders.hxx:555-562): p1 = imat * (pos, 1),
            gl_Position = vpm * p1; imat = instance iid's mat4 from buffer 15

@@ -127,15 +127,16 @@ struct rsrgpu_ctx {
     std::vector<DevDraw> draws;
     std::vector<FrameOp> ops;
     std::vector<GBufferDesc> gbufs;
-    std::vector<DevInst> inst;      // per draw; uploaded when a draw is instanced
-    bool any_inst = false;
+    std::vector<DevDrawExt> dext;   // per draw; uploaded when a draw is instanced or uses OBJ1Program
+    bool any_inst = false;          // an instanced draw
+    bool any_dext = false;          // the frame needs the extended setup (instanced or OBJ1Program draws)
     int ntris = 0;
     bool submitted = false;
     bool ran = false;
     // device memory
     DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
         d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs,
-        d_inst, d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
+        d_dext, d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
     std::map<cudaStream_t, cudaEvent_t> learn_events;   // last learned-shader launch per stream
     int num_sms = 0;
     int* h_mlp_err = nullptr;   // pinned
@@ -207,7 +208,9 @@ uint32_t fragment_state_key(const rsrgpu_glstate& s) {   // GLState::FragmentSta
     return key;
 }
 
-bool draw_program_supported(int pid) { return pid == kProgGouraud || pid == kProgAmy || pid == kProgGBuffer || pid == kProgMany; }
+bool draw_program_supported(int pid) {
+    return pid == kProgGouraud || pid == kProgAmy || pid == kProgGBuffer || pid == kProgMany || pid == kProgOBJ1;
+}
 bool blt_program_supported(int pid) { return pid == kProgDefaultPost || pid == kProgExposurePost || pid == kProgGouraud; }
 
 // the fragment state keys this device implementation covers: no scissor, depth
@@ -330,7 +333,8 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
         d.scissor[0] = left; d.scissor[1] = top; d.scissor[2] = right; d.scissor[3] = bottom;
     }
     d.program = s.program_id;
-    d.nvary = s.program_id == kProgGouraud ? 3 : (s.program_id == kProgAmy || s.program_id == kProgMany ? 2 : (s.program_id == kProgGBuffer ? 4 : 0));
+    d.nvary = (s.program_id == kProgGouraud || s.program_id == kProgOBJ1) ? 3
+            : (s.program_id == kProgAmy || s.program_id == kProgMany) ? 2 : (s.program_id == kProgGBuffer ? 4 : 0);
     d.keep_backs = !(s.culling_enabled && s.cull_face == RSRGPU_GL_BACK);
     d.keep_fronts = !(s.culling_enabled && s.cull_face == RSRGPU_GL_FRONT);
     d.cull_enabled = s.culling_enabled != 0;
@@ -427,7 +431,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_inst, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_dext, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -534,8 +538,9 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
     ctx->draws.clear();
     ctx->ops.clear();
     ctx->gbufs.clear();
-    ctx->inst.clear();
+    ctx->dext.clear();
     ctx->any_inst = false;
+    ctx->any_dext = false;
     ctx->ntris = 0;
     bool gbuffer_frame = false, other_op_since_draw = false, any_draw = false;
     ctx->submitted = false;
@@ -635,7 +640,9 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             dd.first_tri = ctx->ntris;
             dd.ntris = count / 3;
             dd.is_arrays = op == RSRGPU_CMD_DRAW_ARRAYS || op == RSRGPU_CMD_DRAW_ARRAYS_INSTANCED;
-            DevInst di{};
+            DevDrawExt di{};
+            std::memcpy(di.vm, s.view_matrix, sizeof(di.vm));
+            if (s.program_id == kProgOBJ1) ctx->any_dext = true;
             if (instanced) {
                 di.per_inst = dd.ntris;
                 di.ninst = ninst;
@@ -643,6 +650,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
                 if (int64_t(dd.ntris) * ninst > (int64_t(1) << 30)) return fail(ctx, RSRGPU_ECAPACITY, "too many triangles");
                 dd.ntris *= ninst;
                 ctx->any_inst = true;
+                ctx->any_dext = true;
             }
             if (!dd.is_arrays) {
                 // the indices of one instance (every instance reads the same ones)
@@ -660,7 +668,7 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
             fo.kind = kOpDraw;
             fo.arg = int(ctx->draws.size());
             ctx->draws.push_back(dd);
-            ctx->inst.push_back(di);
+            ctx->dext.push_back(di);
             ctx->ops.push_back(fo);
         } break;
         case RSRGPU_CMD_STORE_COLOR_FULL_LINEAR_TC: {
@@ -838,7 +846,7 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
         CK(ctx->d_super.ensure(sizeof(int4) * std::max(nsupers, 1)), "alloc super rects");
         CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
         CK(ctx->d_gbufs.ensure(sizeof(GBufferDesc) * std::max<size_t>(ctx->gbufs.size(), 1)), "alloc gbuffer table");
-        if (ctx->any_inst) CK(ctx->d_inst.ensure(sizeof(DevInst) * ctx->inst.size()), "alloc instance table");
+        if (ctx->any_dext) CK(ctx->d_dext.ensure(sizeof(DevDrawExt) * ctx->dext.size()), "alloc draw extension table");
     }
     CK(ctx->d_tris.ensure(sizeof(TriRecord) * nt), "alloc tris");
     CK(ctx->d_bin_rect.ensure(sizeof(uint64_t) * nt), "alloc bin_rect");
@@ -890,7 +898,7 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
         if (o.kind >= kOpStoreFP) fv.ext = 1;
     for (const DevDraw& d : ctx->draws)
         if (ctx->states[size_t(d.state)].program == kProgMany) fv.ext = 1;
-    fv.inst = (ctx->any_inst && tables == nullptr) ? ctx->d_inst.as<DevInst>() : nullptr;
+    fv.dext = (ctx->any_dext && tables == nullptr) ? ctx->d_dext.as<DevDrawExt>() : nullptr;
     return 0;
 }
 
@@ -914,8 +922,8 @@ int prepare_run(rsrgpu_ctx* ctx, cudaStream_t st) {
             CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
         if (!ctx->gbufs.empty())
             CK(cudaMemcpyAsync(ctx->d_gbufs.p, ctx->gbufs.data(), sizeof(GBufferDesc) * ctx->gbufs.size(), cudaMemcpyHostToDevice, st), "H2D gbuffers");
-        if (ctx->any_inst)
-            CK(cudaMemcpyAsync(ctx->d_inst.p, ctx->inst.data(), sizeof(DevInst) * ctx->inst.size(), cudaMemcpyHostToDevice, st), "H2D instances");
+        if (ctx->any_dext)
+            CK(cudaMemcpyAsync(ctx->d_dext.p, ctx->dext.data(), sizeof(DevDrawExt) * ctx->dext.size(), cudaMemcpyHostToDevice, st), "H2D draw extensions");
         ctx->tables_uploaded = true;
     }
     if (ctx->fv.vis_keys != 0 && late_inputs(ctx))
@@ -1129,7 +1137,7 @@ int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* ne
             else if (o.kind == kOpStoreQuadsFP) { put8(one, RSRGPU_CMD_STORE_COLOR_FULL_QUADS_FP); }
             else if (o.kind == kOpDraw) {
                 const DevDraw& d = ctx->draws[size_t(o.arg)];
-                const DevInst& di = ctx->inst[size_t(o.arg)];
+                const DevDrawExt& di = ctx->dext[size_t(o.arg)];
                 const uint32_t endg = uint32_t(d.first_tri + d.ntris);
                 bool opened = false;
                 while (ic < b.inl_cnt && pool[b.inl_off + ic] < endg) {
@@ -1641,6 +1649,8 @@ int decode_into(rsrgpu_batch* b, rsrgpu_ctx* c, const rsrgpu_frame_desc& d) {
             return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no float colour stores (CMD_STORE_COLOR_*_FP); render them with rsrgpu_run");
     if (c->any_inst)
         return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no instanced draws; render them with rsrgpu_run");
+    if (c->any_dext)
+        return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no OBJ1Program draws; render them with rsrgpu_run");
     c->region_px = d.region_px ? d.region_px : std::min(d.tile_px, kRegionPx);
     if (d.bin_capacity) c->bin_cap = std::max<uint32_t>(d.bin_capacity, 1024u);
     return 0;

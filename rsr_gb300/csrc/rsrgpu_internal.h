@@ -78,12 +78,15 @@ struct DevDraw {
 // The FP stores: rsr's CMD_STORE_COLOR_FULL_LINEAR_FP (kOpStoreFP),
 // CMD_STORE_COLOR_HALF_LINEAR_FP (kOpStoreHalfFP) and
 // CMD_STORE_COLOR_FULL_QUADS_FP (kOpStoreQuadsFP).
-// Per draw of a frame with instanced draws (CMD_DRAW_*_INSTANCED): its
-// triangles are numbered instance by instance, g = first_tri + iid * per_inst + t.
-struct DevInst {
+// Per draw of a frame that needs the extended setup (setup_ext_kernel):
+// instanced draws (CMD_DRAW_*_INSTANCED), whose triangles are numbered
+// instance by instance, g = first_tri + iid * per_inst + t, and OBJ1Program
+// draws, which light vertices in view space.
+struct DevDrawExt {
     const float* matrices;   // buffers[15]: one column-major mat4 per instance (ManyProgram)
     int32_t per_inst;        // triangles per instance; 0: not instanced
     int32_t ninst;
+    float vm[16];            // the draw state's view matrix (OBJ1Program)
 };
 
 enum OpKind : int32_t { kOpState = 0, kOpClear = 1, kOpDraw = 2, kOpStoreTC = 3, kOpStoreDepth = 4, kOpStoreGBuffer = 5,
@@ -176,7 +179,7 @@ struct FrameView {
     float* vis_dep;
     int32_t ext;              // float colour stores or ManyProgram draws: raster_ext_kernel runs the frame
     int32_t pad_ext;
-    const DevInst* inst;      // per draw, for frames with instanced draws (setup_inst_kernel); else null
+    const DevDrawExt* dext;   // per draw, for frames with instanced or OBJ1Program draws (setup_ext_kernel); else null
 };
 
 // Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,

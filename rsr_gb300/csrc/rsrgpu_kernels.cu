@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include "rsrgpu_internal.h"
+#include "rsrgpu_obj1.h"
 
 namespace rsrgpu {
 
@@ -111,6 +112,30 @@ __device__ __forceinline__ void shade_vertex(const DevState& s, int idx, float p
         vary[2] = fetch(s, 5, idx, ctr);
         vary[3] = fetch(s, 6, idx, ctr);
     }
+}
+
+// OBJ1Program's vertex inputs (its Loader::LoadLane, shaders.hxx:623-636:
+// missing position 0, normal (0,0,1), kd (1,1,1)) and its lighting
+// (rsrgpu_obj1.h), with RSRGPU's measured RSQRTPS table
+__device__ const uint32_t kRsqrtTable[4096] = {
+#include "rsqrtps_table.inc"
+};
+__device__ __forceinline__ void shade_vertex_obj1(const DevState& s, const float* __restrict__ vm, int idx,
+                                                  float pos[4], float vary[kMaxVary], FrameCounters* ctr) {
+    float p[3] = { 0.f, 0.f, 0.f }, n[3] = { 0.f, 0.f, 1.f }, kd[3] = { 1.f, 1.f, 1.f };
+    if (s.buffers[0] != nullptr) { p[0] = fetch(s, 0, idx, ctr); p[1] = fetch(s, 1, idx, ctr); p[2] = fetch(s, 2, idx, ctr); }
+    if (s.buffers[3] != nullptr) { n[0] = fetch(s, 3, idx, ctr); n[1] = fetch(s, 4, idx, ctr); n[2] = fetch(s, 5, idx, ctr); }
+    if (s.buffers[6] != nullptr) { kd[0] = fetch(s, 6, idx, ctr); kd[1] = fetch(s, 7, idx, ctr); kd[2] = fetch(s, 8, idx, ctr); }
+    float m[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) m[i] = __ldg(vm + i);
+    float out[3];
+    obj1_shade(m, s.vpm, kRsqrtTable, p, n, kd, pos, out);
+#pragma unroll
+    for (int k = 0; k < kMaxVary; ++k) vary[k] = 0.f;
+    vary[0] = out[0];
+    vary[1] = out[1];
+    vary[2] = out[2];
 }
 
 // ManyProgram::ShadeVertex (src/viewer/shaders.hxx:555-562): the instance's
@@ -305,10 +330,11 @@ __device__ __noinline__ uint64_t clip_triangle(const FrameView& fv, const DevSta
 // ---------------------------------------------------------------------------
 // setup
 // ---------------------------------------------------------------------------
-// kInst: the frame has instanced draws (fv.inst): a draw's triangles are its
-// instances' triangles in instance order (BinTriangles1P/2P's instance loop,
-// rglv_gpu_impl.hxx:364,554), ManyProgram vertices take their instance's matrix.
-template <bool kInst>
+// kExt: the frame has instanced or OBJ1Program draws (fv.dext): a draw's
+// triangles are its instances' triangles in instance order (BinTriangles1P/2P's
+// instance loop, rglv_gpu_impl.hxx:364,554), ManyProgram vertices take their
+// instance's matrix, OBJ1Program vertices are lit with the draw's view matrix.
+template <bool kExt>
 __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
     const int g = block * kSetupBlock + threadIdx.x;
     uint64_t rect = kEmptyRect;
@@ -318,13 +344,16 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
         const DevState& s = fv.states[dr.state];
         int t = g - dr.first_tri;
         const float* imat = nullptr;
-        if (kInst) {
-            const DevInst in = fv.inst[d];
-            if (in.per_inst > 0) {
-                const int iid = t / in.per_inst;
-                t -= iid * in.per_inst;
-                if (s.program == kProgMany) imat = in.matrices + size_t(iid) * 16;
+        const float* vm = nullptr;
+        if (kExt) {
+            const DevDrawExt& de = fv.dext[d];
+            const int per_inst = de.per_inst;
+            if (per_inst > 0) {
+                const int iid = t / per_inst;
+                t -= iid * per_inst;
+                if (s.program == kProgMany) imat = de.matrices + size_t(iid) * 16;
             }
+            if (s.program == kProgOBJ1) vm = de.vm;
         }
         int idx[3];
 #pragma unroll
@@ -334,7 +363,8 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
         uint32_t cf[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            if (kInst && imat != nullptr) shade_vertex_many(s, imat, idx[k], tv.pos[k], tv.vary[k], fv.counters);
+            if (kExt && imat != nullptr) shade_vertex_many(s, imat, idx[k], tv.pos[k], tv.vary[k], fv.counters);
+            else if (kExt && vm != nullptr) shade_vertex_obj1(s, vm, idx[k], tv.pos[k], tv.vary[k], fv.counters);
             else shade_vertex(s, idx[k], tv.pos[k], tv.vary[k], fv.counters);
             cf[k] = frustum_test(s.guard, tv.pos[k]);
             const float iw = oneover(fv.rcp_table, tv.pos[k][3]);
@@ -1743,7 +1773,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 __global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constant__ FrameView fv) {
     setup_body<false>(fv, blockIdx.x);
 }
-__global__ void __launch_bounds__(kSetupBlock) setup_inst_kernel(const __grid_constant__ FrameView fv) {
+__global__ void __launch_bounds__(kSetupBlock) setup_ext_kernel(const __grid_constant__ FrameView fv) {
     setup_body<true>(fv, blockIdx.x);
 }
 __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
@@ -1789,7 +1819,7 @@ __global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_const
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
     const int blocks = (fv.ntris + kSetupBlock - 1) / kSetupBlock;
     if (blocks == 0) return cudaSuccess;
-    if (fv.inst != nullptr) setup_inst_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
+    if (fv.dext != nullptr) setup_ext_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
     else setup_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
     return cudaGetLastError();
 }

@@ -62,7 +62,7 @@ class GPU:
     def InstallDefaults(self):
         """The device counterpart of rqv::Install (src/viewer/shaders.cxx:54-126)
         for the programs this library implements."""
-        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY, abi.PROGRAM_GBUFFER, abi.PROGRAM_MANY):
+        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY, abi.PROGRAM_GBUFFER, abi.PROGRAM_MANY, abi.PROGRAM_OBJ1):
             self.Install(pid, 0, abi.KIND_BIN)
             for key in DRAW_STATE_KEYS:
                 self.Install(pid, key, abi.KIND_DRAW)
@@ -305,7 +305,7 @@ class Batch:
         self._check(self.lib.rsrgpu_batch_install(self.h, int(program_id), int(state_key), int(kind)))
 
     def InstallDefaults(self):
-        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY, abi.PROGRAM_GBUFFER, abi.PROGRAM_MANY):
+        for pid in (abi.PROGRAM_GOURAUD, abi.PROGRAM_AMY, abi.PROGRAM_GBUFFER, abi.PROGRAM_MANY, abi.PROGRAM_OBJ1):
             self.Install(pid, 0, abi.KIND_BIN)
             for key in DRAW_STATE_KEYS:
                 self.Install(pid, key, abi.KIND_DRAW)

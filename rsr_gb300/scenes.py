@@ -705,3 +705,46 @@ def instanced_scene(seed=41, ninst=2000, width=640, height=360, tile_blocks=(4, 
         gl.DrawArraysInstanced(3 * 200, 3)
 
     return Scene("instanced_%d" % ninst, width, height, tile_blocks, arrays, record, ninst * len(tri) + 600)
+
+
+def obj1_scene(seed=51, nspheres=24, divs=3, width=640, height=360, tile_blocks=(4, 4), dense_hint=False):
+    """OBJ1Program (src/viewer/shaders.hxx:586-699): icospheres (radius
+    8-20, smooth normals, random per-vertex kd in [0.2, 1]) placed 60-260
+    units in front of a camera at the origin looking down -z, so the
+    program's point light at the eye gives diffuse * 100/distance mostly
+    below 1; one sphere straddles the near plane (clipped).  Each sphere is
+    one DrawElements (the 1P binning path, or with dense_hint the 2P path)."""
+    verts, faces = icosphere(divs)
+    nv = len(verts)
+    u = uniform01(seed * 977 + 3, nspheres * 5).reshape(nspheres, 5).astype(np.float64)
+    radius = 8.0 + 12.0 * u[:, 0]
+    centre = np.stack([-60 + 120 * u[:, 1], -35 + 70 * u[:, 2], -(60 + 200 * u[:, 3])], 1)
+    # sphere 0 reaches 0.74 units from the eye, closer than the near plane (1):
+    # the plane cuts its visible cap, so front faces are clipped and kept
+    centre[0] = (0.5, 0.3, -4.7)
+    radius[0] = 4.0
+    kd = 0.2 + 0.8 * uniform01(seed * 977 + 11, nspheres * nv * 3).reshape(nspheres, nv, 3)
+    arrays = {"idx": np.ascontiguousarray(faces.reshape(-1), np.uint16)}
+    for i in range(nspheres):
+        p = verts * radius[i] + centre[i]
+        arrays["p%d" % i] = np.ascontiguousarray(np.stack([pad4(p[:, 0]), pad4(p[:, 1]), pad4(p[:, 2])]))
+        arrays["n%d" % i] = np.ascontiguousarray(np.stack([pad4(verts[:, 0]), pad4(verts[:, 1]), pad4(verts[:, 2])]))
+        arrays["k%d" % i] = np.ascontiguousarray(np.stack([pad4(kd[i, :, 0]), pad4(kd[i, :, 1]), pad4(kd[i, :, 2])]))
+    view = look_at((0.0, 0.0, 0.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0))
+    proj = perspective(60.0, width / height, 1.0, 1000.0)
+    hint = (abi.RGL_HINT_DENSE | abi.RGL_HINT_READ4) if dense_hint else 0
+
+    def record(gl, ref):
+        _begin_frame(gl, (0.0, 0.0, 0.0))
+        gl.UseProgram(abi.PROGRAM_OBJ1)
+        gl.Enable(abi.GL_CULL_FACE)
+        gl.CullFace(abi.GL_BACK)
+        gl.ViewMatrix(view)
+        gl.ProjectionMatrix(proj)
+        for i in range(nspheres):
+            gl.UseBuffer(0, tuple(ref("p%d" % i)[k] for k in range(3)))
+            gl.UseBuffer(3, tuple(ref("n%d" % i)[k] for k in range(3)))
+            gl.UseBuffer(6, tuple(ref("k%d" % i)[k] for k in range(3)))
+            gl.DrawElements(len(faces) * 3, ref("idx"), hint)
+
+    return Scene("obj1_%d" % nspheres, width, height, tile_blocks, arrays, record, nspheres * len(faces))

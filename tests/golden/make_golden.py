@@ -48,6 +48,11 @@ GOLDEN_SCENES = {
     "instanced_320_t8_nocull": ("instanced_scene", dict(cull=False, seed=42, ninst=500, width=320, height=180,
                                                          tile_blocks=(1, 1)), 2),
     "instanced_720_t64": ("instanced_scene", dict(seed=43, ninst=3000, width=1280, height=720, tile_blocks=(8, 8)), 2),
+    # OBJ1Program: per-vertex view-space lighting (sqrt, RSQRTPS, divide),
+    # 1P and 2P binning, one sphere clipped at the near plane
+    "obj1_640_t32": ("obj1_scene", {}, 3),
+    "obj1_320_t8_2p": ("obj1_scene", dict(dense_hint=True, seed=52, width=320, height=180, tile_blocks=(1, 1)), 3),
+    "obj1_720_t64": ("obj1_scene", dict(seed=53, nspheres=60, width=1280, height=720, tile_blocks=(8, 8)), 3),
 }
 
 
