@@ -85,6 +85,12 @@ extern "C" {
 #define RSRGPU_CMD_STORE_GBUFFER              40
 
 /* ---- GL enums (src/rgl/rglv/rglv_gl.hxx:20-62) ---- */
+#define RSRGPU_GL_CULL_FACE        1
+#define RSRGPU_GL_SCISSOR_TEST     2
+#define RSRGPU_GL_BLEND            3
+#define RSRGPU_GL_DEPTH_TEST       4
+#define RSRGPU_GL_NEAREST_MIPMAP_NEAREST 0
+#define RSRGPU_GL_LINEAR_MIPMAP_NEAREST  1
 #define RSRGPU_GL_FRONT            1
 #define RSRGPU_GL_BACK             2
 #define RSRGPU_GL_LESS             0
@@ -304,6 +310,70 @@ int rsrgpu_get_stats(rsrgpu_ctx* ctx, rsrgpu_stats* out);
 int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms);
 
 int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
+
+/* ---- recording a frame (the producer side) ----
+ * A native recorder with rglv::GL's calling surface (src/rgl/rglv/
+ * rglv_gl.hxx:182-345, rglv_gl.cxx:13-106), for callers that produce frames
+ * without rsr.  State setters change the current state; the next command
+ * appends a snapshot of it and emits CMD_STATE with the snapshot's index
+ * (GL::MaybeUpdateState, rglv_gl.cxx:100-106), then the command in rsr's byte
+ * protocol.  The state starts (and rsrgpu_gl_reset_state() returns to) the
+ * defaults of GLState::reset (rglv_gl.hxx:152-179) with RB_COLOR_DEPTH
+ * attachments and identity matrices.  rsrgpu_recorder_frame() gives the
+ * stream and the snapshots for rsrgpu_submit() or an rsrgpu_frame_desc; the
+ * recorder owns them and the canvas / G-buffer descriptors the stream points
+ * to (copies of the arguments), valid until the next command,
+ * rsrgpu_recorder_reset() or rsrgpu_recorder_destroy().  Buffers, indices
+ * and canvas data are the caller's and are referenced, not copied.  No CUDA
+ * call is made. */
+typedef struct rsrgpu_recorder rsrgpu_recorder;
+int rsrgpu_recorder_create(rsrgpu_recorder** out);
+int rsrgpu_recorder_destroy(rsrgpu_recorder* rec);
+/* GL::Reset: an empty frame and the default state */
+int rsrgpu_recorder_reset(rsrgpu_recorder* rec);
+int rsrgpu_recorder_frame(rsrgpu_recorder* rec, const uint8_t** commands, size_t* nbytes,
+                          const rsrgpu_glstate** states, int* nstates);
+/* GL::Enable / Disable: RSRGPU_GL_CULL_FACE, _SCISSOR_TEST, _BLEND, _DEPTH_TEST */
+int rsrgpu_gl_enable(rsrgpu_recorder* rec, int cap);
+int rsrgpu_gl_disable(rsrgpu_recorder* rec, int cap);
+/* GL::CullFace, DepthFunc, DepthWriteMask, ColorWriteMask, UseProgram,
+ * RenderbufferType(GL_COLOR_ATTACHMENT0 / GL_DEPTH_ATTACHMENT, type) */
+#define RSRGPU_GLSTATE_CULL_FACE        1
+#define RSRGPU_GLSTATE_DEPTH_FUNC       2
+#define RSRGPU_GLSTATE_DEPTH_WRITE_MASK 3
+#define RSRGPU_GLSTATE_COLOR_WRITE_MASK 4
+#define RSRGPU_GLSTATE_PROGRAM          5
+#define RSRGPU_GLSTATE_COLOR_ATTACHMENT 6
+#define RSRGPU_GLSTATE_DEPTH_ATTACHMENT 7
+int rsrgpu_gl_state_int(rsrgpu_recorder* rec, int what, int value);
+int rsrgpu_gl_scissor(rsrgpu_recorder* rec, int x, int y, int width, int height);
+int rsrgpu_gl_viewport(rsrgpu_recorder* rec, int x, int y, int width, int height);
+/* the state's uniform block: up to 32 floats (the rest zero) */
+int rsrgpu_gl_use_uniforms(rsrgpu_recorder* rec, const float* values, int n);
+int rsrgpu_gl_bind_texture(rsrgpu_recorder* rec, int unit, const float* texels, int width, int height, int stride,
+                           int filter);
+/* GL::UseBuffer(slot, float*): slots 0..15 (a Float3Array is three slots) */
+int rsrgpu_gl_use_buffer(rsrgpu_recorder* rec, int slot, const float* data);
+int rsrgpu_gl_clear_color(rsrgpu_recorder* rec, float red, float green, float blue);
+int rsrgpu_gl_clear_depth(rsrgpu_recorder* rec, float depth);
+/* GL::ViewMatrix, ProjectionMatrix, NormalMatrix: column-major mat4 */
+#define RSRGPU_GLMATRIX_VIEW       0
+#define RSRGPU_GLMATRIX_PROJECTION 1
+#define RSRGPU_GLMATRIX_NORMAL     2
+int rsrgpu_gl_matrix(rsrgpu_recorder* rec, int which, const float m[16]);
+/* GL::ResetX */
+int rsrgpu_gl_reset_state(rsrgpu_recorder* rec);
+/* commands (rglv_gl.cxx:13-89); stride 0 = width (quads: width / 2) */
+int rsrgpu_gl_clear(rsrgpu_recorder* rec, int bits);
+int rsrgpu_gl_draw_elements(rsrgpu_recorder* rec, int count, const uint16_t* indices, int hint);
+int rsrgpu_gl_draw_arrays(rsrgpu_recorder* rec, int count);
+int rsrgpu_gl_draw_elements_instanced(rsrgpu_recorder* rec, int count, const uint16_t* indices, int instances);
+int rsrgpu_gl_draw_arrays_instanced(rsrgpu_recorder* rec, int count, int instances);
+int rsrgpu_gl_store_color_tc(rsrgpu_recorder* rec, uint32_t* data, int width, int height, int stride, int gamma);
+int rsrgpu_gl_store_color_fp(rsrgpu_recorder* rec, float* data, int width, int height, int stride, int downsample);
+int rsrgpu_gl_store_color_quads(rsrgpu_recorder* rec, float* data, int width, int height, int stride);
+int rsrgpu_gl_store_depth(rsrgpu_recorder* rec, float* data);
+int rsrgpu_gl_store_gbuffer(rsrgpu_recorder* rec, const rsrgpu_gbuffer* gbuffer);
 
 /* ---- texture upload and mip chain on the device ----
  * rglr::Texture's layout (src/rgl/rglr/rglr_texture.hxx:10-33): RGBA float

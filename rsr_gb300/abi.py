@@ -210,6 +210,36 @@ SYMBOLS = {
     "rsrgpu_batch_frame": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "rsrgpu_batch_tune": ([ctypes.c_void_p, ctypes.POINTER(FrameDescC), ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "rsrgpu_batch_last_error": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "rsrgpu_recorder_create": ([ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "rsrgpu_recorder_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_recorder_reset": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_recorder_frame": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_size_t),
+                               ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "rsrgpu_gl_enable": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_disable": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_state_int": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_scissor": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_viewport": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_use_uniforms": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_bind_texture": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_use_buffer": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_gl_clear_color": ([ctypes.c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float], ctypes.c_int),
+    "rsrgpu_gl_clear_depth": ([ctypes.c_void_p, ctypes.c_float], ctypes.c_int),
+    "rsrgpu_gl_matrix": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_gl_reset_state": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_gl_clear": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_draw_elements": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_draw_arrays": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_draw_elements_instanced": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_draw_arrays_instanced": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_store_color_tc": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+                                 ctypes.c_int),
+    "rsrgpu_gl_store_color_fp": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+                                 ctypes.c_int),
+    "rsrgpu_gl_store_color_quads": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "rsrgpu_gl_store_depth": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_gl_store_gbuffer": ([ctypes.c_void_p, ctypes.POINTER(GBufferC)], ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
