@@ -19,10 +19,10 @@
 
 struct rsrgpu_recorder {
     std::vector<uint8_t> cmds;
-    std::deque<rsrgpu_glstate> states;      // stable addresses are not needed, contiguity is
-    std::vector<rsrgpu_glstate> frame_states;
+    std::vector<rsrgpu_glstate> states;     // the snapshots, indexed by CMD_STATE
     rsrgpu_glstate cur{};
     bool dirty = false;
+    // descriptors the stream points to: a deque keeps their addresses stable
     std::deque<rsrgpu_truecolor_canvas> tc;
     std::deque<rsrgpu_fp_canvas> fp;
     std::deque<rsrgpu_gbuffer> gb;
@@ -104,7 +104,6 @@ int rsrgpu_recorder_reset(rsrgpu_recorder* r) {
     if (r == nullptr) return RSRGPU_EINVAL;
     r->cmds.clear();
     r->states.clear();
-    r->frame_states.clear();
     r->tc.clear();
     r->fp.clear();
     r->gb.clear();
@@ -117,11 +116,10 @@ int rsrgpu_recorder_frame(rsrgpu_recorder* r, const uint8_t** commands, size_t* 
                           const rsrgpu_glstate** states, int* nstates) {
     if (r == nullptr || commands == nullptr || nbytes == nullptr || states == nullptr || nstates == nullptr)
         return RSRGPU_EINVAL;
-    r->frame_states.assign(r->states.begin(), r->states.end());
     *commands = r->cmds.data();
     *nbytes = r->cmds.size();
-    *states = r->frame_states.data();
-    *nstates = int(r->frame_states.size());
+    *states = r->states.data();
+    *nstates = int(r->states.size());
     return 0;
 }
 
