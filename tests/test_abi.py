@@ -81,3 +81,58 @@ def test_splitmix64_known_values():
     # splitmix64 with seed 0: the published first outputs
     assert [hex(int(v)) for v in splitmix64(0, 3)] == [
         "0xe220a8397b1dcdaf", "0x6e789e6aa1b965f4", "0x6c45d188009454f"]
+
+
+def test_c_caller_links_and_records(built, tmp_path):
+    """A C99 program includes include/rsrgpu.h, links librsrgpu.so and records
+    a frame with the native recorder (no CUDA call); its stream equals the
+    Python recorder's for the same calls, up to the canvas pointer."""
+    import subprocess
+    src = tmp_path / "caller.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "rsrgpu.h"
+int main(void) {
+    static float x[4], y[4], z[4], r[4], g[4], b[4];
+    static uint16_t idx[3] = { 0, 1, 2 };
+    static uint32_t color[64 * 32];
+    rsrgpu_recorder* rec;
+    if (rsrgpu_recorder_create(&rec)) return 1;
+    rsrgpu_gl_state_int(rec, RSRGPU_GLSTATE_COLOR_ATTACHMENT, RSRGPU_RB_RGBF32);
+    rsrgpu_gl_state_int(rec, RSRGPU_GLSTATE_DEPTH_ATTACHMENT, RSRGPU_RB_F32);
+    rsrgpu_gl_clear(rec, RSRGPU_GL_COLOR_BUFFER_BIT | RSRGPU_GL_DEPTH_BUFFER_BIT);
+    rsrgpu_gl_state_int(rec, RSRGPU_GLSTATE_PROGRAM, RSRGPU_PROGRAM_GOURAUD);
+    const float* bufs[6] = { x, y, z, r, g, b };
+    for (int i = 0; i < 6; ++i) rsrgpu_gl_use_buffer(rec, i, bufs[i]);
+    rsrgpu_gl_draw_elements(rec, 3, idx, 0);
+    rsrgpu_gl_state_int(rec, RSRGPU_GLSTATE_PROGRAM, RSRGPU_PROGRAM_DEFAULT_POST);
+    rsrgpu_gl_store_color_tc(rec, color, 64, 32, 0, 1);
+    const uint8_t* cmds; size_t n; const rsrgpu_glstate* states; int ns;
+    if (rsrgpu_recorder_frame(rec, &cmds, &n, &states, &ns)) return 2;
+    printf("%d %lu %lu %lu\n", ns, (unsigned long)(uintptr_t)idx, (unsigned long)(uintptr_t)x, (unsigned long)n);
+    for (size_t i = 0; i < n; ++i) printf("%02x", cmds[i]);
+    printf("\n");
+    rsrgpu_recorder_destroy(rec);
+    return 0;
+}
+''')
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(abi.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-lrsrgpu", "-Wl,-rpath," + libdir], check=True)
+    out = subprocess.run([str(exe)], check=True, stdout=subprocess.PIPE, text=True).stdout.split("\n")
+    ns, idx_addr, x_addr, n = (int(v) for v in out[0].split())
+    got = bytes.fromhex(out[1])
+    assert ns == 3 and len(got) == n
+    gl = GL()
+    gl.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, abi.RB_RGBF32)
+    gl.RenderbufferType(abi.GL_DEPTH_ATTACHMENT, abi.RB_F32)
+    gl.Clear(3)
+    gl.UseProgram(abi.PROGRAM_GOURAUD)
+    gl.UseBuffer(0, (x_addr, x_addr + 16, x_addr + 32))
+    gl.DrawElements(3, idx_addr, 0)
+    gl.UseProgram(abi.PROGRAM_DEFAULT_POST)
+    gl.StoreColor(np.zeros(64 * 32, np.uint32), 64, 32, True)
+    want = gl.stream()
+    # equal up to the last 8 bytes: the TrueColor canvas descriptor's address
+    assert len(got) == len(want) and got[:-8] == want[:-8]
