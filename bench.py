@@ -148,6 +148,20 @@ def max_over_ranks(world, x):
     return float(t.item())
 
 
+def calc_stat(samples_ms, discard=0.05):
+    """The statistic of rsr's perf harness (rmls::CalcStat, src/rml/rmls/
+    rmls_bench.cxx:11-38): sorted samples, the worst `discard` share dropped,
+    then min / p25 / median / p75 / max (entries n/4, n/2, 3n/4 of the kept
+    n), mean and population standard deviation."""
+    s = sorted(samples_ms)
+    s = s[:max(1, int(len(s) * (1.0 - discard)))]
+    n = len(s)
+    mean = sum(s) / n
+    sd = (sum((x - mean) ** 2 for x in s) / n) ** 0.5
+    return {"min": s[0], "p25": s[n // 4], "median": s[n // 2], "p75": s[3 * n // 4], "max": s[-1],
+            "mean": mean, "sd": sd, "kept": n, "discard": discard, "unit": "ms"}
+
+
 def cpu_sample(which, sc, seconds=15.0, max_frames=200, threads=None):
     """Times the CPU implementation on a bounded sample of frames."""
     import oracle
@@ -205,7 +219,8 @@ def run_reference(args):
                              "kind": "reference" if which == "ref" else "port",
                              "sample": "%d timed frames after %d warm-up, all host threads" % (args.steps, args.warmup)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "frames_per_s": args.steps / total}
+            "frames_per_s": args.steps / total,
+            "frame_ms_stats": calc_stat([t * 1e3 for t in times])}
     print(json.dumps(line))
 
 
@@ -254,7 +269,8 @@ def run_gpu(args):
             raster_ms.append(gpu.timings()[1])
         torch.cuda.synchronize()
     barrier(world)
-    dev_ms = sum(s.elapsed_time(e) for s, e in ev)
+    frame_ms = [s.elapsed_time(e) for s, e in ev]
+    dev_ms = sum(frame_ms)
     dev_ms = max_over_ranks(world, dev_ms)
     value = sc.ntris * args.steps * world / (dev_ms / 1e3) / 1e6
     ms_per_step = dev_ms / args.steps
@@ -313,6 +329,7 @@ def run_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_ms / args.steps},
             "frames_per_s": 1e3 / ms_per_step, "e2e_frames_per_s": 1e3 * args.steps / e2e_ms,
+            "frame_ms_stats": calc_stat(frame_ms),
             "gpu_launches": 3 * args.steps, "roofline": roof, "cpu_baseline": cpu,
             "clocks": clocks.summary(local)}
     if not args.no_post:
