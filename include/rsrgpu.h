@@ -126,7 +126,7 @@ extern "C" {
 #define RSRGPU_ECUDA        -3   /* CUDA runtime error */
 #define RSRGPU_ECAPACITY    -4   /* a device capacity was exceeded and could not be grown */
 #define RSRGPU_ETIMEOUT     -5   /* rsrgpu_wait() timed out */
-#define RSRGPU_EUNSUPPORTED -6   /* a protocol feature this build does not implement */
+#define RSRGPU_EUNSUPPORTED -6   /* a protocol feature this library does not implement */
 
 /* Texture unit binding, mirrors rglv::TextureState (rglv_gl.hxx:64-77).
  * ptr: RGBA float32 pixels (PixelToaster::FloatingPointPixel).  For square
@@ -267,7 +267,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx);
 
 /* GPU::Install(programId, stateKey, ptrs) -- rglv_gpu.cxx:26-47.  kind:
  * 0 = bin (vertex) program, 1 = draw (fragment) program, 2 = blt program.
- * Fails with RSRGPU_ENODISPATCH when this build has no device implementation
+ * Fails with RSRGPU_ENODISPATCH when this library has no device implementation
  * of the program for that state key. */
 int rsrgpu_install(rsrgpu_ctx* ctx, int program_id, uint32_t state_key, int kind);
 
