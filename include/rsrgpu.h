@@ -329,7 +329,8 @@ int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
 typedef struct rsrgpu_recorder rsrgpu_recorder;
 int rsrgpu_recorder_create(rsrgpu_recorder** out);
 int rsrgpu_recorder_destroy(rsrgpu_recorder* rec);
-/* GL::Reset: an empty frame and the default state */
+/* GL::Reset: an empty frame and the default state, marked changed, so the
+ * next command records a snapshot of the defaults first (rglv_gl.cxx:92-97) */
 int rsrgpu_recorder_reset(rsrgpu_recorder* rec);
 int rsrgpu_recorder_frame(rsrgpu_recorder* rec, const uint8_t** commands, size_t* nbytes,
                           const rsrgpu_glstate** states, int* nstates);

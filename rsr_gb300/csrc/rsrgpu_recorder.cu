@@ -108,7 +108,9 @@ int rsrgpu_recorder_reset(rsrgpu_recorder* r) {
     r->fp.clear();
     r->gb.clear();
     default_state(r->cur);
-    r->dirty = false;
+    // GL::Reset (rglv_gl.cxx:92-97) leaves the state dirty: the first command
+    // after a reset snapshots the default state
+    r->dirty = true;
     return 0;
 }
 

@@ -231,6 +231,15 @@ class GL:
         self._dirty = True
         self._cs.reset()
 
+    def Reset(self):
+        """GL::Reset (rglv_gl.cxx:92-97): an empty frame, the default state,
+        marked changed so the next command snapshots it."""
+        self.commands = bytearray()
+        self.states = []
+        self._keep = []
+        self._cs.reset()
+        self._dirty = True
+
     # ---- commands (rglv_gl.cxx:13-89) ----
     def _maybe_update_state(self):
         if not self._dirty:

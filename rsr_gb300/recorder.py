@@ -107,6 +107,12 @@ class NativeGL:
     def ResetX(self):
         self._ok(self.lib.rsrgpu_gl_reset_state(self.h))
 
+    def Reset(self):
+        """GL::Reset: an empty frame and the default state, snapshotted by
+        the next command."""
+        self._ok(self.lib.rsrgpu_recorder_reset(self.h))
+        self._keep = []
+
     # ---- commands ----
     def Clear(self, bits):
         self._ok(self.lib.rsrgpu_gl_clear(self.h, int(bits)))

@@ -112,6 +112,31 @@ def test_recorder_reset_and_errors(lib):
     ref.close()
 
 
+def test_reset_snapshots_the_defaults(lib):
+    """GL::Reset leaves the state marked changed (rglv_gl.cxx:92-97): a Clear
+    right after it, with no state setter, is preceded by CMD_STATE and a
+    snapshot of the default state -- in both recorders."""
+    from rsr_gb300.gl import GL
+    fresh = NativeGL(lib)
+    fresh.ResetX()
+    fresh.Clear(3)
+    for g in (NativeGL(lib), GL()):
+        g.DepthFunc(abi.GL_LEQUAL)
+        g.Clear(3)
+        g.Reset()
+        assert g.stream() == b""
+        g.Clear(3)
+        s = g.stream()
+        assert s[0] == abi.CMD_STATE and struct.unpack_from("<Q", s, 1)[0] == 0
+        assert s[9] == abi.CMD_CLEAR and len(s) == 11
+        assert len(g.states) == 1
+        a, b = g.c_states(), fresh.c_states()
+        assert ctypes.string_at(a, ctypes.sizeof(a)) == ctypes.string_at(b, ctypes.sizeof(b))
+        if isinstance(g, NativeGL):
+            g.close()
+    fresh.close()
+
+
 @pytest.mark.gpu
 def test_gpu_renders_a_natively_recorded_frame(built, monkeypatch):
     """A frame recorded by the native recorder renders like the oracle's
