@@ -36,6 +36,10 @@ GOLDEN_SCENES = {
     "plain_1080_t128": ("plain_raster", dict(seed=8, ntris=500, width=1920, height=1080, tile_blocks=(16, 16)), 3),
     "plain_640_t16x32": ("plain_raster", dict(seed=9, ntris=3000, width=640, height=360, tile_blocks=(2, 4)), 3),
     "sphere_1080_t32": ("textured_sphere", dict(divs=6), 2),
+    # the benchmarked frame itself: seed 1, 7 subdivisions (327 680 triangles),
+    # 1920x1080, 32 px tiles, 1024x1024 texture
+    "sphere_1080_t32_d7": ("textured_sphere", dict(seed=1, divs=7, width=1920, height=1080, tile_blocks=(4, 4),
+                                                   tex_dim=1024), 2),
     "clip_640_t64": ("clip_stress", {}, 3),
     "clip_2160_t32": ("clip_stress", dict(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0), 3),
     "mixed_640_t32": ("mixed_states", {}, 3),

@@ -23,6 +23,9 @@ SCENES = {
     "plain_1080_t128": lambda: scenes.plain_raster(seed=8, ntris=500, width=1920, height=1080, tile_blocks=(16, 16)),
     "plain_640_t16x32": lambda: scenes.plain_raster(seed=9, ntris=3000, width=640, height=360, tile_blocks=(2, 4)),
     "sphere_1080_t32": lambda: scenes.textured_sphere(divs=6),
+    # the benchmarked frame (bench.py's workload): 327 680 triangles
+    "sphere_1080_t32_d7": lambda: scenes.textured_sphere(seed=1, divs=7, width=1920, height=1080, tile_blocks=(4, 4),
+                                                         tex_dim=1024),
     "clip_640_t64": lambda: scenes.clip_stress(),
     "clip_2160_t32": lambda: scenes.clip_stress(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0),
     "mixed_640_t32": lambda: scenes.mixed_states(),
