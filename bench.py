@@ -10,13 +10,21 @@ Reported (one JSON line from rank 0):
   value      Mtris/s with inputs resident in HBM, device time of the frame's
              kernels (CUDA events on the launching stream), L2 flushed with a
              256 MiB write before every timed frame (outside the event pair)
-  e2e        the same metric through the C ABI with host (pinned) buffers:
-             every frame moves its inputs to the device (vertex data by one
-             gather kernel, the texture by a copy overlapping setup and
-             binning) and its colour and depth back (written into the host
-             buffers by the raster pass), inside the timed region
-  roofline   dominant kernel (raster) against measured HBM bandwidth
+  e2e        the same metric through the C ABI as rsr's own caller drives
+             it (GPUNode::Main inside rsr's perf loop): every frame is reset,
+             recorded by the native recorder, submitted, run and waited for
+             (rsrgpu_perf_frames, host clock); inputs and outputs live in
+             pinned host memory, so every frame moves its inputs to the device
+             (vertex data by one gather kernel, the texture by a copy
+             overlapping setup and binning) and its colour and depth back
+             (written into the host buffers by the raster pass)
+  roofline   dominant kernel (raster): warp-instruction issue rate against the
+             SMs' issue peak at the sampled clock (the bound it runs against),
+             and the frame's compulsory DRAM bytes against measured HBM
+             bandwidth
   cpu_baseline  the CPU implementation on this machine's cores, bounded sample
+  config1    the 640x360 plain frame (10 000 random triangles): Mtris/s,
+             frames/s, candidate fragments/s, end to end, its CPU baseline
 
 `--impl reference` times the CPU implementation of the same frame instead:
 rsr itself (oracle/_ref) where it can run (x86-64 hosts), else the oracle's
@@ -57,12 +65,36 @@ def config_dict(sc):
             "parallelism": "replicas"}
 
 
-def hbm_peak():
+def _peaks():
     try:
         with open(PEAKS) as f:
-            return float(json.load(f)["hbm_gbs"]), "measured"
+            return json.load(f)
     except Exception:
-        return FALLBACK_HBM_GBS, "fallback"
+        return {}
+
+
+def hbm_peak():
+    p = _peaks()
+    if "hbm_gbs" in p:
+        return float(p["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def cpu_model():
+    """The host CPU's model name (x86: /proc/cpuinfo 'model name'; Arm: the
+    implementer/part fields), and the machine."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+        for key in ("model name", "Model Name"):
+            for line in info.splitlines():
+                if line.startswith(key):
+                    return "%s (%s)" % (line.split(":", 1)[1].strip(), platform.machine())
+        parts = sorted({line.split(":", 1)[1].strip() for line in info.splitlines() if line.startswith("CPU part")})
+        impl = sorted({line.split(":", 1)[1].strip() for line in info.splitlines() if line.startswith("CPU implementer")})
+        return "CPU implementer %s part %s (%s)" % ("/".join(impl), "/".join(parts), platform.machine())
+    except Exception:
+        return platform.machine()
 
 
 class ClockSampler:
@@ -162,12 +194,14 @@ def calc_stat(samples_ms, discard=0.05):
             "mean": mean, "sd": sd, "kept": n, "discard": discard, "unit": "ms"}
 
 
-def cpu_sample(which, sc, seconds=15.0, max_frames=200, threads=None):
-    """Times the CPU implementation on a bounded sample of frames."""
+def cpu_sample(which, sc, seconds=15.0, max_frames=200, threads=None, count_fragments=False):
+    """Times the CPU implementation on a bounded sample of frames (each frame
+    recorded and rendered, all host threads)."""
     import oracle
     threads = threads or os.cpu_count()
     r = oracle.CpuRenderer(which, threads=threads)
     r.render(sc, True)   # warm-up (page-in, allocation)
+    frags = r.candidate_fragments() if count_fragments and which == "oracle" else None
     times = []
     t_end = time.perf_counter() + seconds
     while len(times) < max_frames and (time.perf_counter() < t_end or len(times) < 3):
@@ -176,11 +210,17 @@ def cpu_sample(which, sc, seconds=15.0, max_frames=200, threads=None):
         r.render_gl(gl, sc.width, sc.height, sc.tile_blocks)
         times.append(time.perf_counter() - t0)
     med = statistics.median(times)
-    return {"value": sc.ntris / med / 1e6, "unit": UNIT, "cores": threads,
-            "kind": "reference" if which == "ref" else "port",
-            "sample": "%d frames of the same 1080p frame, median %.2f ms/frame (%s)" % (
-                len(times), med * 1e3, "rsr built from source" if which == "ref" else "C restatement of rsr's path"),
-            "frames_per_s": 1.0 / med}
+    out = {"value": sc.ntris / med / 1e6, "unit": UNIT, "cores": threads,
+           "kind": "reference" if which == "ref" else "port",
+           "sample": "%d frames of the same %dx%d frame, median %.2f ms/frame (%s)" % (
+               len(times), sc.width, sc.height, med * 1e3,
+               "rsr built from source" if which == "ref" else "C restatement of rsr's path"),
+           "frames_per_s": 1.0 / med, "cpu": cpu_model(),
+           "frame_ms_stats": calc_stat([t * 1e3 for t in times])}
+    if frags is not None:
+        out["candidate_fragments_per_frame"] = frags
+        out["candidate_fragments_per_s"] = frags / med
+    return out
 
 
 def cpu_impl_available():
@@ -216,83 +256,119 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)", "config": config_dict(sc),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads,
-                             "kind": "reference" if which == "ref" else "port",
-                             "sample": "%d timed frames after %d warm-up, all host threads" % (args.steps, args.warmup)},
+                             "kind": "reference" if which == "ref" else "port", "cpu": cpu_model(),
+                             "sample": "%d timed frames after %d warm-up, all host threads, each frame recorded "
+                                       "and rendered (%s)" % (args.steps, args.warmup,
+                                                              "rsr built from source" if which == "ref"
+                                                              else "C restatement of rsr's path")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "frames_per_s": args.steps / total,
             "frame_ms_stats": calc_stat([t * 1e3 for t in times])}
+    # the 640x360 plain frame (10 000 random triangles) the same way
+    from rsr_gb300 import scenes
+    c1 = scenes.plain_raster()
+    r.render(c1, True)
+    t1 = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r.render_gl(c1.record(gamma=True), c1.width, c1.height, c1.tile_blocks)
+        t1.append(time.perf_counter() - t0)
+    line["config1"] = {"workload": "plain_640x360: 10 000 random NDC triangles (seed 0), Gouraud, LESS, 64 px tiles",
+                       "value": c1.ntris * len(t1) / sum(t1) / 1e6, "unit": UNIT,
+                       "frames_per_s": len(t1) / sum(t1), "frame_ms_stats": calc_stat([t * 1e3 for t in t1])}
     print(json.dumps(line))
 
 
-def run_gpu(args):
+def _soak(gpu, sptr, seconds):
+    """Untimed frames that keep the GPU under the bench's load (so the clock
+    samples taken around a short timed region see the clocks it ran at)."""
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end:
+        gpu.run(sptr)
+        gpu.Wait()
+
+
+def _script_of(sc, ref, color, depth, gamma=True):
+    """The frame's GL calls as a call script (played natively every frame by
+    the perf harness)."""
+    from rsr_gb300 import scenes
+    from rsr_gb300.recorder import ScriptGL
+    script = ScriptGL()
+    orig = scenes.GL
+    scenes.GL = lambda: script
+    try:
+        sc.record(ref=ref, color=color, depth=depth, gamma=gamma)
+    finally:
+        scenes.GL = orig
+    return script
+
+
+def measure_frame(gpu, sc, args, stream, flush, world, clocks=None):
+    """One frame's figures: device time with inputs resident in HBM (graph
+    replays of the submitted frame, CUDA events on the launching stream, L2
+    flushed before each) and end to end through the C ABI (the perf harness:
+    every frame reset, recorded natively, submitted, run and waited for, with
+    inputs and outputs in pinned host memory)."""
     import torch
-    from rsr_gb300 import build
-    build.build_gpu()
-    from rsr_gb300.gpu import GPU
-
-    world, rank, local = dist_setup()
-    torch.cuda.set_device(local)
-    sc = workload()
-    gpu = GPU(local)
-    gpu.InstallDefaults()
-    stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
-
-    # ---- device-resident inputs and outputs ----
     dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
     col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
     dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     gpu.Reset(sc.width, sc.height, sc.tile_blocks)
-    gl = sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)
-    gpu.submit(gl)
+    gpu.submit(sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True))
     torch.cuda.synchronize()
     for _ in range(max(args.warmup, 3)):
         gpu.run(sptr)
         gpu.Wait()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     raster_ms = []
-    # the raw samples go to RSR_BENCH_CLOCKS_DIR (default: the temp directory);
-    # the line carries their summary
-    import tempfile
-    clocks = ClockSampler(os.path.join(os.environ.get("RSR_BENCH_CLOCKS_DIR", tempfile.gettempdir()),
-                                       "bench_clocks_%d.csv" % rank))
-    barrier(world)
-    torch.cuda.synchronize()
-    with clocks, torch.cuda.stream(stream):
-        for i in range(args.steps):
-            flush.fill_(i & 0xff)                     # evict L2 (outside the timed pair)
-            ev[i][0].record(stream)
-            gpu.run(sptr)
-            ev[i][1].record(stream)
-            gpu.Wait()
-            raster_ms.append(gpu.timings()[1])
+    import contextlib
+    with (clocks if clocks is not None else contextlib.nullcontext()):
+        if clocks is not None:
+            _soak(gpu, sptr, 0.3)
+        barrier(world)
         torch.cuda.synchronize()
-    barrier(world)
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                flush.fill_(i & 0xff)                     # evict L2 (outside the timed pair)
+                ev[i][0].record(stream)
+                gpu.run(sptr)
+                ev[i][1].record(stream)
+                gpu.Wait()
+                raster_ms.append(gpu.timings()[1])
+            torch.cuda.synchronize()
+        barrier(world)
+        if clocks is not None:
+            _soak(gpu, sptr, 0.3)
     frame_ms = [s.elapsed_time(e) for s, e in ev]
-    dev_ms = sum(frame_ms)
-    dev_ms = max_over_ranks(world, dev_ms)
-    value = sc.ntris * args.steps * world / (dev_ms / 1e3) / 1e6
-    ms_per_step = dev_ms / args.steps
+    dev_ms = max_over_ranks(world, sum(frame_ms))
+    stats = gpu.stats()
+    out = {"ms_per_step": dev_ms / args.steps, "frame_ms": frame_ms, "raster_ms": statistics.mean(raster_ms),
+           "value": sc.ntris * args.steps * world / (dev_ms / 1e3) / 1e6, "stats": stats}
 
-    # ---- end to end through the C ABI with pinned host buffers ----
+    # ---- end to end: the perf harness through the C ABI, pinned host buffers ----
     host = {k: torch.from_numpy(v).pin_memory() for k, v in sc.arrays.items()}
     hcol = torch.zeros(sc.width * sc.height, dtype=torch.int32).pin_memory()
     hdep = torch.zeros(sc.width * sc.height, dtype=torch.float32).pin_memory()
     for t in list(host.values()) + [hcol, hdep]:
         gpu.register_host_buffer(t)
-    gpu.Reset(sc.width, sc.height, sc.tile_blocks)
-    gl2 = sc.record(ref=host.__getitem__, color=hcol, depth=hdep, gamma=True)
-    gpu.submit(gl2)
-    for _ in range(max(args.warmup, 3)):
-        gpu.run(sptr)
-        gpu.Wait()
+    script = _script_of(sc, host.__getitem__, hcol, hdep)
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = hcol.numel() * 4 + hdep.numel() * 4
+    gpu.perf_frames(script, sc.width, sc.height, sc.tile_blocks, frames=0, priming=max(args.warmup, 3), stream=sptr)
+    captures0 = gpu.stats()["graph_captures"]
     barrier(world)
     torch.cuda.synchronize()
+    e2e_frames = gpu.perf_frames(script, sc.width, sc.height, sc.tile_blocks, frames=args.steps, stream=sptr)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(world, sum(e2e_frames))
+    st2 = gpu.stats()
+    # the frame is correct end to end (host depth equals the device-resident render)
+    assert torch.equal(hdep, dep.cpu())
+    # replays of the submitted frame only (no per-frame record and submit)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
     e0.record(stream)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -300,40 +376,110 @@ def run_gpu(args):
         gpu.Wait()
     e1.record(stream)
     torch.cuda.synchronize()
-    wall_ms = (time.perf_counter() - t0) * 1e3
-    e2e_ms = max_over_ranks(world, max(wall_ms, e0.elapsed_time(e1)))
-    e2e_value = sc.ntris * args.steps * world / (e2e_ms / 1e3) / 1e6
-    # the frame is correct end to end (depth of the last host frame equals the device one)
-    assert torch.equal(hdep, dep.cpu())
+    replay_ms = max_over_ranks(world, max((time.perf_counter() - t0) * 1e3, e0.elapsed_time(e1)))
+    for t in list(host.values()) + [hcol, hdep]:
+        gpu.unregister_host_buffer(t)
+    out["e2e"] = {"value": sc.ntris * args.steps * world / (e2e_ms / 1e3) / 1e6, "unit": UNIT,
+                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps,
+                  "frames_per_s": 1e3 * args.steps / e2e_ms,
+                  "per_step": "rsrgpu_perf_frames: reset, native recording of the frame's GL calls, rsrgpu_submit, "
+                              "rsrgpu_run, rsrgpu_wait (host clock); inputs and outputs in pinned host memory",
+                  "graph_captures_in_timed_frames": st2["graph_captures"] - captures0,
+                  "frame_ms_stats": calc_stat(e2e_frames),
+                  "replay_only": {"value": sc.ntris * args.steps * world / (replay_ms / 1e3) / 1e6,
+                                  "ms_per_step": replay_ms / args.steps,
+                                  "note": "rsrgpu_run + rsrgpu_wait of a submitted frame, no per-frame recording"}}
+    return out
 
+
+# Warp instructions one raster_kernel launch issues on the headline frame
+# (ncu smsp__inst_executed.sum of one launch; re-measured whenever the
+# kernel changes), and on the 640x360 plain frame.
+RASTER_WARP_INST = {"textured_sphere_1080p": None, "plain_640x360": None}
+
+
+def issue_roofline(kernel_ms, inst, sm_mhz, num_sms):
+    """Issue roofline of a kernel: warp instructions per second against the
+    SMs' issue peak (one warp instruction per cycle per sub-partition, four
+    per SM) at the SM clock sampled during the run."""
+    if inst is None or sm_mhz is None:
+        return None
+    achieved = inst / (kernel_ms / 1e3) / 1e9
+    peak = 4 * num_sms * sm_mhz * 1e6 / 1e9
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gwarp-inst/s", "frac": achieved / peak,
+            "warp_inst_per_launch": inst, "peak_basis": "4 warp-inst/clk/SM x %d SMs x %.0f MHz (sampled)" % (
+                num_sms, sm_mhz)}
+
+
+def run_gpu(args):
+    import torch
+    from rsr_gb300 import build, scenes
+    build.build_gpu()
+    from rsr_gb300.gpu import GPU
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sc = workload()
+    gpu = GPU(local)
+    gpu.InstallDefaults()
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    import tempfile
+    # the raw samples go to RSR_BENCH_CLOCKS_DIR (default: the temp directory);
+    # the line carries their summary
+    clocks = ClockSampler(os.path.join(os.environ.get("RSR_BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                                       "bench_clocks_%d.csv" % rank))
+    head = measure_frame(gpu, sc, args, stream, flush, world, clocks=clocks)
+    clk = clocks.summary(local)
+    sm_mhz = (clk or {}).get("sm_mhz") or _peaks().get("sm_max_mhz")
+    c1sc = scenes.plain_raster()
+    c1 = measure_frame(gpu, c1sc, args, stream, flush, world)
     if rank != 0:
         return
     peak, peak_kind = hbm_peak()
-    raster_avg = statistics.mean(raster_ms)
-    # algorithmic DRAM bytes of one raster launch: the triangle records it reads
-    # (96 B per tile-list entry), the colour and depth it writes (8 B per
-    # pixel) and the sampled mip level-0 texels (16 B each, read once)
-    gpu_tiles_bytes = _raster_bytes(gpu, sc)
-    achieved = gpu_tiles_bytes / (raster_avg / 1e3) / 1e9
-    roof = {"kernel": "raster_kernel", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": _ncu_traffic(), "algorithmic_bytes_per_launch": gpu_tiles_bytes,
-            "avg_launch_ms": raster_avg}
+    # compulsory DRAM bytes of the frame: vertex stream (positions 12 B and uv
+    # 8 B per vertex, 2 B per index), the level-0 texels (16 B each, read
+    # once at most), the sRGB8 colour and fp32 depth written (8 B per pixel)
+    vbytes = sum(v.nbytes for k, v in sc.arrays.items() if k != "tex")
+    comp = vbytes + 1024 * 1024 * 16 + sc.width * sc.height * 8
+    frame_s = head["ms_per_step"] / 1e3
+    roof = issue_roofline(head["raster_ms"], RASTER_WARP_INST["textured_sphere_1080p"], sm_mhz, num_sms) or {
+        "bound": "issue", "achieved": None, "peak": None, "unit": "Gwarp-inst/s", "frac": None}
+    roof.update({"kernel": "raster_kernel", "avg_launch_ms": head["raster_ms"], "traffic": None,
+                 "hbm": {"scope": "whole frame (setup, bin, raster)", "compulsory_bytes": comp,
+                         "achieved_gbs": comp / frame_s / 1e9, "peak_gbs": peak, "frac": comp / frame_s / 1e9 / peak,
+                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}})
     cpu = None
+    c1cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_sample(cpu_impl_available(), sc, seconds=args.cpu_seconds)
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        c1cpu = cpu_sample("oracle", c1sc, seconds=min(args.cpu_seconds, 10.0), count_fragments=True)
+    frags = (c1cpu or {}).get("candidate_fragments_per_frame")
+    c1_fps = 1e3 / c1["ms_per_step"]
+    c1_comp = sum(v.nbytes for v in c1sc.arrays.values()) + c1sc.width * c1sc.height * 8
+    c1roof = issue_roofline(c1["raster_ms"], RASTER_WARP_INST["plain_640x360"], sm_mhz, num_sms)
+    config1 = {"workload": "plain_640x360: 10 000 random NDC triangles (seed 0), Gouraud, LESS, 64 px tiles",
+               "triangles": c1sc.ntris, "value": c1["value"], "unit": UNIT, "ms_per_step": c1["ms_per_step"],
+               "frames_per_s": c1_fps, "frame_ms_stats": calc_stat(c1["frame_ms"]),
+               "candidate_fragments_per_frame": frags,
+               "candidate_fragments_per_s": frags * c1_fps if frags else None,
+               "e2e": c1["e2e"], "raster_ms": c1["raster_ms"],
+               "roofline": dict(c1roof or {"bound": "issue", "frac": None}, kernel="raster_kernel",
+                                hbm={"compulsory_bytes": c1_comp, "achieved_gbs": c1_comp / (c1["ms_per_step"] / 1e3) / 1e9,
+                                     "frac": c1_comp / (c1["ms_per_step"] / 1e3) / 1e9 / peak}),
+               "cpu_baseline": c1cpu}
+    line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere + value-noise texture)",
-            "config": config_dict(sc),
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_ms / args.steps},
-            "frames_per_s": 1e3 / ms_per_step, "e2e_frames_per_s": 1e3 * args.steps / e2e_ms,
-            "frame_ms_stats": calc_stat(frame_ms),
-            "gpu_launches": 3 * args.steps, "roofline": roof, "cpu_baseline": cpu,
-            "clocks": clocks.summary(local)}
+            "config": config_dict(sc), "e2e": head["e2e"],
+            "frames_per_s": 1e3 / head["ms_per_step"], "e2e_frames_per_s": head["e2e"]["frames_per_s"],
+            "frame_ms_stats": calc_stat(head["frame_ms"]),
+            "gpu_launches": head["stats"]["gpu_launches"] * args.steps, "roofline": roof, "cpu_baseline": cpu,
+            "clocks": clk, "config1": config1}
     if not args.no_post:
         try:
+            dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
             line["post"] = run_post(gpu, args, stream, flush, sc, dev)
         except Exception as e:   # the headline line is printed whatever happens here
             line["post"] = {"error": "%s: %s" % (type(e).__name__, e)}
@@ -342,9 +488,6 @@ def run_gpu(args):
     if not args.no_batch:
         line["batch"] = run_batch(gpu, args, stream, flush)
     print(json.dumps(line))
-
-
-_RASTER_BYTES = {}
 
 
 def _time_device(fn, steps, stream, flush):
@@ -635,29 +778,6 @@ def run_batch(gpu, args, stream, flush):
                                         "mtris_per_s": ntris / seq_ms / 1e3,
                                         "note": "wall clock: decode + run + wait per frame"},
             "gpu_launches_per_batch": "setup 1 + bin 1 + raster 1 per CTA shape (graph)"}
-
-
-def _raster_bytes(gpu, sc):
-    """Algorithmic bytes of one raster launch for this frame (see run_gpu)."""
-    tiles = gpu.tiles()
-    st = gpu.stats()
-    records = st["total_tile_records"] + st["total_clipped_records"]
-    texels = 1024 * 1024
-    return int(records * 96 + sc.width * sc.height * 8 + texels * 16)
-
-
-def _ncu_traffic():
-    """DRAM bytes per raster launch from the committed ncu summary (its
-    `traffic_bytes_per_launch:` line), if present."""
-    p = os.path.join(REPO, "profiles", "raster_kernel_textured_sphere_1080p.md")
-    try:
-        with open(p) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return int(line.split(":")[1])
-    except Exception:
-        pass
-    return None
 
 
 def main():

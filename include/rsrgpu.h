@@ -257,6 +257,8 @@ typedef struct rsrgpu_stats {
     int64_t primitives_submitted;
     int64_t primitives_clipped;
     int64_t gpu_launches;            /* kernels launched by the last run */
+    int64_t graph_captures;          /* runs captured into a new CUDA graph, since rsrgpu_create */
+    int64_t table_uploads;           /* frame-table uploads, since rsrgpu_create */
 } rsrgpu_stats;
 
 typedef struct rsrgpu_ctx rsrgpu_ctx;
@@ -281,17 +283,25 @@ int rsrgpu_reset(rsrgpu_ctx* ctx, int width, int height, int tile_blocks_x, int 
 int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t bytes);
 int rsrgpu_unregister_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr);
 
-/* Hand over one frame's commands (GL::commands_ plus its state deque). */
+/* Hand over one frame's commands (GL::commands_ plus its state deque):
+ * GPU::BinImpl's interpretation of the stream (rglv_gpu.cxx:119-260), done on
+ * the host.  The decoded tables (states, draws, ops) are uploaded by the next
+ * rsrgpu_run(), unless they equal the ones already on the device.  Submit
+ * after the previous run has been waited for. */
 int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes,
                   const rsrgpu_glstate* states, int nstates);
 
 /* GPU::Run() -- rglv_gpu.hxx:167, rglv_gpu.cxx:90-116.  Enqueues the frame on
- * `stream` (a cudaStream_t; NULL = the context's own stream).  The first run
- * after a submission captures the run's work into a CUDA graph; later runs
- * replay it (inputs are still read when each run executes).  The graph is
- * dropped by rsrgpu_submit(), rsrgpu_reset(), host-buffer (un)registration
- * and capacity growth.  A run on a stream the caller is capturing, or one
- * that copies pageable host memory, is enqueued directly. */
+ * `stream` (a cudaStream_t; NULL = the context's own stream).  A run
+ * captures its work into a CUDA graph and later runs replay it (inputs are
+ * still read when each run executes).  A new submission keeps the graph when
+ * the frame has the structure of the one captured -- the same target and
+ * tiling, triangle count, table sizes, kernel choices and host-buffer
+ * routes -- so a frame re-recorded every time (GPUNode::Main) costs its
+ * decode, a table upload when states changed, and a graph launch.  Other
+ * submissions, host-buffer (un)registration and capacity growth drop it.
+ * A run on a stream the caller is capturing, or one that copies pageable
+ * host memory, is enqueued directly. */
 int rsrgpu_run(rsrgpu_ctx* ctx, void* stream);
 
 /* Wait for the last run; timeout_ms < 0 waits without limit. */
@@ -375,6 +385,65 @@ int rsrgpu_gl_store_color_fp(rsrgpu_recorder* rec, float* data, int width, int h
 int rsrgpu_gl_store_color_quads(rsrgpu_recorder* rec, float* data, int width, int height, int stride);
 int rsrgpu_gl_store_depth(rsrgpu_recorder* rec, float* data);
 int rsrgpu_gl_store_gbuffer(rsrgpu_recorder* rec, const rsrgpu_gbuffer* gbuffer);
+
+/* ---- GL call scripts and the perf harness ----
+ * A frame's rglv::GL calls as data: one rsrgpu_gl_call per rsrgpu_gl_* call,
+ * with that call's arguments (integers in i[], the pointer in p, floats --
+ * colours, depth, matrix, uniforms -- in f[]):
+ *   ENABLE/DISABLE i0=cap; STATE_INT i0=what i1=value; SCISSOR/VIEWPORT
+ *   i0..i3; USE_UNIFORMS i0=n f; BIND_TEXTURE i0=unit p i1=width i2=height
+ *   i3=stride i4=filter; USE_BUFFER i0=slot p; CLEAR_COLOR f0..f2;
+ *   CLEAR_DEPTH f0; MATRIX i0=which f0..f15; RESET_STATE; CLEAR i0=bits;
+ *   DRAW_ELEMENTS i0=count p i1=hint; DRAW_ARRAYS i0=count;
+ *   DRAW_ELEMENTS_INSTANCED i0=count p i1=instances; DRAW_ARRAYS_INSTANCED
+ *   i0=count i1=instances; STORE_COLOR_TC p i0=width i1=height i2=stride
+ *   i3=gamma; STORE_COLOR_FP p i0..i2 i3=downsample; STORE_COLOR_QUADS p
+ *   i0..i2; STORE_DEPTH p; STORE_GBUFFER p=rsrgpu_gbuffer*.
+ * rsrgpu_gl_play() makes the calls on a recorder, in order, and stops at the
+ * first that fails (its status is returned). */
+#define RSRGPU_CALL_ENABLE                  1
+#define RSRGPU_CALL_DISABLE                 2
+#define RSRGPU_CALL_STATE_INT               3
+#define RSRGPU_CALL_SCISSOR                 4
+#define RSRGPU_CALL_VIEWPORT                5
+#define RSRGPU_CALL_USE_UNIFORMS            6
+#define RSRGPU_CALL_BIND_TEXTURE            7
+#define RSRGPU_CALL_USE_BUFFER              8
+#define RSRGPU_CALL_CLEAR_COLOR             9
+#define RSRGPU_CALL_CLEAR_DEPTH             10
+#define RSRGPU_CALL_MATRIX                  11
+#define RSRGPU_CALL_RESET_STATE             12
+#define RSRGPU_CALL_CLEAR                   13
+#define RSRGPU_CALL_DRAW_ELEMENTS           14
+#define RSRGPU_CALL_DRAW_ARRAYS             15
+#define RSRGPU_CALL_DRAW_ELEMENTS_INSTANCED 16
+#define RSRGPU_CALL_DRAW_ARRAYS_INSTANCED   17
+#define RSRGPU_CALL_STORE_COLOR_TC          18
+#define RSRGPU_CALL_STORE_COLOR_FP          19
+#define RSRGPU_CALL_STORE_COLOR_QUADS       20
+#define RSRGPU_CALL_STORE_DEPTH             21
+#define RSRGPU_CALL_STORE_GBUFFER           22
+typedef struct rsrgpu_gl_call {
+    int32_t fn;
+    int32_t i[7];
+    uint64_t p;
+    float f[32];
+} rsrgpu_gl_call;
+int rsrgpu_gl_play(rsrgpu_recorder* rec, const rsrgpu_gl_call* calls, int ncalls);
+
+/* rsr's perf harness (src/viewer/perf.cxx:200-244: priming frames, then
+ * timed frames, each GPUNode::Main's work, src/viewer/node/gpu.cxx:107-146)
+ * through this library: per frame rsrgpu_reset(target), rsrgpu_recorder_reset,
+ * rsrgpu_gl_play(calls), rsrgpu_submit, rsrgpu_run(stream), rsrgpu_wait.
+ * frame_ms[k] receives the host's steady-clock time of timed frame k, from
+ * the reset to the end of the wait.  The first failing call ends the loop
+ * and its status is returned. */
+typedef struct rsrgpu_perf_target {
+    int width, height, tile_blocks_x, tile_blocks_y;
+} rsrgpu_perf_target;
+int rsrgpu_perf_frames(rsrgpu_ctx* ctx, rsrgpu_recorder* rec, const rsrgpu_perf_target* target,
+                       const rsrgpu_gl_call* calls, int ncalls, int priming, int frames, void* stream,
+                       double* frame_ms);
 
 /* ---- texture upload and mip chain on the device ----
  * rglr::Texture's layout (src/rgl/rglr/rglr_texture.hxx:10-33): RGBA float

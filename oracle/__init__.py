@@ -87,6 +87,16 @@ class CpuRenderer:
         if rc != 0:
             raise RuntimeError("%s render failed: %d" % (self.which, rc))
 
+    def candidate_fragments(self):
+        """Candidate fragments of the last frame (the oracle only): the
+        (pixel, triangle) pairs the coverage test accepts, before depth."""
+        if self.which == "ref":
+            raise RuntimeError("rsr does not count candidate fragments")
+        n = ctypes.c_uint64(0)
+        if self.lib.rsroracle_candidate_fragments(ctypes.byref(n)) != 0:
+            raise RuntimeError("rsroracle_candidate_fragments failed")
+        return int(n.value)
+
     def render(self, scene, gamma=True):
         gl = scene.record(gamma=gamma)
         self.render_gl(gl, scene.width, scene.height, scene.tile_blocks)

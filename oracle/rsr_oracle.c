@@ -332,6 +332,7 @@ typedef struct Frame {
     rsrgpu_clipped_vertex* clipped;
     int nclipped, capclipped;
     const uint8_t* srgb_lut;
+    uint64_t frags;          /* candidate fragments of the frame, all tiles */
 } Frame;
 
 typedef struct Session {
@@ -695,6 +696,7 @@ typedef struct TileCtx {
     float DS[2], DO[2];
     TexUnit tu0;
     int nvary;
+    uint64_t frags;              /* candidate fragments: pixels inside a drawn triangle */
 } TileCtx;
 
 /* installed (program, FragmentStateKey) combinations -- the same table the
@@ -814,6 +816,7 @@ static void walk_quads(TileCtx* tc, const TriSetup* tri, int minx, int miny, int
                 float bs[3][4];
                 for (int l = 0; l < 4; ++l) {
                     trimask[l] = edges[l] >> 31;
+                    tc->frags += edges[l] >= 0;
                     bs[0][l] = itof(cx2[l]) * scale;
                     bs[2][l] = itof(cx1[l]) * scale;
                     bs[1][l] = (1.0f - bs[0][l]) - bs[2][l];
@@ -983,7 +986,7 @@ static int32_t basic8(float v) {   /* to_tc_basic (rglr_canvas_util.hxx:22-31) *
     return ftoi(sse_max(sse_min(v, 1.0f), 0.0f) * 255.0f);
 }
 
-static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8_t* gbflag) {
+static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8_t* gbflag, uint64_t* frags) {
     TileCtx tc;
     memset(&tc, 0, sizeof(tc));
     tc.f = f;
@@ -998,6 +1001,7 @@ static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8
         uint8_t op = *p++;
         switch (op) {
         case RSRGPU_CMD_EOF:
+            *frags = tc.frags;
             return 0;
         case RSRGPU_CMD_STATE: {
             uint64_t idx;
@@ -1144,6 +1148,7 @@ typedef struct Pool {
     const Frame* f;
     int next;
     int rc;
+    uint64_t frags;
     pthread_mutex_t mu;
 } Pool;
 
@@ -1158,7 +1163,11 @@ static void* tile_worker(void* arg) {
         int t = pool->next++;
         pthread_mutex_unlock(&pool->mu);
         if (t >= f->ntiles) break;
-        int rc = draw_tile(f, t, color, depth, gbflag);
+        uint64_t frags = 0;
+        int rc = draw_tile(f, t, color, depth, gbflag, &frags);
+        pthread_mutex_lock(&pool->mu);
+        pool->frags += frags;
+        pthread_mutex_unlock(&pool->mu);
         if (rc) { pthread_mutex_lock(&pool->mu); pool->rc = rc; pthread_mutex_unlock(&pool->mu); }
     }
     free(color); free(depth); free(gbflag);
@@ -1206,7 +1215,7 @@ int rsroracle_render(const uint8_t* cmds, size_t n, const rsrgpu_glstate* states
     int rc = bin_frame(f, cmds, n);
     if (rc) return rc;
     Pool pool;
-    pool.f = f; pool.next = 0; pool.rc = 0;
+    pool.f = f; pool.next = 0; pool.rc = 0; pool.frags = 0;
     pthread_mutex_init(&pool.mu, NULL);
     int nt = g_session.threads;
     pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nt);
@@ -1215,7 +1224,16 @@ int rsroracle_render(const uint8_t* cmds, size_t n, const rsrgpu_glstate* states
     for (int i = 1; i < nt; ++i) pthread_join(th[i], NULL);
     free(th);
     pthread_mutex_destroy(&pool.mu);
+    f->frags = pool.frags;
     return pool.rc;
+}
+
+/* candidate fragments of the last frame: (pixel, triangle) pairs whose pixel
+ * centre the rasteriser's coverage test accepts, before the depth test */
+int rsroracle_candidate_fragments(uint64_t* out) {
+    if (out == NULL) return RSRGPU_EINVAL;
+    *out = g_session.f.frags;
+    return 0;
 }
 
 /* canonical tile streams (same layout as rsrgpu_dump_tiles / rsrref_dump_tiles) */

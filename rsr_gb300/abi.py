@@ -150,7 +150,27 @@ class StatsC(ctypes.Structure):
                 ("max_tile_records", ctypes.c_int64),
                 ("primitives_submitted", ctypes.c_int64),
                 ("primitives_clipped", ctypes.c_int64),
-                ("gpu_launches", ctypes.c_int64)]
+                ("gpu_launches", ctypes.c_int64),
+                ("graph_captures", ctypes.c_int64),
+                ("table_uploads", ctypes.c_int64)]
+
+
+class GLCallC(ctypes.Structure):
+    """rsrgpu_gl_call: one rglv::GL call of a call script."""
+    _fields_ = [("fn", ctypes.c_int32), ("i", ctypes.c_int32 * 7), ("p", ctypes.c_uint64),
+                ("f", ctypes.c_float * 32)]
+
+
+class PerfTargetC(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int), ("tile_blocks_x", ctypes.c_int),
+                ("tile_blocks_y", ctypes.c_int)]
+
+
+# rsrgpu_gl_call.fn
+(CALL_ENABLE, CALL_DISABLE, CALL_STATE_INT, CALL_SCISSOR, CALL_VIEWPORT, CALL_USE_UNIFORMS, CALL_BIND_TEXTURE,
+ CALL_USE_BUFFER, CALL_CLEAR_COLOR, CALL_CLEAR_DEPTH, CALL_MATRIX, CALL_RESET_STATE, CALL_CLEAR, CALL_DRAW_ELEMENTS,
+ CALL_DRAW_ARRAYS, CALL_DRAW_ELEMENTS_INSTANCED, CALL_DRAW_ARRAYS_INSTANCED, CALL_STORE_COLOR_TC, CALL_STORE_COLOR_FP,
+ CALL_STORE_COLOR_QUADS, CALL_STORE_DEPTH, CALL_STORE_GBUFFER) = range(1, 23)
 
 
 _LIB = None
@@ -240,6 +260,10 @@ SYMBOLS = {
     "rsrgpu_gl_store_color_quads": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "rsrgpu_gl_store_depth": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_gl_store_gbuffer": ([ctypes.c_void_p, ctypes.POINTER(GBufferC)], ctypes.c_int),
+    "rsrgpu_gl_play": ([ctypes.c_void_p, ctypes.POINTER(GLCallC), ctypes.c_int], ctypes.c_int),
+    "rsrgpu_perf_frames": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(PerfTargetC), ctypes.POINTER(GLCallC),
+                            ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)],
+                           ctypes.c_int),
     "rsrgpu_render_static": ([ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GLStateC), ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                               ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

@@ -22,7 +22,7 @@ NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=
               "-prec-sqrt=true", "-ftz=false",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I" + os.path.join(REPO, "include")]
 SOURCES = ["rsrgpu_kernels.cu", "rsrgpu_host.cu", "rsrgpu_static.cu", "rsrgpu_deferred.cu", "rsrgpu_mlp.cu", "rsrgpu_learned.cu",
-           "rsrgpu_texture.cu", "rsrgpu_postfx.cu", "rsrgpu_recorder.cu"]
+           "rsrgpu_texture.cu", "rsrgpu_postfx.cu", "rsrgpu_recorder.cu", "rsrgpu_perf.cu"]
 REFERENCE = os.environ.get("RSR_REFERENCE", "/root/reference")
 
 

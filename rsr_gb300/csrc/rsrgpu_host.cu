@@ -133,10 +133,24 @@ struct rsrgpu_ctx {
     int ntris = 0;
     bool submitted = false;
     bool ran = false;
+    // The submission's tables packed as they go to the device: states, draws,
+    // ops, G-buffer descriptors, draw extensions (offsets in `tab_ofs`).
+    // `packed_dev` is what the device tables hold; a submission whose packed
+    // tables equal it uploads nothing.
+    std::vector<uint8_t> packed, packed_dev;
+    size_t tab_ofs[5] = {0, 0, 0, 0, 0};
+    uint8_t* h_tables = nullptr;    // pinned staging of the table upload
+    size_t h_tables_cap = 0;
+    cudaEvent_t ev_tables = nullptr;  // the last upload from h_tables
+    bool ev_tables_live = false;
+    // what the captured graph depends on besides the tables' contents
+    // (sizes, kernel choices, host-buffer routes): a submission with the same
+    // signature keeps the graph
+    std::vector<uint8_t> graph_sig;
     // device memory
-    DevBuf d_states, d_draws, d_ops, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
-        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb, d_gbufs,
-        d_dext, d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
+    DevBuf d_tables, d_tris, d_bin_rect, d_rec16, d_chunk, d_super, d_clip_info,
+        d_clip_verts, d_clip_poly, d_clip_src, d_clip_fan, d_bins, d_pool, d_counters, d_rcp, d_srgb,
+        d_mlp_err, d_learn_err, d_learn_status, d_learn_tiles;
     std::map<cudaStream_t, cudaEvent_t> learn_events;   // last learned-shader launch per stream
     int num_sms = 0;
     int* h_mlp_err = nullptr;   // pinned
@@ -406,6 +420,7 @@ int rsrgpu_create(int device, rsrgpu_ctx** out) {
         cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_tables, cudaEventDisableTiming) != cudaSuccess ||
         cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_counters), sizeof(FrameCounters), cudaHostAllocDefault) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->ev2) != cudaSuccess || cudaEventCreate(&ctx->ev3) != cudaSuccess) {
@@ -431,16 +446,18 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_gbufs, &ctx->d_dext, &ctx->d_states, &ctx->d_draws, &ctx->d_ops, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_tables, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
     for (DevBuf* b : bufs) b->release();
     if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+    if (ctx->ev_tables_live) cudaEventSynchronize(ctx->ev_tables);
+    if (ctx->h_tables) cudaFreeHost(ctx->h_tables);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     drop_graph(ctx);
     if (ctx->cap) cudaStreamDestroy(ctx->cap);
-    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_fork, ctx->ev_late };
+    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_fork, ctx->ev_late, ctx->ev_tables };
     for (cudaEvent_t ev : evs) if (ev) cudaEventDestroy(ev);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -480,7 +497,7 @@ int rsrgpu_reset(rsrgpu_ctx* ctx, int width, int height, int tile_blocks_x, int 
     ctx->tiles_y = (height + ctx->tile_h - 1) / ctx->tile_h;
     ctx->ntiles = ctx->tiles_x * ctx->tiles_y;
     if (ctx->tiles_x > 32767 || ctx->tiles_y > 32767) return fail(ctx, RSRGPU_EINVAL, "too many tiles");
-    ctx->submitted = false;
+    ctx->submitted = false;   // the captured run stays: a submission of the same structure and size replays it
     return 0;
 }
 
@@ -529,9 +546,11 @@ int rsrgpu_unregister_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr) {
     return 0;
 }
 
-int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates) {
-    if (ctx == nullptr || (commands == nullptr && nbytes) || nstates < 0) return RSRGPU_EINVAL;
-    if (ctx->ntiles == 0) return fail(ctx, RSRGPU_EINVAL, "rsrgpu_reset() has not been called");
+namespace {
+
+// GPU::BinImpl's command interpretation (rglv_gpu.cxx:119-260), on the host:
+// the frame's states, draws and op list, and how it uses every caller buffer.
+int decode_frame(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates) {
     for (auto& kv : ctx->host) kv.second.in = kv.second.out = kv.second.early = kv.second.late = kv.second.direct = false;
     ctx->states.assign(size_t(nstates), DevState{});
     ctx->state_ordinal.assign(size_t(nstates), -1);
@@ -543,9 +562,6 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
     ctx->any_dext = false;
     ctx->ntris = 0;
     bool gbuffer_frame = false, other_op_since_draw = false, any_draw = false;
-    ctx->submitted = false;
-    ctx->tables_uploaded = false;
-    drop_graph(ctx);
     std::vector<bool> decoded(size_t(nstates), false);
     int ordinals = 0;
     int cur = -1;
@@ -816,6 +832,86 @@ int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const
         }
         ctx->vis_keys = ok ? 1 + func : 0;
     }
+    return 0;
+}
+
+bool frame_is_ext(const rsrgpu_ctx* ctx) {
+    for (const FrameOp& o : ctx->ops)
+        if (o.kind >= kOpStoreFP) return true;
+    for (const DevDraw& d : ctx->draws)
+        if (ctx->states[size_t(d.state)].program == kProgMany) return true;
+    return false;
+}
+
+void put_raw(std::vector<uint8_t>& v, const void* x, size_t n) {
+    const auto* b = static_cast<const uint8_t*>(x);
+    v.insert(v.end(), b, b + n);
+}
+#define put_bytes(v, x) put_raw((v), &(x), sizeof(x))
+
+// The submission's tables in one block, each part 256-byte aligned.
+void pack_tables(rsrgpu_ctx* ctx) {
+    const size_t sizes[5] = { sizeof(DevState) * ctx->states.size(), sizeof(DevDraw) * ctx->draws.size(),
+                              sizeof(FrameOp) * ctx->ops.size(), sizeof(GBufferDesc) * ctx->gbufs.size(),
+                              ctx->any_dext ? sizeof(DevDrawExt) * ctx->dext.size() : 0 };
+    const void* srcs[5] = { ctx->states.data(), ctx->draws.data(), ctx->ops.data(), ctx->gbufs.data(), ctx->dext.data() };
+    size_t at = 0;
+    for (int k = 0; k < 5; ++k) {
+        ctx->tab_ofs[k] = at;
+        at += (std::max<size_t>(sizes[k], 1) + 255) & ~size_t(255);
+    }
+    ctx->packed.assign(at, 0);
+    for (int k = 0; k < 5; ++k)
+        if (sizes[k]) std::memcpy(ctx->packed.data() + ctx->tab_ofs[k], srcs[k], sizes[k]);
+}
+
+// Everything the captured run depends on other than the tables' contents.
+std::vector<uint8_t> graph_signature(const rsrgpu_ctx* ctx) {
+    std::vector<uint8_t> sig;
+    const int dims[4] = { ctx->width, ctx->height, ctx->tile_w, ctx->tile_h };
+    put_bytes(sig, dims);
+    put_bytes(sig, ctx->ntris);
+    const size_t packed_size = ctx->packed.size();
+    put_bytes(sig, packed_size);
+    for (size_t o : ctx->tab_ofs) put_bytes(sig, o);
+    put_bytes(sig, ctx->vis_keys);
+    put_bytes(sig, ctx->region_px);
+    const uint8_t flags = uint8_t(ctx->any_dext) | uint8_t(ctx->any_inst) << 1 | uint8_t(frame_is_ext(ctx)) << 2;
+    put_bytes(sig, flags);
+    for (const auto& kv : ctx->host) {
+        const HostBuffer& hb = kv.second;
+        put_bytes(sig, kv.first);
+        const uint8_t f = uint8_t(hb.in) | uint8_t(hb.out) << 1 | uint8_t(hb.early) << 2 | uint8_t(hb.late) << 3 |
+                          uint8_t(hb.direct) << 4;
+        put_bytes(sig, f);
+    }
+    return sig;
+}
+#undef put_bytes
+
+}  // namespace
+
+int rsrgpu_submit(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates) {
+    if (ctx == nullptr || (commands == nullptr && nbytes) || nstates < 0) return RSRGPU_EINVAL;
+    if (ctx->ntiles == 0) return fail(ctx, RSRGPU_EINVAL, "rsrgpu_reset() has not been called");
+    ctx->submitted = false;
+    const int rc = decode_frame(ctx, commands, nbytes, states, nstates);
+    if (rc) {
+        drop_graph(ctx);
+        ctx->graph_sig.clear();
+        ctx->packed_dev.clear();
+        return rc;
+    }
+    pack_tables(ctx);
+    // A frame with the structure of the last one (the same sizes, kernels and
+    // host-buffer routes) replays the captured graph; only tables that
+    // changed are uploaded before it.
+    std::vector<uint8_t> sig = graph_signature(ctx);
+    if (ctx->gexec == nullptr || sig != ctx->graph_sig) {
+        drop_graph(ctx);
+        ctx->graph_sig.swap(sig);
+    }
+    ctx->tables_uploaded = ctx->packed == ctx->packed_dev;
     ctx->submitted = true;
     return 0;
 }
@@ -839,14 +935,14 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     const int nchunks = (ntris + kChunk - 1) / kChunk;
     const int nsupers = (ntris + kSuper - 1) / kSuper;
     const size_t nt = size_t(std::max(ntris, 1));
+    uint8_t* tab = nullptr;
     if (tables == nullptr) {
-        CK(ctx->d_states.ensure(sizeof(DevState) * ctx->states.size()), "alloc states");
-        CK(ctx->d_draws.ensure(sizeof(DevDraw) * std::max<size_t>(ctx->draws.size(), 1)), "alloc draws");
-        CK(ctx->d_ops.ensure(sizeof(FrameOp) * std::max<size_t>(ctx->ops.size(), 1)), "alloc ops");
+        const size_t before = ctx->d_tables.cap;
+        CK(ctx->d_tables.ensure(ctx->packed.size()), "alloc frame tables");
+        if (ctx->d_tables.cap != before) ctx->packed_dev.clear();   // a new allocation holds nothing yet
+        tab = ctx->d_tables.as<uint8_t>();
         CK(ctx->d_super.ensure(sizeof(int4) * std::max(nsupers, 1)), "alloc super rects");
         CK(ctx->d_counters.ensure(sizeof(FrameCounters)), "alloc counters");
-        CK(ctx->d_gbufs.ensure(sizeof(GBufferDesc) * std::max<size_t>(ctx->gbufs.size(), 1)), "alloc gbuffer table");
-        if (ctx->any_dext) CK(ctx->d_dext.ensure(sizeof(DevDrawExt) * ctx->dext.size()), "alloc draw extension table");
     }
     CK(ctx->d_tris.ensure(sizeof(TriRecord) * nt), "alloc tris");
     CK(ctx->d_bin_rect.ensure(sizeof(uint64_t) * nt), "alloc bin_rect");
@@ -860,13 +956,13 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     CK(ctx->d_bins.ensure(sizeof(TileBin) * size_t(ctx->ntiles)), "alloc bins");
     CK(ctx->d_pool.ensure(sizeof(uint32_t) * size_t(ctx->bin_cap)), "alloc bin pool");
     FrameView& fv = ctx->fv;
-    fv.states = tables ? tables->states : ctx->d_states.as<DevState>();
-    fv.draws = tables ? tables->draws : ctx->d_draws.as<DevDraw>();
+    fv.states = tables ? tables->states : reinterpret_cast<DevState*>(tab + ctx->tab_ofs[0]);
+    fv.draws = tables ? tables->draws : reinterpret_cast<DevDraw*>(tab + ctx->tab_ofs[1]);
     fv.ndraws = int(ctx->draws.size());
     fv.ntris = ntris;
-    fv.ops = tables ? tables->ops : ctx->d_ops.as<FrameOp>();
+    fv.ops = tables ? tables->ops : reinterpret_cast<FrameOp*>(tab + ctx->tab_ofs[2]);
     fv.nops = int(ctx->ops.size());
-    fv.gbufs = tables ? tables->gbufs : ctx->d_gbufs.as<GBufferDesc>();
+    fv.gbufs = tables ? tables->gbufs : reinterpret_cast<GBufferDesc*>(tab + ctx->tab_ofs[3]);
     fv.width = ctx->width; fv.height = ctx->height;
     fv.tile_w = ctx->tile_w; fv.tile_h = ctx->tile_h;
     fv.tiles_x = ctx->tiles_x; fv.tiles_y = ctx->tiles_y; fv.ntiles = ctx->ntiles;
@@ -893,12 +989,8 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.raster_phase = 0;
     fv.vis_own = nullptr;
     fv.vis_dep = nullptr;
-    fv.ext = 0;
-    for (const FrameOp& o : ctx->ops)
-        if (o.kind >= kOpStoreFP) fv.ext = 1;
-    for (const DevDraw& d : ctx->draws)
-        if (ctx->states[size_t(d.state)].program == kProgMany) fv.ext = 1;
-    fv.dext = (ctx->any_dext && tables == nullptr) ? ctx->d_dext.as<DevDrawExt>() : nullptr;
+    fv.ext = frame_is_ext(ctx) ? 1 : 0;
+    fv.dext = (ctx->any_dext && tables == nullptr) ? reinterpret_cast<DevDrawExt*>(tab + ctx->tab_ofs[4]) : nullptr;
     return 0;
 }
 
@@ -909,23 +1001,45 @@ bool late_inputs(const rsrgpu_ctx* ctx) {
     return false;
 }
 
-// allocations of a run, and the frame's tables, which change only with a
-// submission (before the run's own stream work, which may be captured)
-int prepare_run(rsrgpu_ctx* ctx, cudaStream_t st) {
+// The frame's packed tables to the device, on `st` ahead of the run: one
+// copy from pinned staging, which is refilled only after the previous copy
+// from it has completed.  `capturing`: `st` is being captured by the caller.
+int upload_tables(rsrgpu_ctx* ctx, cudaStream_t st, bool capturing) {
+    if (ctx->tables_uploaded) return 0;
+    const size_t n = ctx->packed.size();
+    if (ctx->ev_tables_live) {
+        CK(cudaEventSynchronize(ctx->ev_tables), "table staging");
+        ctx->ev_tables_live = false;
+    }
+    if (n > ctx->h_tables_cap) {
+        if (ctx->h_tables) cudaFreeHost(ctx->h_tables);
+        ctx->h_tables = nullptr;
+        ctx->h_tables_cap = 0;
+        const size_t cap = std::max<size_t>(n, 64u << 10);
+        CK(cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_tables), cap, cudaHostAllocDefault), "pinned table staging");
+        ctx->h_tables_cap = cap;
+    }
+    std::memcpy(ctx->h_tables, ctx->packed.data(), n);
+    ++ctx->stats.table_uploads;
+    CK(cudaMemcpyAsync(ctx->d_tables.p, ctx->h_tables, n, cudaMemcpyHostToDevice, st), "H2D frame tables");
+    if (!capturing) {
+        CK(cudaEventRecord(ctx->ev_tables, st), "event");
+        ctx->ev_tables_live = true;
+        ctx->packed_dev = ctx->packed;
+    } else {
+        ctx->packed_dev.clear();   // the caller's graph copies them when it runs
+    }
+    ctx->tables_uploaded = true;
+    return 0;
+}
+
+// allocations of a run, and the frame's tables (before the run's own stream
+// work, which may be captured)
+int prepare_run(rsrgpu_ctx* ctx, cudaStream_t st, bool capturing) {
     int rc = prepare_view(ctx);
     if (rc) return rc;
-    if (!ctx->tables_uploaded) {
-        CK(cudaMemcpyAsync(ctx->d_states.p, ctx->states.data(), sizeof(DevState) * ctx->states.size(), cudaMemcpyHostToDevice, st), "H2D states");
-        if (!ctx->draws.empty())
-            CK(cudaMemcpyAsync(ctx->d_draws.p, ctx->draws.data(), sizeof(DevDraw) * ctx->draws.size(), cudaMemcpyHostToDevice, st), "H2D draws");
-        if (!ctx->ops.empty())
-            CK(cudaMemcpyAsync(ctx->d_ops.p, ctx->ops.data(), sizeof(FrameOp) * ctx->ops.size(), cudaMemcpyHostToDevice, st), "H2D ops");
-        if (!ctx->gbufs.empty())
-            CK(cudaMemcpyAsync(ctx->d_gbufs.p, ctx->gbufs.data(), sizeof(GBufferDesc) * ctx->gbufs.size(), cudaMemcpyHostToDevice, st), "H2D gbuffers");
-        if (ctx->any_dext)
-            CK(cudaMemcpyAsync(ctx->d_dext.p, ctx->dext.data(), sizeof(DevDrawExt) * ctx->dext.size(), cudaMemcpyHostToDevice, st), "H2D draw extensions");
-        ctx->tables_uploaded = true;
-    }
+    rc = upload_tables(ctx, st, capturing);
+    if (rc) return rc;
     if (ctx->fv.vis_keys != 0 && late_inputs(ctx))
         CK(ctx->d_vis.ensure(size_t(ctx->fv.width) * size_t(ctx->fv.height) * 8u), "alloc visibility hand-over");
     return 0;
@@ -1013,13 +1127,14 @@ int run_frame(rsrgpu_ctx* ctx) {
     for (const auto& kv : ctx->host)
         if ((kv.second.in || kv.second.out) && kv.second.mapped == nullptr) graph = false;
     if (!graph) {
-        int rc = prepare_run(ctx, st);
+        int rc = prepare_run(ctx, st, cs != cudaStreamCaptureStatusNone);
         return rc ? rc : record_run(ctx, st, false);
     }
     if (ctx->gexec == nullptr) {
-        int rc = prepare_run(ctx, st);
+        int rc = prepare_run(ctx, st, false);
         if (rc) return rc;
         CK(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+        ++ctx->stats.graph_captures;
         rc = record_run(ctx, ctx->cap, true);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(ctx->cap, &g);
@@ -1028,6 +1143,9 @@ int run_frame(rsrgpu_ctx* ctx) {
         ctx->graph = g;
         const cudaError_t ie = cudaGraphInstantiate(&ctx->gexec, g, 0);
         if (ie != cudaSuccess) { drop_graph(ctx); return cuda_fail(ctx, ie, "graph instantiate"); }
+    } else {
+        int rc = upload_tables(ctx, st, false);   // a resubmitted frame of the same structure
+        if (rc) return rc;
     }
     CK(cudaGraphLaunch(ctx->gexec, st), "graph launch");
     return 0;

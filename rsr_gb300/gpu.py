@@ -107,6 +107,25 @@ class GPU:
     def Wait(self, timeout_ms=-1):
         self._check(self.lib.rsrgpu_wait(self.ctx, int(timeout_ms)))
 
+    def perf_frames(self, script, width, height, tile_blocks, frames, priming=0, stream=None):
+        """rsr's perf loop through the C ABI (rsrgpu_perf_frames): per frame
+        Reset, the script's GL calls on a native recorder, submit, run, wait.
+        `script`: a recorder.ScriptGL.  Returns the timed frames' host times
+        in milliseconds."""
+        from .recorder import NativeGL
+        rec = NativeGL(self.lib)
+        try:
+            calls = script.array()
+            target = abi.PerfTargetC(int(width), int(height), int(tile_blocks[0]), int(tile_blocks[1]))
+            out = (ctypes.c_double * max(1, frames))()
+            self._check(self.lib.rsrgpu_perf_frames(self.ctx, rec.h, ctypes.byref(target), calls, len(script.calls),
+                                                    int(priming), int(frames),
+                                                    ctypes.c_void_p(stream) if stream else None, out))
+            self.width, self.height, self.tile_blocks = width, height, tuple(tile_blocks)
+            return list(out)[:frames]
+        finally:
+            rec.close()
+
     # ---- inspection ----
     def tiles(self):
         need = ctypes.c_size_t(0)

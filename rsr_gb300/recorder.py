@@ -167,3 +167,136 @@ class NativeGL:
         if ns:
             ctypes.memmove(arr, states, ctypes.sizeof(abi.GLStateC) * ns)
         return arr
+
+
+class ScriptGL:
+    """rglv::GL's calling surface that writes each call into a call script
+    (include/rsrgpu.h rsrgpu_gl_call) instead of making it.  The script is
+    played on a native recorder by rsrgpu_gl_play(), or every frame by the
+    perf harness rsrgpu_perf_frames(), so the calls are made natively, as a
+    C++ caller makes them, without one Python call each."""
+
+    def __init__(self):
+        self.calls = []
+        self._keep = []
+
+    def _add(self, fn, i=(), p=None, f=()):
+        c = abi.GLCallC()
+        c.fn = fn
+        for k, v in enumerate(i):
+            c.i[k] = int(v)
+        c.p = _addr(p) or 0
+        for k, v in enumerate(f):
+            c.f[k] = float(v)
+        self.calls.append(c)
+
+    def array(self):
+        """The script as a ctypes array of rsrgpu_gl_call."""
+        arr = (abi.GLCallC * max(1, len(self.calls)))()
+        for k, c in enumerate(self.calls):
+            arr[k] = c
+        return arr
+
+    # ---- state ----
+    def Enable(self, v):
+        self._add(abi.CALL_ENABLE, (v,))
+
+    def Disable(self, v):
+        self._add(abi.CALL_DISABLE, (v,))
+
+    def _int(self, what, v):
+        self._add(abi.CALL_STATE_INT, (what, int(v)))
+
+    def CullFace(self, v):
+        self._int(1, v)
+
+    def DepthFunc(self, v):
+        self._int(2, v)
+
+    def DepthWriteMask(self, v):
+        self._int(3, bool(v))
+
+    def ColorWriteMask(self, v):
+        self._int(4, bool(v))
+
+    def UseProgram(self, v):
+        self._int(5, v)
+
+    def RenderbufferType(self, attachment, rbtype):
+        self._int(6 if attachment == abi.GL_COLOR_ATTACHMENT0 else 7, rbtype)
+
+    def Scissor(self, x, y, w, h):
+        self._add(abi.CALL_SCISSOR, (x, y, w, h))
+
+    def Viewport(self, x, y, w, h):
+        self._add(abi.CALL_VIEWPORT, (x, y, w, h))
+
+    def UseUniforms(self, values):
+        v = np.ascontiguousarray(values, np.float32).reshape(-1)
+        if len(v) > 32:
+            raise ValueError("at most 32 uniforms")
+        self._add(abi.CALL_USE_UNIFORMS, (len(v),), f=v)
+
+    def BindTexture(self, unit, ptr, width, height, stride, mode):
+        self._add(abi.CALL_BIND_TEXTURE, (unit, width, height, stride, mode), p=ptr)
+
+    def UseBuffer(self, idx, ptr):
+        if isinstance(ptr, (tuple, list)):
+            for k, q in enumerate(ptr):
+                self._add(abi.CALL_USE_BUFFER, (idx + k,), p=q)
+        else:
+            self._add(abi.CALL_USE_BUFFER, (idx,), p=ptr)
+
+    def ClearColor(self, rgb):
+        self._add(abi.CALL_CLEAR_COLOR, f=rgb[:3])
+
+    def ClearDepth(self, v):
+        self._add(abi.CALL_CLEAR_DEPTH, f=(v,))
+
+    def _matrix(self, which, m):
+        self._add(abi.CALL_MATRIX, (which,), f=np.asarray(m, np.float32).reshape(16))
+
+    def ViewMatrix(self, m):
+        self._matrix(0, m)
+
+    def ProjectionMatrix(self, m):
+        self._matrix(1, m)
+
+    def NormalMatrix(self, m):
+        self._matrix(2, m)
+
+    def ResetX(self):
+        self._add(abi.CALL_RESET_STATE)
+
+    # ---- commands ----
+    def Clear(self, bits):
+        self._add(abi.CALL_CLEAR, (bits,))
+
+    def DrawElements(self, count, indices, hint=0):
+        self._add(abi.CALL_DRAW_ELEMENTS, (count, hint), p=indices)
+
+    def DrawArrays(self, count):
+        self._add(abi.CALL_DRAW_ARRAYS, (count,))
+
+    def DrawElementsInstanced(self, count, indices, instances):
+        self._add(abi.CALL_DRAW_ELEMENTS_INSTANCED, (count, instances), p=indices)
+
+    def DrawArraysInstanced(self, count, instances):
+        self._add(abi.CALL_DRAW_ARRAYS_INSTANCED, (count, instances))
+
+    def StoreColor(self, data, width, height, gamma=True, stride=None):
+        self._add(abi.CALL_STORE_COLOR_TC, (width, height, stride or 0, 1 if gamma else 0), p=data)
+
+    def StoreColorFP(self, data, width, height, downsample=False, stride=None):
+        self._add(abi.CALL_STORE_COLOR_FP, (width, height, stride or 0, 1 if downsample else 0), p=data)
+
+    def StoreColorQuads(self, data, width, height, stride=None):
+        self._add(abi.CALL_STORE_COLOR_QUADS, (width, height, stride or 0), p=data)
+
+    def StoreDepth(self, data):
+        self._add(abi.CALL_STORE_DEPTH, p=data)
+
+    def StoreGBuffer(self, depth, normal_x, normal_y, normal_z, albedo, width, height):
+        g = abi.GBufferC(_addr(depth), _addr(normal_x), _addr(normal_y), _addr(normal_z), _addr(albedo), width, height)
+        self._keep.append(g)
+        self._add(abi.CALL_STORE_GBUFFER, p=ctypes.addressof(g))

@@ -118,7 +118,7 @@ def _begin_frame(gl, clear_rgb=(0.0, 0.0, 0.0)):
     gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
 
 
-def plain_raster(seed=0, ntris=10000, width=640, height=360, tile_blocks=(8, 8), spread=1.0):
+def plain_raster(seed=0, ntris=10000, width=640, height=360, tile_blocks=(8, 8), spread=1.0, clear_rgb=(0.0, 0.0, 0.0)):
     """Random NDC triangles (xyz in [-1,1], w=1), rgb in [0,1], Gouraud, LESS,
     no culling; DrawElements of sequential indices.  spread < 1 shrinks each
     triangle about its own centre: centre uniform in [-(1-s), 1-s]^3 and
@@ -142,7 +142,7 @@ def plain_raster(seed=0, ntris=10000, width=640, height=360, tile_blocks=(8, 8),
     }
 
     def record(gl, ref):
-        _begin_frame(gl)
+        _begin_frame(gl, clear_rgb)
         gl.UseProgram(abi.PROGRAM_GOURAUD)
         if ntris <= per_draw:
             gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))

@@ -38,7 +38,8 @@ def test_struct_layouts_match_header(tmp_path):
     structs = {"rsrgpu_texture_state": abi.TextureState, "rsrgpu_glstate": abi.GLStateC,
                "rsrgpu_truecolor_canvas": abi.TrueColorCanvasC, "rsrgpu_fp_canvas": abi.FloatCanvasC,
                "rsrgpu_qfloat4_canvas": abi.FloatCanvasC,
-               "rsrgpu_clipped_vertex": abi.ClippedVertexC, "rsrgpu_stats": abi.StatsC}
+               "rsrgpu_clipped_vertex": abi.ClippedVertexC, "rsrgpu_stats": abi.StatsC,
+               "rsrgpu_gl_call": abi.GLCallC, "rsrgpu_perf_target": abi.PerfTargetC}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "rsrgpu.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)

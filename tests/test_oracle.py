@@ -111,3 +111,34 @@ def test_rcpps_table_matches_this_cpu():
         out = subprocess.run([exe], check=True, stdout=subprocess.PIPE, text=True).stdout
     with open(os.path.join(os.path.dirname(HERE), "rsr_gb300", "csrc", "rcpps_table.inc")) as f:
         assert f.read() == out
+
+
+def test_candidate_fragment_count(orc):
+    """The oracle's candidate-fragment count (pixels the coverage test
+    accepts, per triangle, before depth): two triangles tiling the screen
+    give each pixel once (the top-left rule assigns the shared edge to one
+    of them); the same quad drawn twice gives each pixel twice."""
+    w, h = 320, 180
+    # two triangles of the square [-1, 1]^2, z = 0.5, drawn twice
+    quad = np.array([[-1, -1], [1, -1], [1, 1], [-1, -1], [1, 1], [-1, 1]], np.float32)
+    pos = np.concatenate([quad, quad])
+    arrays = {"px": scenes.pad4(pos[:, 0]), "py": scenes.pad4(pos[:, 1]),
+              "pz": scenes.pad4(np.full(len(pos), 0.5, np.float32)),
+              "cr": scenes.pad4(np.ones(len(pos), np.float32)), "cg": scenes.pad4(np.zeros(len(pos), np.float32)),
+              "cb": scenes.pad4(np.zeros(len(pos), np.float32)), "idx": np.arange(len(pos), dtype=np.uint16)}
+
+    def record(gl, ref, n):
+        gl.RenderbufferType(2, 1)   # GL_COLOR_ATTACHMENT0, RB_RGBF32
+        gl.RenderbufferType(0, 3)   # GL_DEPTH_ATTACHMENT, RB_F32
+        gl.ClearColor((0.0, 0.0, 0.0))
+        gl.ClearDepth(1.0)
+        gl.Clear(3)
+        gl.UseProgram(90)
+        gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
+        gl.UseBuffer(3, (ref("cr"), ref("cg"), ref("cb")))
+        gl.DrawElements(n, ref("idx"), 0)
+
+    for n, want in ((6, w * h), (12, 2 * w * h)):
+        sc = scenes.Scene("quad", w, h, (2, 2), arrays, lambda gl, ref, n=n: record(gl, ref, n), n // 3)
+        orc.render(sc, False)
+        assert orc.candidate_fragments() == want

@@ -87,6 +87,30 @@ def test_native_recorder_matches_python_recorder(name, lib, monkeypatch):
     nat.close()
 
 
+@pytest.mark.parametrize("name", list(SCENES))
+def test_call_script_plays_like_native_calls(name, lib, monkeypatch):
+    """A frame's calls written as a script (ScriptGL) and played on a native
+    recorder by rsrgpu_gl_play give the stream and snapshots of the same
+    calls made one by one."""
+    from rsr_gb300.recorder import ScriptGL
+    sc = SCENES[name]()
+    monkeypatch.setattr(scenes, "GL", lambda: NativeGL(lib))
+    nat = sc.record()
+    monkeypatch.setattr(scenes, "GL", ScriptGL)
+    script = sc.record()
+    monkeypatch.undo()
+    played = NativeGL(lib)
+    assert lib.rsrgpu_gl_play(played.h, script.array(), len(script.calls)) == 0
+    assert _canonical(played.stream()) == _canonical(nat.stream())
+    a, b = played.c_states(), nat.c_states()
+    assert ctypes.string_at(a, ctypes.sizeof(a)) == ctypes.string_at(b, ctypes.sizeof(b))
+    bad = ScriptGL()
+    bad.UseBuffer(16, None)
+    assert lib.rsrgpu_gl_play(played.h, bad.array(), 1) != 0
+    played.close()
+    nat.close()
+
+
 def test_recorder_reset_and_errors(lib):
     g = NativeGL(lib)
     g.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, abi.RB_RGBF32)
