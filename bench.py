@@ -780,6 +780,31 @@ def run_batch(gpu, args, stream, flush):
             "gpu_launches_per_batch": "setup 1 + bin 1 + raster 1 per CTA shape (graph)"}
 
 
+def run_profile(args):
+    """Renders one frame `--warmup` + `--steps` times with device-resident
+    inputs and no timing: the launch sequence an ncu capture selects from
+    (`-k regex:<kernel> -s <warmup> -c 1`)."""
+    import torch
+    from rsr_gb300 import build, scenes
+    build.build_gpu()
+    from rsr_gb300.gpu import GPU
+    sc = workload() if args.profile == "sphere_1080" else scenes.plain_raster()
+    gpu = GPU(0)
+    gpu.InstallDefaults()
+    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+    col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+    dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+    gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+    gpu.submit(sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True))
+    for _ in range(args.warmup + args.steps):
+        gpu.run()
+        gpu.Wait()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "frames": args.warmup + args.steps, "launches_per_frame":
+                      gpu.stats()["gpu_launches"]}))
+    gpu.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -791,8 +816,12 @@ def main():
     ap.add_argument("--no-deferred", action="store_true", help="skip the deferred / learned shading figures")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames figures")
     ap.add_argument("--no-post", action="store_true", help="skip the texture-upload and glow-chain figures")
+    ap.add_argument("--profile", choices=["sphere_1080", "plain_640"],
+                    help="render that frame warmup+steps times, untimed (for ncu launch selection)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
