@@ -134,7 +134,14 @@ void InstallDrawStates(rglv::GPU& gpu) {
 	gpu.Install(id, 0x6c2, GPUTileImpl<QFloat3FragmentCursor, QFloatFragmentCursor, PGM, false, true, DepthLT, false, true, BlendOff>::MakeDrawProgramPtrs());
 	// RB_COLOR_DEPTH (colour rgb + depth in alpha)
 	gpu.Install(id, 0x62, GPUTileImpl<QFloat4RGBFragmentCursor, QFloat4AFragmentCursor, PGM, false, true, DepthLT, true, true, BlendOff>::MakeDrawProgramPtrs());
-	gpu.Install(id, 0x72, GPUTileImpl<QFloat4RGBFragmentCursor, QFloat4AFragmentCursor, PGM, false, true, DepthLT, true, true, BlendAlpha>::MakeDrawProgramPtrs()); }
+	gpu.Install(id, 0x72, GPUTileImpl<QFloat4RGBFragmentCursor, QFloat4AFragmentCursor, PGM, false, true, DepthLT, true, true, BlendAlpha>::MakeDrawProgramPtrs());
+	// the same states with the scissor test on (SCISSOR_ENABLED = true, key bit 0)
+	gpu.Install(id, 0x6e3, GPUTileImpl<QFloat3FragmentCursor, QFloatFragmentCursor, PGM, true, true, DepthLT, true, true, BlendOff>::MakeDrawProgramPtrs());
+	gpu.Install(id, 0x6e7, GPUTileImpl<QFloat3FragmentCursor, QFloatFragmentCursor, PGM, true, true, DepthLE, true, true, BlendOff>::MakeDrawProgramPtrs());
+	gpu.Install(id, 0x6f3, GPUTileImpl<QFloat3FragmentCursor, QFloatFragmentCursor, PGM, true, true, DepthLT, true, true, BlendAlpha>::MakeDrawProgramPtrs());
+	gpu.Install(id, 0x6c3, GPUTileImpl<QFloat3FragmentCursor, QFloatFragmentCursor, PGM, true, true, DepthLT, false, true, BlendOff>::MakeDrawProgramPtrs());
+	gpu.Install(id, 0x63, GPUTileImpl<QFloat4RGBFragmentCursor, QFloat4AFragmentCursor, PGM, true, true, DepthLT, true, true, BlendOff>::MakeDrawProgramPtrs());
+	gpu.Install(id, 0x73, GPUTileImpl<QFloat4RGBFragmentCursor, QFloat4AFragmentCursor, PGM, true, true, DepthLT, true, true, BlendAlpha>::MakeDrawProgramPtrs()); }
 
 
 struct Session {

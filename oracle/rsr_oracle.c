@@ -687,7 +687,11 @@ static int bin_frame(Frame* f, const uint8_t* cmds, size_t n) {
  * ====================================================================== */
 typedef struct TileCtx {
     const Frame* f;
-    int rect[4];                 /* left, top, right, bottom */
+    int rect[4];                 /* the tile: left, top, right, bottom */
+    int drect[4];                /* the draw's rectangle: the tile, cut to the scissor rectangle when
+                                    the state's scissor test is on (GPUTileImpl::DrawTriangles/DrawClipped,
+                                    rglv_gpu_impl.hxx:848-849,953-954) */
+    int scissor;                 /* the state's scissor test is on */
     float* color;                /* tile-local rgba, row-major, tile_w*tile_h */
     float* depth;
     uint8_t* gbflag;             /* pixel's colour written by the G-buffer program */
@@ -717,6 +721,7 @@ static int draw_dispatch_ok(const rsrgpu_glstate* s) {
     if (program_nvary(s->program_id) < 0) return 0;
     if (s->program_id == RSRGPU_PROGRAM_GBUFFER && s->blending_enabled) return 0;
     uint32_t k = fragment_state_key(s) & 0xffffffu;
+    k &= ~1u;   /* each state is installed with and without the scissor test */
     return k == 0x6e2 || k == 0x6e6 || k == 0x6f2 || k == 0x6c2 || k == 0x62 || k == 0x72;
 }
 
@@ -804,9 +809,19 @@ static void walk_quads(TileCtx* tc, const TriSetup* tri, int minx, int miny, int
     const int32_t s1x = wmul(dy12, 2), s1y = wmul(dx12, 2);
     const int32_t s2x = wmul(dy23, 2), s2y = wmul(dx23, 2);
     const int32_t s3x = wmul(dy31, 2), s3y = wmul(dx31, 2);
+    /* ScissorFlags (rglv_triangle.hxx:23-28) of the draw rectangle: with the
+     * scissor test on, the lanes of quads cut by an odd edge of the rectangle
+     * are masked (rglv_triangle.hxx:268-292) */
+    const int* r = tc->drect;
+    const int fTop = (r[1] & 1) != 0, fBot = (r[3] & 1) != 0, fLeft = (r[0] & 1) != 0, fRight = (r[2] & 1) != 0;
     for (int y = miny; y < endy; y += 2) {
         int32_t cx1[4], cx2[4], cx3[4];
         memcpy(cx1, cb1, 16); memcpy(cx2, cb2, 16); memcpy(cx3, cb3, 16);
+        int32_t sTop = 0, sBot = 0;
+        if (tc->scissor) {
+            if (y == (r[1] & ~1) && fTop) sTop = -1;
+            if (y >= (r[3] & ~1) && fBot) sBot = -1;
+        }
         for (int x = minx; x < endx; x += 2) {
             int32_t edges[4];
             int allout = 1;
@@ -814,9 +829,15 @@ static void walk_quads(TileCtx* tc, const TriSetup* tri, int minx, int miny, int
             if (!allout) {
                 int32_t trimask[4];
                 float bs[3][4];
+                int32_t sLeft = 0, sRight = 0;
+                if (tc->scissor) {
+                    if (x == (r[0] & ~1) && fLeft) sLeft = -1;
+                    if (x >= (r[2] & ~1) && fRight) sRight = -1;
+                }
+                const int32_t smask[4] = { sLeft | sTop, sRight | sTop, sLeft | sBot, sRight | sBot };
                 for (int l = 0; l < 4; ++l) {
-                    trimask[l] = edges[l] >> 31;
-                    tc->frags += edges[l] >= 0;
+                    trimask[l] = (edges[l] >> 31) | smask[l];
+                    tc->frags += trimask[l] == 0;
                     bs[0][l] = itof(cx2[l]) * scale;
                     bs[2][l] = itof(cx1[l]) * scale;
                     bs[1][l] = (1.0f - bs[0][l]) - bs[2][l];
@@ -832,7 +853,7 @@ static void walk_quads(TileCtx* tc, const TriSetup* tri, int minx, int miny, int
 /* VTriangleRasterizer::Draw for one lane (rglv_triangle.hxx:193-304), int32 wrap */
 static void raster_vector(TileCtx* tc, const TriSetup* tri, int32_t x1, int32_t x2, int32_t x3,
                           int32_t y1, int32_t y2, int32_t y3) {
-    const int32_t* r = tc->rect;
+    const int32_t* r = tc->drect;
     int32_t vminx = imax(imin(imin(x1, x2), x3) >> 4, r[0]);
     int32_t vmaxx = imin(wadd(imax(imax(x1, x2), x3), 15) >> 4, r[2]);
     int32_t vminy = imax(imin(imin(y1, y2), y3) >> 4, r[1]);
@@ -861,7 +882,7 @@ static void raster_vector(TileCtx* tc, const TriSetup* tri, int32_t x1, int32_t 
 
 /* TriangleRasterizer::Draw (rglv_triangle.hxx:79-167), int64 setup */
 static void raster_scalar(TileCtx* tc, const TriSetup* tri, int x1, int x2, int x3, int y1, int y2, int y3) {
-    const int32_t* r = tc->rect;
+    const int32_t* r = tc->drect;
     int minx = imax(imin(x1, imin(x2, x3)) >> 4, r[0]);
     int endx = imin((imax(x1, imax(x2, x3)) + 15) >> 4, r[2]);
     int miny = imax(imin(y1, imin(y2, y3)) >> 4, r[1]);
@@ -1012,6 +1033,14 @@ static int draw_tile(const Frame* f, int tile, float* color, float* depth, uint8
             if (!(dt == RSRGPU_RB_F32 || (dt == RSRGPU_RB_COLOR_DEPTH && c0 == RSRGPU_RB_COLOR_DEPTH))) return RSRGPU_EINVAL;
             make_vpm(tc.s, tc.vpm);
             dsdo(f, tc.s, tc.DS, tc.DO);
+            memcpy(tc.drect, tc.rect, sizeof(tc.drect));
+            tc.scissor = tc.s->scissor_enabled != 0;
+            if (tc.scissor) {   /* Intersect(rect, gl_offset_and_size_to_irect(...)) (rmlg_irect.hxx:47-50) */
+                int sc[4];
+                scissor_rect(f, tc.s, sc);
+                tc.drect[0] = imax(tc.rect[0], sc[0]); tc.drect[1] = imax(tc.rect[1], sc[1]);
+                tc.drect[2] = imin(tc.rect[2], sc[2]); tc.drect[3] = imin(tc.rect[3], sc[3]);
+            }
             tc.nvary = program_nvary(tc.s->program_id);
             if (tc.s->program_id == RSRGPU_PROGRAM_AMY && make_texture_unit(&tc.s->tus[0], &tc.tu0) != 0) return RSRGPU_EUNSUPPORTED;
         } break;

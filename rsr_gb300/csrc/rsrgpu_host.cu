@@ -227,12 +227,11 @@ bool draw_program_supported(int pid) {
 }
 bool blt_program_supported(int pid) { return pid == kProgDefaultPost || pid == kProgExposurePost || pid == kProgGouraud; }
 
-// the fragment state keys this device implementation covers: no scissor, depth
-// test on with LESS/LEQUAL/EQUAL, RGB f32 colour with f32 depth, or colour and
-// depth packed in RGBA (RB_COLOR_DEPTH)
+// the fragment state keys this device implementation covers: scissor test on
+// or off, depth test on with LESS/LEQUAL/EQUAL, RGB f32 colour with f32 depth,
+// or colour and depth packed in RGBA (RB_COLOR_DEPTH)
 bool draw_key_supported(uint32_t key) {
-    key &= 0xffffffu;
-    if (key & 1u) return false;
+    key &= 0xffffffu;   // bit 0, the scissor test, is taken with every state
     if (!(key & 2u)) return false;
     if (((key >> 2) & 3u) > 2u) return false;
     const uint32_t ct = (key >> 7) & 3u, dt = (key >> 9) & 3u;
@@ -346,6 +345,7 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
         const int bottom = ctx->height - s.scissor_origin[1] - 1, top = bottom - s.scissor_size[1];
         d.scissor[0] = left; d.scissor[1] = top; d.scissor[2] = right; d.scissor[3] = bottom;
     }
+    d.scissor_test = s.scissor_enabled != 0;
     d.program = s.program_id;
     d.nvary = (s.program_id == kProgGouraud || s.program_id == kProgOBJ1) ? 3
             : (s.program_id == kProgAmy || s.program_id == kProgMany) ? 2 : (s.program_id == kProgGBuffer ? 4 : 0);
@@ -826,7 +826,7 @@ int decode_frame(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const 
             drawn = true;
             const DevState& st = ctx->states[size_t(ctx->draws[size_t(o.arg)].state)];
             if (st.blend || !st.depth_test || !st.depth_write || !st.color_write || st.depth_func < 0 || st.depth_func > 1 ||
-                (func >= 0 && st.depth_func != func))
+                (func >= 0 && st.depth_func != func) || st.scissor_test)
                 ok = false;
             func = st.depth_func;
         }
@@ -2174,7 +2174,8 @@ int decode_frame_without_context(int width, int height, int tile_blocks_x, int t
     for (int pid : programs) {
         if (rc == 0) rc = rsrgpu_install(&tmp, pid, 0, 0);
         for (uint32_t k : keys)
-            if (rc == 0 && draw_key_supported(k)) rc = rsrgpu_install(&tmp, pid, k, 1);
+            for (uint32_t scissor = 0; scissor < 2; ++scissor)
+                if (rc == 0 && draw_key_supported(k | scissor)) rc = rsrgpu_install(&tmp, pid, k | scissor, 1);
     }
     const int blts[] = { kProgDefaultPost, kProgExposurePost, kProgGouraud };
     for (int pid : blts)

@@ -51,7 +51,8 @@ struct DevState {
     float vpm[16];
     float DS[2], DO[2];
     float guard;
-    int32_t scissor[4];   // left, top, right, bottom
+    int32_t scissor[4];   // left, top, right, bottom (GPU::ScissorRect; the whole target when the test is off)
+    int32_t scissor_test; // GL_SCISSOR_TEST: draws are cut to scissor[] in the raster pass
     int32_t program;
     int32_t nvary;
     int32_t keep_backs, keep_fronts;

@@ -1055,15 +1055,31 @@ __device__ __forceinline__ void tex_sample_lane(const DevTexture& tu, float u0, 
 // fragment-stage constants of the current state, held in registers
 struct FragState {
     int program, nvary;
-    int depth_test, depth_func, depth_write, color_write, blend;
+    int depth_test, depth_func, depth_write, color_write, blend, scissor;
     DevTexture tu0;
 };
 
 __device__ __forceinline__ void load_frag_state(const DevState& s, FragState& f) {
     f.program = s.program; f.nvary = s.nvary;
     f.depth_test = s.depth_test; f.depth_func = s.depth_func; f.depth_write = s.depth_write;
-    f.color_write = s.color_write; f.blend = s.blend;
+    f.color_write = s.color_write; f.blend = s.blend; f.scissor = s.scissor_test;
     f.tu0 = s.tu0;
+}
+
+// The rectangle a draw rasterises in: the tile, cut to the scissor rectangle
+// when the state's scissor test is on (GPUTileImpl::DrawTriangles /
+// DrawClipped: Intersect(rect, scissor), rglv_gpu_impl.hxx:848-849,953-954).
+// The quad walk starts at even coordinates, so a quad can reach one pixel
+// past an odd edge of it; the reference masks those lanes (ScissorFlags,
+// rglv_triangle.hxx:23-28,268-292), which is the same as leaving out pixels
+// outside the rectangle.
+__device__ __forceinline__ void draw_rect(const DevState& s, const int tile[4], int out[4]) {
+    if (s.scissor_test) {
+        out[0] = max(tile[0], s.scissor[0]); out[1] = max(tile[1], s.scissor[1]);
+        out[2] = min(tile[2], s.scissor[2]); out[3] = min(tile[3], s.scissor[3]);
+    } else {
+        out[0] = tile[0]; out[1] = tile[1]; out[2] = tile[2]; out[3] = tile[3];
+    }
 }
 
 // sRGB8 encode with this library's own table (see rsrgpu_host.cu)
@@ -1085,13 +1101,15 @@ constexpr uint32_t kClippedBit = 0x80000000u;
 // Per-(triangle, tile) setup and vertex data of one list entry, for the
 // resolve pass: the triangle that last wrote a pixel is set up again exactly
 // as when it was rasterised.
-__device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int rect[4], TriSetup& t,
+__device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
                                          float w[3], float vary[3][kMaxVary], int& state) {
-    int g;
+    const int g = (code & kClippedBit) ? fv.clip_src[fv.clip_poly[code & ~kClippedBit]] : int(code);
+    state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+    int rect[4];
+    draw_rect(fv.states[state], tile, rect);
     if (code & kClippedBit) {
         const uint32_t e = code & ~kClippedBit;
         const int pbase = fv.clip_poly[e];
-        g = fv.clip_src[pbase];
         const ClipVert v0 = fv.clip_verts[pbase], v1 = fv.clip_verts[e], v2 = fv.clip_verts[e + 1];
         setup_scalar(t, rect,
                      __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
@@ -1099,7 +1117,6 @@ __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, con
         w[0] = v0.coord[3]; w[1] = v1.coord[3]; w[2] = v2.coord[3];
         for (int q = 0; q < kMaxVary; ++q) { vary[0][q] = v0.vary[q]; vary[1][q] = v1.vary[q]; vary[2][q] = v2.vary[q]; }
     } else {
-        g = int(code);
         const float4* rp = reinterpret_cast<const float4*>(fv.tris + g);
         TriRecord r;
         float4* rr = reinterpret_cast<float4*>(&r);
@@ -1110,7 +1127,6 @@ __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, con
             for (int q = 0; q < kMaxVary; ++q) vary[k][q] = r.vary[k][q];
         }
     }
-    state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
 }
 
 // perspective-correct barycentrics of one lane (TriangleProgram::Render,
@@ -1437,6 +1453,8 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         } else if (o.kind == kOpDraw) {
             const DevDraw dr = fv.draws[o.arg];
             const int end_tri = dr.first_tri + dr.ntris;
+            int drect[4];   // the tile, or its part inside the scissor rectangle
+            draw_rect(fv.states[dr.state], rect, drect);
             if (visibility) pending = true;
             if (fv.raster_phase == 2) continue;   // drawn by the first launch
             if (key_state == 0) {
@@ -1476,7 +1494,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             float4* rr = reinterpret_cast<float4*>(&r);
 #pragma unroll
                             for (int q = 0; q < 6; ++q) rr[q] = __ldg(rp + q);
-                            setup_vector(t, rect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
+                            setup_vector(t, drect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
 #pragma unroll
                             for (int k = 0; k < 3; ++k) {
                                 S.z[k][tid] = r.z[k]; S.w[k][tid] = r.w[k];
@@ -1488,7 +1506,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             const int pbase = fv.clip_poly[e];
                             const ClipVert v0 = fv.clip_verts[pbase], v1 = fv.clip_verts[e], v2 = fv.clip_verts[e + 1];
                             // DrawClipped: int(dev.x * FP_MUL) (rglv_gpu_impl.hxx:997-998)
-                            setup_scalar(t, rect,
+                            setup_scalar(t, drect,
                                          __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
                                          __float2int_rz(v0.coord[1] * 16.0f), __float2int_rz(v1.coord[1] * 16.0f), __float2int_rz(v2.coord[1] * 16.0f));
                             S.z[0][tid] = v0.coord[2]; S.z[1][tid] = v1.coord[2]; S.z[2][tid] = v2.coord[2];
@@ -1585,7 +1603,14 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             bool inside[4];
                             bool anyin = false;
 #pragma unroll
-                            for (int l = 0; l < 4; ++l) { inside[l] = (l1[l] | l2[l] | l3[l]) >= 0; anyin |= inside[l]; }
+                            for (int l = 0; l < 4; ++l) {
+                                inside[l] = (l1[l] | l2[l] | l3[l]) >= 0;
+                                if (fs.scissor) {
+                                    const int px = qx + (l & 1), py = qy + (l >> 1);
+                                    inside[l] = inside[l] && px >= drect[0] && px < drect[2] && py >= drect[1] && py < drect[3];
+                                }
+                                anyin |= inside[l];
+                            }
                             if (!anyin) continue;
                             const float scale = S.scale[i];
                             const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];

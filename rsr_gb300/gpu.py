@@ -22,7 +22,8 @@ class RsrGpuError(RuntimeError):
 
 # The fragment state keys rsr's viewer installs (src/viewer/shaders.cxx:49-53,
 # 71-126) plus LEQUAL and the no-depth-write variant of the RGB f32 layout.
-DRAW_STATE_KEYS = (0x6E2, 0x6E6, 0x6F2, 0x6C2, 0x62, 0x72)
+# Each is installed with and without the scissor test (key bit 0).
+DRAW_STATE_KEYS = tuple(k | scissor for k in (0x6E2, 0x6E6, 0x6F2, 0x6C2, 0x62, 0x72) for scissor in (0, 1))
 
 
 class GPU:

@@ -87,8 +87,10 @@ class Scene:
     into a GL using ref(name) to obtain the buffer object to point at (the
     numpy array itself, or a device tensor holding a copy of it)."""
 
-    def __init__(self, name, width, height, tile_blocks, arrays, record_fn, ntris, post_program=None):
+    def __init__(self, name, width, height, tile_blocks, arrays, record_fn, ntris, post_program=None,
+                 store_depth=True):
         self.post_program = post_program
+        self.store_depth = store_depth   # RB_COLOR_DEPTH frames have no separate depth to store
         self.name = name
         self.width = width
         self.height = height
@@ -106,7 +108,8 @@ class Scene:
         if self.post_program is None:
             gl.UseProgram(abi.PROGRAM_DEFAULT_POST)
         gl.StoreColor(self.color if color is None else color, self.width, self.height, gamma)
-        gl.StoreDepth(self.depth if depth is None else depth)
+        if self.store_depth:
+            gl.StoreDepth(self.depth if depth is None else depth)
         return gl
 
 
@@ -418,6 +421,91 @@ def mixed_states(seed=13, width=640, height=360, tile_blocks=(4, 4)):
 
     return Scene("mixed_states", width, height, tile_blocks, arrays, record,
                  c1 // 3 + len(faces) + c3 // 3 + c4 // 3, post_program=abi.PROGRAM_EXPOSURE_POST)
+
+
+def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_depth=False):
+    """Draws under scissor rectangles (GL::Scissor, GPU::ScissorRect with
+    rsr's bottom = height - y - 1, rglv_gpu.hxx:258-276): an unscissored draw,
+    then rectangles with odd edges that cut quads, one partly off screen (with
+    blending), the whole-screen rectangle (whose last row the reference
+    leaves out), an empty one, one with depth writes off, and near-plane
+    clipped triangles under a scissor (the clipper's covered-tile walk).
+    color_depth: RB_COLOR_DEPTH attachments (LESS only, with and without
+    blending)."""
+    sets = {"a": 1200, "b": 600, "c": 400, "d": 400, "f": 200, "g": 300}
+    u = uniform01(seed, sum(sets.values()) * 3 * 6).reshape(-1, 3, 6)
+    arrays = {}
+    at = 0
+    counts = {}
+    for tag, n in sets.items():
+        rows = u[at:at + n]
+        at += n
+        pos = lerp(-1.0, 1.0, rows[:, :, 0:3]).reshape(-1, 3)
+        rgb = lerp(0.0, 1.0, rows[:, :, 3:6]).reshape(-1, 3)
+        for k, c in enumerate("xyz"):
+            arrays["%s_p%s" % (tag, c)] = pad4(pos[:, k])
+        for k, c in enumerate("rgb"):
+            arrays["%s_c%s" % (tag, c)] = pad4(rgb[:, k])
+        arrays["%s_idx" % tag] = np.arange(len(pos), dtype=np.uint16)
+        counts[tag] = len(pos)
+    # triangles around a perspective camera: many cross the near plane
+    ne = 800
+    ue = uniform01(seed + 1, ne * 3 * 6).reshape(ne, 3, 6)
+    pos = lerp(-6.0, 6.0, ue[:, :, 0:3]).reshape(-1, 3)
+    rgb = lerp(0.0, 1.0, ue[:, :, 3:6]).reshape(-1, 3)
+    for k, c in enumerate("xyz"):
+        arrays["e_p%s" % c] = pad4(pos[:, k])
+    for k, c in enumerate("rgb"):
+        arrays["e_c%s" % c] = pad4(rgb[:, k])
+    arrays["e_idx"] = np.arange(len(pos), dtype=np.uint16)
+    counts["e"] = len(pos)
+    proj = perspective(90.0, width / height, 0.5, 50.0)
+    ident = np.eye(4, dtype=np.float32).reshape(16)
+
+    def draw(gl, ref, tag):
+        gl.UseBuffer(0, (ref(tag + "_px"), ref(tag + "_py"), ref(tag + "_pz")))
+        gl.UseBuffer(3, (ref(tag + "_cr"), ref(tag + "_cg"), ref(tag + "_cb")))
+        gl.DrawElements(counts[tag], ref(tag + "_idx"), 0)
+
+    def record(gl, ref):
+        rb = abi.RB_COLOR_DEPTH if color_depth else abi.RB_RGBF32
+        gl.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, rb)
+        gl.RenderbufferType(abi.GL_DEPTH_ATTACHMENT, abi.RB_COLOR_DEPTH if color_depth else abi.RB_F32)
+        gl.ClearColor((0.05, 0.1, 0.2))
+        gl.ClearDepth(1.0)
+        gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        draw(gl, ref, "a")                                   # no scissor
+        gl.Enable(abi.GL_SCISSOR_TEST)
+        gl.Scissor(37, 21, 101, 77)                          # odd edges on every side
+        draw(gl, ref, "b")
+        gl.Scissor(0, 0, width, height)                      # the whole screen
+        if not color_depth:
+            gl.DepthFunc(abi.GL_LEQUAL)
+        draw(gl, ref, "c")
+        gl.DepthFunc(abi.GL_LESS)
+        gl.Scissor(width - 51, -13, 200, 90)                 # partly off screen, blending
+        gl.Enable(abi.GL_BLEND)
+        draw(gl, ref, "d")
+        gl.Disable(abi.GL_BLEND)
+        gl.Scissor(10, 10, 0, 0)                             # empty
+        draw(gl, ref, "f")
+        if not color_depth:
+            gl.Scissor(width // 2 - 63, height // 2 - 41, 127, 83)
+            gl.DepthWriteMask(False)
+            draw(gl, ref, "g")
+            gl.DepthWriteMask(True)
+        gl.Scissor(201, 150, 173, 95)                        # clipped triangles
+        gl.ProjectionMatrix(proj)
+        gl.Enable(abi.GL_CULL_FACE)
+        gl.CullFace(abi.GL_BACK)
+        draw(gl, ref, "e")
+        gl.Disable(abi.GL_CULL_FACE)
+        gl.ProjectionMatrix(ident)
+        gl.Disable(abi.GL_SCISSOR_TEST)
+
+    ntris = sum(counts.values()) // 3 - (0 if not color_depth else counts["g"] // 3)
+    return Scene("scissor_scene", width, height, tile_blocks, arrays, record, ntris, store_depth=not color_depth)
 
 
 # ---- deferred scene: many small objects, G-buffer program, 64 point lights ----

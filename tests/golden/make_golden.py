@@ -43,6 +43,11 @@ GOLDEN_SCENES = {
     "clip_640_t64": ("clip_stress", {}, 3),
     "clip_2160_t32": ("clip_stress", dict(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0), 3),
     "mixed_640_t32": ("mixed_states", {}, 3),
+    # scissor-enabled draws: odd rectangle edges, off screen, whole screen,
+    # empty, depth writes off, clipped triangles; both attachment layouts
+    "scissor_640_t32": ("scissor_scene", {}, 3),
+    "scissor_640_t8_color_depth": ("scissor_scene", dict(seed=62, tile_blocks=(1, 1), color_depth=True), 3),
+    "scissor_360_t64": ("scissor_scene", dict(seed=63, width=360, height=202, tile_blocks=(8, 8)), 3),
     # geometry of the deferred (G-buffer) scene drawn with the Gouraud program:
     # pins the G-buffer pass's depth to rsr
     "deferred_gouraud_640": ("deferred_scene", dict(nobj=20000, width=640, height=360, gouraud=True), 3),

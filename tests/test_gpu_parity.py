@@ -30,6 +30,11 @@ SCENES = {
     "clip_2160_t32": lambda: scenes.clip_stress(seed=5, width=3840, height=2160, tile_blocks=(4, 4), extent=3.0),
     "mixed_640_t32": lambda: scenes.mixed_states(),
     "mixed_640_t8": lambda: scenes.mixed_states(seed=14, tile_blocks=(1, 1)),
+    # scissor-enabled draws (odd rectangle edges, off screen, whole screen,
+    # empty, clipped triangles), both attachment layouts, partial tiles
+    "scissor_640_t32": lambda: scenes.scissor_scene(),
+    "scissor_640_t8_color_depth": lambda: scenes.scissor_scene(seed=62, tile_blocks=(1, 1), color_depth=True),
+    "scissor_360_t64": lambda: scenes.scissor_scene(seed=63, width=360, height=202, tile_blocks=(8, 8)),
     # 1250 chunks of 32 large triangles, nearly all overlapping every 8x8 tile:
     # binning takes its windows of 1024 chunks; four draws
     "plain_320_t8_windows": lambda: scenes.plain_raster(seed=31, ntris=40000, width=320, height=180, tile_blocks=(1, 1)),
