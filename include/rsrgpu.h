@@ -594,6 +594,17 @@ int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gb
  * check (the affected tiles were left unwritten), else 0. */
 int rsrgpu_shade_learned_check(rsrgpu_ctx* ctx);
 
+/* Test hooks for the failure paths that a healthy GPU never takes.
+ * RSRGPU_DEBUG_LEARNED_STALL, value = polls > 0: in the following
+ * rsrgpu_shade_learned() calls the tensor-core kernel's producer threads
+ * issue no copy (so no MMA either), and every pipeline wait gives up after
+ * `value` polls; the kernel then raises its error flag, frees its tensor
+ * memory and returns, and rsrgpu_shade_learned_check() reports
+ * RSRGPU_ETIMEOUT.  value 0 restores normal operation.  No fault, trap or
+ * endless wait is involved. */
+#define RSRGPU_DEBUG_LEARNED_STALL 1
+int rsrgpu_set_debug(rsrgpu_ctx* ctx, int knob, int value);
+
 /* The learned shader's inputs and training targets for every pixel:
  * features[W*H][32] BF16 (columns 24..31 and uncovered rows zero), targets
  * (optional) [W*H][3] = sqrt(max(plain linear RGB, 0)) - base, the network's

@@ -389,6 +389,19 @@ static void dsdo(const Frame* f, const rsrgpu_glstate* s, float DS[2], float DO[
     DO[1] = (float)(f->height - (vy / 2 + s->viewport_origin[1]));
 }
 
+/* The tile range a triangle is binned to, kept inside the tile grid.  rsr
+ * indexes tilesHead_[ty * stride + tx] unchecked (rglv_gpu_impl.hxx:490-496,
+ * 808-815): a scissor rectangle reaching past the right or bottom edge of the
+ * target gives tx = tiles_x (the next row's first tile) or ty = tiles_y (past
+ * the array).  Without such a rectangle the range is inside the grid and
+ * this changes nothing. */
+static void clamp_to_grid(const Frame* f, int* tx0, int* ty0, int* tx1, int* ty1) {
+    if (*tx0 < 0) *tx0 = 0;
+    if (*ty0 < 0) *ty0 = 0;
+    if (*tx1 > f->tiles_x - 1) *tx1 = f->tiles_x - 1;
+    if (*ty1 > f->tiles_y - 1) *ty1 = f->tiles_y - 1;
+}
+
 /* GPU::ScissorRect (rglv_gpu.hxx:272-276): left, top, right, bottom */
 static void scissor_rect(const Frame* f, const rsrgpu_glstate* s, int r[4]) {
     if (!s->scissor_enabled) { r[0] = 0; r[1] = 0; r[2] = f->width; r[3] = f->height; return; }
@@ -484,6 +497,7 @@ static int bin_draw(Frame* f, int state_idx, int count, const uint16_t* indices,
         if (!front) ni0 |= 0x8000;
         int tx0 = vminx / f->tile_w, ty0 = vminy / f->tile_h;
         int tx1 = vmaxx / f->tile_w, ty1 = vmaxy / f->tile_h;
+        clamp_to_grid(f, &tx0, &ty0, &tx1, &ty1);
         for (int ty = ty0; ty <= ty1; ++ty) {
             for (int tx = tx0; tx <= tx1; ++tx) {
                 ByteBuf* b = &f->tiles[ty * f->tiles_x + tx];
@@ -593,6 +607,7 @@ static int clip_triangles(Frame* f, const rsrgpu_glstate* s, const ClipEntry* q,
             int vmaxx = imin(imax(x0, imax(x1, x2)) + 1, sc[2] - 1);
             int vmaxy = imin(imax(y0, imax(y1, y2)) + 1, sc[3] - 1);
             int tx0 = vminx / f->tile_w, ty0 = vminy / f->tile_h, tx1 = vmaxx / f->tile_w, ty1 = vmaxy / f->tile_h;
+            clamp_to_grid(f, &tx0, &ty0, &tx1, &ty1);
             for (int ty = ty0; ty <= ty1; ++ty) {
                 for (int tx = tx0; tx <= tx1; ++tx) {
                     ByteBuf* b = &f->tiles[ty * f->tiles_x + tx];

@@ -61,6 +61,8 @@ PROGRAM_GBUFFER = 91
 
 KIND_BIN, KIND_DRAW, KIND_BLT = 0, 1, 2
 
+DEBUG_LEARNED_STALL = 1
+
 RSRGPU_OK = 0
 
 
@@ -217,6 +219,7 @@ SYMBOLS = {
                               ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_float, ctypes.c_void_p,
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "rsrgpu_shade_learned_check": ([ctypes.c_void_p], ctypes.c_int),
+    "rsrgpu_set_debug": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "rsrgpu_learned_features": ([ctypes.c_void_p, ctypes.POINTER(GBufferC), ctypes.POINTER(ctypes.c_float),
                                  ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),

@@ -53,7 +53,7 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
                                  const rsrgpu_light* lights, int nlights, const float background[3], float max_tile_mse,
                                  uint32_t* out_srgb, float* out_linear, uint8_t* tile_status, float* tile_mse,
                                  const uint8_t* srgb_lut, int* error, int* counters, void* scratch,
-                                 int num_sms, cudaStream_t st);
+                                 int num_sms, int stall_polls, cudaStream_t st);
 size_t learned_scratch_bytes(int tiles);
 int texture_power(int width, int height);
 struct FloatCanvasView {
@@ -157,6 +157,7 @@ struct rsrgpu_ctx {
     uint32_t clip_cap = 1u << 18;
     uint32_t bin_cap = 1u << 22;
     int region_px = kRegionPx;      // raster CTA region (the autotuner may pick 16)
+    int debug_learned_stall = 0;    // RSRGPU_DEBUG_LEARNED_STALL (rsrgpu_set_debug)
     int vis_keys = 0;               // FrameView::vis_keys of the submitted frame
     DevBuf d_vis;                   // owners and depths between the two launches of a split raster pass
     // the run's work captured once per submission and replayed by every run
@@ -1641,7 +1642,8 @@ int rsrgpu_shade_learned(rsrgpu_ctx* ctx, const rsrgpu_mlp* mlp, const rsrgpu_gb
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
     CK(launch_shade_learned(*mlp, *gbuffer, inv_view_proj, eye, lights, nlights, background, max_tile_mse, out_srgb,
                             out_linear, tile_status, tile_mse, ctx->d_srgb.as<uint8_t>(), ctx->d_learn_err.as<int>(),
-                            ctx->d_learn_err.as<int>() + 1, ctx->d_learn_tiles.p, ctx->num_sms, st), "shade_learned_kernel");
+                            ctx->d_learn_err.as<int>() + 1, ctx->d_learn_tiles.p, ctx->num_sms, ctx->debug_learned_stall, st),
+       "shade_learned_kernel");
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     CK(cudaStreamIsCapturing(st, &cap), "stream capture status");
     if (cap == cudaStreamCaptureStatusNone) {   // a captured call is checked after its replays are synchronised
@@ -1660,7 +1662,17 @@ int rsrgpu_shade_learned_check(rsrgpu_ctx* ctx) {
     CK(cudaMemcpy(&flag, ctx->d_learn_err.p, sizeof(int), cudaMemcpyDeviceToHost), "D2H learned-shader error");
     if (flag == 0) return 0;
     CK(cudaMemset(ctx->d_learn_err.p, 0, sizeof(int)), "clear learned-shader error flag");
-    return fail(ctx, RSRGPU_ETIMEOUT, "tensor-core MMA did not complete in the learned shader (bounded wait expired)");
+    return fail(ctx, RSRGPU_ETIMEOUT, "a bounded wait of the learned shader's tensor-core kernel expired");
+}
+
+int rsrgpu_set_debug(rsrgpu_ctx* ctx, int knob, int value) {
+    if (ctx == nullptr) return RSRGPU_EINVAL;
+    if (knob == RSRGPU_DEBUG_LEARNED_STALL) {
+        if (value < 0) return fail(ctx, RSRGPU_EINVAL, "RSRGPU_DEBUG_LEARNED_STALL: polls >= 0");
+        ctx->debug_learned_stall = value;
+        return 0;
+    }
+    return fail(ctx, RSRGPU_EINVAL, "unknown debug knob %d", knob);
 }
 
 int rsrgpu_learned_features(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, const float inv_view_proj[16],

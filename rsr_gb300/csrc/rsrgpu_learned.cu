@@ -114,6 +114,8 @@ struct LearnParams {
     int32_t* rejected;        // [tiles] tiles for the fallback pass
     uint8_t* feat;            // [tiles * 8][8 KB] A tiles
     PipeMeta* metas;          // [tiles * 8]
+    uint32_t poll_limit;      // polls of a pipeline wait before it gives up
+    int32_t stall;            // test hook: the producers issue nothing, so the waits run out
 };
 
 __device__ __forceinline__ void store_pixel(const PlainParams& p, int pi, const float rgb[3]) {
@@ -439,8 +441,8 @@ __device__ __forceinline__ void issue(uint32_t d, const uint8_t* a, const uint8_
 }
 
 // bounded wait that also gives up when the CTA is winding down
-__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
-    for (uint32_t i = 0; i < (1u << 22); ++i) {
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; ++i) {
         if (tc::mbar_try_wait(bar, parity)) return true;
         if ((i & 255u) == 255u && *abort) return false;
         if (i > 64) __nanosleep(32);
@@ -455,6 +457,7 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
 // pre-pass still held), where taking blocks first-come would leave them none.
 __device__ void produce(LearnSmem& S, const LearnParams& A, int lane) {
     volatile int* abort = &S.abort;
+    if (A.stall) return;   // nothing issued: the consumers' waits run out with no copy or MMA in flight
     uint32_t eparity = 0xfu;   // per pipeline: the parity to wait for on its empty barrier (fresh: passes)
     int pipe = 0;
     const int nblocks = *reinterpret_cast<volatile int*>(A.counters + 1);
@@ -462,7 +465,7 @@ __device__ void produce(LearnSmem& S, const LearnParams& A, int lane) {
     for (int k = int(blockIdx.x) * kLanes + lane; k < nblocks && !*abort; k += stride) {
         const int blk = A.blocks[k];
         const int pp = lane * kPipes + pipe;
-        if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort)) break;
+        if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort, A.poll_limit)) break;
         eparity ^= 1u << pipe;
         tc::mbar_arrive_expect_tx(&S.full[pp], uint32_t(kFeatBytes + sizeof(PipeMeta)));
         tc::bulk_g2s(S.feat[pp], A.feat + size_t(blk) * kFeatBytes, kFeatBytes, &S.full[pp]);
@@ -472,7 +475,7 @@ __device__ void produce(LearnSmem& S, const LearnParams& A, int lane) {
     // end of work: one sentinel per pipeline
     for (int k = 0; k < kPipes && !*abort; ++k) {
         const int pp = lane * kPipes + pipe;
-        if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort)) break;
+        if (!wait_or_abort(&S.empty[pp], (eparity >> pipe) & 1u, abort, A.poll_limit)) break;
         eparity ^= 1u << pipe;
         S.meta[pp].tile = -1;
         tc::mbar_arrive(&S.full[pp]);
@@ -502,7 +505,7 @@ __device__ __forceinline__ void consume_step(LearnSmem& S, const LearnParams& A,
     const uint32_t trow = dcol + (uint32_t(warp * 32) << 16);
     uint8_t* tileb = S.act[pp];
     if (B.stage == 0) {
-        if (!wait_or_abort(&S.full[pp], (fparity >> pipe) & 1u, abort)) return;
+        if (!wait_or_abort(&S.full[pp], (fparity >> pipe) & 1u, abort, A.poll_limit)) return;
         fparity ^= 1u << pipe;
         const PipeMeta& M = S.meta[pp];
         B.tile = M.tile;
@@ -515,7 +518,7 @@ __device__ __forceinline__ void consume_step(LearnSmem& S, const LearnParams& A,
         B.stage = 1;
         return;
     }
-    if (!wait_or_abort(&S.mma[pp], (mparity >> pipe) & 1u, abort)) return;
+    if (!wait_or_abort(&S.mma[pp], (mparity >> pipe) & 1u, abort, A.poll_limit)) return;
     mparity ^= 1u << pipe;
     tc::fence_after_sync();
     if (B.stage < 4) {
@@ -682,8 +685,10 @@ cudaError_t launch_shade_learned(const rsrgpu_mlp& w, const rsrgpu_gbuffer& gb, 
                                  const rsrgpu_light* lights, int nlights, const float background[3], float max_tile_mse,
                                  uint32_t* out_srgb, float* out_linear, uint8_t* tile_status, float* tile_mse,
                                  const uint8_t* srgb_lut, int* error, int* counters, void* scratch,
-                                 int num_sms, cudaStream_t st) {
+                                 int num_sms, int stall_polls, cudaStream_t st) {
     LearnParams A{};
+    A.poll_limit = stall_polls > 0 ? uint32_t(stall_polls) : (1u << 22);
+    A.stall = stall_polls > 0 ? 1 : 0;
     PlainParams& p = A.pl;
     p.depth = gb.depth; p.nx = gb.normal_x; p.ny = gb.normal_y; p.nz = gb.normal_z; p.albedo = gb.albedo;
     p.width = gb.width; p.height = gb.height;

@@ -255,6 +255,10 @@ class GPU:
     def shade_learned_check(self):
         self._check(self.lib.rsrgpu_shade_learned_check(self.ctx))
 
+    def set_debug(self, knob, value):
+        """rsrgpu_set_debug: test hooks for failure paths (abi.DEBUG_*)."""
+        self._check(self.lib.rsrgpu_set_debug(self.ctx, int(knob), int(value)))
+
     def learned_features(self, gbuf, width, height, ivp, eye, lights, features, targets=None, candidates=None,
                          stream=None):
         """rsrgpu_learned_features: dense BF16 features (H*W, 32), optional targets and candidates."""

@@ -423,7 +423,7 @@ def mixed_states(seed=13, width=640, height=360, tile_blocks=(4, 4)):
                  c1 // 3 + len(faces) + c3 // 3 + c4 // 3, post_program=abi.PROGRAM_EXPOSURE_POST)
 
 
-def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_depth=False):
+def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_depth=False, past_edges=False):
     """Draws under scissor rectangles (GL::Scissor, GPU::ScissorRect with
     rsr's bottom = height - y - 1, rglv_gpu.hxx:258-276): an unscissored draw,
     then rectangles with odd edges that cut quads, one partly off screen (with
@@ -431,7 +431,9 @@ def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_dept
     leaves out), an empty one, one with depth writes off, and near-plane
     clipped triangles under a scissor (the clipper's covered-tile walk).
     color_depth: RB_COLOR_DEPTH attachments (LESS only, with and without
-    blending)."""
+    blending).  past_edges: one more rectangle reaching past the right and
+    bottom edges of the target, where rsr bins to tile indices outside its
+    grid (this library and the oracle keep to the grid)."""
     sets = {"a": 1200, "b": 600, "c": 400, "d": 400, "f": 200, "g": 300}
     u = uniform01(seed, sum(sets.values()) * 3 * 6).reshape(-1, 3, 6)
     arrays = {}
@@ -484,7 +486,7 @@ def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_dept
             gl.DepthFunc(abi.GL_LEQUAL)
         draw(gl, ref, "c")
         gl.DepthFunc(abi.GL_LESS)
-        gl.Scissor(width - 51, -13, 200, 90)                 # partly off screen, blending
+        gl.Scissor(-13, height - 41, 160, 90)                # partly off screen (left, top), blending
         gl.Enable(abi.GL_BLEND)
         draw(gl, ref, "d")
         gl.Disable(abi.GL_BLEND)
@@ -495,6 +497,9 @@ def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_dept
             gl.DepthWriteMask(False)
             draw(gl, ref, "g")
             gl.DepthWriteMask(True)
+        if past_edges:
+            gl.Scissor(width - 37, -11, 100, 60)             # past the right and bottom edges
+            draw(gl, ref, "b")
         gl.Scissor(201, 150, 173, 95)                        # clipped triangles
         gl.ProjectionMatrix(proj)
         gl.Enable(abi.GL_CULL_FACE)
@@ -504,7 +509,7 @@ def scissor_scene(seed=61, width=640, height=360, tile_blocks=(4, 4), color_dept
         gl.ProjectionMatrix(ident)
         gl.Disable(abi.GL_SCISSOR_TEST)
 
-    ntris = sum(counts.values()) // 3 - (0 if not color_depth else counts["g"] // 3)
+    ntris = sum(counts.values()) // 3 - (0 if not color_depth else counts["g"] // 3) + (counts["b"] // 3 if past_edges else 0)
     return Scene("scissor_scene", width, height, tile_blocks, arrays, record, ntris, store_depth=not color_depth)
 
 

@@ -35,6 +35,9 @@ SCENES = {
     "scissor_640_t32": lambda: scenes.scissor_scene(),
     "scissor_640_t8_color_depth": lambda: scenes.scissor_scene(seed=62, tile_blocks=(1, 1), color_depth=True),
     "scissor_360_t64": lambda: scenes.scissor_scene(seed=63, width=360, height=202, tile_blocks=(8, 8)),
+    # a scissor rectangle past the right and bottom edges: rsr bins outside its
+    # tile grid there; the oracle and the device keep to the grid (no rsr digest)
+    "scissor_640_t32_past_edges": lambda: scenes.scissor_scene(seed=64, past_edges=True),
     # 1250 chunks of 32 large triangles, nearly all overlapping every 8x8 tile:
     # binning takes its windows of 1024 chunks; four draws
     "plain_320_t8_windows": lambda: scenes.plain_raster(seed=31, ntris=40000, width=320, height=180, tile_blocks=(1, 1)),

@@ -212,6 +212,33 @@ def _reference_forward(params, feat_bf16_bits, base):
 
 
 @pytest.mark.gpu
+def test_expired_wait_reports_timeout_and_recovers(gpu, frame):
+    """Failure detection without a fault: with RSRGPU_DEBUG_LEARNED_STALL the
+    tensor-core kernel's producers issue no copy, so no MMA is ever in
+    flight; the consumers' bounded waits run out after 4096 polls, the kernel
+    raises its error flag, frees its tensor memory and returns, and the
+    check reports RSRGPU_ETIMEOUT.  The next call, hook off, shades the frame
+    exactly as before."""
+    from rsr_gb300 import abi
+    from rsr_gb300.gpu import RsrGpuError
+    fr, _, _ = frame
+    net = _net(3)
+    want = _shade(gpu, fr, net, float("inf"))
+    gpu.set_debug(abi.DEBUG_LEARNED_STALL, 4096)
+    try:
+        with pytest.raises(RsrGpuError) as err:
+            _shade(gpu, fr, net, float("inf"))
+        assert err.value.code == -5   # RSRGPU_ETIMEOUT
+    finally:
+        gpu.set_debug(abi.DEBUG_LEARNED_STALL, 0)
+    got = _shade(gpu, fr, net, float("inf"))
+    for a, b in zip(got, want):
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+    with pytest.raises(RsrGpuError):
+        gpu.set_debug(99, 1)
+
+
+@pytest.mark.gpu
 def test_no_fallback_matches_reference_forward(gpu, frame):
     """Pixels reached by two or more candidate lights go through the network,
     the others take the analytic base (their Blinn-Phong shading)."""
