@@ -680,7 +680,9 @@ int rsrgpu_batch_last_error(rsrgpu_batch* batch, char* buf, size_t len);
  * library holds until the process exits.  Inputs and outputs must be device
  * pointers; there is no context and no host staging.  The first call on a
  * device sets the array up (symbol address lookup and two synchronous table
- * uploads), so make it before any stream capture.  Calls share the array
+ * uploads, under a lock, so first calls from several host threads are safe),
+ * so make it before any stream capture; the address it caches does not
+ * survive cudaDeviceReset().  Calls share the array
  * (the counters that must start at zero are cleared on every call), so
  * calls that overlap on the GPU race: serialise them.  The call returns once
  * the frame has finished on `stream` (a cudaStream_t, NULL = legacy stream);

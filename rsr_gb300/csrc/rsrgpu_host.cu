@@ -241,10 +241,12 @@ bool draw_key_supported(uint32_t key) {
     return false;
 }
 
+}  // namespace
+
 // sRGB8 encode table of this library: for each of the 13*2048 float classes
 // the clamped input falls into (exponent and top 11 mantissa bits), the
 // correctly rounded 8-bit sRGB value of the class midpoint.
-void build_srgb_lut(std::vector<uint8_t>& lut) {
+void rsrgpu::build_srgb_lut(std::vector<uint8_t>& lut) {
     lut.resize(26624);
     for (uint32_t k = 0; k < 26624; ++k) {
         const uint32_t bits = ((k + ((127u - 13u) << 11)) << 12) | 0x800u;
@@ -256,6 +258,8 @@ void build_srgb_lut(std::vector<uint8_t>& lut) {
         lut[k] = uint8_t(v < 0 ? 0 : (v > 255 ? 255 : v));
     }
 }
+
+namespace {
 
 // Maps a caller pointer to a device address and the number of bytes that
 // are valid from it (to the end of the registered host buffer, or of the
@@ -2178,7 +2182,8 @@ namespace rsrgpu {
 int decode_frame_without_context(int width, int height, int tile_blocks_x, int tile_blocks_y,
                                  const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates,
                                  std::vector<DevState>& out_states, std::vector<DevDraw>& out_draws,
-                                 std::vector<FrameOp>& out_ops, int& ntris, int& ntiles, std::string& err) {
+                                 std::vector<FrameOp>& out_ops, int& ntris, int& ntiles, int& vis_keys,
+                                 std::string& err) {
     rsrgpu_ctx tmp;
     int rc = rsrgpu_reset(&tmp, width, height, tile_blocks_x, tile_blocks_y);
     const int programs[] = { kProgGouraud, kProgAmy, kProgMany };
@@ -2210,6 +2215,7 @@ int decode_frame_without_context(int width, int height, int tile_blocks_x, int t
     out_ops = std::move(tmp.ops);
     ntris = tmp.ntris;
     ntiles = tmp.ntiles;
+    vis_keys = tmp.vis_keys;
     return 0;
 }
 }  // namespace rsrgpu

@@ -16,6 +16,7 @@
 //                       clipped fan-triangle ids
 #pragma once
 #include <cstdint>
+#include <vector>
 
 namespace rsrgpu {
 
@@ -200,5 +201,9 @@ struct BatchLaunch {
     int32_t start[kMaxBatch + 1];
     FrameView fv[kMaxBatch];
 };
+
+// the sRGB8 encode table the raster pass stores through (26 624 entries; the
+// context path and rsrgpu_render_static upload the same table)
+void build_srgb_lut(std::vector<uint8_t>& lut);
 
 }  // namespace rsrgpu

@@ -17,15 +17,19 @@
 //  * The first call on a device does the set-up (looks up the array's device
 //    address with cudaGetSymbolAddress and uploads the rcpps and sRGB tables
 //    with synchronous copies); make that first call before any stream capture.
+//    The set-up runs under a lock, so first calls from several host threads
+//    are safe.  The address is cached per device for the life of the process:
+//    after cudaDeviceReset() the cache is stale.
 //  * Every call shares the array and it keeps the last call's contents; the
 //    counters and rectangles that must start at zero are cleared each call.
 //    Calls that overlap on the GPU (concurrent streams or threads) race on
 //    the array: serialise them.
 //  * The call returns when the frame has finished on `stream`, so it can
 //    report capacity overflow and out-of-range vertex indices.
-#include <cmath>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -41,7 +45,8 @@ cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
 int decode_frame_without_context(int width, int height, int tile_blocks_x, int tile_blocks_y,
                                  const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates,
                                  std::vector<DevState>& out_states, std::vector<DevDraw>& out_draws,
-                                 std::vector<FrameOp>& out_ops, int& ntris, int& ntiles, std::string& err);
+                                 std::vector<FrameOp>& out_ops, int& ntris, int& ntiles, int& vis_keys,
+                                 std::string& err);
 static const uint32_t kStaticRcpTable[2048] = {
 #include "rcpps_table.inc"
 };
@@ -80,35 +85,24 @@ static_assert(kScratchBytes == RSRGPU_STATIC_SCRATCH_BYTES, "scratch size in rsr
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
-unsigned char* g_base[kMaxDevices] = {};   // device address of g_scratch, per device
-
-// sRGB8 encode table (same construction as the context path in rsrgpu_host.cu)
-void srgb_table(std::vector<uint8_t>& lut) {
-    lut.resize(26624);
-    for (uint32_t k = 0; k < 26624; ++k) {
-        const uint32_t bits = ((k + ((127u - 13u) << 11)) << 12) | 0x800u;
-        float f;
-        std::memcpy(&f, &bits, 4);
-        const double x = f;
-        const double s = x <= 0.0031308 ? 12.92 * x : 1.055 * std::pow(x, 1.0 / 2.4) - 0.055;
-        const double v = std::floor(s * 255.0 + 0.5);
-        lut[k] = uint8_t(v < 0 ? 0 : (v > 255 ? 255 : v));
-    }
-}
+std::atomic<unsigned char*> g_base[kMaxDevices];   // device address of g_scratch, per device (set up once)
+std::mutex g_setup_mu;                             // serialises the set-up of first calls
 
 int set_up_device(int dev, unsigned char** base, std::string& err) {
     if (dev < 0 || dev >= kMaxDevices) { err = "device ordinal out of range"; return RSRGPU_EINVAL; }
-    if (g_base[dev] != nullptr) { *base = g_base[dev]; return 0; }
+    if ((*base = g_base[dev].load(std::memory_order_acquire)) != nullptr) return 0;
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if ((*base = g_base[dev].load(std::memory_order_acquire)) != nullptr) return 0;
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
     if (e != cudaSuccess) { err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e); return RSRGPU_ECUDA; }
     unsigned char* b = static_cast<unsigned char*>(p);
     std::vector<uint8_t> lut;
-    srgb_table(lut);
+    build_srgb_lut(lut);
     e = cudaMemcpy(b + kOffRcp, kStaticRcpTable, sizeof(kStaticRcpTable), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(b + kOffSrgb, lut.data(), lut.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { err = std::string("table upload: ") + cudaGetErrorString(e); return RSRGPU_ECUDA; }
-    g_base[dev] = b;
+    g_base[dev].store(b, std::memory_order_release);
     *base = b;
     return 0;
 }
@@ -145,10 +139,10 @@ int render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* 
     std::vector<DevState> st;
     std::vector<DevDraw> dr;
     std::vector<FrameOp> ops;
-    int ntris = 0, ntiles = 0;
+    int ntris = 0, ntiles = 0, vis_keys = 0;
     std::string err;
     int rc = decode_frame_without_context(width, height, tile_blocks_x, tile_blocks_y, commands, nbytes, states,
-                                          nstates, st, dr, ops, ntris, ntiles, err);
+                                          nstates, st, dr, ops, ntris, ntiles, vis_keys, err);
     if (rc != 0) return fail_static(rc, err);
     char msg[256];
     if (st.size() > RSRGPU_STATIC_MAX_STATES || dr.size() > RSRGPU_STATIC_MAX_DRAWS || ops.size() > RSRGPU_STATIC_MAX_OPS ||
@@ -200,6 +194,7 @@ int render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* 
     fv.rcp_table = reinterpret_cast<const uint32_t*>(base + kOffRcp);
     fv.srgb_lut = reinterpret_cast<const uint8_t*>(base + kOffSrgb);
     fv.region_px = kRegionPx;
+    fv.vis_keys = vis_keys;   // visibility by (depth, order) keys where the frame allows it, as rsrgpu_run
     for (const FrameOp& o : ops)
         if (o.kind >= kOpStoreFP) fv.ext = 1;
 

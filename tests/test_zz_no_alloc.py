@@ -28,8 +28,8 @@ def _render_with_context(gpu, sc, dev, col, dep, gamma):
     gpu.Wait()
 
 
-def _render_static(lib, sc, dev, col, dep, gamma, stream):
-    gl = sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=gamma)
+def _render_static(lib, sc, dev, col, dep, gamma, stream, gl=None):
+    gl = gl or sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=gamma)
     cmds = gl.stream()
     buf = ctypes.create_string_buffer(cmds, len(cmds))
     states = gl.c_states()
@@ -72,6 +72,57 @@ def test_static_entry_point_matches_context_path(built):
                 assert np.abs(_channels(gc) - _channels(wc)).max() <= 1
             else:
                 assert np.array_equal(gc, wc)
+    finally:
+        gpu.close()
+
+
+def test_static_entry_point_float_stores_and_no_device_allocation(built):
+    """A frame with rsr's float colour stores (the extended raster
+    instantiation) matches the context path bit for bit, and repeated calls
+    leave the device's free memory unchanged: the entry point allocates
+    nothing (the set-up and the kernels' modules are loaded by a first,
+    untimed call)."""
+    torch = pytest.importorskip("torch")
+    lib = abi.load_library()
+    gpu = GPU(0)
+    gpu.InstallDefaults()
+    stream = torch.cuda.current_stream().cuda_stream
+    sc = scenes.float_store_frame(seed=23, mid=True)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+
+    def outputs(fill):
+        return {k: torch.full((v.size,), fill, dtype=torch.float32 if v.dtype == np.float32 else torch.int32,
+                              device="cuda") for k, v in sc.outputs.items()}
+
+    try:
+        want = outputs(0)
+        gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+        gpu.Run(sc.record(ref=dev.__getitem__, outputs=want, gamma=False))
+        gpu.Wait()
+        got = outputs(7)
+        gl = sc.record(ref=dev.__getitem__, outputs=got, gamma=False)
+        _render_static(lib, sc, dev, None, None, False, stream, gl=gl)
+        torch.cuda.synchronize()
+        for k in want:
+            assert np.array_equal(got[k].cpu().numpy().view(np.uint32), want[k].cpu().numpy().view(np.uint32)), k
+        # the opaque plain frame takes the keys path; repeated calls allocate nothing
+        pl = scenes.plain_raster(seed=24, ntris=8000)
+        pdev = {k: torch.from_numpy(v).cuda() for k, v in pl.arrays.items()}
+        pc = torch.zeros(pl.width * pl.height, dtype=torch.int32, device="cuda")
+        pd = torch.zeros(pl.width * pl.height, dtype=torch.float32, device="cuda")
+        _render_static(lib, pl, pdev, pc, pd, False, stream)
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        for _ in range(5):
+            _render_static(lib, pl, pdev, pc, pd, False, stream)
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 >= free0
+        wc = torch.zeros_like(pc)
+        wd = torch.zeros_like(pd)
+        _render_with_context(gpu, pl, pdev, wc, wd, False)
+        torch.cuda.synchronize()
+        assert torch.equal(pc, wc) and torch.equal(pd.view(torch.int32), wd.view(torch.int32))
     finally:
         gpu.close()
 
