@@ -434,6 +434,10 @@ int rsrgpu_create(int device, rsrgpu_ctx** out) {
     }
     std::vector<uint8_t> lut;
     build_srgb_lut(lut);
+    if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        rsrgpu_destroy(ctx);
+        return RSRGPU_ECUDA;
+    }
     if (ctx->d_rcp.ensure(sizeof(kRcpTable)) != cudaSuccess || ctx->d_srgb.ensure(lut.size()) != cudaSuccess ||
         cudaMemcpy(ctx->d_rcp.p, kRcpTable, sizeof(kRcpTable), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(ctx->d_srgb.p, lut.data(), lut.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -990,6 +994,13 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.rcp_table = ctx->d_rcp.as<uint32_t>();
     fv.srgb_lut = ctx->d_srgb.as<uint8_t>();
     fv.region_px = std::min(ctx->region_px, std::min(ctx->tile_w, ctx->tile_h));
+    if (tables == nullptr && fv.region_px > 16 && ctx->num_sms > 0) {
+        // few, large tiles (config 1: 60 tiles of 64 px): raster CTAs of
+        // 16x16-pixel regions, so every SM gets several (the region changes
+        // which CTA draws a pixel, not what it draws)
+        const int subs = ((ctx->tile_w + fv.region_px - 1) / fv.region_px) * ((ctx->tile_h + fv.region_px - 1) / fv.region_px);
+        if (int64_t(ctx->ntiles) * subs < 2 * int64_t(ctx->num_sms)) fv.region_px = 16;
+    }
     fv.vis_keys = ctx->vis_keys;
     fv.raster_phase = 0;
     fv.vis_own = nullptr;

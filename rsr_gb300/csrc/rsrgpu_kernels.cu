@@ -861,6 +861,8 @@ struct RasterSmem {
     float vary[3][kMaxVary][kRasterBatch];
     uint32_t code[kRasterBatch];   // fragment owner: triangle id, or clipped fan id | bit 31
     uint8_t big[kRasterBatch];     // visibility by keys: the triangle covers many quads of the region
+    uint32_t zr[kRasterBatch];     // visibility by keys: a depth rank no covered pixel of the triangle goes below
+                                   // (0 where no such bound is known)
     int qsum;                      // visibility by keys: the batch's boxes, in quads of the region
 };
 
@@ -1239,6 +1241,58 @@ __device__ __forceinline__ unsigned long long clear_key(float z, bool leq) {
     return (static_cast<unsigned long long>(depth_rank(z)) << 32) | (leq ? 0xffffffffu : 0u);
 }
 
+// A lower bound of the depth rank of every fragment the triangle covers in
+// the tile, or 0 (no bound) where none is known.  Inside the triangle the
+// barycentric weights bx = l2 * scale, bz = l1 * scale, by = (1 - bx) - bz are
+// within a few float roundings of [0, 1] and sum to 1 within a few ulps, as
+// long as the edge values keep their exact integer values there (no 32-bit
+// wrap in the tile: |c| + |dy| (tile width + 2) + |dx| (tile height + 2) below
+// 2^31 for every edge), so every fragment depth
+// (bx z0 + by z1) + bz z2 is at least min(z) - 2^-18 max|z|.
+__device__ __forceinline__ uint32_t tri_min_rank(const TriSetup& t, float z0, float z1, float z2, int tw, int th) {
+    if (!(t.scale > 0.0f && t.scale <= 3.4e38f)) return 0u;
+    const float zabs = fmaxf(fmaxf(fabsf(z0), fabsf(z1)), fabsf(z2));
+    if (!(zabs <= 3.4e38f)) return 0u;   // an infinite or NaN vertex depth
+    const long long W = tw + 2, H = th + 2;
+    const long long lim = 1ll << 31;
+    if (llabs(t.c1) + llabs(t.dy12) * W + llabs(t.dx12) * H >= lim ||
+        llabs(t.c2) + llabs(t.dy23) * W + llabs(t.dx23) * H >= lim ||
+        llabs(t.c3) + llabs(t.dy31) * W + llabs(t.dx31) * H >= lim)
+        return 0u;
+    const float lo = fminf(fminf(z0, z1), z2) - (zabs * 0x1p-18f + 0x1p-126f);
+    return depth_rank(lo);
+}
+
+// Whether edge (c, dy, dx) is negative at every pixel of [x0, x1) x [y0, y1):
+// its exact value at the rectangle's corners (int64) is below zero and not
+// below -2^31, so the 32-bit lane values, which wrap, equal the exact ones
+// there and all lanes of the rectangle are outside the triangle.
+__device__ __forceinline__ bool edge_outside(int32_t c, int32_t dy, int32_t dx, int32_t kx0, int32_t ky0, int32_t kx1,
+                                             int32_t ky1) {
+    const long long hi = (long long)c + (long long)dy * (dy > 0 ? kx1 : kx0) + (long long)dx * (dx > 0 ? ky1 : ky0);
+    const long long lo = (long long)c + (long long)dy * (dy > 0 ? kx0 : kx1) + (long long)dx * (dx > 0 ? ky0 : ky1);
+    return hi < 0 && lo >= -(1ll << 31);
+}
+// Batch triangle i covers no pixel of [x0, x1) x [y0, y1) (pixel coordinates).
+__device__ __forceinline__ bool footprint_outside(const RasterSmem& S, int i, int x0, int y0, int x1, int y1) {
+    const int32_t kx0 = x0 - S.minx[i], kx1 = x1 - 1 - S.minx[i];
+    const int32_t ky0 = y0 - S.miny[i], ky1 = y1 - 1 - S.miny[i];
+    return edge_outside(S.c1[i], S.dy12[i], S.dx12[i], kx0, ky0, kx1, ky1) ||
+           edge_outside(S.c2[i], S.dy23[i], S.dx23[i], kx0, ky0, kx1, ky1) ||
+           edge_outside(S.c3[i], S.dy31[i], S.dx31[i], kx0, ky0, kx1, ky1);
+}
+
+// The largest depth rank among the keys of the warp's quads: a fragment of
+// greater rank changes none of them (keys only decrease).
+__device__ __forceinline__ uint32_t warp_max_rank(const unsigned long long kq[4], bool active) {
+    uint32_t r = 0u;
+    if (active) {
+#pragma unroll
+        for (int l = 0; l < 4; ++l) r = max(r, uint32_t(kq[l] >> 32));
+    }
+    return __reduce_max_sync(FULL_MASK, r);
+}
+
 // Quads of the region [rx0, rx1) x [ry0, ry1) in batch triangle i's box.
 __device__ __forceinline__ int region_quads(const RasterSmem& S, int i, int rx0, int ry0, int rx1, int ry1) {
     const int x0 = max(S.minx[i], rx0), x1 = min(S.maxx[i], rx1);
@@ -1518,7 +1572,10 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             S.code[tid] = e | kClippedBit;
                         }
                         put_setup(S, tid, t);
-                        if (key_state == 1) atomicAdd(&S.qsum, region_quads(S, tid, rx0, ry0, rx1, ry1));
+                        if (key_state == 1) {
+                            atomicAdd(&S.qsum, region_quads(S, tid, rx0, ry0, rx1, ry1));
+                            S.zr[tid] = tri_min_rank(t, S.z[0][tid], S.z[1][tid], S.z[2][tid], fv.tile_w, fv.tile_h);
+                        }
                     }
                     __syncthreads();
                     if (key_state == 1) {
@@ -1554,19 +1611,26 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 #pragma unroll
                             for (int l = 0; l < 4; ++l) kq[l] = keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))];
                         }
+                        // the warp skips triangles that cannot change any of its keys:
+                        // no fragment of theirs goes below the warp's largest depth
+                        // rank, or an edge excludes every pixel of its quads
+                        uint32_t wmax = warp_max_rank(kq, active);
                         for (int b0 = 0; b0 < n; b0 += 32) {
                             bool hit = false;
                             if (b0 + lane < n && S.big[b0 + lane]) {
                                 const int j = b0 + lane;
-                                hit = !(S.maxx[j] <= wx0 || S.minx[j] > wx1 || S.maxy[j] <= wy0 || S.miny[j] > wy1);
+                                hit = !(S.maxx[j] <= wx0 || S.minx[j] > wx1 || S.maxy[j] <= wy0 || S.miny[j] > wy1) &&
+                                      S.zr[j] <= wmax && !footprint_outside(S, j, wx0, wy0, wx1 + 2, wy1 + 2);
                             }
                             uint32_t m = __ballot_sync(FULL_MASK, hit);
+                            const bool drawn = m != 0u;
                             while (m) {
                                 const int i = b0 + __ffs(m) - 1;
                                 m &= m - 1;
                                 if (!active || qx < S.minx[i] || qx >= S.maxx[i] || qy < S.miny[i] || qy >= S.maxy[i]) continue;
                                 key_quad_own(S, kq, i, qx, qy, order0 + uint32_t(i), leq);
                             }
+                            if (drawn) wmax = warp_max_rank(kq, active);
                         }
                         if (active) {
 #pragma unroll
