@@ -1006,6 +1006,8 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.vis_own = nullptr;
     fv.vis_dep = nullptr;
     fv.ext = frame_is_ext(ctx) ? 1 : 0;
+    fv.any_scissor = 0;
+    for (const DevState& st : ctx->states) fv.any_scissor |= st.scissor_test;
     fv.dext = (ctx->any_dext && tables == nullptr) ? reinterpret_cast<DevDrawExt*>(tab + ctx->tab_ofs[4]) : nullptr;
     return 0;
 }

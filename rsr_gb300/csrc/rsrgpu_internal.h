@@ -180,7 +180,7 @@ struct FrameView {
     uint32_t* vis_own;        // [height * width] per pixel, phases 1 and 2
     float* vis_dep;
     int32_t ext;              // float colour stores or ManyProgram draws: raster_ext_kernel runs the frame
-    int32_t pad_ext;
+    int32_t any_scissor;      // a draw of the frame has the scissor test on
     const DevDrawExt* dext;   // per draw, for frames with instanced or OBJ1Program draws (setup_ext_kernel); else null
 };
 

@@ -1106,9 +1106,11 @@ constexpr uint32_t kClippedBit = 0x80000000u;
 __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
                                          float w[3], float vary[3][kMaxVary], int& state) {
     const int g = (code & kClippedBit) ? fv.clip_src[fv.clip_poly[code & ~kClippedBit]] : int(code);
-    state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
-    int rect[4];
-    draw_rect(fv.states[state], tile, rect);
+    int rect[4] = { tile[0], tile[1], tile[2], tile[3] };
+    if (fv.any_scissor) {   // the draw's rectangle depends on its state
+        state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+        draw_rect(fv.states[state], tile, rect);
+    }
     if (code & kClippedBit) {
         const uint32_t e = code & ~kClippedBit;
         const int pbase = fv.clip_poly[e];
@@ -1129,6 +1131,7 @@ __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, con
             for (int q = 0; q < kMaxVary; ++q) vary[k][q] = r.vary[k][q];
         }
     }
+    if (!fv.any_scissor) state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
 }
 
 // perspective-correct barycentrics of one lane (TriangleProgram::Render,
@@ -1249,15 +1252,17 @@ __device__ __forceinline__ unsigned long long clear_key(float z, bool leq) {
 // wrap in the tile: |c| + |dy| (tile width + 2) + |dx| (tile height + 2) below
 // 2^31 for every edge), so every fragment depth
 // (bx z0 + by z1) + bz z2 is at least min(z) - 2^-18 max|z|.
-__device__ __forceinline__ uint32_t tri_min_rank(const TriSetup& t, float z0, float z1, float z2, int tw, int th) {
-    if (!(t.scale > 0.0f && t.scale <= 3.4e38f)) return 0u;
+__device__ __forceinline__ uint32_t tri_min_rank(const RasterSmem& S, int i, int tw, int th) {
+    const float scale = S.scale[i];
+    if (!(scale > 0.0f && scale <= 3.4e38f)) return 0u;
+    const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];
     const float zabs = fmaxf(fmaxf(fabsf(z0), fabsf(z1)), fabsf(z2));
     if (!(zabs <= 3.4e38f)) return 0u;   // an infinite or NaN vertex depth
     const long long W = tw + 2, H = th + 2;
     const long long lim = 1ll << 31;
-    if (llabs(t.c1) + llabs(t.dy12) * W + llabs(t.dx12) * H >= lim ||
-        llabs(t.c2) + llabs(t.dy23) * W + llabs(t.dx23) * H >= lim ||
-        llabs(t.c3) + llabs(t.dy31) * W + llabs(t.dx31) * H >= lim)
+    if (llabs(S.c1[i]) + llabs(S.dy12[i]) * W + llabs(S.dx12[i]) * H >= lim ||
+        llabs(S.c2[i]) + llabs(S.dy23[i]) * W + llabs(S.dx23[i]) * H >= lim ||
+        llabs(S.c3[i]) + llabs(S.dy31[i]) * W + llabs(S.dx31[i]) * H >= lim)
         return 0u;
     const float lo = fminf(fminf(z0, z1), z2) - (zabs * 0x1p-18f + 0x1p-126f);
     return depth_rank(lo);
@@ -1507,8 +1512,8 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         } else if (o.kind == kOpDraw) {
             const DevDraw dr = fv.draws[o.arg];
             const int end_tri = dr.first_tri + dr.ntris;
-            int drect[4];   // the tile, or its part inside the scissor rectangle
-            draw_rect(fv.states[dr.state], rect, drect);
+            int drect[4] = { rect[0], rect[1], rect[2], rect[3] };   // the tile, or its part inside the scissor rectangle
+            if (fv.any_scissor) draw_rect(fv.states[dr.state], rect, drect);
             if (visibility) pending = true;
             if (fv.raster_phase == 2) continue;   // drawn by the first launch
             if (key_state == 0) {
@@ -1572,10 +1577,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             S.code[tid] = e | kClippedBit;
                         }
                         put_setup(S, tid, t);
-                        if (key_state == 1) {
-                            atomicAdd(&S.qsum, region_quads(S, tid, rx0, ry0, rx1, ry1));
-                            S.zr[tid] = tri_min_rank(t, S.z[0][tid], S.z[1][tid], S.z[2][tid], fv.tile_w, fv.tile_h);
-                        }
+                        if (key_state == 1) atomicAdd(&S.qsum, region_quads(S, tid, rx0, ry0, rx1, ry1));
                     }
                     __syncthreads();
                     if (key_state == 1) {
@@ -1591,6 +1593,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             const int y0 = max(S.miny[tid], ry0), y1 = min(S.maxy[tid], ry1);
                             const int nq = x0 < x1 && y0 < y1 ? ((x1 - x0 + 1) >> 1) * ((y1 - y0 + 1) >> 1) : 0;
                             big = nq > small_max;
+                            if (big) S.zr[tid] = tri_min_rank(S, tid, fv.tile_w, fv.tile_h);
                             if (!big) {
                                 for (int qyy = y0; qyy < y1; qyy += 2)
                                     for (int qxx = x0; qxx < x1; qxx += 2)

@@ -195,6 +195,7 @@ int render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* 
     fv.srgb_lut = reinterpret_cast<const uint8_t*>(base + kOffSrgb);
     fv.region_px = kRegionPx;
     fv.vis_keys = vis_keys;   // visibility by (depth, order) keys where the frame allows it, as rsrgpu_run
+    for (const DevState& d : st) fv.any_scissor |= d.scissor_test;
     for (const FrameOp& o : ops)
         if (o.kind >= kOpStoreFP) fv.ext = 1;
 
