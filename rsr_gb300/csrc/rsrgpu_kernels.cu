@@ -1103,11 +1103,12 @@ constexpr uint32_t kClippedBit = 0x80000000u;
 // Per-(triangle, tile) setup and vertex data of one list entry, for the
 // resolve pass: the triangle that last wrote a pixel is set up again exactly
 // as when it was rasterised.
+template <bool kScissor>
 __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
                                          float w[3], float vary[3][kMaxVary], int& state) {
     const int g = (code & kClippedBit) ? fv.clip_src[fv.clip_poly[code & ~kClippedBit]] : int(code);
     int rect[4] = { tile[0], tile[1], tile[2], tile[3] };
-    if (fv.any_scissor) {   // the draw's rectangle depends on its state
+    if (kScissor && fv.any_scissor) {   // the draw's rectangle depends on its state
         state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
         draw_rect(fv.states[state], tile, rect);
     }
@@ -1131,7 +1132,7 @@ __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, con
             for (int q = 0; q < kMaxVary; ++q) vary[k][q] = r.vary[k][q];
         }
     }
-    if (!fv.any_scissor) state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+    if (!(kScissor && fv.any_scissor)) state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
 }
 
 // perspective-correct barycentrics of one lane (TriangleProgram::Render,
@@ -1165,7 +1166,7 @@ __device__ __forceinline__ void quad_put_rgb(float col[4][3], int l, float r, fl
     else { col[3][0] = r; col[3][1] = g; col[3][2] = b; }
 }
 
-template <bool kExt>
+template <bool kExt, bool kScissor>
 __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect[4], int qx, int qy,
                                              uint32_t own[4], float col[4][3]) {
     uint32_t cur = kNoOwner;
@@ -1178,7 +1179,7 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
         if (ol == kNoOwner) continue;
         if (ol != cur) {
             cur = ol;
-            owner_setup(fv, cur, rect, t, w, vary, state);
+            owner_setup<kScissor>(fv, cur, rect, t, w, vary, state);
         }
         const DevState& s = fv.states[state];
         float bpx, bpy, bpz;
@@ -1394,8 +1395,9 @@ __device__ __noinline__ float owner_depth(const FrameView& fv, uint32_t code, co
 
 // kExt: the frame has float colour stores (rsr's CMD_STORE_COLOR_*_FP) or
 // ManyProgram draws; frames without them run the instantiation that has no
-// code for them.
-template <bool kExt>
+// code for them.  kScissor: the instantiation for frames with scissored
+// draws (the others keep the draw rectangle, the tile, out of registers).
+template <bool kExt, bool kScissor>
 __device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
     if (fv.counters->overflow != 0u) return;
 
@@ -1495,7 +1497,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         // replaces colour first resolves the pending pixels.
         const bool visibility = o.kind == kOpDraw && !fs.blend;
         if (!visibility && o.kind != kOpStoreGBuffer && pending && fv.raster_phase != 1) {
-            if (active) resolve_quad<kExt>(fv, rect, qx, qy, own, col);
+            if (active) resolve_quad<kExt, kScissor>(fv, rect, qx, qy, own, col);
             pending = false;
         }
         if (o.kind == kOpClear) {
@@ -1513,7 +1515,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             const DevDraw dr = fv.draws[o.arg];
             const int end_tri = dr.first_tri + dr.ntris;
             int drect[4] = { rect[0], rect[1], rect[2], rect[3] };   // the tile, or its part inside the scissor rectangle
-            if (fv.any_scissor) draw_rect(fv.states[dr.state], rect, drect);
+            if (kScissor && fv.any_scissor) draw_rect(fv.states[dr.state], rect, drect);
             if (visibility) pending = true;
             if (fv.raster_phase == 2) continue;   // drawn by the first launch
             if (key_state == 0) {
@@ -1672,7 +1674,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 #pragma unroll
                             for (int l = 0; l < 4; ++l) {
                                 inside[l] = (l1[l] | l2[l] | l3[l]) >= 0;
-                                if (fs.scissor) {
+                                if (kScissor && fs.scissor) {
                                     const int px = qx + (l & 1), py = qy + (l >> 1);
                                     inside[l] = inside[l] && px >= drect[0] && px < drect[2] && py >= drect[1] && py < drect[3];
                                 }
@@ -1781,7 +1783,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                     TriSetup t;
                     float w[3], vary[3][kMaxVary];
                     int state;
-                    owner_setup(fv, ol, rect, t, w, vary, state);
+                    owner_setup<kScissor>(fv, ol, rect, t, w, vary, state);
                     if (fv.states[state].program != kProgGBuffer) continue;
                     float bpx, bpy, bpz;
                     lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
@@ -1874,11 +1876,15 @@ __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ 
 }
 __global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
-    raster_body<false>(fv, blockIdx.x, S);
+    raster_body<false, false>(fv, blockIdx.x, S);
+}
+__global__ void __launch_bounds__(256, 2) raster_scissor_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem S;
+    raster_body<false, true>(fv, blockIdx.x, S);
 }
 __global__ void __launch_bounds__(256, 2) raster_ext_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
-    raster_body<true>(fv, blockIdx.x, S);
+    raster_body<true, true>(fv, blockIdx.x, S);
 }
 
 // frame of a block: the last f with start[f] <= block (start[] ascending)
@@ -1902,7 +1908,12 @@ __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_const
 __global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ RasterSmem S;
     const int f = batch_frame(b, blockIdx.x);
-    raster_body<false>(b.fv[f], blockIdx.x - b.start[f], S);
+    raster_body<false, false>(b.fv[f], blockIdx.x - b.start[f], S);
+}
+__global__ void __launch_bounds__(256, 2) raster_batch_scissor_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ RasterSmem S;
+    const int f = batch_frame(b, blockIdx.x);
+    raster_body<false, true>(b.fv[f], blockIdx.x - b.start[f], S);
 }
 
 // ---------------------------------------------------------------------------
@@ -1960,6 +1971,7 @@ cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
 
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
     if (fv.ext) raster_ext_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
+    else if (fv.any_scissor) raster_scissor_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
     else raster_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
     return cudaGetLastError();
 }
@@ -1976,7 +1988,10 @@ cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st) 
 }
 cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st) {
     if (blocks == 0) return cudaSuccess;
-    raster_batch_kernel<<<blocks, threads, 0, st>>>(b);
+    bool scissor = false;
+    for (int f = 0; f < b.nframes; ++f) scissor = scissor || b.fv[f].any_scissor;
+    if (scissor) raster_batch_scissor_kernel<<<blocks, threads, 0, st>>>(b);
+    else raster_batch_kernel<<<blocks, threads, 0, st>>>(b);
     return cudaGetLastError();
 }
 
