@@ -860,6 +860,7 @@ struct RasterSmem {
     float z[3][kRasterBatch], w[3][kRasterBatch];
     float vary[3][kMaxVary][kRasterBatch];
     uint32_t code[kRasterBatch];   // fragment owner: triangle id, or clipped fan id | bit 31
+    uint32_t order[kRasterBatch];  // visibility by keys: the entry's drawing order (see frag_key)
     uint8_t big[kRasterBatch];     // visibility by keys: the triangle covers many quads of the region
     uint32_t zr[kRasterBatch];     // visibility by keys: a depth rank no covered pixel of the triangle goes below
                                    // (0 where no such bound is known)
@@ -1513,7 +1514,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             }
         } else if (o.kind == kOpDraw) {
             const DevDraw dr = fv.draws[o.arg];
-            const int end_tri = dr.first_tri + dr.ntris;
+            int end_tri = dr.first_tri + dr.ntris;
             int drect[4] = { rect[0], rect[1], rect[2], rect[3] };   // the tile, or its part inside the scissor rectangle
             if (kScissor && fv.any_scissor) draw_rect(fv.states[dr.state], rect, drect);
             if (visibility) pending = true;
@@ -1529,7 +1530,15 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 #pragma unroll
                     for (int l = 0; l < 4; ++l) keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))] = clear_key(dep[l], leq);
                 }
+            } else if (key_state == 1) {
+                continue;   // the first draw took the whole list
             }
+            // With keys, a fragment's drawing order is part of its key, so the
+            // first draw sweeps the tile's whole list -- every draw's
+            // triangles, then every draw's fans -- in full batches; each entry
+            // carries the order of its own draw.
+            const bool sweep = key_state == 1;
+            if (sweep) end_tri = INT_MAX;
             // inline triangles of this draw, then its clipped fans (rglv_gpu_impl.hxx:506-508)
             for (int pass = 0; pass < 2; ++pass) {
                 const uint32_t base = pass == 0 ? bin.inl_off : bin.clip_off;
@@ -1544,6 +1553,10 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                         e = fv.bin_pool[base + cur + tid];
                         const int src = pass == 0 ? int(e) : fv.clip_src[fv.clip_poly[e]];
                         valid = src < end_tri;
+                        if (sweep) {
+                            const uint32_t d = uint32_t(find_draw(fv.draws, fv.ndraws, src));
+                            S.order[tid] = (d << (kKeyPosBits + 1)) | (uint32_t(pass) << kKeyPosBits) | (cur + uint32_t(tid));
+                        }
                     }
                     const int n = __syncthreads_count(valid);
                     if (n == 0) break;
@@ -1583,7 +1596,6 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                     }
                     __syncthreads();
                     if (key_state == 1) {
-                        const uint32_t order0 = (uint32_t(o.arg) << (kKeyPosBits + 1)) | (uint32_t(pass) << kKeyPosBits) | cur;
                         // small triangles: one per lane, over its quads in the region.
                         // Where the batch covers the region many times over, lanes
                         // would contend for the same keys: then only the smallest go
@@ -1599,7 +1611,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                             if (!big) {
                                 for (int qyy = y0; qyy < y1; qyy += 2)
                                     for (int qxx = x0; qxx < x1; qxx += 2)
-                                        key_quad(S, keys, rx0, ry0, rw, tid, qxx, qyy, order0 + uint32_t(tid), leq);
+                                        key_quad(S, keys, rx0, ry0, rw, tid, qxx, qyy, S.order[tid], leq);
                             }
                         }
                         // larger ones: every lane its own quad, a triangle at a time,
@@ -1633,7 +1645,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                                 const int i = b0 + __ffs(m) - 1;
                                 m &= m - 1;
                                 if (!active || qx < S.minx[i] || qx >= S.maxx[i] || qy < S.miny[i] || qy >= S.maxy[i]) continue;
-                                key_quad_own(S, kq, i, qx, qy, order0 + uint32_t(i), leq);
+                                key_quad_own(S, kq, i, qx, qy, S.order[i], leq);
                             }
                             if (drawn) wmax = warp_max_rank(kq, active);
                         }
