@@ -695,7 +695,7 @@ int rsrgpu_batch_last_error(rsrgpu_batch* batch, char* buf, size_t len);
 #define RSRGPU_STATIC_MAX_STATES       64
 #define RSRGPU_STATIC_MAX_DRAWS        256
 #define RSRGPU_STATIC_MAX_OPS          1024
-#define RSRGPU_STATIC_SCRATCH_BYTES    7341824
+#define RSRGPU_STATIC_SCRATCH_BYTES    7374592
 int rsrgpu_render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates,
                          int width, int height, int tile_blocks_x, int tile_blocks_y, void* stream,
                          char* errbuf, size_t errlen);

@@ -841,6 +841,28 @@ int decode_frame(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const 
         }
         ctx->vis_keys = ok ? 1 + func : 0;
     }
+    // what the raster pass reads of each op, inline (no state or draw load)
+    int st = -1;
+    for (FrameOp& o : ctx->ops) {
+        if (o.kind == kOpState) {
+            st = o.arg;
+            const DevState& d = ctx->states[size_t(st)];
+            o.info[0] = d.program;
+            o.info[1] = (d.depth_test ? kFragDepthTest : 0) | (d.depth_func << kFragDepthFuncShift) |
+                        (d.depth_write ? kFragDepthWrite : 0) | (d.color_write ? kFragColorWrite : 0) |
+                        (d.blend ? kFragBlend : 0) | (d.scissor_test ? kFragScissor : 0);
+        } else if (o.kind == kOpClear && st >= 0) {
+            const DevState& d = ctx->states[size_t(st)];
+            for (int k = 0; k < 3; ++k) o.val[k] = d.clear_color[k];
+            o.val[3] = d.clear_depth;
+            o.info[2] = d.color_type == RSRGPU_RB_COLOR_DEPTH ? 1 : 0;
+        } else if (o.kind == kOpDraw) {
+            const DevDraw& dd = ctx->draws[size_t(o.arg)];
+            o.info[0] = dd.first_tri;
+            o.info[1] = dd.ntris;
+            o.info[2] = dd.state;
+        }
+    }
     return 0;
 }
 
@@ -1002,6 +1024,17 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
         if (int64_t(ctx->ntiles) * subs < 2 * int64_t(ctx->num_sms)) fv.region_px = 16;
     }
     fv.vis_keys = ctx->vis_keys;
+    fv.keys_resume_op = 0;
+    fv.keys_resume_state_op = 0;
+    if (fv.vis_keys) {   // the raster pass jumps from the first draw to the op after the last
+        int last_draw = -1, st_at = 0;
+        for (int i = 0; i < int(ctx->ops.size()); ++i)
+            if (ctx->ops[size_t(i)].kind == kOpDraw) last_draw = i;
+        for (int i = 0; i <= last_draw; ++i)
+            if (ctx->ops[size_t(i)].kind == kOpState) st_at = i;
+        fv.keys_resume_op = last_draw + 1;
+        fv.keys_resume_state_op = st_at;
+    }
     fv.raster_phase = 0;
     fv.vis_own = nullptr;
     fv.vis_dep = nullptr;

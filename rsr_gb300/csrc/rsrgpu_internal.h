@@ -29,6 +29,7 @@ constexpr int kRegionPx = 32;     // default raster region: a CTA covers at most
 constexpr int kBinBlock = 256;    // bin CTA: one tile, eight warps
 constexpr int kMaxBatch = 64;     // frames per batched launch
 constexpr int kRasterBatch = 256; // triangles set up per shared-memory batch
+constexpr int kOpCache = 64;      // frame ops a raster CTA keeps in shared memory
 
 enum ProgramId : int32_t {
     kProgDefaultPost = 1,
@@ -111,7 +112,16 @@ struct FrameOp {
     int32_t pad;
     void* ptr;        // output base (device address)
     int32_t width, height, stride, pad2;
+    // What the raster pass needs of the op without another load (filled by
+    // the host decode): kOpState info[0] program, info[1] kFrag* flags;
+    // kOpClear val = clear colour rgb and depth, info[2] 1 for RB_COLOR_DEPTH;
+    // kOpDraw info[0] first triangle, info[1] triangles, info[2] state.
+    int32_t info[4];
+    float val[4];
 };
+// kOpState info[1]: the fragment stage's switches
+constexpr int32_t kFragDepthTest = 1, kFragDepthFuncShift = 1, kFragDepthWrite = 8, kFragColorWrite = 16,
+                  kFragBlend = 32, kFragScissor = 64;
 
 struct TriRecord {        // 96 bytes, 16-byte aligned
     int32_t fx[3], fy[3];
@@ -181,6 +191,8 @@ struct FrameView {
     float* vis_dep;
     int32_t ext;              // float colour stores or ManyProgram draws: raster_ext_kernel runs the frame
     int32_t any_scissor;      // a draw of the frame has the scissor test on
+    int32_t keys_resume_op;   // vis_keys frames: the first op after the last draw (0: not given)
+    int32_t keys_resume_state_op; // the last state op before it
     const DevDrawExt* dext;   // per draw, for frames with instanced or OBJ1Program draws (setup_ext_kernel); else null
 };
 

@@ -861,6 +861,8 @@ struct RasterSmem {
     float vary[3][kMaxVary][kRasterBatch];
     uint32_t code[kRasterBatch];   // fragment owner: triangle id, or clipped fan id | bit 31
     uint32_t order[kRasterBatch];  // visibility by keys: the entry's drawing order (see frag_key)
+    FrameOp ops[kOpCache];         // the frame's ops, when they fit
+    int32_t dfirst[kOpCache];      // the draws' first triangles, when they fit
     uint8_t big[kRasterBatch];     // visibility by keys: the triangle covers many quads of the region
     uint32_t zr[kRasterBatch];     // visibility by keys: a depth rank no covered pixel of the triangle goes below
                                    // (0 where no such bound is known)
@@ -1062,11 +1064,15 @@ struct FragState {
     DevTexture tu0;
 };
 
-__device__ __forceinline__ void load_frag_state(const DevState& s, FragState& f) {
-    f.program = s.program; f.nvary = s.nvary;
-    f.depth_test = s.depth_test; f.depth_func = s.depth_func; f.depth_write = s.depth_write;
-    f.color_write = s.color_write; f.blend = s.blend; f.scissor = s.scissor_test;
-    f.tu0 = s.tu0;
+// from a kOpState op (its switches are inline); the texture unit only for
+// blended draws, which shade as they draw
+__device__ __forceinline__ void load_frag_state(const FrameView& fv, const FrameOp& o, FragState& f) {
+    const int32_t fl = o.info[1];
+    f.program = o.info[0];
+    f.depth_test = (fl & kFragDepthTest) != 0; f.depth_func = (fl >> kFragDepthFuncShift) & 3;
+    f.depth_write = (fl & kFragDepthWrite) != 0; f.color_write = (fl & kFragColorWrite) != 0;
+    f.blend = (fl & kFragBlend) != 0; f.scissor = (fl & kFragScissor) != 0;
+    if (f.blend) f.tu0 = fv.states[o.arg].tu0;
 }
 
 // The rectangle a draw rasterises in: the tile, cut to the scissor rectangle
@@ -1435,8 +1441,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
     bool pending = false;
     uint32_t inl_cur = 0, clip_cur = 0;
     int cur_state = 0;
-    FragState fs;
-    load_frag_state(fv.states[0], fs);
+    FragState fs{};   // every frame starts with a state op
     // visibility by keys (see frag_key): decided at the first draw, resolved
     // into own / dep before the first store
     __shared__ unsigned long long keys[32 * 32];
@@ -1445,11 +1450,19 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
     int key_state = 0;   // 0 not decided, 1 keys in use, 2 not used, 3 resolved
     bool phase_pending = true;   // second launch of a split pass: the hand-over is still to take
 
+    // the op list is read by every thread at every step: one load into shared memory
+    const bool ops_cached = fv.nops <= kOpCache;
+    if (ops_cached)
+        for (int i = tid; i < fv.nops; i += blockDim.x) S.ops[i] = fv.ops[i];
+    const bool draws_cached = fv.ndraws <= kOpCache;
+    if (draws_cached)
+        for (int i = tid; i < fv.ndraws; i += blockDim.x) S.dfirst[i] = fv.draws[i].first_tri;
+    __syncthreads();
     for (int op = 0; op < fv.nops; ++op) {
-        const FrameOp o = fv.ops[op];
+        const FrameOp o = ops_cached ? S.ops[op] : fv.ops[op];
         if (o.kind == kOpState) {
             cur_state = o.arg;
-            load_frag_state(fv.states[cur_state], fs);
+            load_frag_state(fv, o, fs);
             continue;
         }
         if (key_state == 1 && o.kind != kOpDraw && o.kind != kOpState) {
@@ -1502,21 +1515,19 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             pending = false;
         }
         if (o.kind == kOpClear) {
-            const DevState& s = fv.states[cur_state];
-            const bool packed = s.color_type == 0;   // RB_COLOR_DEPTH clears both
+            const bool packed = o.info[2] != 0;   // RB_COLOR_DEPTH clears both
             if (packed || (o.arg & 1)) {
 #pragma unroll
-                for (int l = 0; l < 4; ++l) { col[l][0] = s.clear_color[0]; col[l][1] = s.clear_color[1]; col[l][2] = s.clear_color[2]; }
+                for (int l = 0; l < 4; ++l) { col[l][0] = o.val[0]; col[l][1] = o.val[1]; col[l][2] = o.val[2]; }
             }
             if (packed || (o.arg & 2)) {
 #pragma unroll
-                for (int l = 0; l < 4; ++l) dep[l] = s.clear_depth;
+                for (int l = 0; l < 4; ++l) dep[l] = o.val[3];
             }
         } else if (o.kind == kOpDraw) {
-            const DevDraw dr = fv.draws[o.arg];
-            int end_tri = dr.first_tri + dr.ntris;
+            int end_tri = o.info[0] + o.info[1];
             int drect[4] = { rect[0], rect[1], rect[2], rect[3] };   // the tile, or its part inside the scissor rectangle
-            if (kScissor && fv.any_scissor) draw_rect(fv.states[dr.state], rect, drect);
+            if (kScissor && fv.any_scissor) draw_rect(fv.states[o.info[2]], rect, drect);
             if (visibility) pending = true;
             if (fv.raster_phase == 2) continue;   // drawn by the first launch
             if (key_state == 0) {
@@ -1554,8 +1565,18 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                         const int src = pass == 0 ? int(e) : fv.clip_src[fv.clip_poly[e]];
                         valid = src < end_tri;
                         if (sweep) {
-                            const uint32_t d = uint32_t(find_draw(fv.draws, fv.ndraws, src));
-                            S.order[tid] = (d << (kKeyPosBits + 1)) | (uint32_t(pass) << kKeyPosBits) | (cur + uint32_t(tid));
+                            int d = 0;
+                            if (draws_cached) {   // the last draw starting at or before src
+                                int lo = 0, hi = fv.ndraws - 1;
+                                while (lo < hi) {
+                                    const int mid = (lo + hi + 1) >> 1;
+                                    if (S.dfirst[mid] <= src) lo = mid; else hi = mid - 1;
+                                }
+                                d = lo;
+                            } else {
+                                d = find_draw(fv.draws, fv.ndraws, src);
+                            }
+                            S.order[tid] = (uint32_t(d) << (kKeyPosBits + 1)) | (uint32_t(pass) << kKeyPosBits) | (cur + uint32_t(tid));
                         }
                     }
                     const int n = __syncthreads_count(valid);
@@ -1764,6 +1785,14 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                     cur += uint32_t(n);
                     if (n < int(blockDim.x)) break;
                 }
+            }
+            if (sweep && fv.keys_resume_op > op) {
+                // the later draws and the states between them have nothing
+                // left to do: go on at the op after the last draw
+                op = fv.keys_resume_op - 1;
+                const FrameOp so = ops_cached ? S.ops[fv.keys_resume_state_op] : fv.ops[fv.keys_resume_state_op];
+                cur_state = so.arg;
+                load_frag_state(fv, so, fs);
             }
         } else if (o.kind == kOpStoreTC) {
             // GPUBltImpl::StoreTrueColor -> FilterTile (rglr_algorithm.hxx:31-104)
