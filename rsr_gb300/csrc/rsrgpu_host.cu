@@ -167,7 +167,8 @@ struct rsrgpu_ctx {
     cudaGraph_t graph = nullptr;
     bool tables_uploaded = false;   // states, draws, ops and G-buffer tables of this submission
     cudaGraphExec_t gexec = nullptr;
-    FrameCounters* h_counters = nullptr;   // pinned
+    FrameCounters* h_counters = nullptr;   // pinned, mapped: the raster pass writes it
+    FrameCounters* h_counters_dev = nullptr;   // its device address
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     // textures from host buffers are copied on `side` while setup and binning run
     cudaStream_t side = nullptr;
@@ -426,7 +427,8 @@ int rsrgpu_create(int device, rsrgpu_ctx** out) {
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_tables, cudaEventDisableTiming) != cudaSuccess ||
-        cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_counters), sizeof(FrameCounters), cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc(reinterpret_cast<void**>(&ctx->h_counters), sizeof(FrameCounters), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->h_counters_dev), ctx->h_counters, 0) != cudaSuccess ||
         cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
         cudaEventCreate(&ctx->ev2) != cudaSuccess || cudaEventCreate(&ctx->ev3) != cudaSuccess) {
         rsrgpu_destroy(ctx);
@@ -1026,6 +1028,7 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.vis_keys = ctx->vis_keys;
     fv.keys_resume_op = 0;
     fv.keys_resume_state_op = 0;
+    fv.host_counters = tables == nullptr ? ctx->h_counters_dev : nullptr;
     if (fv.vis_keys) {   // the raster pass jumps from the first draw to the op after the last
         int last_draw = -1, st_at = 0;
         for (int i = 0; i < int(ctx->ops.size()); ++i)
@@ -1158,7 +1161,7 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
     // outputs written in place need no copy back
     for (auto& kv : ctx->host)
         if (kv.second.out) CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
-    CK(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters.p, sizeof(FrameCounters), cudaMemcpyDeviceToHost, st), "D2H counters");
+    // the counters reach h_counters from the raster pass (FrameView::host_counters)
     CK(cudaEventRecordWithFlags(ctx->ev3, st, evflags), "event");
     ctx->stats.gpu_launches = 3 + (gl.n > 0 ? 1 : 0) + (split ? 1 : 0);
     return 0;

@@ -193,6 +193,7 @@ struct FrameView {
     int32_t any_scissor;      // a draw of the frame has the scissor test on
     int32_t keys_resume_op;   // vis_keys frames: the first op after the last draw (0: not given)
     int32_t keys_resume_state_op; // the last state op before it
+    FrameCounters* host_counters; // pinned host copy of *counters, written by the raster pass (or null)
     const DevDrawExt* dext;   // per draw, for frames with instanced or OBJ1Program draws (setup_ext_kernel); else null
 };
 

@@ -1106,6 +1106,7 @@ __device__ __forceinline__ bool depth_pass(int func, float frag, float dest) {
 
 constexpr uint32_t kNoOwner = 0xffffffffu;
 constexpr uint32_t kClippedBit = 0x80000000u;
+constexpr uint32_t kKeyPosBits = 19;   // the list-position bits of a key's order (see frag_key)
 
 // Per-(triangle, tile) setup and vertex data of one list entry, for the
 // resolve pass: the triangle that last wrote a pixel is set up again exactly
@@ -1232,7 +1233,6 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
 //     as the comparison treats them; NaN depths never pass and are skipped);
 //   order rank: draw index (12 bits), inline / clipped pass (1 bit),
 //     position in the tile's list (19 bits) -- the drawing order within a tile.
-constexpr uint32_t kKeyPosBits = 19;
 constexpr int kKeySmallQuads = 16;  // triangles covering at most this many quads of the region go one per lane,
 constexpr int kKeyTinyQuads = 2;    // or this many where the batch's boxes cover the region more than
 constexpr int kKeyCrowded = 6;      // kKeyCrowded times over
@@ -1905,26 +1905,39 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 // ---------------------------------------------------------------------------
 // kernels: one frame, and a batch of frames in one launch per stage
 // ---------------------------------------------------------------------------
+// The binning launch is programmatically dependent on setup (launched while
+// setup's CTAs drain; it waits for their results before it reads them).
 __global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constant__ FrameView fv) {
     setup_body<false>(fv, blockIdx.x);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 __global__ void __launch_bounds__(kSetupBlock) setup_ext_kernel(const __grid_constant__ FrameView fv) {
     setup_body<true>(fv, blockIdx.x);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
     __shared__ BinShared S;
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     bin_body(fv, blockIdx.x, S);
+}
+// The frame's counters, final once setup and binning are done, go to the
+// caller-visible pinned copy from the raster pass (no copy after the frame).
+__device__ __forceinline__ void publish_counters(const FrameView& fv) {
+    if (fv.host_counters != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *fv.host_counters = *fv.counters;
 }
 __global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
+    publish_counters(fv);
     raster_body<false, false>(fv, blockIdx.x, S);
 }
 __global__ void __launch_bounds__(256, 2) raster_scissor_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
+    publish_counters(fv);
     raster_body<false, true>(fv, blockIdx.x, S);
 }
 __global__ void __launch_bounds__(256, 2) raster_ext_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
+    publish_counters(fv);
     raster_body<true, true>(fv, blockIdx.x, S);
 }
 
@@ -2006,8 +2019,16 @@ int raster_threads(const FrameView& fv) {
 }
 
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
-    bin_kernel<<<bin_blocks(fv), kBinBlock, 0, st>>>(fv);
-    return cudaGetLastError();
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(bin_blocks(fv));
+    cfg.blockDim = dim3(kBinBlock);
+    cfg.stream = st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, bin_kernel, fv);
 }
 
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
