@@ -93,9 +93,15 @@ struct DevBuf {
     template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
+// The part of a texture's mip chain the samplers address: level 0 (rows
+// [0, w), w texels each) and the mip levels (rows [w, 2w), the first w/2
+// texels of each); rsr's Texture leaves the rest of those rows zero.
+struct TexRegion { size_t offset; int32_t edge; };   // bytes from the buffer start; edge 0: the whole rest
+
 struct HostBuffer {
     const uint8_t* host = nullptr;
     size_t bytes = 0;
+    std::vector<TexRegion> tex;   // this frame's textures in the buffer (late inputs)
     void* dev = nullptr;          // device mirror
     void* mapped = nullptr;       // device address of the host memory itself (pinned and mapped), else null
     bool in = false, out = false; // this frame reads it through the mirror / writes the mirror
@@ -269,8 +275,10 @@ namespace {
 // place by the kernels (the transfer overlaps the raster pass instead of
 // following it); other uses go through the device mirror, copied in before
 // the pass that reads it or out after the frame.
-int resolve(rsrgpu_ctx* ctx, const void* p, Use use, void** out, const char* what, size_t* avail = nullptr) {
+int resolve(rsrgpu_ctx* ctx, const void* p, Use use, void** out, const char* what, size_t* avail = nullptr,
+            HostBuffer** owner = nullptr) {
     *out = nullptr;
+    if (owner) *owner = nullptr;
     if (avail) *avail = 0;
     if (p == nullptr) return 0;
     const uint8_t* bp = static_cast<const uint8_t*>(p);
@@ -293,6 +301,7 @@ int resolve(rsrgpu_ctx* ctx, const void* p, Use use, void** out, const char* wha
             }
             *out = static_cast<uint8_t*>(base) + (bp - hb.host);
             if (avail) *avail = hb.bytes - size_t(bp - hb.host);
+            if (owner) *owner = &hb;
             return 0;
         }
     }
@@ -389,8 +398,16 @@ int decode_state(rsrgpu_ctx* ctx, const rsrgpu_glstate& s, DevState& d) {
             return fail(ctx, RSRGPU_EUNSUPPORTED, "can't make TextureUnit for pow2 size %d", t.width);
         void* dp = nullptr;
         size_t avail = 0;
-        int rc = resolve(ctx, t.ptr, kLateInput, &dp, "texture", &avail);
+        HostBuffer* hb = nullptr;
+        int rc = resolve(ctx, t.ptr, kLateInput, &dp, "texture", &avail, &hb);
         if (rc) return rc;
+        if (hb != nullptr && hb->late) {   // each texture once, however many states bind it
+            const TexRegion reg{ size_t(static_cast<const uint8_t*>(static_cast<const void*>(t.ptr)) - hb->host),
+                                 pow2 ? t.width : 0 };
+            bool seen = false;
+            for (const TexRegion& r : hb->tex) seen = seen || (r.offset == reg.offset && r.edge == reg.edge);
+            if (!seen) hb->tex.push_back(reg);
+        }
         // the mip chain of a square power-of-two texture (2*W*W texels), else H rows of stride texels
         const size_t need = pow2 ? size_t(2) * size_t(t.width) * size_t(t.width) * 16u
                                  : size_t(std::max(t.height, 1)) * size_t(std::max(t.stride, 1)) * 16u;
@@ -536,6 +553,9 @@ int rsrgpu_register_host_buffer(rsrgpu_ctx* ctx, const void* host_ptr, size_t by
     hb.host = p;
     hb.bytes = bytes;
     CK(cudaMalloc(&hb.dev, bytes), "cudaMalloc(host mirror)");
+    // texture mirrors take only the texels the samplers address (the rest of
+    // the mip rows is zero in rsr's layout): start from zeros
+    CK(cudaMemset(hb.dev, 0, bytes), "clear host mirror");
     // pinned host memory the device can address (cudaHostAlloc, or registered as mapped)
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer != nullptr)
@@ -562,7 +582,10 @@ namespace {
 // GPU::BinImpl's command interpretation (rglv_gpu.cxx:119-260), on the host:
 // the frame's states, draws and op list, and how it uses every caller buffer.
 int decode_frame(rsrgpu_ctx* ctx, const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates) {
-    for (auto& kv : ctx->host) kv.second.in = kv.second.out = kv.second.early = kv.second.late = kv.second.direct = false;
+    for (auto& kv : ctx->host) {
+        kv.second.in = kv.second.out = kv.second.early = kv.second.late = kv.second.direct = false;
+        kv.second.tex.clear();
+    }
     ctx->states.assign(size_t(nstates), DevState{});
     ctx->state_ordinal.assign(size_t(nstates), -1);
     ctx->draws.clear();
@@ -917,6 +940,7 @@ std::vector<uint8_t> graph_signature(const rsrgpu_ctx* ctx) {
         const uint8_t f = uint8_t(hb.in) | uint8_t(hb.out) << 1 | uint8_t(hb.early) << 2 | uint8_t(hb.late) << 3 |
                           uint8_t(hb.direct) << 4;
         put_bytes(sig, f);
+        for (const TexRegion& r : hb.tex) { put_bytes(sig, r.offset); put_bytes(sig, r.edge); }
     }
     return sig;
 }
@@ -1120,18 +1144,48 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
             gl.src[gl.n] = static_cast<const uint8_t*>(hb.mapped);
             gl.dst[gl.n] = static_cast<uint8_t*>(hb.dev);
             gl.bytes[gl.n] = hb.bytes;
+            gl.rows[gl.n] = 1;
             ++gl.n;
         } else {
             CK(cudaMemcpyAsync(hb.dev, hb.host, hb.bytes, cudaMemcpyHostToDevice, st), "H2D input");
         }
     }
+    // the vertex data first (setup waits for it), then the textures on the
+    // side stream (the link is shared: the gather goes first)
     if (gl.n > 0) CK(launch_gather(gl, st), "gather_kernel");
     if (any_late) {
         CK(cudaEventRecord(ctx->ev_fork, st), "event");
         CK(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0), "stream wait");
-        for (auto& kv : ctx->host)
-            if (kv.second.in && !kv.second.early)
-                CK(cudaMemcpyAsync(kv.second.dev, kv.second.host, kv.second.bytes, cudaMemcpyHostToDevice, ctx->side), "H2D texture");
+        for (auto& kv : ctx->host) {
+            const HostBuffer& hb = kv.second;
+            if (!hb.in || hb.early) continue;
+            // the whole buffer unless every texture in it is a mip chain of
+            // pinned, mapped memory (pageable memory goes by plain copies)
+            bool whole = hb.tex.empty() || hb.mapped == nullptr || hb.tex.size() > size_t(kMaxGather);
+            for (const TexRegion& r : hb.tex) whole = whole || r.edge < 4;
+            if (whole) {
+                CK(cudaMemcpyAsync(hb.dev, hb.host, hb.bytes, cudaMemcpyHostToDevice, ctx->side), "H2D texture");
+                continue;
+            }
+            // square power-of-two textures: level 0 (one copy), then the used
+            // half of each mip row, read from mapped memory by gather_kernel
+            GatherList tg{};
+            for (const TexRegion& r : hb.tex) {
+                const size_t row = size_t(r.edge) * 16u;
+                uint8_t* d = static_cast<uint8_t*>(hb.dev) + r.offset;
+                const uint8_t* h = hb.host + r.offset;
+                CK(cudaMemcpyAsync(d, h, row * size_t(r.edge), cudaMemcpyHostToDevice, ctx->side), "H2D texture level 0");
+                if (tg.n < kMaxGather && r.edge >= 4) {
+                    tg.src[tg.n] = static_cast<const uint8_t*>(hb.mapped) + r.offset + row * size_t(r.edge);
+                    tg.dst[tg.n] = d + row * size_t(r.edge);
+                    tg.bytes[tg.n] = row / 2;
+                    tg.rows[tg.n] = uint32_t(r.edge);
+                    tg.pitch[tg.n] = uint32_t(row);
+                    ++tg.n;
+                }
+            }
+            if (tg.n > 0) CK(launch_gather(tg, ctx->side), "gather_kernel (texture mip rows)");
+        }
         CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
     }
     CK(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(FrameCounters), st), "memset counters");

@@ -200,11 +200,16 @@ struct FrameView {
 // Copies of up to kMaxGather byte ranges in one launch (inputs from pinned,
 // mapped host memory into their device mirrors).
 constexpr int kMaxGather = 64;
+// Copies of gather_kernel: range r is rows[r] rows (0 counts as 1) of
+// bytes[r] bytes, pitch[r] bytes apart in both source and destination
+// (rows > 1: 16-byte aligned ends and pitch).
 struct GatherList {
     int n;
     const uint8_t* src[kMaxGather];
     uint8_t* dst[kMaxGather];
     size_t bytes[kMaxGather];
+    uint32_t rows[kMaxGather];
+    uint32_t pitch[kMaxGather];
 };
 
 // One launch of a stage over many frames: block b belongs to frame f when

@@ -1990,11 +1990,42 @@ __global__ void __launch_bounds__(256) gather_kernel(const __grid_constant__ Gat
     uint8_t* __restrict__ dst = g.dst[r];
     const size_t n = g.bytes[r];
     const size_t first = size_t(blockIdx.x) * blockDim.x + threadIdx.x, step = size_t(gridDim.x) * blockDim.x;
+    // Reads from host memory have a long latency: each thread keeps four
+    // 16-byte loads in flight before it stores them.
+    if (g.rows[r] > 1) {   // a block of rows (16-byte units; checked by the host)
+        const uint32_t per = uint32_t(n / 16), pitch16 = g.pitch[r] / 16;
+        const size_t total = size_t(per) * g.rows[r];
+        for (size_t i0 = first; i0 < total; i0 += 4 * step) {
+            uint4 v[4];
+            size_t at[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const size_t i = i0 + size_t(k) * step;
+                at[k] = ~size_t(0);
+                if (i < total) {
+                    const size_t row = i / per;
+                    at[k] = row * pitch16 + (i - row * per);
+                    v[k] = reinterpret_cast<const uint4*>(src)[at[k]];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (at[k] != ~size_t(0)) reinterpret_cast<uint4*>(dst)[at[k]] = v[k];
+        }
+        return;
+    }
     size_t done = 0;
     if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
         const size_t n16 = n / 16;
-        for (size_t i = first; i < n16; i += step)
-            reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(src)[i];
+        for (size_t i0 = first; i0 < n16; i0 += 4 * step) {
+            uint4 v[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (i0 + size_t(k) * step < n16) v[k] = reinterpret_cast<const uint4*>(src)[i0 + size_t(k) * step];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (i0 + size_t(k) * step < n16) reinterpret_cast<uint4*>(dst)[i0 + size_t(k) * step] = v[k];
+        }
         done = n16 * 16;
     }
     for (size_t i = done + first; i < n; i += step) dst[i] = src[i];
@@ -2002,7 +2033,7 @@ __global__ void __launch_bounds__(256) gather_kernel(const __grid_constant__ Gat
 
 cudaError_t launch_gather(const GatherList& g, cudaStream_t st) {
     if (g.n <= 0) return cudaSuccess;
-    gather_kernel<<<dim3(32, unsigned(g.n)), 256, 0, st>>>(g);
+    gather_kernel<<<dim3(128, unsigned(g.n)), 256, 0, st>>>(g);
     return cudaGetLastError();
 }
 
