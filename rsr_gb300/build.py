@@ -87,6 +87,17 @@ def build_reference():
     return os.path.join(REPO, "oracle", "_ref", "librsrref.so")
 
 
+def build_shim_test():
+    """Builds oracle/_ref/rsr_translate (include/rsrgpu_rglv.hpp against
+    rsr's own headers and GL recorder) when the reference checkout is present
+    on an x86-64 host; returns its path or None."""
+    if not os.path.isdir(REFERENCE) or platform.machine() not in ("x86_64", "AMD64"):
+        return None
+    build_gpu()
+    _run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", "REF=" + REFERENCE, "shim"])
+    return os.path.join(REPO, "oracle", "_ref", "rsr_translate")
+
+
 def build_all(verbose=False):
     with ThreadPoolExecutor(max_workers=3) as ex:
         f_gpu = ex.submit(build_gpu, verbose)
