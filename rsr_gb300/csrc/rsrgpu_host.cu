@@ -166,6 +166,7 @@ struct rsrgpu_ctx {
     int debug_learned_stall = 0;    // RSRGPU_DEBUG_LEARNED_STALL (rsrgpu_set_debug)
     int vis_keys = 0;               // FrameView::vis_keys of the submitted frame
     DevBuf d_vis;                   // owners and depths between the two launches of a split raster pass
+    DevBuf d_queue;                 // the raster work queue: tiles by cost bucket
     // the run's work captured once per submission and replayed by every run
     // (one launch instead of a dozen API calls); dropped when anything it
     // holds changes (submit, reset, host buffers, capacity growth)
@@ -474,7 +475,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_tables, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_queue, &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_tables, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -1053,6 +1054,11 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.keys_resume_op = 0;
     fv.keys_resume_state_op = 0;
     fv.host_counters = tables == nullptr ? ctx->h_counters_dev : nullptr;
+    fv.tile_queue = nullptr;
+    if (tables == nullptr) {   // the raster pass's work queue: tiles by cost bucket
+        CK(ctx->d_queue.ensure(sizeof(uint32_t) * size_t(kCostBuckets) * size_t(ctx->ntiles)), "alloc tile queue");
+        fv.tile_queue = ctx->d_queue.as<uint32_t>();
+    }
     if (fv.vis_keys) {   // the raster pass jumps from the first draw to the op after the last
         int last_draw = -1, st_at = 0;
         for (int i = 0; i < int(ctx->ops.size()); ++i)
@@ -1200,6 +1206,7 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
     CK(cudaEventRecordWithFlags(ctx->ev1, st, evflags), "event");
     if (split) {
         FrameView f = fv;
+        f.tile_queue = nullptr;   // two launches over the same items: each takes them in grid order
         f.vis_own = ctx->d_vis.as<uint32_t>();
         f.vis_dep = reinterpret_cast<float*>(f.vis_own + size_t(fv.width) * size_t(fv.height));
         f.raster_phase = 1;

@@ -189,6 +189,15 @@ __device__ __forceinline__ bool rect_has(uint64_t r, int tx, int ty) {
     return x0 <= tx && tx <= x1 && y0 <= ty && ty <= y1;
 }
 
+// files a binned tile in the raster pass's work queue (bucket: the power of
+// two of its list length)
+__device__ __forceinline__ void enqueue_tile(const FrameView& fv, int tile, uint32_t cost) {
+    if (fv.tile_queue == nullptr) return;
+    const int b = min(kCostBuckets - 1, 32 - __clz(int(cost)));
+    const uint32_t pos = atomicAdd(&fv.counters->bucket[b], 1u);
+    fv.tile_queue[size_t(b) * size_t(fv.ntiles) + pos] = uint32_t(tile);
+}
+
 __device__ __forceinline__ int find_draw(const DevDraw* __restrict__ draws, int ndraws, int g) {
     int lo = 0, hi = ndraws - 1;
     while (lo < hi) {
@@ -595,6 +604,7 @@ __device__ __forceinline__ void bin_tile_warp(const FrameView& fv, int tile, int
         } else {
             fv.bins[tile] = TileBin{off, ninl, off + ninl, nclip};
         }
+        enqueue_tile(fv, tile, ninl + nclip);
     }
     off = __shfl_sync(FULL_MASK, off, 0);
     if (off == 0xffffffffu) return;
@@ -710,7 +720,7 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShare
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (tile >= fv.ntiles) return;
     if (fv.counters->overflow & 1u) {
-        if (t == 0) fv.bins[tile] = TileBin{0, 0, 0, 0};
+        if (t == 0) { fv.bins[tile] = TileBin{0, 0, 0, 0}; enqueue_tile(fv, tile, 0); }
         return;
     }
     const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
@@ -779,6 +789,7 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShare
         } else {
             fv.bins[tile] = TileBin{off, uint32_t(tinl), off + uint32_t(tinl), uint32_t(tcl)};
         }
+        enqueue_tile(fv, tile, uint32_t(tinl + tcl));
         S.base = off;
     }
     __syncthreads();
@@ -1925,20 +1936,61 @@ __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ 
 __device__ __forceinline__ void publish_counters(const FrameView& fv) {
     if (fv.host_counters != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *fv.host_counters = *fv.counters;
 }
+// The raster work items (tile, region) of a frame with a work queue: a
+// persistent grid takes them from a counter, the tiles' regions in the
+// order of their cost buckets, heaviest first.  Without a queue, CTA b draws
+// item b.
+template <bool kExt, bool kScissor>
+__device__ __forceinline__ void raster_items(const FrameView& fv, RasterSmem& S) {
+    if (fv.tile_queue == nullptr) {
+        raster_body<kExt, kScissor>(fv, blockIdx.x, S);
+        return;
+    }
+    __shared__ int item_tile, item_sub;
+    __shared__ int bucket_end[kCostBuckets];   // tiles in the buckets from the heaviest down to b
+    const int subs = ((fv.tile_w + fv.region_px - 1) / fv.region_px) * ((fv.tile_h + fv.region_px - 1) / fv.region_px);
+    const int nitems = fv.ntiles * subs;
+    if (threadIdx.x == 0) {
+        int sum = 0;
+        for (int b = kCostBuckets - 1; b >= 0; --b) bucket_end[b] = (sum += int(fv.counters->bucket[b]));
+    }
+    while (true) {
+        __syncthreads();   // the previous item is done with the shared state
+        if (threadIdx.x == 0) {
+            const int i = int(atomicAdd(&fv.counters->next_item, 1u));
+            int tile = -1;
+            if (i < nitems) {
+                const int rank = i / subs;
+                int b = kCostBuckets - 1;
+                while (b > 0 && rank >= bucket_end[b]) --b;
+                if (rank < bucket_end[b]) {
+                    const int first = b == kCostBuckets - 1 ? 0 : bucket_end[b + 1];
+                    tile = int(fv.tile_queue[size_t(b) * size_t(fv.ntiles) + size_t(rank - first)]);
+                }
+            }
+            item_tile = i < nitems ? tile : -2;
+            item_sub = i % subs;
+        }
+        __syncthreads();
+        const int tile = item_tile, sub = item_sub;
+        if (tile == -2) return;
+        if (tile >= 0) raster_body<kExt, kScissor>(fv, tile * subs + sub, S);
+    }
+}
 __global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
     publish_counters(fv);
-    raster_body<false, false>(fv, blockIdx.x, S);
+    raster_items<false, false>(fv, S);
 }
 __global__ void __launch_bounds__(256, 2) raster_scissor_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
     publish_counters(fv);
-    raster_body<false, true>(fv, blockIdx.x, S);
+    raster_items<false, true>(fv, S);
 }
 __global__ void __launch_bounds__(256, 2) raster_ext_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem S;
     publish_counters(fv);
-    raster_body<true, true>(fv, blockIdx.x, S);
+    raster_items<true, true>(fv, S);
 }
 
 // frame of a block: the last f with start[f] <= block (start[] ascending)
@@ -2063,9 +2115,21 @@ cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
 }
 
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
-    if (fv.ext) raster_ext_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
-    else if (fv.any_scissor) raster_scissor_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
-    else raster_kernel<<<raster_blocks(fv), raster_threads(fv), 0, st>>>(fv);
+    int blocks = raster_blocks(fv);
+    if (fv.tile_queue != nullptr) {   // a persistent grid: every CTA slot of the GPU, at most one per item
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const void* k = fv.ext ? reinterpret_cast<const void*>(raster_ext_kernel)
+                      : fv.any_scissor ? reinterpret_cast<const void*>(raster_scissor_kernel)
+                                       : reinterpret_cast<const void*>(raster_kernel);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, raster_threads(fv), 0);
+        const int slots = sms * (per > 0 ? per : 1);
+        blocks = blocks < slots ? blocks : slots;
+    }
+    if (fv.ext) raster_ext_kernel<<<blocks, raster_threads(fv), 0, st>>>(fv);
+    else if (fv.any_scissor) raster_scissor_kernel<<<blocks, raster_threads(fv), 0, st>>>(fv);
+    else raster_kernel<<<blocks, raster_threads(fv), 0, st>>>(fv);
     return cudaGetLastError();
 }
 
