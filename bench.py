@@ -392,10 +392,13 @@ def measure_frame(gpu, sc, args, stream, flush, world, clocks=None):
     return out
 
 
-# Warp instructions one raster_kernel launch issues on the headline frame
-# (ncu smsp__inst_executed.sum of one launch; re-measured whenever the
-# kernel changes), and on the 640x360 plain frame.
-RASTER_WARP_INST = {"textured_sphere_1080p": 45_710_897, "plain_640x360": 534_816_066}
+# Warp instructions the raster pass issues on the headline frame and on the
+# 640x360 plain frame: the pass of these opaque frames is raster_vis_kernel
+# then shade_pixels_kernel (ncu smsp__inst_executed.sum of one launch of
+# each, `bench.py --profile sphere_1080` / `plain_640`; re-measured whenever
+# the kernels change).
+RASTER_WARP_INST = {"textured_sphere_1080p": 21_426_672 + 19_095_709, "plain_640x360": 121_205_039 + 3_067_125}
+RASTER_PASS = "raster pass (raster_vis_kernel + shade_pixels_kernel)"
 
 
 def issue_roofline(kernel_ms, inst, sm_mhz, num_sms):
@@ -446,7 +449,7 @@ def run_gpu(args):
     frame_s = head["ms_per_step"] / 1e3
     roof = issue_roofline(head["raster_ms"], RASTER_WARP_INST["textured_sphere_1080p"], sm_mhz, num_sms) or {
         "bound": "issue", "achieved": None, "peak": None, "unit": "Gwarp-inst/s", "frac": None}
-    roof.update({"kernel": "raster_kernel", "avg_launch_ms": head["raster_ms"], "traffic": None,
+    roof.update({"kernel": RASTER_PASS, "avg_launch_ms": head["raster_ms"], "traffic": None,
                  "hbm": {"scope": "whole frame (setup, bin, raster)", "compulsory_bytes": comp,
                          "achieved_gbs": comp / frame_s / 1e9, "peak_gbs": peak, "frac": comp / frame_s / 1e9 / peak,
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}})
@@ -465,7 +468,7 @@ def run_gpu(args):
                "candidate_fragments_per_frame": frags,
                "candidate_fragments_per_s": frags * c1_fps if frags else None,
                "e2e": c1["e2e"], "raster_ms": c1["raster_ms"],
-               "roofline": dict(c1roof or {"bound": "issue", "frac": None}, kernel="raster_kernel",
+               "roofline": dict(c1roof or {"bound": "issue", "frac": None}, kernel=RASTER_PASS,
                                 hbm={"compulsory_bytes": c1_comp, "achieved_gbs": c1_comp / (c1["ms_per_step"] / 1e3) / 1e9,
                                      "frac": c1_comp / (c1["ms_per_step"] / 1e3) / 1e9 / peak}),
                "cpu_baseline": c1cpu}
@@ -662,8 +665,7 @@ def run_deferred(gpu, args, stream, flush):
                       "speedup_vs_plain_shading": plain_ms / learned_ms,
                       "psnr_db_vs_plain": db, "max_abs_vs_plain": maxabs, "gate_max_tile_mse": thr,
                       "served_tiles": served, "covered_pixels": covered,
-                      "weights": {k: net.meta.get(k) for k in ("train_seeds", "samples", "steps")},
-                      "profile": "profiles/deferred_shading_1080p_64_lights.md (tensor pipe, stalls)"}
+                      "weights": {k: net.meta.get(k) for k in ("train_seeds", "samples", "steps")}}
     # more lights on the same G-buffer (positions, colours, radii as the scene's 64)
     from rsr_gb300 import scenes
     scaling = []
@@ -745,6 +747,27 @@ def run_batch(gpu, args, stream, flush):
 
     tuned_ms = timed_batch(choice)
     fixed_ms = timed_batch([(32, 32, 0)] * len(frames))
+    # per resolution class: the class's frames alone as one batch (tuned tilings)
+    classes = []
+    for (w, h) in scenes.BATCH_RESOLUTIONS:
+        pick = [k for k, sc in enumerate(frames) if (sc.width, sc.height) == (w, h)]
+        if not pick:
+            continue
+        b.submit([(made[k][3], frames[k].width, frames[k].height) + tuple(choice[k]) for k in pick])
+        for _ in range(3):
+            b.run(sptr)
+            b.wait()
+        cms = []
+        for i in range(steps):
+            flush.fill_(i & 0xff)
+            torch.cuda.synchronize()
+            b.run(sptr)
+            b.wait()
+            cms.append(b.last_ms())
+        cm = statistics.median(cms)
+        ct = sum(frames[k].ntris for k in pick)
+        classes.append({"resolution": "%dx%d" % (w, h), "frames": len(pick), "triangles": ct, "ms": cm,
+                        "mtris_per_s": ct / cm / 1e3, "frames_per_s": len(pick) / cm * 1e3})
     # the same frames one after another through the single-frame path (tuned tilings)
     seq = []
     for (sc, m), (t, r, c) in zip(zip(frames, made), choice):
@@ -777,31 +800,126 @@ def run_batch(gpu, args, stream, flush):
             "sequential_single_frame": {"ms": seq_ms, "frames_per_s": len(frames) / seq_ms * 1e3,
                                         "mtris_per_s": ntris / seq_ms / 1e3,
                                         "note": "wall clock: decode + run + wait per frame"},
-            "gpu_launches_per_batch": "setup 1 + bin 1 + raster 1 per CTA shape (graph)"}
+            "by_resolution": classes,
+            "cpu_baseline": None if args.no_cpu_baseline else batch_cpu_sample(frames, args.cpu_seconds),
+            "gpu_launches_per_batch": "setup 1 + bin 1 + raster 1 per CTA shape (graph); raster grids "
+                                      "persistent, taking every frame's tiles from one work queue per "
+                                      "CTA shape, heaviest first"}
+
+
+def batch_cpu_sample(frames, seconds):
+    """The batch's frames on the CPU (the oracle's C restatement, all host
+    threads), one after another in batch order, until `seconds` have passed:
+    a bounded sample of the batch workload."""
+    import oracle
+    threads = os.cpu_count()
+    r = oracle.CpuRenderer("oracle", threads=threads)
+    done, tris, t_all = 0, 0, 0.0
+    for sc in frames:
+        if t_all >= seconds:
+            break
+        t0 = time.perf_counter()
+        r.render_gl(sc.record(gamma=True), sc.width, sc.height, sc.tile_blocks)
+        t_all += time.perf_counter() - t0
+        done += 1
+        tris += sc.ntris
+    return {"value": tris / t_all / 1e6, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
+            "frames_per_s": done / t_all,
+            "sample": "the first %d of the %d batch frames (%d triangles), each recorded and rendered in turn, "
+                      "%.1f s (C restatement of rsr's path)" % (done, len(frames), tris, t_all)}
+
+
+PROFILE_CASES = {
+    "sphere_1080": "the headline frame (setup, bin, raster_vis, shade_pixels kernels)",
+    "plain_640": "the 640x360 frame of 10 000 random triangles (setup, bin, raster_vis, shade_pixels kernels)",
+    "glow_1080": "the headline frame with quad and half-size float stores (raster_ext_kernel), "
+                 "then the 1024^2 texture upload (mip_block_kernel), 4 Kawase passes (kawase_kernel) "
+                 "and the glow resolve (glow_kernel)",
+    "instanced_640": "2 000 instanced cubes with ManyProgram, 640x360 (setup_ext_kernel, raster_ext_kernel)",
+    "batch16": "16 frames of the batch generator, 1k..200k triangles, fixed 32 px tiles "
+               "(setup/bin/raster_batch_kernel)",
+    "train_1080": "features of the 1080p deferred scene (learned_features_kernel), then Adam steps of "
+                  "batch 8 192 (mlp_train_kernel, adam_kernel)",
+}
 
 
 def run_profile(args):
-    """Renders one frame `--warmup` + `--steps` times with device-resident
-    inputs and no timing: the launch sequence an ncu capture selects from
-    (`-k regex:<kernel> -s <warmup> -c 1`)."""
+    """Runs one of PROFILE_CASES `--warmup` + `--steps` times with
+    device-resident inputs and no timing: the launch sequence an ncu capture
+    selects from (`-k regex:<kernel> -s <launches to skip> -c <count>`)."""
     import torch
     from rsr_gb300 import build, scenes
     build.build_gpu()
-    from rsr_gb300.gpu import GPU
-    sc = workload() if args.profile == "sphere_1080" else scenes.plain_raster()
+    from rsr_gb300.gpu import GPU, Batch
+    reps = args.warmup + args.steps
     gpu = GPU(0)
     gpu.InstallDefaults()
-    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
-    col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
-    dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
-    gpu.Reset(sc.width, sc.height, sc.tile_blocks)
-    gpu.submit(sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True))
-    for _ in range(args.warmup + args.steps):
-        gpu.run()
-        gpu.Wait()
-    torch.cuda.synchronize()
-    print(json.dumps({"profile": args.profile, "frames": args.warmup + args.steps, "launches_per_frame":
-                      gpu.stats()["gpu_launches"]}))
+    info = {"profile": args.profile, "case": PROFILE_CASES[args.profile], "reps": reps}
+    if args.profile == "batch16":
+        frames = scenes.batch_frames(seed=0, nframes=16, tris=(1_000, 200_000))
+        made = []
+        for sc in frames:
+            dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+            col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+            dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+            made.append((dev, col, dep, sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)))
+        b = Batch(0)
+        b.InstallDefaults()
+        b.submit([(m[3], sc.width, sc.height, 32, 32, 0) for sc, m in zip(frames, made)])
+        for _ in range(reps):
+            b.run()
+            b.wait()
+        torch.cuda.synchronize()
+        info["triangles"] = sum(f.ntris for f in frames)
+        b.close()
+    elif args.profile == "train_1080":
+        from rsr_gb300 import learned
+        fr = learned.DeferredFrame(gpu, 100, 1920, 1080, 2_000_000)
+        for _ in range(max(1, args.warmup)):
+            f, t = fr.features(gpu)
+        idx = torch.nonzero(fr.covered).reshape(-1)
+        g = torch.Generator(device="cuda").manual_seed(0)
+        net = learned.LearnedShader(seed=0)
+        for s in range(reps):
+            pick = idx[torch.randint(0, len(idx), (8192,), generator=g, device="cuda")].to(torch.int32)
+            net.train_step(gpu, f, t, pick, 1e-3)
+        torch.cuda.synchronize()
+        info["loss"] = net.loss.item()
+    else:
+        if args.profile == "instanced_640":
+            sc = scenes.instanced_scene()
+        elif args.profile == "plain_640":
+            sc = scenes.plain_raster()
+        else:
+            sc = workload()
+        dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+        col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+        dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+        gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+        gl = sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)
+        if args.profile == "glow_1080":
+            W, H = sc.width, sc.height
+            nq = (H // 2) * (W // 2)
+            quads = torch.zeros(nq * 16, dtype=torch.float32, device="cuda")
+            half = torch.zeros(nq * 4, dtype=torch.float32, device="cuda")
+            ta = torch.zeros(nq * 4, dtype=torch.float32, device="cuda")
+            tb = torch.zeros(nq * 4, dtype=torch.float32, device="cuda")
+            out = torch.zeros(W * H, dtype=torch.int32, device="cuda")
+            gl.StoreColorQuads(quads, W, H)
+            gl.StoreColorFP(half, W // 2, H // 2, downsample=True)
+            px = torch.randint(0, 256, (1024 * 1024 * 4,), dtype=torch.uint8, device="cuda")
+            texels = torch.empty(2 * 1024 * 1024 * 4, dtype=torch.float32, device="cuda")
+        gpu.submit(gl)
+        for _ in range(reps):
+            gpu.run()
+            gpu.Wait()
+            if args.profile == "glow_1080":
+                gpu.texture_from_rgba8(px, 1024, 1024, texels)
+                r = gpu.kawase_chain(half, ta, tb, W // 2, H // 2, 4)
+                gpu.glow(quads, r, out, W, H, srgb=True)
+        torch.cuda.synchronize()
+        info["launches_per_frame"] = gpu.stats()["gpu_launches"]
+    print(json.dumps(info))
     gpu.close()
 
 
@@ -816,7 +934,7 @@ def main():
     ap.add_argument("--no-deferred", action="store_true", help="skip the deferred / learned shading figures")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames figures")
     ap.add_argument("--no-post", action="store_true", help="skip the texture-upload and glow-chain figures")
-    ap.add_argument("--profile", choices=["sphere_1080", "plain_640"],
+    ap.add_argument("--profile", choices=sorted(PROFILE_CASES),
                     help="render that frame warmup+steps times, untimed (for ncu launch selection)")
     args = ap.parse_args()
     if args.profile:

@@ -22,7 +22,7 @@
  *     (the draw's triangles once per instance, instance ids 0 .. instances-1,
  *     at most 65536; ManyProgram reads instance i's column-major mat4 from
  *     buffer 15 at floats [16i, 16i+16) and is drawn only this way; frames with
- *     instanced draws are not taken by batches or rsrgpu_render_static)
+ *     instanced draws are not taken by rsrgpu_render_static)
  *   CMD_CLEAR           op u8, bits u8
  *   CMD_STORE_COLOR_FULL_LINEAR_TC  op u8, gamma u8, rsrgpu_truecolor_canvas*
  *   CMD_STORE_DEPTH_FULL_LINEAR_FP  op u8, float* (width*height, row-major)
@@ -113,8 +113,7 @@ extern "C" {
                                             position 0-2, uv 9-10; colour (u, v, uniform 0)),
                                             shaders.hxx:482-585 */
 #define RSRGPU_PROGRAM_OBJ1          7   /* OBJ1Program (Gouraud kd lit per vertex by a light at the eye;
-                                            position 0-2, normal 3-5, kd 6-8), shaders.hxx:586-699;
-                                            not taken by batches */
+                                            position 0-2, normal 3-5, kd 6-8), shaders.hxx:586-699 */
 #define RSRGPU_PROGRAM_GOURAUD       90  /* test program: per-vertex rgb, no lighting */
 #define RSRGPU_PROGRAM_GBUFFER       91  /* G-buffer program: position 0-2, normal 3-5,
                                             RGBA8 albedo bits (as float) in 6 */
@@ -621,9 +620,11 @@ int rsrgpu_learned_features(rsrgpu_ctx* ctx, const rsrgpu_gbuffer* gbuffer, cons
  * frames' decoded tables and one read-back of their counters, is captured
  * once in a CUDA graph and replayed by rsrgpu_batch_run().  Each frame is
  * rsr's byte stream as for rsrgpu_submit() with its own target size and
- * tiling; every pointer it holds must be a device pointer.  A frame's
- * results equal those of rsrgpu_submit()/rsrgpu_run() on a context reset to
- * the same size and tiling. */
+ * tiling (float colour stores, instanced and OBJ1Program draws included);
+ * every pointer it holds must be a device pointer.  A frame's results equal
+ * those of rsrgpu_submit()/rsrgpu_run() on a context reset to the same size
+ * and tiling.  Each raster launch is a persistent grid taking the blocks of
+ * all its frames from one device work queue, heaviest tiles first. */
 #define RSRGPU_MAX_BATCH 64
 typedef struct rsrgpu_batch rsrgpu_batch;
 typedef struct rsrgpu_frame_desc {

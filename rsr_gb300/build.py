@@ -23,7 +23,16 @@ NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I" + os.path.join(REPO, "include")]
 SOURCES = ["rsrgpu_kernels.cu", "rsrgpu_host.cu", "rsrgpu_static.cu", "rsrgpu_deferred.cu", "rsrgpu_mlp.cu", "rsrgpu_learned.cu",
            "rsrgpu_texture.cu", "rsrgpu_postfx.cu", "rsrgpu_recorder.cu", "rsrgpu_perf.cu"]
-REFERENCE = os.environ.get("RSR_REFERENCE", "/root/reference")
+
+
+def _reference_dir():
+    """The reference checkout the oracle's reference build reads: $RSR_REFERENCE,
+    else the default location the recipe oracle/ref/Makefile names."""
+    if os.environ.get("RSR_REFERENCE"):
+        return os.environ["RSR_REFERENCE"]
+    r = subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), "where"],
+                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
 
 
 def _nvcc():
@@ -81,9 +90,10 @@ def build_oracle():
 
 def build_reference():
     """Builds oracle/_ref when the reference checkout is present on an x86-64 host."""
-    if not os.path.isdir(REFERENCE) or platform.machine() not in ("x86_64", "AMD64"):
+    ref = _reference_dir()
+    if not ref or not os.path.isdir(ref) or platform.machine() not in ("x86_64", "AMD64"):
         return None
-    _run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", "REF=" + REFERENCE])
+    _run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", "REF=" + ref])
     return os.path.join(REPO, "oracle", "_ref", "librsrref.so")
 
 
@@ -91,10 +101,11 @@ def build_shim_test():
     """Builds oracle/_ref/rsr_translate (include/rsrgpu_rglv.hpp against
     rsr's own headers and GL recorder) when the reference checkout is present
     on an x86-64 host; returns its path or None."""
-    if not os.path.isdir(REFERENCE) or platform.machine() not in ("x86_64", "AMD64"):
+    ref = _reference_dir()
+    if not ref or not os.path.isdir(ref) or platform.machine() not in ("x86_64", "AMD64"):
         return None
     build_gpu()
-    _run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", "REF=" + REFERENCE, "shim"])
+    _run(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref"), "-j8", "REF=" + ref, "shim"])
     return os.path.join(REPO, "oracle", "_ref", "rsr_translate")
 
 

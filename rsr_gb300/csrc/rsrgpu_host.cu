@@ -28,7 +28,7 @@
 namespace rsrgpu {
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
-cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase = 0);
 cudaError_t launch_gather(const GatherList& g, cudaStream_t st);
 cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
@@ -984,6 +984,7 @@ struct ViewTables {
     GBufferDesc* gbufs;
     FrameCounters* counters;
     int4* super_rect;
+    DevDrawExt* dext;         // per draw, for frames with instanced or OBJ1Program draws
 };
 
 // Allocates the frame's scratch and fills ctx->fv; `tables` (batches) points
@@ -1054,9 +1055,11 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.keys_resume_op = 0;
     fv.keys_resume_state_op = 0;
     fv.host_counters = tables == nullptr ? ctx->h_counters_dev : nullptr;
-    fv.tile_queue = nullptr;
-    if (tables == nullptr) {   // the raster pass's work queue: tiles by cost bucket
-        CK(ctx->d_queue.ensure(sizeof(uint32_t) * size_t(kCostBuckets) * size_t(ctx->ntiles)), "alloc tile queue");
+    fv.tile_queue = nullptr;   // a batch places its frames' queues (build_batch)
+    fv.queue_cap = uint32_t(raster_blocks(fv));
+    fv.taken = fv.counters;
+    if (tables == nullptr) {   // the raster pass's work queue: raster blocks by cost bucket
+        CK(ctx->d_queue.ensure(sizeof(uint32_t) * size_t(kCostBuckets) * size_t(fv.queue_cap)), "alloc tile queue");
         fv.tile_queue = ctx->d_queue.as<uint32_t>();
     }
     if (fv.vis_keys) {   // the raster pass jumps from the first draw to the op after the last
@@ -1074,7 +1077,7 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.ext = frame_is_ext(ctx) ? 1 : 0;
     fv.any_scissor = 0;
     for (const DevState& st : ctx->states) fv.any_scissor |= st.scissor_test;
-    fv.dext = (ctx->any_dext && tables == nullptr) ? reinterpret_cast<DevDrawExt*>(tab + ctx->tab_ofs[4]) : nullptr;
+    fv.dext = !ctx->any_dext ? nullptr : tables ? tables->dext : reinterpret_cast<DevDrawExt*>(tab + ctx->tab_ofs[4]);
     return 0;
 }
 
@@ -1124,7 +1127,7 @@ int prepare_run(rsrgpu_ctx* ctx, cudaStream_t st, bool capturing) {
     if (rc) return rc;
     rc = upload_tables(ctx, st, capturing);
     if (rc) return rc;
-    if (ctx->fv.vis_keys != 0 && late_inputs(ctx))
+    if (ctx->fv.vis_keys != 0 && (late_inputs(ctx) || (!ctx->fv.ext && !ctx->fv.any_scissor)))
         CK(ctx->d_vis.ensure(size_t(ctx->fv.width) * size_t(ctx->fv.height) * 8u), "alloc visibility hand-over");
     return 0;
 }
@@ -1199,21 +1202,34 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
     CK(cudaEventRecordWithFlags(ctx->ev0, st, evflags), "event");
     CK(launch_setup(fv, st), "setup_kernel");
     CK(launch_bin(fv, st), "bin_kernel");
-    // With textures still on their way, a frame whose visibility is resolved
-    // by keys rasterises first (the visibility launch needs no texture) and
-    // shades after the copy.
-    const bool split = any_late && fv.vis_keys != 0;
+    // A frame whose visibility is resolved by keys rasterises in two
+    // launches: visibility (owners and depths handed over through d_vis),
+    // then shading and stores.  Without float stores, ManyProgram draws or
+    // scissor, the two are kernels compiled for their half (the visibility
+    // kernel fits three CTAs per SM), the first taking its tiles from the
+    // work queue; otherwise both are the frame's raster kernel, split only
+    // to let textures still on their way arrive during the visibility launch.
+    const bool compiled_split = fv.vis_keys != 0 && !fv.ext && !fv.any_scissor;
+    const bool split = fv.vis_keys != 0 && (any_late || compiled_split);
     CK(cudaEventRecordWithFlags(ctx->ev1, st, evflags), "event");
     if (split) {
         FrameView f = fv;
-        f.tile_queue = nullptr;   // two launches over the same items: each takes them in grid order
         f.vis_own = ctx->d_vis.as<uint32_t>();
         f.vis_dep = reinterpret_cast<float*>(f.vis_own + size_t(fv.width) * size_t(fv.height));
         f.raster_phase = 1;
-        CK(launch_raster(f, st), "raster_kernel");
-        CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
+        if (!compiled_split) f.tile_queue = nullptr;   // both launches take the blocks in grid order
+        CK(launch_raster(f, st, compiled_split ? 1 : 0), "raster_kernel (visibility)");
+        if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
         f.raster_phase = 2;
-        CK(launch_raster(f, st), "raster_kernel");
+        f.tile_queue = nullptr;
+        // a frame whose ops after the last draw are state changes and
+        // TrueColor / depth stores is shaded one thread per pixel
+        bool per_pixel = compiled_split;
+        for (size_t k = size_t(fv.keys_resume_op); k < ctx->ops.size(); ++k) {
+            const int32_t kind = ctx->ops[k].kind;
+            per_pixel = per_pixel && (kind == kOpState || kind == kOpStoreTC || kind == kOpStoreDepth);
+        }
+        CK(launch_raster(f, st, per_pixel ? 3 : compiled_split ? 2 : 0), "raster_kernel (shading)");
     } else {
         if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
         CK(launch_raster(fv, st), "raster_kernel");
@@ -1827,10 +1843,11 @@ struct rsrgpu_batch {
     int nframes = 0;
     // all frames' tables in one device buffer, staged in pinned memory
     DevBuf d_tables, d_counters, d_super;
+    DevBuf d_queue;                       // the raster launches' work queues
     uint8_t* h_tables = nullptr;
     size_t h_tables_cap = 0, tables_bytes = 0, super_count = 0;
     FrameCounters* h_counters = nullptr;  // pinned, kMaxBatch entries
-    std::vector<size_t> off_states, off_draws, off_ops, off_gbufs, off_super;
+    std::vector<size_t> off_states, off_draws, off_ops, off_gbufs, off_dext, off_super;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1888,13 +1905,6 @@ int decode_into(rsrgpu_batch* b, rsrgpu_ctx* c, const rsrgpu_frame_desc& d) {
     if (rc == 0) rc = rsrgpu_submit(c, d.commands, d.nbytes, d.states, d.nstates);
     if (rc) { b->err = c->err; return rc; }
     if (!c->host.empty()) return bfail(b, RSRGPU_EINVAL, "batched frames take device pointers only");
-    for (const FrameOp& o : c->ops)
-        if (o.kind >= kOpStoreFP)
-            return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no float colour stores (CMD_STORE_COLOR_*_FP); render them with rsrgpu_run");
-    if (c->any_inst)
-        return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no instanced draws; render them with rsrgpu_run");
-    if (c->any_dext)
-        return bfail(b, RSRGPU_EUNSUPPORTED, "batched frames take no OBJ1Program draws; render them with rsrgpu_run");
     c->region_px = d.region_px ? d.region_px : std::min(d.tile_px, kRegionPx);
     if (d.bin_capacity) c->bin_cap = std::max<uint32_t>(d.bin_capacity, 1024u);
     return 0;
@@ -1906,7 +1916,7 @@ int build_batch(rsrgpu_batch* b) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
     b->off_states.assign(size_t(n), 0); b->off_draws.assign(size_t(n), 0); b->off_ops.assign(size_t(n), 0);
-    b->off_gbufs.assign(size_t(n), 0); b->off_super.assign(size_t(n), 0);
+    b->off_gbufs.assign(size_t(n), 0); b->off_dext.assign(size_t(n), 0); b->off_super.assign(size_t(n), 0);
     size_t bytes = 0, supers = 0;
     for (int i = 0; i < n; ++i) {
         rsrgpu_ctx* c = b->frames[size_t(i)];
@@ -1914,6 +1924,7 @@ int build_batch(rsrgpu_batch* b) {
         b->off_draws[size_t(i)] = bytes; bytes = align256(bytes + sizeof(DevDraw) * c->draws.size());
         b->off_ops[size_t(i)] = bytes; bytes = align256(bytes + sizeof(FrameOp) * c->ops.size());
         b->off_gbufs[size_t(i)] = bytes; bytes = align256(bytes + sizeof(GBufferDesc) * c->gbufs.size());
+        b->off_dext[size_t(i)] = bytes; bytes = align256(bytes + (c->any_dext ? sizeof(DevDrawExt) * c->dext.size() : 0));
         b->off_super[size_t(i)] = supers; supers += size_t((c->ntris + kSuper - 1) / kSuper);
     }
     b->tables_bytes = std::max<size_t>(bytes, 256);
@@ -1933,26 +1944,52 @@ int build_batch(rsrgpu_batch* b) {
     int sblocks = 0, bblocks = 0;
     std::map<int, BatchLaunch> raster;      // by CTA size
     std::map<int, int> rblocks;
+    // Each raster launch (one per CTA size) takes its frames' blocks from one
+    // counter, the slot after the frames' own counters (n + the launch's place
+    // among the CTA sizes); each frame's queue, [kCostBuckets][its blocks], is
+    // at kCostBuckets x its first block in the launch's part of d_queue.
+    std::map<int, int> group_blocks, group_index;
+    for (int i = 0; i < n; ++i) {
+        rsrgpu_ctx* c = b->frames[size_t(i)];
+        FrameView probe{};
+        probe.tile_w = c->tile_w; probe.tile_h = c->tile_h; probe.ntiles = c->ntiles;
+        probe.region_px = std::min(c->region_px, std::min(c->tile_w, c->tile_h));
+        group_blocks[raster_threads(probe)] += raster_blocks(probe);
+    }
+    size_t queue_entries = 0;
+    std::map<int, size_t> group_queue;
+    for (auto& kv : group_blocks) {
+        group_index[kv.first] = int(group_index.size());
+        group_queue[kv.first] = queue_entries;
+        queue_entries += size_t(kCostBuckets) * size_t(kv.second);
+    }
+    BCK(b->d_queue.ensure(sizeof(uint32_t) * std::max<size_t>(queue_entries, 1)), "alloc batch work queues");
+    const int ngroups = int(group_blocks.size());
+    BCK(b->d_counters.ensure(sizeof(FrameCounters) * size_t(n + ngroups)), "alloc batch counters");
     for (int i = 0; i < n; ++i) {
         rsrgpu_ctx* c = b->frames[size_t(i)];
         std::memcpy(b->h_tables + b->off_states[size_t(i)], c->states.data(), sizeof(DevState) * c->states.size());
         if (!c->draws.empty()) std::memcpy(b->h_tables + b->off_draws[size_t(i)], c->draws.data(), sizeof(DevDraw) * c->draws.size());
         if (!c->ops.empty()) std::memcpy(b->h_tables + b->off_ops[size_t(i)], c->ops.data(), sizeof(FrameOp) * c->ops.size());
         if (!c->gbufs.empty()) std::memcpy(b->h_tables + b->off_gbufs[size_t(i)], c->gbufs.data(), sizeof(GBufferDesc) * c->gbufs.size());
+        if (c->any_dext) std::memcpy(b->h_tables + b->off_dext[size_t(i)], c->dext.data(), sizeof(DevDrawExt) * c->dext.size());
         ViewTables vt{ reinterpret_cast<DevState*>(dt + b->off_states[size_t(i)]),
                        reinterpret_cast<DevDraw*>(dt + b->off_draws[size_t(i)]),
                        reinterpret_cast<FrameOp*>(dt + b->off_ops[size_t(i)]),
                        reinterpret_cast<GBufferDesc*>(dt + b->off_gbufs[size_t(i)]),
                        b->d_counters.as<FrameCounters>() + i,
-                       b->d_super.as<int4>() + b->off_super[size_t(i)] };
+                       b->d_super.as<int4>() + b->off_super[size_t(i)],
+                       reinterpret_cast<DevDrawExt*>(dt + b->off_dext[size_t(i)]) };
         int rc = prepare_view(c, &vt);
         if (rc) { b->err = c->err; return rc; }
-        const FrameView& fv = c->fv;
-        setup[0].start[i] = sblocks; setup[0].fv[i] = fv; sblocks += setup_blocks(fv);
-        bin[0].start[i] = bblocks; bin[0].fv[i] = fv; bblocks += bin_blocks(fv);
+        FrameView& fv = c->fv;
         const int th = raster_threads(fv);
         BatchLaunch& rl = raster[th];
         int& rb = rblocks[th];
+        fv.tile_queue = b->d_queue.as<uint32_t>() + group_queue[th] + size_t(kCostBuckets) * size_t(rb);
+        fv.taken = b->d_counters.as<FrameCounters>() + n + group_index[th];
+        setup[0].start[i] = sblocks; setup[0].fv[i] = fv; sblocks += setup_blocks(fv);
+        bin[0].start[i] = bblocks; bin[0].fv[i] = fv; bblocks += bin_blocks(fv);
         rl.start[rl.nframes] = rb;
         rl.fv[rl.nframes] = fv;
         rl.nframes++;
@@ -1969,7 +2006,7 @@ int build_batch(rsrgpu_batch* b) {
         if (rc == 0 && e != cudaSuccess) rc = bfail(b, RSRGPU_ECUDA, "%s: %s", what, cudaGetErrorString(e));
     };
     step(cudaMemcpyAsync(b->d_tables.p, b->h_tables, b->tables_bytes, cudaMemcpyHostToDevice, st), "H2D tables");
-    step(cudaMemsetAsync(b->d_counters.p, 0, sizeof(FrameCounters) * size_t(n), st), "memset counters");
+    step(cudaMemsetAsync(b->d_counters.p, 0, sizeof(FrameCounters) * size_t(n + ngroups), st), "memset counters");
     step(cudaMemsetAsync(b->d_super.p, 0x7f, sizeof(int4) * b->super_count, st), "memset super rects");
     step(launch_setup_batch(setup[0], sblocks, st), "setup_batch_kernel");
     step(launch_bin_batch(bin[0], bblocks, st), "bin_batch_kernel");
@@ -2037,7 +2074,7 @@ int rsrgpu_batch_destroy(rsrgpu_batch* b) {
     for (rsrgpu_ctx* c : b->frames) rsrgpu_destroy(c);
     if (b->h_tables) cudaFreeHost(b->h_tables);
     if (b->h_counters) cudaFreeHost(b->h_counters);
-    b->d_tables.release(); b->d_counters.release(); b->d_super.release();
+    b->d_tables.release(); b->d_counters.release(); b->d_super.release(); b->d_queue.release();
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->fork) cudaEventDestroy(b->fork);

@@ -143,17 +143,18 @@ struct ClipInfo {         // per source triangle (valid when nverts > 0)
 
 // frame-global counters, cleared at the start of every run
 // Tiles go to the raster pass heaviest first (rsr sorts its tile jobs by
-// stream length, rglv_gpu.cxx:100-104): binning files each tile in the
-// bucket of its list length's power of two, the raster CTAs take work items
-// from a counter, highest bucket first.
+// stream length, rglv_gpu.cxx:100-104): binning files each tile's raster
+// blocks in the bucket of its list length's power of two, the raster CTAs
+// take work items from a counter, highest bucket first.  In a batch the
+// items of a raster launch run frame by frame, each frame's heaviest first.
 constexpr int kCostBuckets = 16;
 
 struct FrameCounters {
     uint32_t clip_verts;      // staging vertices allocated
     uint32_t bin_used;        // tile-list entries allocated
     uint32_t overflow;        // bit 0: clip staging, bit 1: bin pool, bit 2: vertex index out of range
-    uint32_t next_item;       // raster work items taken (the work queue)
-    uint32_t bucket[kCostBuckets];   // tiles filed per cost bucket
+    uint32_t next_item;       // raster work items taken (the frame's, or in a batch the launch's)
+    uint32_t bucket[kCostBuckets];   // the frame's raster blocks filed per cost bucket
 };
 
 struct TileBin {
@@ -201,7 +202,10 @@ struct FrameView {
     int32_t keys_resume_op;   // vis_keys frames: the first op after the last draw (0: not given)
     int32_t keys_resume_state_op; // the last state op before it
     FrameCounters* host_counters; // pinned host copy of *counters, written by the raster pass (or null)
-    uint32_t* tile_queue;     // [kCostBuckets][ntiles] tiles by cost bucket; null: CTA b draws item b
+    uint32_t* tile_queue;     // [kCostBuckets][queue_cap] the frame's raster blocks by cost bucket
+                              // (counts in counters->bucket); null: CTA b draws block b
+    uint32_t queue_cap;       // the frame's raster blocks
+    FrameCounters* taken;     // next_item of the raster launch: the frame's counters, or its batch launch's
     const DevDrawExt* dext;   // per draw, for frames with instanced or OBJ1Program draws (setup_ext_kernel); else null
 };
 

@@ -189,13 +189,20 @@ __device__ __forceinline__ bool rect_has(uint64_t r, int tx, int ty) {
     return x0 <= tx && tx <= x1 && y0 <= ty && ty <= y1;
 }
 
-// files a binned tile in the raster pass's work queue (bucket: the power of
-// two of its list length)
+// raster blocks (CTA regions) per tile
+__device__ __forceinline__ int raster_subs(const FrameView& fv) {
+    return ((fv.tile_w + fv.region_px - 1) / fv.region_px) * ((fv.tile_h + fv.region_px - 1) / fv.region_px);
+}
+
+// files a binned tile's raster blocks in the raster pass's work queue
+// (bucket: the power of two of the tile's list length); one thread
 __device__ __forceinline__ void enqueue_tile(const FrameView& fv, int tile, uint32_t cost) {
     if (fv.tile_queue == nullptr) return;
     const int b = min(kCostBuckets - 1, 32 - __clz(int(cost)));
-    const uint32_t pos = atomicAdd(&fv.counters->bucket[b], 1u);
-    fv.tile_queue[size_t(b) * size_t(fv.ntiles) + pos] = uint32_t(tile);
+    const int subs = raster_subs(fv);
+    const uint32_t pos = atomicAdd(&fv.counters->bucket[b], uint32_t(subs));
+    uint32_t* row = fv.tile_queue + size_t(b) * size_t(fv.queue_cap) + pos;
+    for (int k = 0; k < subs; ++k) row[k] = uint32_t(tile * subs + k);
 }
 
 __device__ __forceinline__ int find_draw(const DevDraw* __restrict__ draws, int ndraws, int g) {
@@ -862,20 +869,21 @@ struct TriSetup {
 };
 
 // structure of arrays in shared memory, one batch of triangles
+template <int N>
 struct RasterSmem {
-    int32_t minx[kRasterBatch], miny[kRasterBatch], maxx[kRasterBatch], maxy[kRasterBatch];
-    int32_t c1[kRasterBatch], c2[kRasterBatch], c3[kRasterBatch];
-    int32_t dy12[kRasterBatch], dx12[kRasterBatch], dy23[kRasterBatch], dx23[kRasterBatch];
-    int32_t dy31[kRasterBatch], dx31[kRasterBatch];
-    float scale[kRasterBatch];
-    float z[3][kRasterBatch], w[3][kRasterBatch];
-    float vary[3][kMaxVary][kRasterBatch];
-    uint32_t code[kRasterBatch];   // fragment owner: triangle id, or clipped fan id | bit 31
-    uint32_t order[kRasterBatch];  // visibility by keys: the entry's drawing order (see frag_key)
+    int32_t minx[N], miny[N], maxx[N], maxy[N];
+    int32_t c1[N], c2[N], c3[N];
+    int32_t dy12[N], dx12[N], dy23[N], dx23[N];
+    int32_t dy31[N], dx31[N];
+    float scale[N];
+    float z[3][N], w[3][N];
+    float vary[3][kMaxVary][N];
+    uint32_t code[N];   // fragment owner: triangle id, or clipped fan id | bit 31
+    uint32_t order[N];  // visibility by keys: the entry's drawing order (see frag_key)
     FrameOp ops[kOpCache];         // the frame's ops, when they fit
     int32_t dfirst[kOpCache];      // the draws' first triangles, when they fit
-    uint8_t big[kRasterBatch];     // visibility by keys: the triangle covers many quads of the region
-    uint32_t zr[kRasterBatch];     // visibility by keys: a depth rank no covered pixel of the triangle goes below
+    uint8_t big[N];     // visibility by keys: the triangle covers many quads of the region
+    uint32_t zr[N];     // visibility by keys: a depth rank no covered pixel of the triangle goes below
                                    // (0 where no such bound is known)
     int qsum;                      // visibility by keys: the batch's boxes, in quads of the region
 };
@@ -938,7 +946,8 @@ __device__ __forceinline__ void setup_scalar(TriSetup& t, const int rect[4],
     t.scale = __fdiv_rn(1.0f, __ll2float_rn(c1 + c2 + c3));
 }
 
-__device__ __forceinline__ void put_setup(RasterSmem& S, int i, const TriSetup& t) {
+template <int N>
+__device__ __forceinline__ void put_setup(RasterSmem<N>& S, int i, const TriSetup& t) {
     S.minx[i] = t.minx; S.miny[i] = t.miny; S.maxx[i] = t.maxx; S.maxy[i] = t.maxy;
     S.c1[i] = t.c1; S.c2[i] = t.c2; S.c3[i] = t.c3;
     S.dy12[i] = t.dy12; S.dx12[i] = t.dx12; S.dy23[i] = t.dy23; S.dx23[i] = t.dx23;
@@ -1123,8 +1132,8 @@ constexpr uint32_t kKeyPosBits = 19;   // the list-position bits of a key's orde
 // resolve pass: the triangle that last wrote a pixel is set up again exactly
 // as when it was rasterised.
 template <bool kScissor>
-__device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
-                                         float w[3], float vary[3][kMaxVary], int& state) {
+__device__ __forceinline__ void owner_setup_inline(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
+                                                   float w[3], float vary[3][kMaxVary], int& state) {
     const int g = (code & kClippedBit) ? fv.clip_src[fv.clip_poly[code & ~kClippedBit]] : int(code);
     int rect[4] = { tile[0], tile[1], tile[2], tile[3] };
     if (kScissor && fv.any_scissor) {   // the draw's rectangle depends on its state
@@ -1152,6 +1161,12 @@ __device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, con
         }
     }
     if (!(kScissor && fv.any_scissor)) state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+}
+// the raster kernels call it out of line (their register budget)
+template <bool kScissor>
+__device__ __noinline__ void owner_setup(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
+                                         float w[3], float vary[3][kMaxVary], int& state) {
+    owner_setup_inline<kScissor>(fv, code, tile, t, w, vary, state);
 }
 
 // perspective-correct barycentrics of one lane (TriangleProgram::Render,
@@ -1185,6 +1200,36 @@ __device__ __forceinline__ void quad_put_rgb(float col[4][3], int l, float r, fl
     else { col[3][0] = r; col[3][1] = g; col[3][2] = b; }
 }
 
+// The colour of lane l of the quad at (qx, qy), shaded by its owning
+// triangle (set up by owner_setup) with the owner's program.
+template <bool kExt>
+__device__ __forceinline__ void owner_color(const FrameView& fv, const TriSetup& t, const float w[3],
+                                            const float vary[3][kMaxVary], int state, int qx, int qy, int l, float c[3]) {
+    const DevState& s = fv.states[state];
+    float bpx, bpy, bpz;
+    lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
+    if (s.program == kProgAmy) {
+        float b0x, b0y, b0z, b1x, b1y, b1z;
+        lane_bary(fv, t, w, qx, qy, 0, b0x, b0y, b0z);
+        lane_bary(fv, t, w, qx, qy, 1, b1x, b1y, b1z);
+        const float u0 = (b0x * vary[0][0] + b0y * vary[1][0]) + b0z * vary[2][0];
+        const float v0 = (b0x * vary[0][1] + b0y * vary[1][1]) + b0z * vary[2][1];
+        const float u1 = (b1x * vary[0][0] + b1y * vary[1][0]) + b1z * vary[2][0];
+        const float v1 = (b1x * vary[0][1] + b1y * vary[1][1]) + b1z * vary[2][1];
+        const float ul = (bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0];
+        const float vl = (bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1];
+        float o[4];
+        const DevTexture tu = s.tu0;
+        tex_sample_lane(tu, u0, v0, u1, v1, ul, vl, o);
+        c[0] = o[0]; c[1] = o[1]; c[2] = o[2];
+    } else {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) c[q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
+        // ManyProgram::ShadeFragment (shaders.hxx:567-582): (u, v, magic, 1)
+        if (kExt && s.program == kProgMany) c[2] = s.uniforms[0];
+    }
+}
+
 template <bool kExt, bool kScissor>
 __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect[4], int qx, int qy,
                                              uint32_t own[4], float col[4][3]) {
@@ -1200,31 +1245,9 @@ __device__ __forceinline__ void resolve_quad(const FrameView& fv, const int rect
             cur = ol;
             owner_setup<kScissor>(fv, cur, rect, t, w, vary, state);
         }
-        const DevState& s = fv.states[state];
-        float bpx, bpy, bpz;
-        lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
-        if (s.program == kProgAmy) {
-            float b0x, b0y, b0z, b1x, b1y, b1z;
-            lane_bary(fv, t, w, qx, qy, 0, b0x, b0y, b0z);
-            lane_bary(fv, t, w, qx, qy, 1, b1x, b1y, b1z);
-            const float u0 = (b0x * vary[0][0] + b0y * vary[1][0]) + b0z * vary[2][0];
-            const float v0 = (b0x * vary[0][1] + b0y * vary[1][1]) + b0z * vary[2][1];
-            const float u1 = (b1x * vary[0][0] + b1y * vary[1][0]) + b1z * vary[2][0];
-            const float v1 = (b1x * vary[0][1] + b1y * vary[1][1]) + b1z * vary[2][1];
-            const float ul = (bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0];
-            const float vl = (bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1];
-            float o[4];
-            const DevTexture tu = s.tu0;
-            tex_sample_lane(tu, u0, v0, u1, v1, ul, vl, o);
-            quad_put_rgb(col, l, o[0], o[1], o[2]);
-        } else {
-            float c[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) c[q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
-            // ManyProgram::ShadeFragment (shaders.hxx:567-582): (u, v, magic, 1)
-            if (kExt && s.program == kProgMany) c[2] = s.uniforms[0];
-            quad_put_rgb(col, l, c[0], c[1], c[2]);
-        }
+        float c[3];
+        owner_color<kExt>(fv, t, w, vary, state, qx, qy, l, c);
+        quad_put_rgb(col, l, c[0], c[1], c[2]);
     }
 #pragma unroll
     for (int l = 0; l < 4; ++l) own[l] = kNoOwner;
@@ -1271,7 +1294,8 @@ __device__ __forceinline__ unsigned long long clear_key(float z, bool leq) {
 // wrap in the tile: |c| + |dy| (tile width + 2) + |dx| (tile height + 2) below
 // 2^31 for every edge), so every fragment depth
 // (bx z0 + by z1) + bz z2 is at least min(z) - 2^-18 max|z|.
-__device__ __forceinline__ uint32_t tri_min_rank(const RasterSmem& S, int i, int tw, int th) {
+template <int N>
+__device__ __forceinline__ uint32_t tri_min_rank(const RasterSmem<N>& S, int i, int tw, int th) {
     const float scale = S.scale[i];
     if (!(scale > 0.0f && scale <= 3.4e38f)) return 0u;
     const float z0 = S.z[0][i], z1 = S.z[1][i], z2 = S.z[2][i];
@@ -1298,7 +1322,8 @@ __device__ __forceinline__ bool edge_outside(int32_t c, int32_t dy, int32_t dx, 
     return hi < 0 && lo >= -(1ll << 31);
 }
 // Batch triangle i covers no pixel of [x0, x1) x [y0, y1) (pixel coordinates).
-__device__ __forceinline__ bool footprint_outside(const RasterSmem& S, int i, int x0, int y0, int x1, int y1) {
+template <int N>
+__device__ __forceinline__ bool footprint_outside(const RasterSmem<N>& S, int i, int x0, int y0, int x1, int y1) {
     const int32_t kx0 = x0 - S.minx[i], kx1 = x1 - 1 - S.minx[i];
     const int32_t ky0 = y0 - S.miny[i], ky1 = y1 - 1 - S.miny[i];
     return edge_outside(S.c1[i], S.dy12[i], S.dx12[i], kx0, ky0, kx1, ky1) ||
@@ -1318,7 +1343,8 @@ __device__ __forceinline__ uint32_t warp_max_rank(const unsigned long long kq[4]
 }
 
 // Quads of the region [rx0, rx1) x [ry0, ry1) in batch triangle i's box.
-__device__ __forceinline__ int region_quads(const RasterSmem& S, int i, int rx0, int ry0, int rx1, int ry1) {
+template <int N>
+__device__ __forceinline__ int region_quads(const RasterSmem<N>& S, int i, int rx0, int ry0, int rx1, int ry1) {
     const int x0 = max(S.minx[i], rx0), x1 = min(S.maxx[i], rx1);
     const int y0 = max(S.miny[i], ry0), y1 = min(S.maxy[i], ry1);
     return x0 < x1 && y0 < y1 ? ((x1 - x0 + 1) >> 1) * ((y1 - y0 + 1) >> 1) : 0;
@@ -1327,7 +1353,8 @@ __device__ __forceinline__ int region_quads(const RasterSmem& S, int i, int rx0,
 // Coverage and depth of the pixels of quad (qx, qy) for batch triangle i,
 // with the arithmetic of the lockstep loop in raster_body; false (and no
 // depths) when the triangle covers none of them.
-__device__ __forceinline__ bool batch_quad(const RasterSmem& S, int i, int qx, int qy, bool inside[4], float fz[4]) {
+template <int N>
+__device__ __forceinline__ bool batch_quad(const RasterSmem<N>& S, int i, int qx, int qy, bool inside[4], float fz[4]) {
     const int32_t kx = qx - S.minx[i], ky = qy - S.miny[i];
     const int32_t dy12 = S.dy12[i], dx12 = S.dx12[i];
     const int32_t dy23 = S.dy23[i], dx23 = S.dx23[i];
@@ -1357,7 +1384,8 @@ __device__ __forceinline__ bool batch_quad(const RasterSmem& S, int i, int qx, i
 
 // The keys of quad (qx, qy) for batch triangle i, by atomicMin: other lanes
 // may update the same pixels.
-__device__ __forceinline__ void key_quad(const RasterSmem& S, unsigned long long* keys, int rx0, int ry0, int rw,
+template <int N>
+__device__ __forceinline__ void key_quad(const RasterSmem<N>& S, unsigned long long* keys, int rx0, int ry0, int rw,
                                          int i, int qx, int qy, uint32_t order, bool leq) {
     bool inside[4];
     float fz[4];
@@ -1372,7 +1400,8 @@ __device__ __forceinline__ void key_quad(const RasterSmem& S, unsigned long long
 }
 
 // The same for the lane's own quad, whose keys it holds in registers.
-__device__ __forceinline__ void key_quad_own(const RasterSmem& S, unsigned long long kq[4], int i, int qx, int qy,
+template <int N>
+__device__ __forceinline__ void key_quad_own(const RasterSmem<N>& S, unsigned long long kq[4], int i, int qx, int qy,
                                              uint32_t order, bool leq) {
     bool inside[4];
     float fz[4];
@@ -1415,8 +1444,12 @@ __device__ __noinline__ float owner_depth(const FrameView& fv, uint32_t code, co
 // ManyProgram draws; frames without them run the instantiation that has no
 // code for them.  kScissor: the instantiation for frames with scissored
 // draws (the others keep the draw rectangle, the tile, out of registers).
-template <bool kExt, bool kScissor>
-__device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem& S) {
+// kPhase 0: the pass of FrameView::raster_phase (0 whole, 1 or 2 a split
+// pass's launch); kPhase 1 / 2: compiled for one launch of a split pass of an
+// opaque frame (visibility only, or shading and stores only), whose smaller
+// register demand lets more CTAs share an SM.
+template <bool kExt, bool kScissor, int kPhase = 0, int N>
+__device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem<N>& S) {
     if (fv.counters->overflow != 0u) return;
 
     const int region = fv.region_px;
@@ -1455,7 +1488,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
     FragState fs{};   // every frame starts with a state op
     // visibility by keys (see frag_key): decided at the first draw, resolved
     // into own / dep before the first store
-    __shared__ unsigned long long keys[32 * 32];
+    __shared__ unsigned long long keys[4 * N];   // one per pixel of the region (a quad per thread)
     const int rw = rx1 - rx0;
     const bool leq = fv.vis_keys == 2;
     int key_state = 0;   // 0 not decided, 1 keys in use, 2 not used, 3 resolved
@@ -1476,7 +1509,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             load_frag_state(fv, o, fs);
             continue;
         }
-        if (key_state == 1 && o.kind != kOpDraw && o.kind != kOpState) {
+        if (kPhase != 2 && key_state == 1 && o.kind != kOpDraw && o.kind != kOpState) {
             // owners and depths from the keys
             __syncthreads();
             if (active) {
@@ -1499,9 +1532,9 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         // depth and hands over the owners and depths at its end; the second
         // replays states and clears, skips the draws and depth stores, takes
         // the owners and depths at the first store and shades.
-        if (fv.raster_phase != 0 && op_is_store(o.kind)) {
-            if (fv.raster_phase == 1 && o.kind != kOpStoreDepth) continue;
-            if (fv.raster_phase == 2) {
+        if ((kPhase != 0 || fv.raster_phase != 0) && op_is_store(o.kind)) {
+            if ((kPhase == 1 || fv.raster_phase == 1) && o.kind != kOpStoreDepth) continue;
+            if (kPhase == 2 || fv.raster_phase == 2) {
                 if (phase_pending) {
                     if (active) {
 #pragma unroll
@@ -1521,7 +1554,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         // that fragment's owner and shade it once; anything that reads or
         // replaces colour first resolves the pending pixels.
         const bool visibility = o.kind == kOpDraw && !fs.blend;
-        if (!visibility && o.kind != kOpStoreGBuffer && pending && fv.raster_phase != 1) {
+        if (kPhase != 1 && !visibility && o.kind != kOpStoreGBuffer && pending && fv.raster_phase != 1) {
             if (active) resolve_quad<kExt, kScissor>(fv, rect, qx, qy, own, col);
             pending = false;
         }
@@ -1540,7 +1573,17 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             int drect[4] = { rect[0], rect[1], rect[2], rect[3] };   // the tile, or its part inside the scissor rectangle
             if (kScissor && fv.any_scissor) draw_rect(fv.states[o.info[2]], rect, drect);
             if (visibility) pending = true;
-            if (fv.raster_phase == 2) continue;   // drawn by the first launch
+            if (kPhase == 2 || fv.raster_phase == 2) {   // drawn by the first launch
+                // the frame's draws are all opaque: none needs a visit, so
+                // jump to the op after the last, in the state it leaves
+                if (fv.keys_resume_op > op) {
+                    op = fv.keys_resume_op - 1;
+                    const FrameOp so = ops_cached ? S.ops[fv.keys_resume_state_op] : fv.ops[fv.keys_resume_state_op];
+                    cur_state = so.arg;
+                    load_frag_state(fv, so, fs);
+                }
+                continue;
+            }
             if (key_state == 0) {
                 bool ok = fv.vis_keys != 0 && bin.inl_cnt < (1u << kKeyPosBits) && bin.clip_cnt < (1u << kKeyPosBits);
                 if (active) {
@@ -1752,6 +1795,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                                 for (int l = 0; l < 4; ++l) if (mask[l]) own[l] = code;
                                 continue;
                             }
+                            if (kPhase == 1) continue;   // split passes are of opaque frames: never reached
                             // immediate shading (blending draws)
                             const float w0 = S.w[0][i], w1 = S.w[1][i], w2 = S.w[2][i];
                             float bpx[4], bpy[4], bpz[4];
@@ -1903,7 +1947,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             }
         }
     }
-    if (fv.raster_phase == 1 && active) {   // the hand-over to the second launch
+    if ((kPhase == 1 || fv.raster_phase == 1) && active) {   // the hand-over to the second launch
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
             const size_t i = size_t(qy + (l >> 1)) * size_t(fv.width) + size_t(qx + (l & 1));
@@ -1936,59 +1980,134 @@ __global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ 
 __device__ __forceinline__ void publish_counters(const FrameView& fv) {
     if (fv.host_counters != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *fv.host_counters = *fv.counters;
 }
-// The raster work items (tile, region) of a frame with a work queue: a
-// persistent grid takes them from a counter, the tiles' regions in the
-// order of their cost buckets, heaviest first.  Without a queue, CTA b draws
-// item b.
-template <bool kExt, bool kScissor>
-__device__ __forceinline__ void raster_items(const FrameView& fv, RasterSmem& S) {
+// A frame's work queue, read by thread 0 of a raster CTA: bucket_end[b] is
+// the number of entries in the buckets from the heaviest down to b, and the
+// k-th item is the k-th entry in that order (-1 past the filed entries: a
+// tile that was never filed draws nothing).
+__device__ __forceinline__ void load_bucket_ends(const FrameView& fv, int* bucket_end) {
+    int sum = 0;
+    for (int b = kCostBuckets - 1; b >= 0; --b) bucket_end[b] = (sum += int(fv.counters->bucket[b]));
+}
+__device__ __forceinline__ int queue_entry(const FrameView& fv, const int* bucket_end, int k) {
+    int b = kCostBuckets - 1;
+    while (b > 0 && k >= bucket_end[b]) --b;
+    if (k >= bucket_end[b]) return -1;
+    const int first = b == kCostBuckets - 1 ? 0 : bucket_end[b + 1];
+    return int(fv.tile_queue[size_t(b) * size_t(fv.queue_cap) + size_t(k - first)]);
+}
+// The raster blocks of a frame: a persistent grid takes them from the work
+// queue, heaviest tiles first, until it is empty; without a queue, CTA b
+// draws block b.
+template <bool kExt, bool kScissor, int kPhase = 0, int N>
+__device__ __forceinline__ void raster_items(const FrameView& fv, RasterSmem<N>& S) {
     if (fv.tile_queue == nullptr) {
-        raster_body<kExt, kScissor>(fv, blockIdx.x, S);
+        raster_body<kExt, kScissor, kPhase>(fv, blockIdx.x, S);
         return;
     }
-    __shared__ int item_tile, item_sub;
-    __shared__ int bucket_end[kCostBuckets];   // tiles in the buckets from the heaviest down to b
-    const int subs = ((fv.tile_w + fv.region_px - 1) / fv.region_px) * ((fv.tile_h + fv.region_px - 1) / fv.region_px);
-    const int nitems = fv.ntiles * subs;
-    if (threadIdx.x == 0) {
-        int sum = 0;
-        for (int b = kCostBuckets - 1; b >= 0; --b) bucket_end[b] = (sum += int(fv.counters->bucket[b]));
-    }
+    __shared__ int item;
+    __shared__ int bucket_end[kCostBuckets];
+    if (threadIdx.x == 0) load_bucket_ends(fv, bucket_end);
     while (true) {
         __syncthreads();   // the previous item is done with the shared state
         if (threadIdx.x == 0) {
-            const int i = int(atomicAdd(&fv.counters->next_item, 1u));
-            int tile = -1;
-            if (i < nitems) {
-                const int rank = i / subs;
-                int b = kCostBuckets - 1;
-                while (b > 0 && rank >= bucket_end[b]) --b;
-                if (rank < bucket_end[b]) {
-                    const int first = b == kCostBuckets - 1 ? 0 : bucket_end[b + 1];
-                    tile = int(fv.tile_queue[size_t(b) * size_t(fv.ntiles) + size_t(rank - first)]);
-                }
-            }
-            item_tile = i < nitems ? tile : -2;
-            item_sub = i % subs;
+            const int i = int(atomicAdd(&fv.taken->next_item, 1u));
+            item = i < int(fv.queue_cap) ? queue_entry(fv, bucket_end, i) : -2;   // -2: empty
         }
         __syncthreads();
-        const int tile = item_tile, sub = item_sub;
-        if (tile == -2) return;
-        if (tile >= 0) raster_body<kExt, kScissor>(fv, tile * subs + sub, S);
+        const int e = item;
+        if (e == -2) return;
+        if (e >= 0) raster_body<kExt, kScissor, kPhase>(fv, e, S);
     }
 }
-__global__ void __launch_bounds__(256, 2) raster_kernel(const __grid_constant__ FrameView fv) {
-    __shared__ RasterSmem S;
+// Raster kernels are compiled for CTAs of N threads (one 2x2 quad each): 256
+// for 32 px regions, 64 for 16 and 8 px regions, with shared memory for
+// batches of N triangles, so that small CTAs are not held to the large ones'
+// shared-memory share of an SM.  kRasterCtas: CTAs per SM the launch bounds
+// allow (registers).
+template <int N> constexpr int raster_ctas(int per256) { return N == 256 ? per256 : per256 * 4; }
+
+// The split pass of an opaque frame without float stores, ManyProgram draws or
+// scissor: visibility (80 registers), then shading.
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(3)) raster_vis_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem<N> S;
+    raster_items<false, false, 1>(fv, S);
+}
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_shade_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem<N> S;
+    publish_counters(fv);
+    raster_items<false, false, 2>(fv, S);
+}
+// The shading launch of a split pass, one thread per pixel, for an opaque
+// frame whose ops after its last draw are state changes and TrueColor and
+// depth stores (no float stores, ManyProgram draws or scissor): the pixel's
+// colour is the clear colour or its owner's (as resolve_quad shades it), then
+// the stores run in op order.  32x8 pixels per CTA: a warp stores 128
+// contiguous bytes of a row (outputs may be mapped host memory).
+constexpr int kPixelW = 32, kPixelH = 8;
+__global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const __grid_constant__ FrameView fv) {
+    publish_counters(fv);
+    if (fv.counters->overflow != 0u) return;
+    const int x = blockIdx.x * kPixelW + (threadIdx.x % kPixelW);
+    const int y = blockIdx.y * kPixelH + (threadIdx.x / kPixelW);
+    if (x >= (fv.width & ~1) || y >= (fv.height & ~1)) return;   // the pixels of whole quads, as the raster pass
+    const size_t i = size_t(y) * size_t(fv.width) + size_t(x);
+    const uint32_t own = fv.vis_own[i];
+    const float dep = fv.vis_dep[i];
+    // the colour: the last colour clear before the first draw, or the owner's
+    float c[3] = { 0.0f, 0.0f, 0.0f };
+    for (int op = 0; op < fv.nops; ++op) {
+        const FrameOp o = fv.ops[op];
+        if (o.kind == kOpDraw) break;
+        if (o.kind == kOpClear && (o.info[2] != 0 || (o.arg & 1))) { c[0] = o.val[0]; c[1] = o.val[1]; c[2] = o.val[2]; }
+    }
+    if (own != kNoOwner) {
+        const int tx = x / fv.tile_w, ty = y / fv.tile_h;
+        const int rect[4] = { tx * fv.tile_w, ty * fv.tile_h, min(tx * fv.tile_w + fv.tile_w, fv.width),
+                              min(ty * fv.tile_h + fv.tile_h, fv.height) };
+        TriSetup t;
+        float w[3], vary[3][kMaxVary];
+        int state = 0;
+        owner_setup_inline<false>(fv, own, rect, t, w, vary, state);
+        owner_color<false>(fv, t, w, vary, state, x & ~1, y & ~1, (x & 1) | ((y & 1) << 1), c);
+    }
+    int cur_state = fv.ops[fv.keys_resume_state_op].arg;
+    for (int op = fv.keys_resume_op; op < fv.nops; ++op) {
+        const FrameOp o = fv.ops[op];
+        if (o.kind == kOpState) {
+            cur_state = o.arg;
+        } else if (o.kind == kOpStoreTC) {
+            // GPUBltImpl::StoreTrueColor -> FilterTile (rglr_algorithm.hxx:31-104), as raster_body
+            const DevState& s = fv.states[cur_state];
+            float c3[3] = { c[0], c[1], c[2] };
+            if (s.program == kProgExposurePost) {
+                const float ex = s.uniforms[0];
+                c3[0] = c3[0] * ex; c3[1] = c3[1] * ex; c3[2] = c3[2] * ex;
+            }
+            const uint32_t px = o.arg ? (srgb8(fv.srgb_lut, c3[0]) << 16) | (srgb8(fv.srgb_lut, c3[1]) << 8) | srgb8(fv.srgb_lut, c3[2])
+                                      : (basic8(c3[0]) << 16) | (basic8(c3[1]) << 8) | basic8(c3[2]);
+            static_cast<uint32_t*>(o.ptr)[size_t(y) * o.stride + x] = px;
+        } else if (o.kind == kOpStoreDepth) {
+            static_cast<float*>(o.ptr)[size_t(y) * o.stride + x] = dep;
+        }
+    }
+}
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem<N> S;
     publish_counters(fv);
     raster_items<false, false>(fv, S);
 }
-__global__ void __launch_bounds__(256, 2) raster_scissor_kernel(const __grid_constant__ FrameView fv) {
-    __shared__ RasterSmem S;
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_scissor_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem<N> S;
     publish_counters(fv);
     raster_items<false, true>(fv, S);
 }
-__global__ void __launch_bounds__(256, 2) raster_ext_kernel(const __grid_constant__ FrameView fv) {
-    __shared__ RasterSmem S;
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_ext_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ RasterSmem<N> S;
     publish_counters(fv);
     raster_items<true, true>(fv, S);
 }
@@ -2006,20 +2125,71 @@ __global__ void __launch_bounds__(kSetupBlock) setup_batch_kernel(const __grid_c
     const int f = batch_frame(b, blockIdx.x);
     setup_body<false>(b.fv[f], blockIdx.x - b.start[f]);
 }
+// batches with a frame of instanced or OBJ1Program draws: the extended setup
+// for those frames, the plain one for the others
+__global__ void __launch_bounds__(kSetupBlock) setup_batch_ext_kernel(const __grid_constant__ BatchLaunch b) {
+    const int f = batch_frame(b, blockIdx.x);
+    if (b.fv[f].dext != nullptr) setup_body<true>(b.fv[f], blockIdx.x - b.start[f]);
+    else setup_body<false>(b.fv[f], blockIdx.x - b.start[f]);
+}
 __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ BinShared S;
     const int f = batch_frame(b, blockIdx.x);
     bin_body(b.fv[f], blockIdx.x - b.start[f], S);
 }
-__global__ void __launch_bounds__(256, 2) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
-    __shared__ RasterSmem S;
-    const int f = batch_frame(b, blockIdx.x);
-    raster_body<false, false>(b.fv[f], blockIdx.x - b.start[f], S);
+// The raster blocks of a batch launch's frames: a persistent grid takes the
+// launch's items from one counter, frame after frame in launch order (a
+// frame's triangle records and tile lists stay in L2 while its tiles are
+// drawn), each frame's tiles heaviest first; without queues, CTA b draws
+// block b.
+template <bool kExt, bool kScissor, int N>
+__device__ __forceinline__ void raster_batch_items(const BatchLaunch& b, RasterSmem<N>& S) {
+    if (b.fv[0].tile_queue == nullptr) {
+        const int f = batch_frame(b, blockIdx.x);
+        raster_body<kExt, kScissor>(b.fv[f], blockIdx.x - b.start[f], S);
+        return;
+    }
+    __shared__ int item, item_frame, cached_frame;
+    __shared__ int bucket_end[kCostBuckets];   // of cached_frame
+    if (threadIdx.x == 0) cached_frame = -1;
+    while (true) {
+        __syncthreads();   // the previous item is done with the shared state
+        if (threadIdx.x == 0) {
+            const int i = int(atomicAdd(&b.fv[0].taken->next_item, 1u));
+            int e = -2, f = 0;   // -2: empty
+            if (i < b.start[b.nframes]) {
+                f = batch_frame(b, i);
+                if (f != cached_frame) {
+                    load_bucket_ends(b.fv[f], bucket_end);
+                    cached_frame = f;
+                }
+                e = queue_entry(b.fv[f], bucket_end, i - b.start[f]);
+            }
+            item = e;
+            item_frame = f;
+        }
+        __syncthreads();
+        const int e = item;
+        if (e == -2) return;
+        if (e >= 0) raster_body<kExt, kScissor>(b.fv[item_frame], e, S);
+    }
 }
-__global__ void __launch_bounds__(256, 2) raster_batch_scissor_kernel(const __grid_constant__ BatchLaunch b) {
-    __shared__ RasterSmem S;
-    const int f = batch_frame(b, blockIdx.x);
-    raster_body<false, true>(b.fv[f], blockIdx.x - b.start[f], S);
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ RasterSmem<N> S;
+    raster_batch_items<false, false>(b, S);
+}
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_batch_scissor_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ RasterSmem<N> S;
+    raster_batch_items<false, true>(b, S);
+}
+// launches with a frame of float colour stores or ManyProgram draws (the
+// code of raster_ext_kernel, which renders the other frames alike)
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_batch_ext_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ RasterSmem<N> S;
+    raster_batch_items<true, true>(b, S);
 }
 
 // ---------------------------------------------------------------------------
@@ -2114,28 +2284,52 @@ cudaError_t launch_bin(const FrameView& fv, cudaStream_t st) {
     return cudaLaunchKernelEx(&cfg, bin_kernel, fv);
 }
 
-cudaError_t launch_raster(const FrameView& fv, cudaStream_t st) {
+// a persistent grid for a work queue: every CTA slot of the GPU, at most one per block
+static int persistent_blocks(const void* kernel, int threads, int blocks) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+    const int slots = sms * (per > 0 ? per : 1);
+    return blocks < slots ? blocks : slots;
+}
+
+template <int N>
+static cudaError_t launch_raster_n(const FrameView& fv, cudaStream_t st, int phase) {
     int blocks = raster_blocks(fv);
-    if (fv.tile_queue != nullptr) {   // a persistent grid: every CTA slot of the GPU, at most one per item
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const void* k = fv.ext ? reinterpret_cast<const void*>(raster_ext_kernel)
-                      : fv.any_scissor ? reinterpret_cast<const void*>(raster_scissor_kernel)
-                                       : reinterpret_cast<const void*>(raster_kernel);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, raster_threads(fv), 0);
-        const int slots = sms * (per > 0 ? per : 1);
-        blocks = blocks < slots ? blocks : slots;
-    }
-    if (fv.ext) raster_ext_kernel<<<blocks, raster_threads(fv), 0, st>>>(fv);
-    else if (fv.any_scissor) raster_scissor_kernel<<<blocks, raster_threads(fv), 0, st>>>(fv);
-    else raster_kernel<<<blocks, raster_threads(fv), 0, st>>>(fv);
+    const int threads = raster_threads(fv);
+    const void* k = phase == 1 ? reinterpret_cast<const void*>(raster_vis_kernel<N>)
+                  : phase == 2 ? reinterpret_cast<const void*>(raster_shade_kernel<N>)
+                  : fv.ext ? reinterpret_cast<const void*>(raster_ext_kernel<N>)
+                  : fv.any_scissor ? reinterpret_cast<const void*>(raster_scissor_kernel<N>)
+                                   : reinterpret_cast<const void*>(raster_kernel<N>);
+    if (fv.tile_queue != nullptr) blocks = persistent_blocks(k, threads, blocks);
+    if (phase == 1) raster_vis_kernel<N><<<blocks, threads, 0, st>>>(fv);
+    else if (phase == 2) raster_shade_kernel<N><<<blocks, threads, 0, st>>>(fv);
+    else if (fv.ext) raster_ext_kernel<N><<<blocks, threads, 0, st>>>(fv);
+    else if (fv.any_scissor) raster_scissor_kernel<N><<<blocks, threads, 0, st>>>(fv);
+    else raster_kernel<N><<<blocks, threads, 0, st>>>(fv);
     return cudaGetLastError();
+}
+// phase 1 / 2: the launches of a split pass compiled for it (a frame with
+// vis_keys and neither ext nor any_scissor); 3: its shading launch per pixel
+// (shade_pixels_kernel); 0: raster_phase decides.  CTAs of up to 64 threads
+// (16 and 8 px regions) run the 64-thread instantiation.
+cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase) {
+    if (phase == 3) {
+        const dim3 grid(unsigned((fv.width + kPixelW - 1) / kPixelW), unsigned((fv.height + kPixelH - 1) / kPixelH));
+        shade_pixels_kernel<<<grid, kPixelW * kPixelH, 0, st>>>(fv);
+        return cudaGetLastError();
+    }
+    return raster_threads(fv) <= 64 ? launch_raster_n<64>(fv, st, phase) : launch_raster_n<kRasterBatch>(fv, st, phase);
 }
 
 cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st) {
     if (blocks == 0) return cudaSuccess;
-    setup_batch_kernel<<<blocks, kSetupBlock, 0, st>>>(b);
+    bool ext = false;
+    for (int f = 0; f < b.nframes; ++f) ext = ext || b.fv[f].dext != nullptr;
+    if (ext) setup_batch_ext_kernel<<<blocks, kSetupBlock, 0, st>>>(b);
+    else setup_batch_kernel<<<blocks, kSetupBlock, 0, st>>>(b);
     return cudaGetLastError();
 }
 cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st) {
@@ -2143,13 +2337,26 @@ cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st) 
     bin_batch_kernel<<<blocks, kBinBlock, 0, st>>>(b);
     return cudaGetLastError();
 }
+template <int N>
+static cudaError_t launch_raster_batch_n(const BatchLaunch& b, int blocks, int threads, cudaStream_t st) {
+    bool scissor = false, ext = false;
+    for (int f = 0; f < b.nframes; ++f) {
+        scissor = scissor || b.fv[f].any_scissor;
+        ext = ext || b.fv[f].ext;
+    }
+    const void* k = ext ? reinterpret_cast<const void*>(raster_batch_ext_kernel<N>)
+                  : scissor ? reinterpret_cast<const void*>(raster_batch_scissor_kernel<N>)
+                            : reinterpret_cast<const void*>(raster_batch_kernel<N>);
+    if (b.fv[0].tile_queue != nullptr) blocks = persistent_blocks(k, threads, blocks);
+    if (ext) raster_batch_ext_kernel<N><<<blocks, threads, 0, st>>>(b);
+    else if (scissor) raster_batch_scissor_kernel<N><<<blocks, threads, 0, st>>>(b);
+    else raster_batch_kernel<N><<<blocks, threads, 0, st>>>(b);
+    return cudaGetLastError();
+}
 cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st) {
     if (blocks == 0) return cudaSuccess;
-    bool scissor = false;
-    for (int f = 0; f < b.nframes; ++f) scissor = scissor || b.fv[f].any_scissor;
-    if (scissor) raster_batch_scissor_kernel<<<blocks, threads, 0, st>>>(b);
-    else raster_batch_kernel<<<blocks, threads, 0, st>>>(b);
-    return cudaGetLastError();
+    return threads <= 64 ? launch_raster_batch_n<64>(b, blocks, threads, st)
+                         : launch_raster_batch_n<kRasterBatch>(b, blocks, threads, st);
 }
 
 }  // namespace rsrgpu

@@ -41,7 +41,7 @@
 namespace rsrgpu {
 cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
-cudaError_t launch_raster(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase = 0);
 int decode_frame_without_context(int width, int height, int tile_blocks_x, int tile_blocks_y,
                                  const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* states, int nstates,
                                  std::vector<DevState>& out_states, std::vector<DevDraw>& out_draws,

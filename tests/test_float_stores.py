@@ -177,22 +177,3 @@ def test_gpu_float_stores_pinned_split_pass(gpu, orc):
             gpu.unregister_host_buffer(t)
     assert launches == 5   # gather, setup, bin, raster (visibility), raster (shading and stores)
     _check_outputs({k: v.numpy() for k, v in out.items()}, want, False)
-
-
-@pytest.mark.gpu
-def test_batch_rejects_float_stores(built):
-    import torch
-    from rsr_gb300.gpu import Batch, RsrGpuError
-    sc = scenes.float_store_frame(ntris=200)
-    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
-    out = {k: torch.zeros(v.size, dtype=torch.float32 if v.dtype == np.float32 else torch.int32, device="cuda")
-           for k, v in sc.outputs.items()}
-    gl = sc.record(ref=dev.__getitem__, outputs=out)
-    b = Batch(0)
-    try:
-        b.InstallDefaults()
-        with pytest.raises(RsrGpuError) as e:
-            b.submit([(gl, sc.width, sc.height, 32, 0, 0)])
-        assert e.value.code == -6 and "float colour stores" in str(e.value)   # RSRGPU_EUNSUPPORTED
-    finally:
-        b.close()

@@ -75,9 +75,10 @@ def test_pinned_and_pageable_host_buffers_match_device_inputs(gpu, which):
     (outs, launches) = _pinned_render(gpu, sc)
     c, d = outs[0]
     assert np.array_equal(d, want_d) and np.array_equal(c, want_c)
-    # gather, setup, bin, raster; with a texture on its way the raster pass of
-    # this opaque frame runs as two launches (visibility, then shading)
-    assert launches == (5 if which == "sphere" else 4)
+    # gather, setup, bin, and the raster pass of these opaque frames as two
+    # launches (visibility, then shading; the texture of the sphere arrives
+    # during the first)
+    assert launches == 5
 
 
 @pytest.mark.gpu

@@ -134,11 +134,12 @@ def test_gpu_instanced_device_and_pinned_routes(gpu, orc):
 
 @pytest.mark.gpu
 def test_gpu_instanced_rejections(gpu, built):
-    """ManyProgram without instancing, instanced frames in a batch or in the
-    allocation-free entry: RSRGPU_EUNSUPPORTED with a message."""
+    """ManyProgram without instancing, and instanced frames in the
+    allocation-free entry: RSRGPU_EUNSUPPORTED with a message.  (Batches take
+    instanced frames: tests/test_batch_ext.py.)"""
     import ctypes
     import torch
-    from rsr_gb300.gpu import Batch, RsrGpuError
+    from rsr_gb300.gpu import RsrGpuError
     sc = scenes.instanced_scene(ninst=10, width=320, height=180)
     dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
     col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
@@ -156,16 +157,7 @@ def test_gpu_instanced_rejections(gpu, built):
     with pytest.raises(RsrGpuError) as e:
         gpu.submit(gl)
     assert e.value.code == -6
-    # batches
     gl2 = sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=False)
-    b = Batch(0)
-    try:
-        b.InstallDefaults()
-        with pytest.raises(RsrGpuError) as e:
-            b.submit([(gl2, sc.width, sc.height, 32, 0, 0)])
-        assert e.value.code == -6 and "instanced" in str(e.value)
-    finally:
-        b.close()
     # the allocation-free entry
     lib = abi.load_library()
     cmds = gl2.stream()
