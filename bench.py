@@ -802,9 +802,10 @@ def run_batch(gpu, args, stream, flush):
                                         "note": "wall clock: decode + run + wait per frame"},
             "by_resolution": classes,
             "cpu_baseline": None if args.no_cpu_baseline else batch_cpu_sample(frames, args.cpu_seconds),
-            "gpu_launches_per_batch": "setup 1 + bin 1 + raster 1 per CTA shape (graph); raster grids "
-                                      "persistent, taking every frame's tiles from one work queue per "
-                                      "CTA shape, heaviest first"}
+            "gpu_launches_per_batch": "setup 1 + bin 1 + raster visibility 1 per CTA shape + per-pixel "
+                                      "shading 1 (graph); visibility grids persistent, taking the frames' "
+                                      "tiles from one work queue per CTA shape, frame by frame, each "
+                                      "frame's heaviest tiles first"}
 
 
 def batch_cpu_sample(frames, seconds):

@@ -660,12 +660,14 @@ int rsrgpu_batch_frame(rsrgpu_batch* batch, int i, rsrgpu_ctx** ctx);
  * (tile 8/16/32/64 px, raster region 8/16/32 px; tilings whose tile lists
  * exceed the device capacity are skipped) `reps` times, keeps the
  * fastest median device time, and sizes its tile-list capacity from the
- * entries the frame used (plus a quarter).  The tuned tilings are then kept
- * only if the whole batch runs faster with them than with the default 32/32
- * tiling everywhere (a small frame timed alone is mostly launch latency,
- * which the batch shares); otherwise the default is written.  Frames of the same size whose
+ * entries the frame used (plus a quarter).  Frames of the same size whose
  * triangle counts fall in the same power of two reuse a measured tiling
- * (one run of the frame then sizes its capacity).
+ * (one run of the frame then sizes its capacity).  These choices start a
+ * search on the whole batch's time (a small frame timed alone is mostly
+ * launch latency, which the batch shares): the default 32/32 tiling
+ * everywhere, then, one resolution class at a time, every candidate tiling
+ * for all frames of the class, each kept when the batch runs faster; the
+ * capacities come from a run of the final tilings.
  * Writes tile_px, region_px and bin_capacity into frames[] (the commands
  * are rendered, so their outputs are written too). */
 int rsrgpu_batch_tune(rsrgpu_batch* batch, rsrgpu_frame_desc* frames, int nframes, int reps);

@@ -32,7 +32,9 @@ cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase = 0);
 cudaError_t launch_gather(const GatherList& g, cudaStream_t st);
 cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
-cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st);
+cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st, bool vis);
+int pixel_blocks(const FrameView& fv);
+cudaError_t launch_shade_pixels_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 int setup_blocks(const FrameView& fv);
 int bin_blocks(const FrameView& fv);
 int raster_blocks(const FrameView& fv);
@@ -1081,6 +1083,20 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     return 0;
 }
 
+// whether the prepared frame's raster pass runs as the compiled split with
+// per-pixel shading: opaque (vis_keys), no float stores, ManyProgram draws
+// or scissor, and only state changes and TrueColor / depth stores after the
+// last draw
+bool pixel_split(const rsrgpu_ctx* ctx) {
+    const FrameView& fv = ctx->fv;
+    if (fv.vis_keys == 0 || fv.ext || fv.any_scissor) return false;
+    for (size_t k = size_t(fv.keys_resume_op); k < ctx->ops.size(); ++k) {
+        const int32_t kind = ctx->ops[k].kind;
+        if (kind != kOpState && kind != kOpStoreTC && kind != kOpStoreDepth) return false;
+    }
+    return true;
+}
+
 // whether a registered host buffer only the raster pass reads comes with the run
 bool late_inputs(const rsrgpu_ctx* ctx) {
     for (const auto& kv : ctx->host)
@@ -1217,19 +1233,21 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         f.vis_own = ctx->d_vis.as<uint32_t>();
         f.vis_dep = reinterpret_cast<float*>(f.vis_own + size_t(fv.width) * size_t(fv.height));
         f.raster_phase = 1;
-        if (!compiled_split) f.tile_queue = nullptr;   // both launches take the blocks in grid order
+        // With textures on their way the visibility launch runs one CTA per
+        // block (CTAs retire and leave SMs to the texture gather); the
+        // shading launch always does.
+        if (!compiled_split || any_late) f.tile_queue = nullptr;
         CK(launch_raster(f, st, compiled_split ? 1 : 0), "raster_kernel (visibility)");
         if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
         f.raster_phase = 2;
         f.tile_queue = nullptr;
-        // a frame whose ops after the last draw are state changes and
-        // TrueColor / depth stores is shaded one thread per pixel
-        bool per_pixel = compiled_split;
-        for (size_t k = size_t(fv.keys_resume_op); k < ctx->ops.size(); ++k) {
-            const int32_t kind = ctx->ops[k].kind;
-            per_pixel = per_pixel && (kind == kOpState || kind == kOpStoreTC || kind == kOpStoreDepth);
-        }
-        CK(launch_raster(f, st, per_pixel ? 3 : compiled_split ? 2 : 0), "raster_kernel (shading)");
+        // A frame whose ops after the last draw are state changes and
+        // TrueColor / depth stores is shaded one thread per pixel, launched
+        // programmatically dependent on the visibility launch; with textures
+        // arriving during the frame the quad kernel shades (measured faster
+        // there: 0.253 against 0.295 ms per end-to-end headline frame).
+        const int shade = any_late ? (compiled_split ? 2 : 0) : pixel_split(ctx) ? 4 : compiled_split ? 2 : 0;
+        CK(launch_raster(f, st, shade), "raster_kernel (shading)");
     } else {
         if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
         CK(launch_raster(fv, st), "raster_kernel");
@@ -1844,6 +1862,7 @@ struct rsrgpu_batch {
     // all frames' tables in one device buffer, staged in pinned memory
     DevBuf d_tables, d_counters, d_super;
     DevBuf d_queue;                       // the raster launches' work queues
+    DevBuf d_vis;                         // owners and depths of every frame (split pass)
     uint8_t* h_tables = nullptr;
     size_t h_tables_cap = 0, tables_bytes = 0, super_count = 0;
     FrameCounters* h_counters = nullptr;  // pinned, kMaxBatch entries
@@ -1966,6 +1985,16 @@ int build_batch(rsrgpu_batch* b) {
     BCK(b->d_queue.ensure(sizeof(uint32_t) * std::max<size_t>(queue_entries, 1)), "alloc batch work queues");
     const int ngroups = int(group_blocks.size());
     BCK(b->d_counters.ensure(sizeof(FrameCounters) * size_t(n + ngroups)), "alloc batch counters");
+    // the split pass (visibility, then per-pixel shading) when every frame
+    // takes it; owners and depths of frame i at vis_at[i] in d_vis
+    std::vector<size_t> vis_at(size_t(n), 0);
+    size_t vis_px = 0;
+    bool split = true;
+    std::map<int, std::vector<int>> group_frames;   // the frames of each raster launch, in launch order
+    for (int i = 0; i < n; ++i) {
+        vis_at[size_t(i)] = vis_px;
+        vis_px += size_t(b->frames[size_t(i)]->width) * size_t(b->frames[size_t(i)]->height);
+    }
     for (int i = 0; i < n; ++i) {
         rsrgpu_ctx* c = b->frames[size_t(i)];
         std::memcpy(b->h_tables + b->off_states[size_t(i)], c->states.data(), sizeof(DevState) * c->states.size());
@@ -1982,6 +2011,7 @@ int build_batch(rsrgpu_batch* b) {
                        reinterpret_cast<DevDrawExt*>(dt + b->off_dext[size_t(i)]) };
         int rc = prepare_view(c, &vt);
         if (rc) { b->err = c->err; return rc; }
+        split = split && pixel_split(c);
         FrameView& fv = c->fv;
         const int th = raster_threads(fv);
         BatchLaunch& rl = raster[th];
@@ -1993,12 +2023,36 @@ int build_batch(rsrgpu_batch* b) {
         rl.start[rl.nframes] = rb;
         rl.fv[rl.nframes] = fv;
         rl.nframes++;
+        group_frames[th].push_back(i);
         rb += raster_blocks(fv);
         c->stats.gpu_launches = 0;
     }
     setup[0].start[n] = sblocks;
     bin[0].start[n] = bblocks;
     for (auto& kv : raster) kv.second.start[kv.second.nframes] = rblocks[kv.first];
+    BatchLaunch shade;
+    int pblocks = 0;
+    if (split) {
+        BCK(b->d_vis.ensure(std::max<size_t>(vis_px, 1) * 8u), "alloc batch visibility hand-over");
+        shade.nframes = n;
+        auto place = [&](FrameView& f, int i) {
+            f.vis_own = b->d_vis.as<uint32_t>() + vis_at[size_t(i)];
+            f.vis_dep = reinterpret_cast<float*>(b->d_vis.as<uint32_t>() + vis_px) + vis_at[size_t(i)];
+        };
+        for (auto& kv : raster)
+            for (int k = 0; k < kv.second.nframes; ++k) {
+                place(kv.second.fv[k], group_frames[kv.first][size_t(k)]);
+                kv.second.fv[k].raster_phase = 1;
+            }
+        for (int i = 0; i < n; ++i) {
+            shade.fv[i] = b->frames[size_t(i)]->fv;
+            place(shade.fv[i], i);
+            shade.fv[i].raster_phase = 2;
+            shade.start[i] = pblocks;
+            pblocks += pixel_blocks(shade.fv[i]);
+        }
+        shade.start[n] = pblocks;
+    }
     cudaStream_t st = b->own;
     BCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
     int rc = 0;
@@ -2016,11 +2070,12 @@ int build_batch(rsrgpu_batch* b) {
     for (auto it = raster.rbegin(); it != raster.rend(); ++it, ++branch) {
         cudaStream_t rs = branch == 0 ? st : b->aux[(branch - 1) % rsrgpu_batch::kBranches];
         if (branch > 0) step(cudaStreamWaitEvent(rs, b->fork, 0), "fork wait");
-        step(launch_raster_batch(it->second, rblocks[it->first], it->first, rs), "raster_batch_kernel");
+        step(launch_raster_batch(it->second, rblocks[it->first], it->first, rs, split), "raster_batch_kernel");
         if (branch > 0) step(cudaEventRecord(b->join[(branch - 1) % rsrgpu_batch::kBranches], rs), "join");
     }
     for (int k = 0; k + 1 < branch && k < rsrgpu_batch::kBranches; ++k)
         step(cudaStreamWaitEvent(st, b->join[k], 0), "join wait");
+    if (split) step(launch_shade_pixels_batch(shade, pblocks, st), "shade_pixels_batch_kernel");
     step(cudaMemcpyAsync(b->h_counters, b->d_counters.p, sizeof(FrameCounters) * size_t(n), cudaMemcpyDeviceToHost, st), "D2H counters");
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -2028,7 +2083,7 @@ int build_batch(rsrgpu_batch* b) {
     BCK(e, "end capture");
     b->graph = g;
     BCK(cudaGraphInstantiate(&b->exec, b->graph, 0), "instantiate graph");
-    const int launches = 2 + int(raster.size());
+    const int launches = 2 + int(raster.size()) + (split ? 1 : 0);
     for (int i = 0; i < n; ++i) b->frames[size_t(i)]->stats.gpu_launches = launches;
     return 0;
 }
@@ -2074,7 +2129,7 @@ int rsrgpu_batch_destroy(rsrgpu_batch* b) {
     for (rsrgpu_ctx* c : b->frames) rsrgpu_destroy(c);
     if (b->h_tables) cudaFreeHost(b->h_tables);
     if (b->h_counters) cudaFreeHost(b->h_counters);
-    b->d_tables.release(); b->d_counters.release(); b->d_super.release(); b->d_queue.release();
+    b->d_tables.release(); b->d_counters.release(); b->d_super.release(); b->d_queue.release(); b->d_vis.release();
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->fork) cudaEventDestroy(b->fork);
@@ -2273,33 +2328,56 @@ int rsrgpu_batch_tune(rsrgpu_batch* b, rsrgpu_frame_desc* frames, int nframes, i
         frames[i].bin_capacity = choice.bin_capacity;
     }
     // Timed alone, a small frame is mostly launch latency, while in the batch
-    // it shares the launches (and another region size adds a raster launch):
-    // the tuned tilings are kept only if the whole batch runs faster with them
-    // than with the default tiling everywhere.
+    // it shares the launches (and another region size adds a raster launch).
+    // So the per-frame choices are only the start of a search on the batch's
+    // own time: the default tiling everywhere is tried, then, for each
+    // resolution class in turn, every candidate tiling for all of the class's
+    // frames, the rest held; a change is kept when the batch runs faster.
     if (nframes > 1) {
-        std::vector<rsrgpu_frame_desc> deflt(frames, frames + nframes);
-        bool differs = false;
-        for (auto& f : deflt) {
-            if (f.tile_px != kTuneDefault[0] || f.region_px != kTuneDefault[1]) {
-                differs = true;
-                f.tile_px = kTuneDefault[0];
-                f.region_px = kTuneDefault[1];
-                f.bin_capacity = 0;
+        std::vector<rsrgpu_frame_desc> cur(frames, frames + nframes);
+        float t_cur = 0.f;
+        rc = time_batch(b, cur.data(), nframes, reps, &t_cur);
+        if (rc) return rc;
+        auto try_set = [&](const std::vector<rsrgpu_frame_desc>& trial) -> int {
+            float t = 0.f;
+            const int r = time_batch(b, trial.data(), nframes, reps, &t);
+            if (r == RSRGPU_ECAPACITY) return 0;   // this tiling's lists cannot be held
+            if (r) return r;
+            if (t < t_cur) { t_cur = t; cur = trial; }
+            return 0;
+        };
+        std::vector<rsrgpu_frame_desc> deflt = cur;
+        for (auto& f : deflt) { f.tile_px = kTuneDefault[0]; f.region_px = kTuneDefault[1]; f.bin_capacity = 0; }
+        rc = try_set(deflt);
+        if (rc) return rc;
+        std::vector<std::pair<int, int>> classes;
+        for (int i = 0; i < nframes; ++i) {
+            const std::pair<int, int> wh(frames[i].width, frames[i].height);
+            if (std::find(classes.begin(), classes.end(), wh) == classes.end()) classes.push_back(wh);
+        }
+        for (const auto& wh : classes) {
+            for (const auto& cand : kCandidates) {
+                std::vector<rsrgpu_frame_desc> trial = cur;
+                bool changed = false;
+                for (auto& f : trial) {
+                    if (f.width != wh.first || f.height != wh.second) continue;
+                    if (f.tile_px == cand[0] && f.region_px == cand[1]) continue;
+                    f.tile_px = cand[0]; f.region_px = cand[1]; f.bin_capacity = 0;
+                    changed = true;
+                }
+                if (!changed) continue;
+                rc = try_set(trial);
+                if (rc) return rc;
             }
         }
-        if (differs) {
-            float t_tuned = 0.f, t_default = 0.f;
-            rc = time_batch(b, frames, nframes, reps, &t_tuned);
-            if (rc == 0) rc = time_batch(b, deflt.data(), nframes, reps, &t_default);
-            if (rc) return rc;
-            if (t_default < t_tuned) {
-                // capacities from the entries each frame used in those runs
-                for (int i = 0; i < nframes; ++i) {
-                    const uint32_t used = b->frames[size_t(i)]->h_counters->bin_used;
-                    frames[i] = deflt[size_t(i)];
-                    frames[i].bin_capacity = used + used / 4 + 1024;
-                }
-            }
+        // capacities from the entries each frame uses with the chosen tilings
+        float t = 0.f;
+        rc = time_batch(b, cur.data(), nframes, reps, &t);
+        if (rc) return rc;
+        for (int i = 0; i < nframes; ++i) {
+            const uint32_t used = b->frames[size_t(i)]->h_counters->bin_used;
+            frames[i] = cur[size_t(i)];
+            frames[i].bin_capacity = used + used / 4 + 1024;
         }
     }
     return 0;

@@ -2028,10 +2028,14 @@ template <int N> constexpr int raster_ctas(int per256) { return N == 256 ? per25
 
 // The split pass of an opaque frame without float stores, ManyProgram draws or
 // scissor: visibility (80 registers), then shading.
+// The shading launch is programmatically dependent on this one: it is
+// scheduled as these CTAs finish their last items and waits for the whole
+// grid's results.
 template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(3)) raster_vis_kernel(const __grid_constant__ FrameView fv) {
     __shared__ RasterSmem<N> S;
     raster_items<false, false, 1>(fv, S);
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_shade_kernel(const __grid_constant__ FrameView fv) {
@@ -2046,11 +2050,8 @@ __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_shade_kernel(cons
 // the stores run in op order.  32x8 pixels per CTA: a warp stores 128
 // contiguous bytes of a row (outputs may be mapped host memory).
 constexpr int kPixelW = 32, kPixelH = 8;
-__global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const __grid_constant__ FrameView fv) {
-    publish_counters(fv);
+__device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y) {
     if (fv.counters->overflow != 0u) return;
-    const int x = blockIdx.x * kPixelW + (threadIdx.x % kPixelW);
-    const int y = blockIdx.y * kPixelH + (threadIdx.x / kPixelW);
     if (x >= (fv.width & ~1) || y >= (fv.height & ~1)) return;   // the pixels of whole quads, as the raster pass
     const size_t i = size_t(y) * size_t(fv.width) + size_t(x);
     const uint32_t own = fv.vis_own[i];
@@ -2092,6 +2093,11 @@ __global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const _
             static_cast<float*>(o.ptr)[size_t(y) * o.stride + x] = dep;
         }
     }
+}
+__global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const __grid_constant__ FrameView fv) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");   // the visibility launch's owners and depths
+    publish_counters(fv);
+    shade_pixel(fv, blockIdx.x * kPixelW + (threadIdx.x % kPixelW), blockIdx.y * kPixelH + (threadIdx.x / kPixelW));
 }
 template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_kernel(const __grid_constant__ FrameView fv) {
@@ -2142,11 +2148,11 @@ __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_const
 // frame's triangle records and tile lists stay in L2 while its tiles are
 // drawn), each frame's tiles heaviest first; without queues, CTA b draws
 // block b.
-template <bool kExt, bool kScissor, int N>
+template <bool kExt, bool kScissor, int kPhase = 0, int N>
 __device__ __forceinline__ void raster_batch_items(const BatchLaunch& b, RasterSmem<N>& S) {
     if (b.fv[0].tile_queue == nullptr) {
         const int f = batch_frame(b, blockIdx.x);
-        raster_body<kExt, kScissor>(b.fv[f], blockIdx.x - b.start[f], S);
+        raster_body<kExt, kScissor, kPhase>(b.fv[f], blockIdx.x - b.start[f], S);
         return;
     }
     __shared__ int item, item_frame, cached_frame;
@@ -2171,7 +2177,7 @@ __device__ __forceinline__ void raster_batch_items(const BatchLaunch& b, RasterS
         __syncthreads();
         const int e = item;
         if (e == -2) return;
-        if (e >= 0) raster_body<kExt, kScissor>(b.fv[item_frame], e, S);
+        if (e >= 0) raster_body<kExt, kScissor, kPhase>(b.fv[item_frame], e, S);
     }
 }
 template <int N>
@@ -2183,6 +2189,21 @@ template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_batch_scissor_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ RasterSmem<N> S;
     raster_batch_items<false, true>(b, S);
+}
+// The split pass of a batch of opaque frames (as raster_vis_kernel and
+// shade_pixels_kernel): visibility per CTA shape, then one launch shading
+// every frame's pixels (block b of frame f: start[f] <= b < start[f + 1], in
+// rows of ceil(width / kPixelW) blocks).
+template <int N>
+__global__ void __launch_bounds__(N, raster_ctas<N>(3)) raster_batch_vis_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ RasterSmem<N> S;
+    raster_batch_items<false, false, 1>(b, S);
+}
+__global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    const int f = batch_frame(b, blockIdx.x);
+    const FrameView& fv = b.fv[f];
+    const int k = blockIdx.x - b.start[f], bx = (fv.width + kPixelW - 1) / kPixelW;
+    shade_pixel(fv, (k % bx) * kPixelW + (threadIdx.x % kPixelW), (k / bx) * kPixelH + (threadIdx.x / kPixelW));
 }
 // launches with a frame of float colour stores or ManyProgram draws (the
 // code of raster_ext_kernel, which renders the other frames alike)
@@ -2313,13 +2334,21 @@ static cudaError_t launch_raster_n(const FrameView& fv, cudaStream_t st, int pha
 }
 // phase 1 / 2: the launches of a split pass compiled for it (a frame with
 // vis_keys and neither ext nor any_scissor); 3: its shading launch per pixel
-// (shade_pixels_kernel); 0: raster_phase decides.  CTAs of up to 64 threads
+// (shade_pixels_kernel), 4: the same launched programmatically dependent on
+// the visibility launch just before it; 0: raster_phase decides.  CTAs of up to 64 threads
 // (16 and 8 px regions) run the 64-thread instantiation.
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase) {
-    if (phase == 3) {
-        const dim3 grid(unsigned((fv.width + kPixelW - 1) / kPixelW), unsigned((fv.height + kPixelH - 1) / kPixelH));
-        shade_pixels_kernel<<<grid, kPixelW * kPixelH, 0, st>>>(fv);
-        return cudaGetLastError();
+    if (phase == 3 || phase == 4) {   // 4: launched programmatically dependent on the visibility launch
+        cudaLaunchAttribute pdl[1];
+        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(unsigned((fv.width + kPixelW - 1) / kPixelW), unsigned((fv.height + kPixelH - 1) / kPixelH));
+        cfg.blockDim = dim3(kPixelW * kPixelH);
+        cfg.stream = st;
+        cfg.attrs = pdl;
+        cfg.numAttrs = phase == 4 ? 1 : 0;
+        return cudaLaunchKernelEx(&cfg, shade_pixels_kernel, fv);
     }
     return raster_threads(fv) <= 64 ? launch_raster_n<64>(fv, st, phase) : launch_raster_n<kRasterBatch>(fv, st, phase);
 }
@@ -2338,7 +2367,13 @@ cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st) 
     return cudaGetLastError();
 }
 template <int N>
-static cudaError_t launch_raster_batch_n(const BatchLaunch& b, int blocks, int threads, cudaStream_t st) {
+static cudaError_t launch_raster_batch_n(const BatchLaunch& b, int blocks, int threads, cudaStream_t st, bool vis) {
+    if (vis) {
+        if (b.fv[0].tile_queue != nullptr)
+            blocks = persistent_blocks(reinterpret_cast<const void*>(raster_batch_vis_kernel<N>), threads, blocks);
+        raster_batch_vis_kernel<N><<<blocks, threads, 0, st>>>(b);
+        return cudaGetLastError();
+    }
     bool scissor = false, ext = false;
     for (int f = 0; f < b.nframes; ++f) {
         scissor = scissor || b.fv[f].any_scissor;
@@ -2353,10 +2388,21 @@ static cudaError_t launch_raster_batch_n(const BatchLaunch& b, int blocks, int t
     else raster_batch_kernel<N><<<blocks, threads, 0, st>>>(b);
     return cudaGetLastError();
 }
-cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st) {
+// vis: the visibility launch of a split pass (every frame of the launch is
+// opaque, without float stores, ManyProgram draws or scissor)
+cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st, bool vis) {
     if (blocks == 0) return cudaSuccess;
-    return threads <= 64 ? launch_raster_batch_n<64>(b, blocks, threads, st)
-                         : launch_raster_batch_n<kRasterBatch>(b, blocks, threads, st);
+    return threads <= 64 ? launch_raster_batch_n<64>(b, blocks, threads, st, vis)
+                         : launch_raster_batch_n<kRasterBatch>(b, blocks, threads, st, vis);
+}
+// the shading launch of a batch's split pass: start[] counts pixel blocks
+int pixel_blocks(const FrameView& fv) {
+    return ((fv.width + kPixelW - 1) / kPixelW) * ((fv.height + kPixelH - 1) / kPixelH);
+}
+cudaError_t launch_shade_pixels_batch(const BatchLaunch& b, int blocks, cudaStream_t st) {
+    if (blocks == 0) return cudaSuccess;
+    shade_pixels_batch_kernel<<<blocks, kPixelW * kPixelH, 0, st>>>(b);
+    return cudaGetLastError();
 }
 
 }  // namespace rsrgpu
