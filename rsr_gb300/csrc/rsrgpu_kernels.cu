@@ -1962,7 +1962,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 // ---------------------------------------------------------------------------
 // The binning launch is programmatically dependent on setup (launched while
 // setup's CTAs drain; it waits for their results before it reads them).
-__global__ void __launch_bounds__(kSetupBlock) setup_kernel(const __grid_constant__ FrameView fv) {
+__global__ void __launch_bounds__(kSetupBlock, 5) setup_kernel(const __grid_constant__ FrameView fv) {
     setup_body<false>(fv, blockIdx.x);
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
@@ -1970,7 +1970,7 @@ __global__ void __launch_bounds__(kSetupBlock) setup_ext_kernel(const __grid_con
     setup_body<true>(fv, blockIdx.x);
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
-__global__ void __launch_bounds__(kBinBlock) bin_kernel(const __grid_constant__ FrameView fv) {
+__global__ void __launch_bounds__(kBinBlock, 6) bin_kernel(const __grid_constant__ FrameView fv) {
     __shared__ BinShared S;
     asm volatile("griddepcontrol.wait;" ::: "memory");
     bin_body(fv, blockIdx.x, S);
