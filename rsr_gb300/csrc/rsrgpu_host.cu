@@ -34,6 +34,7 @@ cudaError_t launch_setup_batch(const BatchLaunch& b, int blocks, cudaStream_t st
 cudaError_t launch_bin_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 cudaError_t launch_raster_batch(const BatchLaunch& b, int blocks, int threads, cudaStream_t st, bool vis);
 int pixel_blocks(const FrameView& fv);
+int vis_slots(const FrameView& fv);
 cudaError_t launch_shade_pixels_batch(const BatchLaunch& b, int blocks, cudaStream_t st);
 int setup_blocks(const FrameView& fv);
 int bin_blocks(const FrameView& fv);
@@ -169,6 +170,8 @@ struct rsrgpu_ctx {
     int vis_keys = 0;               // FrameView::vis_keys of the submitted frame
     DevBuf d_vis;                   // owners and depths between the two launches of a split raster pass
     DevBuf d_queue;                 // the raster work queue: tiles by cost bucket
+    DevBuf d_slice_keys;            // sliced visibility: merged keys per pixel
+    DevBuf d_slice_done;            // sliced visibility: slices merged per raster block
     // the run's work captured once per submission and replayed by every run
     // (one launch instead of a dozen API calls); dropped when anything it
     // holds changes (submit, reset, host buffers, capacity growth)
@@ -477,7 +480,7 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     for (auto& kv : ctx->host) if (kv.second.dev) cudaFree(kv.second.dev);
     if (ctx->h_mlp_err) cudaFreeHost(ctx->h_mlp_err);
     for (auto& kv : ctx->learn_events) { cudaEventSynchronize(kv.second); cudaEventDestroy(kv.second); }
-    DevBuf* bufs[] = { &ctx->d_queue, &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_tables, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
+    DevBuf* bufs[] = { &ctx->d_slice_keys, &ctx->d_slice_done, &ctx->d_queue, &ctx->d_vis, &ctx->d_mlp_err, &ctx->d_learn_err, &ctx->d_learn_status, &ctx->d_learn_tiles, &ctx->d_tables, &ctx->d_tris, &ctx->d_bin_rect, &ctx->d_rec16,
                        &ctx->d_chunk, &ctx->d_super, &ctx->d_clip_info, &ctx->d_clip_verts, &ctx->d_clip_poly,
                        &ctx->d_clip_src, &ctx->d_clip_fan, &ctx->d_bins, &ctx->d_pool, &ctx->d_counters,
                        &ctx->d_rcp, &ctx->d_srgb };
@@ -991,6 +994,7 @@ struct ViewTables {
 
 // Allocates the frame's scratch and fills ctx->fv; `tables` (batches) points
 // the frame's tables, counters and super-chunk rectangles elsewhere.
+bool late_inputs(const rsrgpu_ctx* ctx);
 int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     const int ntris = ctx->ntris;
     const int nchunks = (ntris + kChunk - 1) / kChunk;
@@ -1060,10 +1064,9 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.tile_queue = nullptr;   // a batch places its frames' queues (build_batch)
     fv.queue_cap = uint32_t(raster_blocks(fv));
     fv.taken = fv.counters;
-    if (tables == nullptr) {   // the raster pass's work queue: raster blocks by cost bucket
-        CK(ctx->d_queue.ensure(sizeof(uint32_t) * size_t(kCostBuckets) * size_t(fv.queue_cap)), "alloc tile queue");
-        fv.tile_queue = ctx->d_queue.as<uint32_t>();
-    }
+    fv.slices = 1;
+    fv.slice_keys = nullptr;
+    fv.slice_done = nullptr;
     if (fv.vis_keys) {   // the raster pass jumps from the first draw to the op after the last
         int last_draw = -1, st_at = 0;
         for (int i = 0; i < int(ctx->ops.size()); ++i)
@@ -1080,6 +1083,26 @@ int prepare_view(rsrgpu_ctx* ctx, const ViewTables* tables = nullptr) {
     fv.any_scissor = 0;
     for (const DevState& st : ctx->states) fv.any_scissor |= st.scissor_test;
     fv.dext = !ctx->any_dext ? nullptr : tables ? tables->dext : reinterpret_cast<DevDrawExt*>(tab + ctx->tab_ofs[4]);
+    if (tables == nullptr) {
+        // A frame with too few raster blocks to fill the GPU's visibility
+        // slots (an opaque frame split in two launches, textures resident)
+        // has each block's tile list swept by several CTAs, about two work
+        // items per slot, at most eight per block.
+        if (fv.vis_keys != 0 && !fv.ext && !fv.any_scissor && !late_inputs(ctx)) {
+            const int blocks = std::max(1, raster_blocks(fv));
+            fv.slices = std::min(8, std::max(1, (2 * vis_slots(fv) + blocks - 1) / blocks));
+        }
+        fv.queue_cap = uint32_t(raster_blocks(fv) * fv.slices);
+        // the raster pass's work queue: raster blocks by cost bucket
+        CK(ctx->d_queue.ensure(sizeof(uint32_t) * size_t(kCostBuckets) * size_t(fv.queue_cap)), "alloc tile queue");
+        fv.tile_queue = ctx->d_queue.as<uint32_t>();
+        if (fv.slices > 1) {
+            CK(ctx->d_slice_keys.ensure(sizeof(unsigned long long) * size_t(fv.width) * size_t(fv.height)), "alloc slice keys");
+            CK(ctx->d_slice_done.ensure(sizeof(uint32_t) * size_t(raster_blocks(fv))), "alloc slice counters");
+            fv.slice_keys = ctx->d_slice_keys.as<unsigned long long>();
+            fv.slice_done = ctx->d_slice_done.as<uint32_t>();
+        }
+    }
     return 0;
 }
 
@@ -1214,6 +1237,10 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
     }
     CK(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(FrameCounters), st), "memset counters");
+    if (fv.slices > 1) {   // merged keys start above every key; no slice has merged
+        CK(cudaMemsetAsync(fv.slice_keys, 0xff, sizeof(unsigned long long) * size_t(fv.width) * size_t(fv.height), st), "memset slice keys");
+        CK(cudaMemsetAsync(fv.slice_done, 0, sizeof(uint32_t) * size_t(raster_blocks(fv)), st), "memset slice counters");
+    }
     if (fv.nsupers > 0) CK(cudaMemsetAsync(ctx->d_super.p, 0x7f, sizeof(int4) * size_t(fv.nsupers), st), "memset super rects");
     CK(cudaEventRecordWithFlags(ctx->ev0, st, evflags), "event");
     CK(launch_setup(fv, st), "setup_kernel");

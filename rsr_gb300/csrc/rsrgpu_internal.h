@@ -206,6 +206,9 @@ struct FrameView {
                               // (counts in counters->bucket); null: CTA b draws block b
     uint32_t queue_cap;       // the frame's raster blocks
     FrameCounters* taken;     // next_item of the raster launch: the frame's counters, or its batch launch's
+    int32_t slices;           // visibility launch: CTAs sharing each raster block's tile list (1: one)
+    unsigned long long* slice_keys;   // slices > 1: the blocks' merged (depth, order) keys, one per pixel
+    uint32_t* slice_done;     // slices > 1: per raster block, the slices that have merged their keys
     const DevDrawExt* dext;   // per draw, for frames with instanced or OBJ1Program draws (setup_ext_kernel); else null
 };
 

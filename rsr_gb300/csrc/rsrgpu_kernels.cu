@@ -199,7 +199,7 @@ __device__ __forceinline__ int raster_subs(const FrameView& fv) {
 __device__ __forceinline__ void enqueue_tile(const FrameView& fv, int tile, uint32_t cost) {
     if (fv.tile_queue == nullptr) return;
     const int b = min(kCostBuckets - 1, 32 - __clz(int(cost)));
-    const int subs = raster_subs(fv);
+    const int subs = raster_subs(fv) * fv.slices;   // items: (block, slice), slice fastest
     const uint32_t pos = atomicAdd(&fv.counters->bucket[b], uint32_t(subs));
     uint32_t* row = fv.tile_queue + size_t(b) * size_t(fv.queue_cap) + pos;
     for (int k = 0; k < subs; ++k) row[k] = uint32_t(tile * subs + k);
@@ -1448,8 +1448,10 @@ __device__ __noinline__ float owner_depth(const FrameView& fv, uint32_t code, co
 // pass's launch); kPhase 1 / 2: compiled for one launch of a split pass of an
 // opaque frame (visibility only, or shading and stores only), whose smaller
 // register demand lets more CTAs share an SM.
+// slice: with fv.slices > 1 (visibility launches of opaque frames), this
+// CTA's share of the block's tile list (see the key merge below).
 template <bool kExt, bool kScissor, int kPhase = 0, int N>
-__device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem<N>& S) {
+__device__ __forceinline__ void raster_body(const FrameView& fv, int block, RasterSmem<N>& S, int slice = 0) {
     if (fv.counters->overflow != 0u) return;
 
     const int region = fv.region_px;
@@ -1512,6 +1514,34 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         if (kPhase != 2 && key_state == 1 && o.kind != kOpDraw && o.kind != kOpState) {
             // owners and depths from the keys
             __syncthreads();
+            if (kPhase == 1 && fv.slices > 1) {
+                // The block's slices each swept a part of the list: their keys
+                // merge by minimum in slice_keys, and the last slice to merge
+                // (counted in slice_done; no CTA waits for another) goes on
+                // with the merged keys.  The minimum is that of one sweep.
+                __shared__ int last_slice;
+                if (active) {
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) {
+                        const int px = qx + (l & 1), py = qy + (l >> 1);
+                        atomicMin(fv.slice_keys + size_t(py) * size_t(fv.width) + size_t(px),
+                                  keys[(py - ry0) * rw + (px - rx0)]);
+                    }
+                }
+                __threadfence();
+                __syncthreads();
+                if (tid == 0) last_slice = atomicAdd(fv.slice_done + block, 1u) == uint32_t(fv.slices - 1);
+                __syncthreads();
+                if (!last_slice) return;
+                __threadfence();
+                if (active) {
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) {
+                        const int px = qx + (l & 1), py = qy + (l >> 1);
+                        keys[(py - ry0) * rw + (px - rx0)] = __ldcg(fv.slice_keys + size_t(py) * size_t(fv.width) + size_t(px));
+                    }
+                }
+            }
             if (active) {
 #pragma unroll
                 for (int l = 0; l < 4; ++l) {
@@ -1591,6 +1621,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                     for (int l = 0; l < 4; ++l) if (dep[l] != dep[l]) ok = false;   // a NaN clear depth: nothing passes
                 }
                 key_state = __syncthreads_and(ok) ? 1 : 2;
+                if (kPhase == 1 && key_state == 2 && slice > 0) return;   // slice 0 walks the whole list
                 if (key_state == 1 && active) {
 #pragma unroll
                     for (int l = 0; l < 4; ++l) keys[(qy - ry0 + (l >> 1)) * rw + (qx - rx0 + (l & 1))] = clear_key(dep[l], leq);
@@ -1607,8 +1638,13 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
             // inline triangles of this draw, then its clipped fans (rglv_gpu_impl.hxx:506-508)
             for (int pass = 0; pass < 2; ++pass) {
                 const uint32_t base = pass == 0 ? bin.inl_off : bin.clip_off;
-                const uint32_t cnt = pass == 0 ? bin.inl_cnt : bin.clip_cnt;
+                uint32_t cnt = pass == 0 ? bin.inl_cnt : bin.clip_cnt;
                 uint32_t& cur = pass == 0 ? inl_cur : clip_cur;
+                if (kPhase == 1 && sweep && fv.slices > 1) {   // this slice's share of the list
+                    const uint32_t all = cnt;
+                    cur = uint32_t((uint64_t(all) * uint32_t(slice)) / uint32_t(fv.slices));
+                    cnt = uint32_t((uint64_t(all) * uint32_t(slice + 1)) / uint32_t(fv.slices));
+                }
                 while (true) {
                     __syncthreads();
                     if (tid == 0) S.qsum = 0;
@@ -2001,7 +2037,8 @@ __device__ __forceinline__ int queue_entry(const FrameView& fv, const int* bucke
 template <bool kExt, bool kScissor, int kPhase = 0, int N>
 __device__ __forceinline__ void raster_items(const FrameView& fv, RasterSmem<N>& S) {
     if (fv.tile_queue == nullptr) {
-        raster_body<kExt, kScissor, kPhase>(fv, blockIdx.x, S);
+        const int sl = kPhase == 1 ? fv.slices : 1;
+        raster_body<kExt, kScissor, kPhase>(fv, int(blockIdx.x) / sl, S, int(blockIdx.x) % sl);
         return;
     }
     __shared__ int item;
@@ -2016,7 +2053,8 @@ __device__ __forceinline__ void raster_items(const FrameView& fv, RasterSmem<N>&
         __syncthreads();
         const int e = item;
         if (e == -2) return;
-        if (e >= 0) raster_body<kExt, kScissor, kPhase>(fv, e, S);
+        const int sl = kPhase == 1 ? fv.slices : 1;
+        if (e >= 0) raster_body<kExt, kScissor, kPhase>(fv, e / sl, S, e % sl);
     }
 }
 // Raster kernels are compiled for CTAs of N threads (one 2x2 quad each): 256
@@ -2317,7 +2355,7 @@ static int persistent_blocks(const void* kernel, int threads, int blocks) {
 
 template <int N>
 static cudaError_t launch_raster_n(const FrameView& fv, cudaStream_t st, int phase) {
-    int blocks = raster_blocks(fv);
+    int blocks = raster_blocks(fv) * (phase == 1 ? fv.slices : 1);
     const int threads = raster_threads(fv);
     const void* k = phase == 1 ? reinterpret_cast<const void*>(raster_vis_kernel<N>)
                   : phase == 2 ? reinterpret_cast<const void*>(raster_shade_kernel<N>)
@@ -2331,6 +2369,13 @@ static cudaError_t launch_raster_n(const FrameView& fv, cudaStream_t st, int pha
     else if (fv.any_scissor) raster_scissor_kernel<N><<<blocks, threads, 0, st>>>(fv);
     else raster_kernel<N><<<blocks, threads, 0, st>>>(fv);
     return cudaGetLastError();
+}
+// CTAs of the visibility kernel the GPU holds at once for this frame's CTA size
+int vis_slots(const FrameView& fv) {
+    const int threads = raster_threads(fv);
+    const void* k = threads <= 64 ? reinterpret_cast<const void*>(raster_vis_kernel<64>)
+                                  : reinterpret_cast<const void*>(raster_vis_kernel<kRasterBatch>);
+    return persistent_blocks(k, threads, 1 << 30);
 }
 // phase 1 / 2: the launches of a split pass compiled for it (a frame with
 // vis_keys and neither ext nor any_scissor); 3: its shading launch per pixel

@@ -163,6 +163,7 @@ int render_static(const uint8_t* commands, size_t nbytes, const rsrgpu_glstate* 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     FrameView fv{};
+    fv.slices = 1;
     fv.states = reinterpret_cast<const DevState*>(base + kOffStates);
     fv.draws = reinterpret_cast<const DevDraw*>(base + kOffDraws);
     fv.ndraws = int(dr.size());
