@@ -840,7 +840,16 @@ PROFILE_CASES = {
     "batch16": "16 frames of the batch generator, 1k..200k triangles, fixed 32 px tiles "
                "(setup/bin/raster_batch_kernel)",
     "train_1080": "features of the 1080p deferred scene (learned_features_kernel), then Adam steps of "
-                  "batch 8 192 (mlp_train_kernel, adam_kernel)",
+                  "batch 8 192 (mlp_train_kernel, adam_kernel) and a forward pass over the frame "
+                  "(mlp_forward_kernel)",
+    "sphere_1080_host": "the headline frame from pinned host buffers (gather_kernel, setup, bin, "
+                        "raster_vis_kernel in grid order while the texture arrives, raster_shade_kernel)",
+    "scissor_640": "a 640x360 frame with scissored draws (raster_scissor_kernel), then a 1000x1000 "
+                   "texture without a mip chain (rgba8_to_float_kernel)",
+    "batch_ext": "a batch of a plain, two float-store, an instanced and an OBJ1Program frame "
+                 "(setup_batch_ext_kernel, raster_batch_ext_kernel)",
+    "gbuffer_1080": "the G-buffer pass of the 1080p deferred scene, 2 M objects, seed 100 (setup, bin, "
+                    "raster_vis_kernel, raster_shade_kernel with the G-buffer store)",
 }
 
 
@@ -856,17 +865,31 @@ def run_profile(args):
     gpu = GPU(0)
     gpu.InstallDefaults()
     info = {"profile": args.profile, "case": PROFILE_CASES[args.profile], "reps": reps}
-    if args.profile == "batch16":
-        frames = scenes.batch_frames(seed=0, nframes=16, tris=(1_000, 200_000))
+    if args.profile in ("batch16", "batch_ext"):
         made = []
+        if args.profile == "batch16":
+            frames = scenes.batch_frames(seed=0, nframes=16, tris=(1_000, 200_000))
+            tiling = (32, 32)
+        else:
+            frames = [scenes.plain_raster(seed=5, ntris=3000, width=320, height=180, tile_blocks=(4, 4), spread=0.4),
+                      scenes.float_store_frame(seed=23, ntris=2000, width=320, height=180),
+                      scenes.float_store_frame(seed=24, ntris=2000, width=192, height=128, color_depth=True, mid=True),
+                      scenes.instanced_scene(seed=45, ninst=600, width=320, height=180),
+                      scenes.obj1_scene(seed=55, nspheres=10, width=320, height=180)]
+            tiling = (32, 0)
         for sc in frames:
             dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+            if hasattr(sc, "outputs"):
+                out = {k: torch.zeros(v.size, dtype=torch.float32 if v.dtype == np.float32 else torch.int32,
+                                      device="cuda") for k, v in sc.outputs.items()}
+                made.append((dev, out, None, sc.record(ref=dev.__getitem__, outputs=out, gamma=True)))
+                continue
             col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
             dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
             made.append((dev, col, dep, sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=True)))
         b = Batch(0)
         b.InstallDefaults()
-        b.submit([(m[3], sc.width, sc.height, 32, 32, 0) for sc, m in zip(frames, made)])
+        b.submit([(m[3], sc.width, sc.height) + tiling + (0,) for sc, m in zip(frames, made)])
         for _ in range(reps):
             b.run()
             b.wait()
@@ -884,11 +907,41 @@ def run_profile(args):
         for s in range(reps):
             pick = idx[torch.randint(0, len(idx), (8192,), generator=g, device="cuda")].to(torch.int32)
             net.train_step(gpu, f, t, pick, 1e-3)
+        y = torch.zeros(f.shape[0], 3, dtype=torch.float32, device="cuda")
+        gpu.mlp_forward(net.views(), f, y)
         torch.cuda.synchronize()
         info["loss"] = net.loss.item()
+    elif args.profile == "gbuffer_1080":
+        from rsr_gb300.gpu import render_gbuffer
+        sc = scenes.deferred_scene(seed=100, width=1920, height=1080, nobj=2_000_000)
+        gbuf, dev = render_gbuffer(gpu, sc)
+        for _ in range(reps - 1):
+            gpu.run()
+            gpu.Wait()
+        torch.cuda.synchronize()
+        info["launches_per_frame"] = gpu.stats()["gpu_launches"]
+    elif args.profile == "sphere_1080_host":
+        sc = workload()
+        host = {k: torch.from_numpy(v.copy()).pin_memory() for k, v in sc.arrays.items()}
+        hcol = torch.zeros(sc.width * sc.height, dtype=torch.int32).pin_memory()
+        hdep = torch.zeros(sc.width * sc.height, dtype=torch.float32).pin_memory()
+        bufs = list(host.values()) + [hcol, hdep]
+        for t in bufs:
+            gpu.register_host_buffer(t)
+        gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+        gpu.submit(sc.record(ref=host.__getitem__, color=hcol, depth=hdep, gamma=True))
+        for _ in range(reps):
+            gpu.run()
+            gpu.Wait()
+        torch.cuda.synchronize()
+        info["launches_per_frame"] = gpu.stats()["gpu_launches"]
+        for t in bufs:
+            gpu.unregister_host_buffer(t)
     else:
         if args.profile == "instanced_640":
             sc = scenes.instanced_scene()
+        elif args.profile == "scissor_640":
+            sc = scenes.scissor_scene()
         elif args.profile == "plain_640":
             sc = scenes.plain_raster()
         else:
@@ -910,6 +963,9 @@ def run_profile(args):
             gl.StoreColorFP(half, W // 2, H // 2, downsample=True)
             px = torch.randint(0, 256, (1024 * 1024 * 4,), dtype=torch.uint8, device="cuda")
             texels = torch.empty(2 * 1024 * 1024 * 4, dtype=torch.float32, device="cuda")
+        if args.profile == "scissor_640":
+            px = torch.randint(0, 256, (1000 * 1000 * 4,), dtype=torch.uint8, device="cuda")
+            texels = torch.empty(1000 * 1000 * 4, dtype=torch.float32, device="cuda")
         gpu.submit(gl)
         for _ in range(reps):
             gpu.run()
@@ -918,6 +974,8 @@ def run_profile(args):
                 gpu.texture_from_rgba8(px, 1024, 1024, texels)
                 r = gpu.kawase_chain(half, ta, tb, W // 2, H // 2, 4)
                 gpu.glow(quads, r, out, W, H, srgb=True)
+            if args.profile == "scissor_640":
+                gpu.texture_from_rgba8(px, 1000, 1000, texels)
         torch.cuda.synchronize()
         info["launches_per_frame"] = gpu.stats()["gpu_launches"]
     print(json.dumps(info))
