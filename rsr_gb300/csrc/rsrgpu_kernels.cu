@@ -592,34 +592,6 @@ __device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, in
     }
 }
 
-// The tile's entries by one warp (lane order within a warp): count, take
-// pool space, write.  The fallback of bin_body for tiles beyond its limits.
-__device__ __forceinline__ void bin_tile_warp(const FrameView& fv, int tile, int tx, int ty, int lane) {
-    const int ngroups = (fv.nsupers + 31) / 32;
-    uint32_t ninl = 0, nclip = 0;
-    // up to 1024 super-chunks (1M triangles) the masks are found once for both passes
-    const uint32_t gm0 = super_masks(fv, tx, ty, lane, 0);
-    for (int g0 = 0; g0 < ngroups; g0 += 32)
-        bin_walk<false>(fv, tx, ty, lane, g0 == 0 ? gm0 : super_masks(fv, tx, ty, lane, g0), g0, ninl, nclip, nullptr, nullptr);
-    uint32_t off = 0;
-    if (lane == 0) {
-        off = atomicAdd(&fv.counters->bin_used, ninl + nclip);
-        if (off + ninl + nclip > fv.bin_cap) {
-            atomicOr(&fv.counters->overflow, 2u);
-            fv.bins[tile] = TileBin{0, 0, 0, 0};
-            off = 0xffffffffu;
-        } else {
-            fv.bins[tile] = TileBin{off, ninl, off + ninl, nclip};
-        }
-        enqueue_tile(fv, tile, ninl + nclip);
-    }
-    off = __shfl_sync(FULL_MASK, off, 0);
-    if (off == 0xffffffffu) return;
-    uint32_t w_inl = 0, w_clip = 0;
-    for (int g0 = 0; g0 < ngroups; g0 += 32)
-        bin_walk<true>(fv, tx, ty, lane, g0 == 0 ? gm0 : super_masks(fv, tx, ty, lane, g0), g0, w_inl, w_clip,
-                       fv.bin_pool + off, fv.bin_pool + off + ninl);
-}
 
 // ---- binning: one CTA of kBinBlock threads per tile ----
 // The tile's overlapping chunks are listed in triangle order (super-chunk
@@ -627,10 +599,10 @@ __device__ __forceinline__ void bin_tile_warp(const FrameView& fv, int tile, int
 // the warps count the chunks' entries in parallel (chunk k: warp k % 8), a
 // prefix over the counts gives every chunk its place, and the warps write.
 // Chunks are taken in windows of up to kBinChunks (consecutive overlapping
-// super-chunks), counted in one pass and written in a second.  The lists
-// equal the one-warp walk's (order within a chunk: lane order; clipped fans:
-// lane order, then fan order).  Frames of more than 1024 super-chunks take
-// the one-warp walk.
+// super-chunks), and super-chunks 1024 at a time, counted in one pass and
+// written in a second.  The lists are those of walking the chunks in order
+// (order within a chunk: lane order; clipped fans: lane order, then fan
+// order).
 constexpr int kBinWarps = kBinBlock / 32;
 constexpr int kBinChunks = 1024;
 struct BinShared {
@@ -723,22 +695,15 @@ __device__ __forceinline__ int bin_window_count(const FrameView& fv, BinShared& 
     return nc;
 }
 
-__device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShared& S) {
+// Lists the super-chunks of groups g0 .. g0 + gn - 1 (gn <= 32, 1024
+// super-chunks) that overlap tile (tx, ty), in order, into S.sup / S.nsup,
+// with their chunk masks in S.cm and the exclusive prefix of their
+// overlapping chunks in S.pre (all threads of the CTA call it).
+__device__ __forceinline__ void bin_list_supers(const FrameView& fv, BinShared& S, int g0, int gn, int tx, int ty) {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    if (tile >= fv.ntiles) return;
-    if (fv.counters->overflow & 1u) {
-        if (t == 0) { fv.bins[tile] = TileBin{0, 0, 0, 0}; enqueue_tile(fv, tile, 0); }
-        return;
-    }
-    const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
-    const int ngroups = (fv.nsupers + 31) / 32;
-    if (ngroups > 32) {
-        if (warp == 0) bin_tile_warp(fv, tile, tx, ty, lane);
-        return;
-    }
     // super-chunk group masks: group g by warp g % 8
-    for (int g = warp; g < ngroups; g += kBinWarps) {
-        const int sidx = g * 32 + lane;
+    for (int g = warp; g < gn; g += kBinWarps) {
+        const int sidx = (g0 + g) * 32 + lane;
         bool hs = false;
         if (sidx < fv.nsupers) {
             const int4 r = fv.super_rect[sidx];
@@ -750,7 +715,7 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShare
     __syncthreads();
     // the overlapping super-chunks in order (warp 0: lane g lists group g)
     if (warp == 0) {
-        const uint32_t m = lane < ngroups ? S.gm[lane] : 0u;
+        const uint32_t m = lane < gn ? S.gm[lane] : 0u;
         const int c = __popc(m);
         int incl = c;
 #pragma unroll
@@ -759,7 +724,7 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShare
             if (lane >= o) incl += y;
         }
         int at = incl - c;
-        for (uint32_t mm = m; mm; mm &= mm - 1) S.sup[at++] = lane * 32 + __ffs(mm) - 1;
+        for (uint32_t mm = m; mm; mm &= mm - 1) S.sup[at++] = (g0 + lane) * 32 + __ffs(mm) - 1;
         if (lane == 31) S.nsup = incl;
     }
     __syncthreads();
@@ -777,14 +742,34 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShare
     }
     __syncthreads();
     bin_scan(S.pre, nsup, S);
+}
+
+// One tile's lists: the overlapping super-chunks are taken 1024 at a time
+// (super windows), their overlapping chunks up to kBinChunks at a time
+// (chunk windows); the counts of all windows size the tile's lists, then
+// the windows are visited again to write them.
+__device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShared& S) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (tile >= fv.ntiles) return;
+    if (fv.counters->overflow & 1u) {
+        if (t == 0) { fv.bins[tile] = TileBin{0, 0, 0, 0}; enqueue_tile(fv, tile, 0); }
+        return;
+    }
+    const int tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
+    const int ngroups = (fv.nsupers + 31) / 32;
+    const int nsw = (ngroups + 31) / 32;
     // count, window by window
     int tinl = 0, tcl = 0;
-    for (int k0 = 0; k0 < nsup;) {
-        const int k1 = bin_window_end(S, k0, nsup);
-        const int nc = bin_window_count(fv, S, k0, k1, tx, ty);
-        tinl += bin_scan(S.ninl, nc, S);
-        tcl += bin_scan(S.ncl, nc, S);
-        k0 = k1;
+    for (int sw = 0; sw < nsw; ++sw) {
+        bin_list_supers(fv, S, sw * 32, min(32, ngroups - sw * 32), tx, ty);
+        const int nsup = S.nsup;
+        for (int k0 = 0; k0 < nsup;) {
+            const int k1 = bin_window_end(S, k0, nsup);
+            const int nc = bin_window_count(fv, S, k0, k1, tx, ty);
+            tinl += bin_scan(S.ninl, nc, S);
+            tcl += bin_scan(S.ncl, nc, S);
+            k0 = k1;
+        }
     }
     if (t == 0) {
         uint32_t off = 0;
@@ -805,53 +790,57 @@ __device__ __forceinline__ void bin_body(const FrameView& fv, int tile, BinShare
     uint32_t* inl_out = fv.bin_pool + base;
     uint32_t* clip_out = fv.bin_pool + base + tinl;
     const uint32_t lt = (1u << lane) - 1u;
-    // write, window by window (the first window's counts are recounted
-    // unless it was the only one)
+    // write, window by window (the first chunk window's counts are recounted
+    // unless it was the only window)
     int winl = 0, wcl = 0;
-    for (int k0 = 0; k0 < nsup;) {
-        const int k1 = bin_window_end(S, k0, nsup);
-        int nc;
-        if (k0 == 0 && k1 == nsup) {
-            nc = S.pre[nsup - 1] + __popc(S.cm[nsup - 1]);   // still in place from the count
-        } else {
-            nc = bin_window_count(fv, S, k0, k1, tx, ty);
-            bin_scan(S.ninl, nc, S);
-            bin_scan(S.ncl, nc, S);
-        }
-        for (int k = warp; k < nc; k += kBinWarps) {
-            const int c = S.chunk[k];
-            const uint32_t mi = S.imask[k];
-            if (mi & (1u << lane)) inl_out[winl + S.ninl[k] + __popc(mi & lt)] = uint32_t(c * 32 + lane);
-            bool inl;
-            int fans;
-            const bool has_fans = k + 1 < nc ? S.ncl[k + 1] != S.ncl[k] : true;
-            if (!has_fans) continue;
-            chunk_entries(fv, c, tx, ty, lane, inl, fans);
-            if (!__any_sync(FULL_MASK, fans != 0)) continue;
-            int incl = fans;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(FULL_MASK, incl, o);
-                if (lane >= o) incl += y;
+    for (int sw = 0; sw < nsw; ++sw) {
+        if (nsw > 1) bin_list_supers(fv, S, sw * 32, min(32, ngroups - sw * 32), tx, ty);
+        const int nsup = S.nsup;
+        for (int k0 = 0; k0 < nsup;) {
+            const int k1 = bin_window_end(S, k0, nsup);
+            int nc;
+            if (nsw == 1 && k0 == 0 && k1 == nsup) {
+                nc = S.pre[nsup - 1] + __popc(S.cm[nsup - 1]);   // still in place from the count
+            } else {
+                nc = bin_window_count(fv, S, k0, k1, tx, ty);
+                bin_scan(S.ninl, nc, S);
+                bin_scan(S.ncl, nc, S);
             }
-            if (fans) {
-                const ClipInfo ci = fv.clip_info[c * 32 + lane];
-                uint32_t pos = uint32_t(wcl + S.ncl[k] + incl - fans);
-                for (int vi = 1; vi < ci.nverts - 1; ++vi)
-                    if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
+            for (int k = warp; k < nc; k += kBinWarps) {
+                const int c = S.chunk[k];
+                const uint32_t mi = S.imask[k];
+                if (mi & (1u << lane)) inl_out[winl + S.ninl[k] + __popc(mi & lt)] = uint32_t(c * 32 + lane);
+                bool inl;
+                int fans;
+                const bool has_fans = k + 1 < nc ? S.ncl[k + 1] != S.ncl[k] : true;
+                if (!has_fans) continue;
+                chunk_entries(fv, c, tx, ty, lane, inl, fans);
+                if (!__any_sync(FULL_MASK, fans != 0)) continue;
+                int incl = fans;
+    #pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(FULL_MASK, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (fans) {
+                    const ClipInfo ci = fv.clip_info[c * 32 + lane];
+                    uint32_t pos = uint32_t(wcl + S.ncl[k] + incl - fans);
+                    for (int vi = 1; vi < ci.nverts - 1; ++vi)
+                        if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
+                }
             }
+            // the window's totals (from the last chunk's prefix and count)
+            if (nc > 0) {
+                winl += S.ninl[nc - 1] + __popc(S.imask[nc - 1]);
+                // clip total: recount the last chunk's fans (cheap; rarely any)
+                bool inl;
+                int fans;
+                chunk_entries(fv, S.chunk[nc - 1], tx, ty, lane, inl, fans);
+                wcl += S.ncl[nc - 1] + __reduce_add_sync(FULL_MASK, fans);
+            }
+            __syncthreads();
+            k0 = k1;
         }
-        // the window's totals (from the last chunk's prefix and count)
-        if (nc > 0) {
-            winl += S.ninl[nc - 1] + __popc(S.imask[nc - 1]);
-            // clip total: recount the last chunk's fans (cheap; rarely any)
-            bool inl;
-            int fans;
-            chunk_entries(fv, S.chunk[nc - 1], tx, ty, lane, inl, fans);
-            wcl += S.ncl[nc - 1] + __reduce_add_sync(FULL_MASK, fans);
-        }
-        __syncthreads();
-        k0 = k1;
     }
 }
 

@@ -89,3 +89,38 @@ def test_keys_match_oracle(gpu, func, zero):
     else:
         gpu.tiles()
         assert gpu.stats()["total_clipped_records"] > 0
+
+
+def test_nan_cleared_depth_walks_the_list(gpu):
+    """A NaN cleared depth: no fragment passes, and the tiles cannot use keys
+    (the clear key would not order).  With this frame's few raster blocks
+    the visibility launch shares each block's list among several CTAs, so
+    the first of them walks the whole list alone and the others leave it:
+    colour is the clear colour and depth the NaN, as in the oracle."""
+    import oracle
+    import torch
+    from rsr_gb300.gpu import render_scene
+    base = twice_drawn(abi.GL_LESS)
+
+    def record(gl, ref):
+        gl.RenderbufferType(abi.GL_COLOR_ATTACHMENT0, abi.RB_RGBF32)
+        gl.RenderbufferType(abi.GL_DEPTH_ATTACHMENT, abi.RB_F32)
+        gl.ClearColor((0.25, 0.5, 0.75))
+        gl.ClearDepth(float("nan"))
+        gl.Clear(abi.GL_COLOR_BUFFER_BIT | abi.GL_DEPTH_BUFFER_BIT)
+        gl.UseProgram(abi.PROGRAM_GOURAUD)
+        gl.UseBuffer(0, (ref("px"), ref("py"), ref("pz")))
+        gl.UseBuffer(3, (ref("ar"), ref("ag"), ref("ab")))
+        gl.DrawElements(len(base.arrays["idx"]), ref("idx"), 0)
+
+    sc = scenes.Scene("nan_clear", base.width, base.height, base.tile_blocks, base.arrays, record, base.ntris // 2)
+    oc, od = oracle.CpuRenderer("oracle").render(sc, False)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+    col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+    dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+    render_scene(gpu, sc, gamma=False, device_inputs=dev, color=col, depth=dep)
+    torch.cuda.synchronize()
+    gc, gd = col.cpu().numpy().view(np.uint32), dep.cpu().numpy().view(np.uint32)
+    assert np.array_equal(gd, od.view(np.uint32))
+    assert np.array_equal(gc, oc.view(np.uint32))
+    assert np.isnan(dep.cpu().numpy()).all()
