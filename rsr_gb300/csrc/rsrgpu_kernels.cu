@@ -1120,9 +1120,12 @@ constexpr uint32_t kKeyPosBits = 19;   // the list-position bits of a key's orde
 // Per-(triangle, tile) setup and vertex data of one list entry, for the
 // resolve pass: the triangle that last wrote a pixel is set up again exactly
 // as when it was rasterised.
+// first_s / state_s (or null): the draws' first triangles and states in
+// shared memory, for the draw search
 template <bool kScissor>
 __device__ __forceinline__ void owner_setup_inline(const FrameView& fv, uint32_t code, const int tile[4], TriSetup& t,
-                                                   float w[3], float vary[3][kMaxVary], int& state) {
+                                                   float w[3], float vary[3][kMaxVary], int& state,
+                                                   const int* first_s = nullptr, const int* state_s = nullptr) {
     const int g = (code & kClippedBit) ? fv.clip_src[fv.clip_poly[code & ~kClippedBit]] : int(code);
     int rect[4] = { tile[0], tile[1], tile[2], tile[3] };
     if (kScissor && fv.any_scissor) {   // the draw's rectangle depends on its state
@@ -1149,7 +1152,18 @@ __device__ __forceinline__ void owner_setup_inline(const FrameView& fv, uint32_t
             for (int q = 0; q < kMaxVary; ++q) vary[k][q] = r.vary[k][q];
         }
     }
-    if (!(kScissor && fv.any_scissor)) state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+    if (!(kScissor && fv.any_scissor)) {
+        if (first_s != nullptr) {
+            int lo = 0, hi = fv.ndraws - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (first_s[mid] <= g) lo = mid; else hi = mid - 1;
+            }
+            state = state_s[lo];
+        } else {
+            state = fv.draws[find_draw(fv.draws, fv.ndraws, g)].state;
+        }
+    }
 }
 // the raster kernels call it out of line (their register budget)
 template <bool kScissor>
@@ -2077,19 +2091,36 @@ __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_shade_kernel(cons
 // the stores run in op order.  32x8 pixels per CTA: a warp stores 128
 // contiguous bytes of a row (outputs may be mapped host memory).
 constexpr int kPixelW = 32, kPixelH = 8;
-__device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y) {
+// What every pixel of a CTA reads: the clear colour (the last colour clear
+// before the first draw) and, for frames of up to kOpCache draws, the draws'
+// first triangles and states.
+struct PixelShared {
+    float clear[3];
+    int first[kOpCache];
+    int state[kOpCache];
+};
+__device__ __forceinline__ void pixel_shared_load(const FrameView& fv, PixelShared& P) {
+    if (fv.ndraws <= kOpCache)
+        for (int i = threadIdx.x; i < fv.ndraws; i += blockDim.x) { P.first[i] = fv.draws[i].first_tri; P.state[i] = fv.draws[i].state; }
+    if (threadIdx.x == 0) {
+        float c[3] = { 0.0f, 0.0f, 0.0f };
+        for (int op = 0; op < fv.nops; ++op) {
+            const FrameOp o = fv.ops[op];
+            if (o.kind == kOpDraw) break;
+            if (o.kind == kOpClear && (o.info[2] != 0 || (o.arg & 1))) { c[0] = o.val[0]; c[1] = o.val[1]; c[2] = o.val[2]; }
+        }
+        P.clear[0] = c[0]; P.clear[1] = c[1]; P.clear[2] = c[2];
+    }
+    __syncthreads();
+}
+__device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y, const PixelShared& P) {
     if (fv.counters->overflow != 0u) return;
     if (x >= (fv.width & ~1) || y >= (fv.height & ~1)) return;   // the pixels of whole quads, as the raster pass
     const size_t i = size_t(y) * size_t(fv.width) + size_t(x);
     const uint32_t own = fv.vis_own[i];
     const float dep = fv.vis_dep[i];
-    // the colour: the last colour clear before the first draw, or the owner's
-    float c[3] = { 0.0f, 0.0f, 0.0f };
-    for (int op = 0; op < fv.nops; ++op) {
-        const FrameOp o = fv.ops[op];
-        if (o.kind == kOpDraw) break;
-        if (o.kind == kOpClear && (o.info[2] != 0 || (o.arg & 1))) { c[0] = o.val[0]; c[1] = o.val[1]; c[2] = o.val[2]; }
-    }
+    // the colour: the clear colour, or the owner's
+    float c[3] = { P.clear[0], P.clear[1], P.clear[2] };
     if (own != kNoOwner) {
         const int tx = x / fv.tile_w, ty = y / fv.tile_h;
         const int rect[4] = { tx * fv.tile_w, ty * fv.tile_h, min(tx * fv.tile_w + fv.tile_w, fv.width),
@@ -2097,7 +2128,8 @@ __device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y) {
         TriSetup t;
         float w[3], vary[3][kMaxVary];
         int state = 0;
-        owner_setup_inline<false>(fv, own, rect, t, w, vary, state);
+        const bool cached = fv.ndraws <= kOpCache;
+        owner_setup_inline<false>(fv, own, rect, t, w, vary, state, cached ? P.first : nullptr, cached ? P.state : nullptr);
         owner_color<false>(fv, t, w, vary, state, x & ~1, y & ~1, (x & 1) | ((y & 1) << 1), c);
     }
     int cur_state = fv.ops[fv.keys_resume_state_op].arg;
@@ -2122,9 +2154,11 @@ __device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y) {
     }
 }
 __global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const __grid_constant__ FrameView fv) {
+    __shared__ PixelShared P;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // the visibility launch's owners and depths
     publish_counters(fv);
-    shade_pixel(fv, blockIdx.x * kPixelW + (threadIdx.x % kPixelW), blockIdx.y * kPixelH + (threadIdx.x / kPixelW));
+    pixel_shared_load(fv, P);
+    shade_pixel(fv, blockIdx.x * kPixelW + (threadIdx.x % kPixelW), blockIdx.y * kPixelH + (threadIdx.x / kPixelW), P);
 }
 template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_kernel(const __grid_constant__ FrameView fv) {
@@ -2227,10 +2261,12 @@ __global__ void __launch_bounds__(N, raster_ctas<N>(3)) raster_batch_vis_kernel(
     raster_batch_items<false, false, 1>(b, S);
 }
 __global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_batch_kernel(const __grid_constant__ BatchLaunch b) {
+    __shared__ PixelShared P;
     const int f = batch_frame(b, blockIdx.x);
     const FrameView& fv = b.fv[f];
+    pixel_shared_load(fv, P);
     const int k = blockIdx.x - b.start[f], bx = (fv.width + kPixelW - 1) / kPixelW;
-    shade_pixel(fv, (k % bx) * kPixelW + (threadIdx.x % kPixelW), (k / bx) * kPixelH + (threadIdx.x / kPixelW));
+    shade_pixel(fv, (k % bx) * kPixelW + (threadIdx.x % kPixelW), (k / bx) * kPixelH + (threadIdx.x / kPixelW), P);
 }
 // launches with a frame of float colour stores or ManyProgram draws (the
 // code of raster_ext_kernel, which renders the other frames alike)
