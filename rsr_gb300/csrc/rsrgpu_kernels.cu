@@ -620,9 +620,29 @@ struct BinShared {
 };
 
 // Exclusive prefix of v[0 .. n) in place (n <= 4 * kBinBlock), total returned
-// (all threads of the CTA call it).
+// (all threads of the CTA call it).  For n <= 128 one warp scans and the
+// total is also left in v[n], which nothing else reads.
 __device__ __forceinline__ int bin_scan(int32_t* v, int n, BinShared& S) {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (n <= 128) {   // one warp scans (four values a lane): one barrier instead of two
+        if (warp == 0) {
+            int x[4], sum = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { const int i = 4 * lane + k; x[k] = i < n ? v[i] : 0; sum += x[k]; }
+            int incl = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, incl, o);
+                if (lane >= o) incl += y;
+            }
+            int before = incl - sum;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { const int i = 4 * lane + k; if (i < n) v[i] = before; before += x[k]; }
+            if (lane == 31) v[n] = incl;   // the total, past the prefix (every array scanned here has room)
+        }
+        __syncthreads();
+        return v[n];
+    }
     int x[4], sum = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) { const int i = 4 * t + k; x[k] = i < n ? v[i] : 0; sum += x[k]; }
@@ -1648,6 +1668,7 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                     cur = uint32_t((uint64_t(all) * uint32_t(slice)) / uint32_t(fv.slices));
                     cnt = uint32_t((uint64_t(all) * uint32_t(slice + 1)) / uint32_t(fv.slices));
                 }
+                if (cur >= cnt) continue;   // nothing left in this list (the same for every thread)
                 while (true) {
                     __syncthreads();
                     if (tid == 0) S.qsum = 0;
