@@ -1698,17 +1698,23 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                     if (valid) {
                         TriSetup t;
                         if (pass == 0) {
+                            // the visibility launch reads positions and depths only
+                            // (the record's first 36 bytes); w and varyings are for shading
                             const float4* rp = reinterpret_cast<const float4*>(fv.tris + e);
                             TriRecord r;
                             float4* rr = reinterpret_cast<float4*>(&r);
+                            constexpr int kParts = kPhase == 1 ? 3 : 6;
 #pragma unroll
-                            for (int q = 0; q < 6; ++q) rr[q] = __ldg(rp + q);
+                            for (int q = 0; q < kParts; ++q) rr[q] = __ldg(rp + q);
                             setup_vector(t, drect, r.fx[0], r.fx[1], r.fx[2], r.fy[0], r.fy[1], r.fy[2]);
 #pragma unroll
                             for (int k = 0; k < 3; ++k) {
-                                S.z[k][tid] = r.z[k]; S.w[k][tid] = r.w[k];
+                                S.z[k][tid] = r.z[k];
+                                if (kPhase != 1) {
+                                    S.w[k][tid] = r.w[k];
 #pragma unroll
-                                for (int q = 0; q < kMaxVary; ++q) S.vary[k][q][tid] = r.vary[k][q];
+                                    for (int q = 0; q < kMaxVary; ++q) S.vary[k][q][tid] = r.vary[k][q];
+                                }
                             }
                             S.code[tid] = e;
                         } else {
@@ -1719,10 +1725,12 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                                          __float2int_rz(v0.coord[0] * 16.0f), __float2int_rz(v1.coord[0] * 16.0f), __float2int_rz(v2.coord[0] * 16.0f),
                                          __float2int_rz(v0.coord[1] * 16.0f), __float2int_rz(v1.coord[1] * 16.0f), __float2int_rz(v2.coord[1] * 16.0f));
                             S.z[0][tid] = v0.coord[2]; S.z[1][tid] = v1.coord[2]; S.z[2][tid] = v2.coord[2];
-                            S.w[0][tid] = v0.coord[3]; S.w[1][tid] = v1.coord[3]; S.w[2][tid] = v2.coord[3];
+                            if (kPhase != 1) {
+                                S.w[0][tid] = v0.coord[3]; S.w[1][tid] = v1.coord[3]; S.w[2][tid] = v2.coord[3];
 #pragma unroll
-                            for (int q = 0; q < kMaxVary; ++q) {
-                                S.vary[0][q][tid] = v0.vary[q]; S.vary[1][q][tid] = v1.vary[q]; S.vary[2][q][tid] = v2.vary[q];
+                                for (int q = 0; q < kMaxVary; ++q) {
+                                    S.vary[0][q][tid] = v0.vary[q]; S.vary[1][q][tid] = v1.vary[q]; S.vary[2][q][tid] = v2.vary[q];
+                                }
                             }
                             S.code[tid] = e | kClippedBit;
                         }
