@@ -1679,8 +1679,12 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
                         const int src = pass == 0 ? int(e) : fv.clip_src[fv.clip_poly[e]];
                         valid = src < end_tri;
                         if (sweep) {
+                            // Without clipped fans the list position alone orders the
+                            // tile's fragments (the list is in drawing order): the
+                            // draw field stays zero.
                             int d = 0;
-                            if (draws_cached) {   // the last draw starting at or before src
+                            if (bin.clip_cnt == 0) {
+                            } else if (draws_cached) {   // the last draw starting at or before src
                                 int lo = 0, hi = fv.ndraws - 1;
                                 while (lo < hi) {
                                     const int mid = (lo + hi + 1) >> 1;
@@ -2016,11 +2020,22 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
         }
     }
     if ((kPhase == 1 || fv.raster_phase == 1) && active) {   // the hand-over to the second launch
+        const bool pairs = (fv.width & 1) == 0 && ((reinterpret_cast<uintptr_t>(fv.vis_own) |
+                                                    reinterpret_cast<uintptr_t>(fv.vis_dep)) & 7u) == 0;
+        if (pairs) {   // the quad's rows as 8-byte stores
 #pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            const size_t i = size_t(qy + (l >> 1)) * size_t(fv.width) + size_t(qx + (l & 1));
-            fv.vis_own[i] = own[l];
-            fv.vis_dep[i] = dep[l];
+            for (int r = 0; r < 2; ++r) {
+                const size_t i = size_t(qy + r) * size_t(fv.width) + size_t(qx);
+                *reinterpret_cast<uint2*>(fv.vis_own + i) = make_uint2(own[2 * r], own[2 * r + 1]);
+                *reinterpret_cast<float2*>(fv.vis_dep + i) = make_float2(dep[2 * r], dep[2 * r + 1]);
+            }
+        } else {
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const size_t i = size_t(qy + (l >> 1)) * size_t(fv.width) + size_t(qx + (l & 1));
+                fv.vis_own[i] = own[l];
+                fv.vis_dep[i] = dep[l];
+            }
         }
     }
 }
