@@ -895,6 +895,8 @@ struct RasterSmem {
     uint32_t zr[N];     // visibility by keys: a depth rank no covered pixel of the triangle goes below
                                    // (0 where no such bound is known)
     int qsum;                      // visibility by keys: the batch's boxes, in quads of the region
+    const FrameOp* ops_of;         // the frame whose ops and draw starts are in ops / dfirst (a CTA
+                                   // taking several blocks of one frame loads them once)
 };
 
 // VTriangleRasterizer setup for one lane (rglv_triangle.hxx:209-240), int32 wrap
@@ -1521,12 +1523,15 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 
     // the op list is read by every thread at every step: one load into shared memory
     const bool ops_cached = fv.nops <= kOpCache;
-    if (ops_cached)
-        for (int i = tid; i < fv.nops; i += blockDim.x) S.ops[i] = fv.ops[i];
     const bool draws_cached = fv.ndraws <= kOpCache;
-    if (draws_cached)
-        for (int i = tid; i < fv.ndraws; i += blockDim.x) S.dfirst[i] = fv.draws[i].first_tri;
-    __syncthreads();
+    if (S.ops_of != fv.ops) {   // the same for every thread (set below, after a barrier)
+        if (ops_cached)
+            for (int i = tid; i < fv.nops; i += blockDim.x) S.ops[i] = fv.ops[i];
+        if (draws_cached)
+            for (int i = tid; i < fv.ndraws; i += blockDim.x) S.dfirst[i] = fv.draws[i].first_tri;
+        __syncthreads();
+        if (tid == 0) S.ops_of = fv.ops;
+    }
     for (int op = 0; op < fv.nops; ++op) {
         const FrameOp o = ops_cached ? S.ops[op] : fv.ops[op];
         if (o.kind == kOpState) {
@@ -2083,6 +2088,8 @@ __device__ __forceinline__ int queue_entry(const FrameView& fv, const int* bucke
 // draws block b.
 template <bool kExt, bool kScissor, int kPhase = 0, int N>
 __device__ __forceinline__ void raster_items(const FrameView& fv, RasterSmem<N>& S) {
+    if (threadIdx.x == 0) S.ops_of = nullptr;   // no frame's ops loaded yet
+    __syncthreads();
     if (fv.tile_queue == nullptr) {
         const int sl = kPhase == 1 ? fv.slices : 1;
         raster_body<kExt, kScissor, kPhase>(fv, int(blockIdx.x) / sl, S, int(blockIdx.x) % sl);
@@ -2197,12 +2204,17 @@ __device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y, c
         }
     }
 }
+// A persistent grid: each CTA reads the draw table once and takes pixel
+// blocks (32x8) in grid-stride order.
 __global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const __grid_constant__ FrameView fv) {
     __shared__ PixelShared P;
     asm volatile("griddepcontrol.wait;" ::: "memory");   // the visibility launch's owners and depths
     publish_counters(fv);
     pixel_shared_load(fv, P);
-    shade_pixel(fv, blockIdx.x * kPixelW + (threadIdx.x % kPixelW), blockIdx.y * kPixelH + (threadIdx.x / kPixelW), P);
+    const int bx = (fv.width + kPixelW - 1) / kPixelW;
+    const int nblocks = bx * ((fv.height + kPixelH - 1) / kPixelH);
+    for (int b = blockIdx.x; b < nblocks; b += gridDim.x)
+        shade_pixel(fv, (b % bx) * kPixelW + (threadIdx.x % kPixelW), (b / bx) * kPixelH + (threadIdx.x / kPixelW), P);
 }
 template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_kernel(const __grid_constant__ FrameView fv) {
@@ -2255,6 +2267,8 @@ __global__ void __launch_bounds__(kBinBlock) bin_batch_kernel(const __grid_const
 // block b.
 template <bool kExt, bool kScissor, int kPhase = 0, int N>
 __device__ __forceinline__ void raster_batch_items(const BatchLaunch& b, RasterSmem<N>& S) {
+    if (threadIdx.x == 0) S.ops_of = nullptr;   // no frame's ops loaded yet
+    __syncthreads();
     if (b.fv[0].tile_queue == nullptr) {
         const int f = batch_frame(b, blockIdx.x);
         raster_body<kExt, kScissor, kPhase>(b.fv[f], blockIdx.x - b.start[f], S);
@@ -2457,7 +2471,9 @@ cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase) {
         pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
         pdl[0].val.programmaticStreamSerializationAllowed = 1;
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(unsigned((fv.width + kPixelW - 1) / kPixelW), unsigned((fv.height + kPixelH - 1) / kPixelH));
+        const int nblocks = ((fv.width + kPixelW - 1) / kPixelW) * ((fv.height + kPixelH - 1) / kPixelH);
+        cfg.gridDim = dim3(unsigned(persistent_blocks(reinterpret_cast<const void*>(shade_pixels_kernel),
+                                                      kPixelW * kPixelH, nblocks)));
         cfg.blockDim = dim3(kPixelW * kPixelH);
         cfg.stream = st;
         cfg.attrs = pdl;
