@@ -189,6 +189,14 @@ __device__ __forceinline__ bool rect_has(uint64_t r, int tx, int ty) {
     return x0 <= tx && tx <= x1 && y0 <= ty && ty <= y1;
 }
 
+// v / d (C's truncating division) for a tile size d > 0: by a shift when d is
+// a power of two (every frame's d is uniform, so the test is a uniform branch
+// and a runtime division is left only for other sizes)
+__device__ __forceinline__ int div_tile(int v, int d) {
+    if ((d & (d - 1)) == 0) return (v + ((v >> 31) & (d - 1))) >> (__ffs(d) - 1);
+    return v / d;
+}
+
 // raster blocks (CTA regions) per tile
 __device__ __forceinline__ int raster_subs(const FrameView& fv) {
     return ((fv.tile_w + fv.region_px - 1) / fv.region_px) * ((fv.tile_h + fv.region_px - 1) / fv.region_px);
@@ -247,7 +255,7 @@ __device__ __forceinline__ uint64_t fan_rect(const FrameView& fv, const int sc[4
     const int vminy = max(min(y0, min(y1, y2)), sc[1]);
     const int vmaxx = min(max(x0, max(x1, x2)) + 1, sc[2] - 1);
     const int vmaxy = min(max(y0, max(y1, y2)) + 1, sc[3] - 1);
-    return pack_rect(vminx / fv.tile_w, vminy / fv.tile_h, vmaxx / fv.tile_w, vmaxy / fv.tile_h);
+    return pack_rect(div_tile(vminx, fv.tile_w), div_tile(vminy, fv.tile_h), div_tile(vmaxx, fv.tile_w), div_tile(vmaxy, fv.tile_h));
 }
 
 // The three transformed vertices of a triangle, passed by value to the
@@ -430,7 +438,7 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
             const uint32_t ni0 = uint32_t(uint16_t(i0)) | (front ? 0u : 0x8000u);
             fv.rec16[2 * g] = (ni0 & 0xffffu) | (uint32_t(uint16_t(idx[1])) << 16);
             fv.rec16[2 * g + 1] = uint32_t(uint16_t(i2));
-            rect = pack_rect(vminx / fv.tile_w, vminy / fv.tile_h, vmaxx / fv.tile_w, vmaxy / fv.tile_h);
+            rect = pack_rect(div_tile(vminx, fv.tile_w), div_tile(vminy, fv.tile_h), div_tile(vmaxx, fv.tile_w), div_tile(vmaxy, fv.tile_h));
         }
         if (needClip) {
             rect = clip_triangle(fv, s, g, tv, rect);
@@ -465,133 +473,6 @@ __device__ __forceinline__ void setup_body(const FrameView& fv, int block) {
 // ---------------------------------------------------------------------------
 // binning
 // ---------------------------------------------------------------------------
-// Which of the super-chunks g0 * 32 .. (g0 + 32) * 32 - 1 overlap tile (tx, ty):
-// lane j returns the mask of group g0 + j (32 super-chunks).  Eight groups'
-// rectangles are in flight per lane at a time.
-__device__ __forceinline__ uint32_t super_masks(const FrameView& fv, int tx, int ty, int lane, int g0) {
-    const int ngroups = min((fv.nsupers + 31) / 32 - g0, 32);
-    uint32_t gm = 0u;
-    for (int gg = 0; gg < ngroups; gg += 8) {
-        bool hs[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int sidx = (g0 + gg + k) * 32 + lane;
-            hs[k] = false;
-            if (gg + k < ngroups && sidx < fv.nsupers) {
-                const int4 r = fv.super_rect[sidx];
-                hs[k] = r.x <= tx && tx <= -r.z && r.y <= ty && ty <= -r.w;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t m = __ballot_sync(FULL_MASK, hs[k]);
-            if (lane == gg + k) gm = m;
-        }
-    }
-    return gm;
-}
-
-// The tile's entries from super-chunk groups g0 .. g0 + 31 (gm: super_masks),
-// in triangle order: counted, or written from inl_out / clip_out on.
-template <bool WRITE>
-__device__ __forceinline__ void bin_walk(const FrameView& fv, int tx, int ty, int lane, uint32_t gm, int g0,
-                                         uint32_t& ninl, uint32_t& nclip,
-                                         uint32_t* __restrict__ inl_out, uint32_t* __restrict__ clip_out) {
-    const uint32_t lt = (1u << lane) - 1u;
-    const int ngroups = min((fv.nsupers + 31) / 32 - g0, 32);
-    for (int gi = 0; gi < ngroups; ++gi) {
-        const int sb = (g0 + gi) * 32;
-        uint32_t ms = __shfl_sync(FULL_MASK, gm, gi);
-        // likewise the chunk rectangles of up to kSuperAhead overlapping super-chunks
-        constexpr int kSuperAhead = 4;
-        int4 sahead[kSuperAhead];
-        int snahead = 0, staken = 0;
-        while (ms) {
-            const int s2 = sb + __ffs(ms) - 1;
-            if (staken == snahead) {
-                uint32_t mm = ms;
-                snahead = 0;
-#pragma unroll
-                for (int k = 0; k < kSuperAhead; ++k) {
-                    sahead[k] = make_int4(1, 1, 0, 0);   // empty: x > z
-                    if (mm) {
-                        const int ck = (sb + __ffs(mm) - 1) * 32 + lane;
-                        mm &= mm - 1;
-                        if (ck < fv.nchunks) sahead[k] = fv.chunk_rect[ck];
-                        ++snahead;
-                    }
-                }
-                staken = 0;
-            }
-            int4 r = sahead[0];
-#pragma unroll
-            for (int k = 1; k < kSuperAhead; ++k) if (staken == k) r = sahead[k];
-            ++staken;
-            ms &= ms - 1;
-            const int c = s2 * 32 + lane;
-            const bool hc = c < fv.nchunks && r.x <= tx && tx <= r.z && r.y <= ty && ty <= r.w;
-            uint32_t mc = __ballot_sync(FULL_MASK, hc);
-            // the tile's overlapping chunks of this super-chunk, up to
-            // kBinStep at a time: their rectangles are loaded and tested
-            // together (independent chains), then appended in chunk order
-            constexpr int kBinStep = 4;
-            while (mc) {
-                int g[kBinStep];
-                uint64_t br[kBinStep];
-#pragma unroll
-                for (int k = 0; k < kBinStep; ++k) {
-                    g[k] = -1;
-                    br[k] = kEmptyRect;
-                    if (mc) {
-                        g[k] = (s2 * 32 + __ffs(mc) - 1) * 32 + lane;
-                        mc &= mc - 1;
-                        if (g[k] < fv.ntris) br[k] = fv.bin_rect[g[k]];
-                    }
-                }
-                bool inl[kBinStep], clp[kBinStep];
-                uint32_t mi[kBinStep];
-                bool anyclip = false;
-#pragma unroll
-                for (int k = 0; k < kBinStep; ++k) {
-                    const bool has = g[k] >= 0 && g[k] < fv.ntris && rect_has(br[k], tx, ty);
-                    inl[k] = has && (br[k] >> 63) == 0;
-                    clp[k] = has && (br[k] >> 63) != 0;
-                    mi[k] = __ballot_sync(FULL_MASK, inl[k]);
-                    anyclip |= clp[k];
-                }
-                anyclip = __any_sync(FULL_MASK, anyclip);
-#pragma unroll
-                for (int k = 0; k < kBinStep; ++k) {
-                    if (WRITE && inl[k]) inl_out[ninl + __popc(mi[k] & lt)] = uint32_t(g[k]);
-                    ninl += __popc(mi[k]);
-                    if (!anyclip) continue;
-                    // clipped fans: warp exclusive scan of per-lane counts
-                    int cnt = 0;
-                    if (clp[k]) {
-                        const ClipInfo ci = fv.clip_info[g[k]];
-                        for (int vi = 1; vi < ci.nverts - 1; ++vi)
-                            cnt += rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty) ? 1 : 0;
-                    }
-                    int incl = cnt;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int v = __shfl_up_sync(FULL_MASK, incl, o);
-                        if (lane >= o) incl += v;
-                    }
-                    const int total = __shfl_sync(FULL_MASK, incl, 31);
-                    if (WRITE && cnt) {
-                        const ClipInfo ci = fv.clip_info[g[k]];
-                        uint32_t pos = nclip + uint32_t(incl - cnt);
-                        for (int vi = 1; vi < ci.nverts - 1; ++vi)
-                            if (rect_has(fv.clip_fan_rect[ci.vbase + vi], tx, ty)) clip_out[pos++] = uint32_t(ci.vbase + vi);
-                    }
-                    nclip += uint32_t(total);
-                }
-            }
-        }
-    }
-}
-
 
 // ---- binning: one CTA of kBinBlock threads per tile ----
 // The tile's overlapping chunks are listed in triangle order (super-chunk
@@ -2173,7 +2054,7 @@ __device__ __forceinline__ void shade_pixel(const FrameView& fv, int x, int y, c
     // the colour: the clear colour, or the owner's
     float c[3] = { P.clear[0], P.clear[1], P.clear[2] };
     if (own != kNoOwner) {
-        const int tx = x / fv.tile_w, ty = y / fv.tile_h;
+        const int tx = div_tile(x, fv.tile_w), ty = div_tile(y, fv.tile_h);
         const int rect[4] = { tx * fv.tile_w, ty * fv.tile_h, min(tx * fv.tile_w + fv.tile_w, fv.width),
                               min(ty * fv.tile_h + fv.tile_h, fv.height) };
         TriSetup t;
@@ -2213,8 +2094,17 @@ __global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_kernel(const _
     pixel_shared_load(fv, P);
     const int bx = (fv.width + kPixelW - 1) / kPixelW;
     const int nblocks = bx * ((fv.height + kPixelH - 1) / kPixelH);
-    for (int b = blockIdx.x; b < nblocks; b += gridDim.x)
-        shade_pixel(fv, (b % bx) * kPixelW + (threadIdx.x % kPixelW), (b / bx) * kPixelH + (threadIdx.x / kPixelW), P);
+    // block b = by * bx + bxi, stepped by the grid size without a division
+    // per block
+    const int step = int(gridDim.x), step_x = step % bx, step_y = step / bx;
+    int bxi = int(blockIdx.x) % bx, by = int(blockIdx.x) / bx;
+    const int px = threadIdx.x % kPixelW, py = threadIdx.x / kPixelW;
+    for (int b = blockIdx.x; b < nblocks; b += step) {
+        shade_pixel(fv, bxi * kPixelW + px, by * kPixelH + py, P);
+        bxi += step_x;
+        by += step_y;
+        if (bxi >= bx) { bxi -= bx; ++by; }
+    }
 }
 template <int N>
 __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_kernel(const __grid_constant__ FrameView fv) {
