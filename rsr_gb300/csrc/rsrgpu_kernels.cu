@@ -2210,11 +2210,16 @@ __global__ void __launch_bounds__(N, raster_ctas<N>(3)) raster_batch_vis_kernel(
 }
 __global__ void __launch_bounds__(kPixelW * kPixelH) shade_pixels_batch_kernel(const __grid_constant__ BatchLaunch b) {
     __shared__ PixelShared P;
+    __shared__ int blk[2];   // the block's column and row in its frame (divided once per CTA)
     const int f = batch_frame(b, blockIdx.x);
     const FrameView& fv = b.fv[f];
-    pixel_shared_load(fv, P);
-    const int k = blockIdx.x - b.start[f], bx = (fv.width + kPixelW - 1) / kPixelW;
-    shade_pixel(fv, (k % bx) * kPixelW + (threadIdx.x % kPixelW), (k / bx) * kPixelH + (threadIdx.x / kPixelW), P);
+    if (threadIdx.x == 0) {
+        const int k = blockIdx.x - b.start[f], bx = (fv.width + kPixelW - 1) / kPixelW;
+        blk[0] = k % bx;
+        blk[1] = k / bx;
+    }
+    pixel_shared_load(fv, P);   // ends with a barrier
+    shade_pixel(fv, blk[0] * kPixelW + (threadIdx.x % kPixelW), blk[1] * kPixelH + (threadIdx.x / kPixelW), P);
 }
 // launches with a frame of float colour stores or ManyProgram draws (the
 // code of raster_ext_kernel, which renders the other frames alike)
