@@ -1112,9 +1112,9 @@ template <bool kExt>
 __device__ __forceinline__ void owner_color(const FrameView& fv, const TriSetup& t, const float w[3],
                                             const float vary[3][kMaxVary], int state, int qx, int qy, int l, float c[3]) {
     const DevState& s = fv.states[state];
-    float bpx, bpy, bpz;
-    lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
     if (s.program == kProgAmy) {
+        // the LoD's lanes 0 and 1, and this lane's coordinates (a lane of the
+        // quad's top row is one of those two)
         float b0x, b0y, b0z, b1x, b1y, b1z;
         lane_bary(fv, t, w, qx, qy, 0, b0x, b0y, b0z);
         lane_bary(fv, t, w, qx, qy, 1, b1x, b1y, b1z);
@@ -1122,13 +1122,24 @@ __device__ __forceinline__ void owner_color(const FrameView& fv, const TriSetup&
         const float v0 = (b0x * vary[0][1] + b0y * vary[1][1]) + b0z * vary[2][1];
         const float u1 = (b1x * vary[0][0] + b1y * vary[1][0]) + b1z * vary[2][0];
         const float v1 = (b1x * vary[0][1] + b1y * vary[1][1]) + b1z * vary[2][1];
-        const float ul = (bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0];
-        const float vl = (bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1];
+        float ul, vl;
+        if (l == 0) {
+            ul = u0; vl = v0;
+        } else if (l == 1) {
+            ul = u1; vl = v1;
+        } else {
+            float bpx, bpy, bpz;
+            lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
+            ul = (bpx * vary[0][0] + bpy * vary[1][0]) + bpz * vary[2][0];
+            vl = (bpx * vary[0][1] + bpy * vary[1][1]) + bpz * vary[2][1];
+        }
         float o[4];
         const DevTexture tu = s.tu0;
         tex_sample_lane(tu, u0, v0, u1, v1, ul, vl, o);
         c[0] = o[0]; c[1] = o[1]; c[2] = o[2];
     } else {
+        float bpx, bpy, bpz;
+        lane_bary(fv, t, w, qx, qy, l, bpx, bpy, bpz);
 #pragma unroll
         for (int q = 0; q < 3; ++q) c[q] = (bpx * vary[0][q] + bpy * vary[1][q]) + bpz * vary[2][q];
         // ManyProgram::ShadeFragment (shaders.hxx:567-582): (u, v, magic, 1)
