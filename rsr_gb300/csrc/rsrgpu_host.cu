@@ -26,7 +26,8 @@
 #include "rsrgpu_internal.h"
 
 namespace rsrgpu {
-cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_frame_init(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_setup(const FrameView& fv, cudaStream_t st, bool after_init = false);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase = 0);
 cudaError_t launch_gather(const GatherList& g, cudaStream_t st);
@@ -1236,14 +1237,15 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         }
         CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
     }
-    CK(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(FrameCounters), st), "memset counters");
     if (fv.slices > 1) {   // merged keys start above every key; no slice has merged
         CK(cudaMemsetAsync(fv.slice_keys, 0xff, sizeof(unsigned long long) * size_t(fv.width) * size_t(fv.height), st), "memset slice keys");
         CK(cudaMemsetAsync(fv.slice_done, 0, sizeof(uint32_t) * size_t(raster_blocks(fv)), st), "memset slice counters");
     }
-    if (fv.nsupers > 0) CK(cudaMemsetAsync(ctx->d_super.p, 0x7f, sizeof(int4) * size_t(fv.nsupers), st), "memset super rects");
     CK(cudaEventRecordWithFlags(ctx->ev0, st, evflags), "event");
-    CK(launch_setup(fv, st), "setup_kernel");
+    // counters and super-chunk rectangles, then setup launched programmatically
+    // dependent on that launch (nothing may come between the two on st)
+    CK(launch_frame_init(fv, st), "frame_init_kernel");
+    CK(launch_setup(fv, st, true), "setup_kernel");
     CK(launch_bin(fv, st), "bin_kernel");
     // A frame whose visibility is resolved by keys rasterises in two
     // launches: visibility (owners and depths handed over through d_vis),
@@ -1285,7 +1287,7 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         if (kv.second.out) CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
     // the counters reach h_counters from the raster pass (FrameView::host_counters)
     CK(cudaEventRecordWithFlags(ctx->ev3, st, evflags), "event");
-    ctx->stats.gpu_launches = 3 + (gl.n > 0 ? 1 : 0) + (split ? 1 : 0);
+    ctx->stats.gpu_launches = 4 + (gl.n > 0 ? 1 : 0) + (split ? 1 : 0);
     return 0;
 }
 

@@ -1940,13 +1940,30 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 // ---------------------------------------------------------------------------
 // kernels: one frame, and a batch of frames in one launch per stage
 // ---------------------------------------------------------------------------
+// A frame starts from zeroed counters and empty super-chunk rectangles
+// (0x7f7f7f7f: setup's atomicMin lands below), written by one small launch
+// that lets setup launch at once (setup waits for it before its first access).
+__global__ void __launch_bounds__(256) frame_init_kernel(FrameCounters* __restrict__ counters, int4* __restrict__ supers,
+                                                         int nsupers) {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    static_assert(sizeof(FrameCounters) % 4 == 0, "counters as words");
+    constexpr int kWords = int(sizeof(FrameCounters) / 4);
+    const int i = int(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i < kWords) reinterpret_cast<uint32_t*>(counters)[i] = 0u;
+    for (int k = i; k < nsupers; k += int(gridDim.x * blockDim.x))
+        supers[k] = make_int4(0x7f7f7f7f, 0x7f7f7f7f, 0x7f7f7f7f, 0x7f7f7f7f);
+}
 // The binning launch is programmatically dependent on setup (launched while
-// setup's CTAs drain; it waits for their results before it reads them).
+// setup's CTAs drain; it waits for their results before it reads them), and
+// setup on frame_init_kernel where that runs (without a prerequisite launch
+// the wait returns at once).
 __global__ void __launch_bounds__(kSetupBlock, 5) setup_kernel(const __grid_constant__ FrameView fv) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     setup_body<false>(fv, blockIdx.x);
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 __global__ void __launch_bounds__(kSetupBlock) setup_ext_kernel(const __grid_constant__ FrameView fv) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     setup_body<true>(fv, blockIdx.x);
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
@@ -2243,12 +2260,35 @@ __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_batch_ext_kernel(
 // ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
-cudaError_t launch_setup(const FrameView& fv, cudaStream_t st) {
+cudaError_t launch_frame_init(const FrameView& fv, cudaStream_t st) {
+    const int words = int(sizeof(FrameCounters) / 4);
+    const int n = fv.nsupers > words ? fv.nsupers : words;
+    const int blocks = (n + 255) / 256 < 64 ? (n + 255) / 256 : 64;
+    frame_init_kernel<<<blocks, 256, 0, st>>>(fv.counters, fv.super_rect, fv.nsupers);
+    return cudaGetLastError();
+}
+
+// after_init: launched programmatically dependent on frame_init_kernel, the
+// launch just before it on st
+cudaError_t launch_setup(const FrameView& fv, cudaStream_t st, bool after_init) {
     const int blocks = (fv.ntris + kSetupBlock - 1) / kSetupBlock;
     if (blocks == 0) return cudaSuccess;
-    if (fv.dext != nullptr) setup_ext_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
-    else setup_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
-    return cudaGetLastError();
+    if (!after_init) {
+        if (fv.dext != nullptr) setup_ext_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
+        else setup_kernel<<<blocks, kSetupBlock, 0, st>>>(fv);
+        return cudaGetLastError();
+    }
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(blocks));
+    cfg.blockDim = dim3(kSetupBlock);
+    cfg.stream = st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = 1;
+    if (fv.dext != nullptr) return cudaLaunchKernelEx(&cfg, setup_ext_kernel, fv);
+    return cudaLaunchKernelEx(&cfg, setup_kernel, fv);
 }
 
 int setup_blocks(const FrameView& fv) { return (fv.ntris + kSetupBlock - 1) / kSetupBlock; }

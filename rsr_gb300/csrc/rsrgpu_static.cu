@@ -39,7 +39,7 @@
 #include "rsrgpu_internal.h"
 
 namespace rsrgpu {
-cudaError_t launch_setup(const FrameView& fv, cudaStream_t st);
+cudaError_t launch_setup(const FrameView& fv, cudaStream_t st, bool after_init = false);
 cudaError_t launch_bin(const FrameView& fv, cudaStream_t st);
 cudaError_t launch_raster(const FrameView& fv, cudaStream_t st, int phase = 0);
 int decode_frame_without_context(int width, int height, int tile_blocks_x, int tile_blocks_y,

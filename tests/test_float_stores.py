@@ -175,5 +175,5 @@ def test_gpu_float_stores_pinned_split_pass(gpu, orc):
     finally:
         for t in bufs:
             gpu.unregister_host_buffer(t)
-    assert launches == 5   # gather, setup, bin, raster (visibility), raster (shading and stores)
+    assert launches == 6   # gather, counters, setup, bin, raster (visibility), raster (shading and stores)
     _check_outputs({k: v.numpy() for k, v in out.items()}, want, False)

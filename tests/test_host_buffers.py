@@ -75,10 +75,10 @@ def test_pinned_and_pageable_host_buffers_match_device_inputs(gpu, which):
     (outs, launches) = _pinned_render(gpu, sc)
     c, d = outs[0]
     assert np.array_equal(d, want_d) and np.array_equal(c, want_c)
-    # gather, setup, bin, and the raster pass of these opaque frames as two
-    # launches (visibility, then shading; the texture of the sphere arrives
-    # during the first)
-    assert launches == 5
+    # gather, the frame's counters, setup, bin, and the raster pass of these
+    # opaque frames as two launches (visibility, then shading; the texture of
+    # the sphere arrives during the first)
+    assert launches == 6
 
 
 @pytest.mark.gpu
