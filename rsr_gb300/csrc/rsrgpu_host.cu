@@ -183,6 +183,7 @@ struct rsrgpu_ctx {
     FrameCounters* h_counters = nullptr;   // pinned, mapped: the raster pass writes it
     FrameCounters* h_counters_dev = nullptr;   // its device address
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    cudaEvent_t ev_done = nullptr;   // ev2 or ev3: the last event of a run (not owned)
     // textures from host buffers are copied on `side` while setup and binning run
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_late = nullptr;
@@ -1237,13 +1238,10 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         }
         CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
     }
-    if (fv.slices > 1) {   // merged keys start above every key; no slice has merged
-        CK(cudaMemsetAsync(fv.slice_keys, 0xff, sizeof(unsigned long long) * size_t(fv.width) * size_t(fv.height), st), "memset slice keys");
-        CK(cudaMemsetAsync(fv.slice_done, 0, sizeof(uint32_t) * size_t(raster_blocks(fv)), st), "memset slice counters");
-    }
     CK(cudaEventRecordWithFlags(ctx->ev0, st, evflags), "event");
-    // counters and super-chunk rectangles, then setup launched programmatically
-    // dependent on that launch (nothing may come between the two on st)
+    // counters, super-chunk rectangles and slice keys, then setup launched
+    // programmatically dependent on that launch (nothing may come between the
+    // two on st)
     CK(launch_frame_init(fv, st), "frame_init_kernel");
     CK(launch_setup(fv, st, true), "setup_kernel");
     CK(launch_bin(fv, st), "bin_kernel");
@@ -1283,10 +1281,17 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
     }
     CK(cudaEventRecordWithFlags(ctx->ev2, st, evflags), "event");
     // outputs written in place need no copy back
+    bool copies = false;
     for (auto& kv : ctx->host)
-        if (kv.second.out) CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
-    // the counters reach h_counters from the raster pass (FrameView::host_counters)
-    CK(cudaEventRecordWithFlags(ctx->ev3, st, evflags), "event");
+        if (kv.second.out) {
+            CK(cudaMemcpyAsync(const_cast<uint8_t*>(kv.second.host), kv.second.dev, kv.second.bytes, cudaMemcpyDeviceToHost, st), "D2H output");
+            copies = true;
+        }
+    // the run's completion: after the output copies, or the end of the raster
+    // pass (the counters reach h_counters from the raster pass,
+    // FrameView::host_counters)
+    if (copies) CK(cudaEventRecordWithFlags(ctx->ev3, st, evflags), "event");
+    ctx->ev_done = copies ? ctx->ev3 : ctx->ev2;
     ctx->stats.gpu_launches = 4 + (gl.n > 0 ? 1 : 0) + (split ? 1 : 0);
     return 0;
 }
@@ -1346,7 +1351,7 @@ int rsrgpu_wait(rsrgpu_ctx* ctx, int timeout_ms) {
     for (int attempt = 0; attempt < 8; ++attempt) {
         const auto t0 = std::chrono::steady_clock::now();
         while (true) {
-            cudaError_t q = cudaEventQuery(ctx->ev3);
+            cudaError_t q = cudaEventQuery(ctx->ev_done);
             if (q == cudaSuccess) break;
             if (q != cudaErrorNotReady) return cuda_fail(ctx, q, "run");
             if (timeout_ms >= 0) {

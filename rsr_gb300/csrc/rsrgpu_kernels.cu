@@ -1941,17 +1941,23 @@ __device__ __forceinline__ void raster_body(const FrameView& fv, int block, Rast
 // kernels: one frame, and a batch of frames in one launch per stage
 // ---------------------------------------------------------------------------
 // A frame starts from zeroed counters and empty super-chunk rectangles
-// (0x7f7f7f7f: setup's atomicMin lands below), written by one small launch
-// that lets setup launch at once (setup waits for it before its first access).
-__global__ void __launch_bounds__(256) frame_init_kernel(FrameCounters* __restrict__ counters, int4* __restrict__ supers,
-                                                         int nsupers) {
+// (0x7f7f7f7f: setup's atomicMin lands below), and, where the visibility
+// launch slices tile lists, merged keys above every key and no slice merged;
+// one small launch writes them and lets setup launch at once (setup waits
+// for it before its first access).
+__global__ void __launch_bounds__(256) frame_init_kernel(const __grid_constant__ FrameView fv, int nblocks) {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     static_assert(sizeof(FrameCounters) % 4 == 0, "counters as words");
     constexpr int kWords = int(sizeof(FrameCounters) / 4);
-    const int i = int(blockIdx.x * blockDim.x + threadIdx.x);
-    if (i < kWords) reinterpret_cast<uint32_t*>(counters)[i] = 0u;
-    for (int k = i; k < nsupers; k += int(gridDim.x * blockDim.x))
-        supers[k] = make_int4(0x7f7f7f7f, 0x7f7f7f7f, 0x7f7f7f7f, 0x7f7f7f7f);
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x, step = size_t(gridDim.x) * blockDim.x;
+    if (i < size_t(kWords)) reinterpret_cast<uint32_t*>(fv.counters)[i] = 0u;
+    for (size_t k = i; k < size_t(fv.nsupers); k += step)
+        fv.super_rect[k] = make_int4(0x7f7f7f7f, 0x7f7f7f7f, 0x7f7f7f7f, 0x7f7f7f7f);
+    if (fv.slices > 1) {
+        const size_t nkeys = size_t(fv.width) * size_t(fv.height);
+        for (size_t k = i; k < nkeys; k += step) fv.slice_keys[k] = ~0ull;
+        for (size_t k = i; k < size_t(nblocks); k += step) fv.slice_done[k] = 0u;
+    }
 }
 // The binning launch is programmatically dependent on setup (launched while
 // setup's CTAs drain; it waits for their results before it reads them), and
@@ -2260,11 +2266,15 @@ __global__ void __launch_bounds__(N, raster_ctas<N>(2)) raster_batch_ext_kernel(
 // ---------------------------------------------------------------------------
 // launch wrappers
 // ---------------------------------------------------------------------------
+int raster_blocks(const FrameView& fv);
+
 cudaError_t launch_frame_init(const FrameView& fv, cudaStream_t st) {
-    const int words = int(sizeof(FrameCounters) / 4);
-    const int n = fv.nsupers > words ? fv.nsupers : words;
-    const int blocks = (n + 255) / 256 < 64 ? (n + 255) / 256 : 64;
-    frame_init_kernel<<<blocks, 256, 0, st>>>(fv.counters, fv.super_rect, fv.nsupers);
+    const int nblocks = raster_blocks(fv);
+    size_t n = sizeof(FrameCounters) / 4;
+    if (size_t(fv.nsupers) > n) n = size_t(fv.nsupers);
+    if (fv.slices > 1 && size_t(fv.width) * size_t(fv.height) / 4 > n) n = size_t(fv.width) * size_t(fv.height) / 4;
+    const size_t blocks = (n + 255) / 256 < 152 ? (n + 255) / 256 : 152;
+    frame_init_kernel<<<unsigned(blocks), 256, 0, st>>>(fv, nblocks);
     return cudaGetLastError();
 }
 
