@@ -187,6 +187,10 @@ struct rsrgpu_ctx {
     // textures from host buffers are copied on `side` while setup and binning run
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_late = nullptr;
+    // the timing marks ev0 and ev1 are recorded on `marks`, a branch the
+    // kernels do not wait for
+    cudaStream_t marks = nullptr;
+    cudaEvent_t ev_mark_fork = nullptr, ev_mark_join = nullptr;
     FrameView fv{};
     rsrgpu_stats stats{};
 };
@@ -449,6 +453,9 @@ int rsrgpu_create(int device, rsrgpu_ctx** out) {
     if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->marks, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_mark_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_mark_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_late, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_tables, cudaEventDisableTiming) != cudaSuccess ||
@@ -491,10 +498,13 @@ int rsrgpu_destroy(rsrgpu_ctx* ctx) {
     if (ctx->ev_tables_live) cudaEventSynchronize(ctx->ev_tables);
     if (ctx->h_tables) cudaFreeHost(ctx->h_tables);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->marks) cudaStreamSynchronize(ctx->marks);
     drop_graph(ctx);
     if (ctx->cap) cudaStreamDestroy(ctx->cap);
-    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_fork, ctx->ev_late, ctx->ev_tables };
+    cudaEvent_t evs[] = { ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_fork, ctx->ev_late, ctx->ev_tables,
+                          ctx->ev_mark_fork, ctx->ev_mark_join };
     for (cudaEvent_t ev : evs) if (ev) cudaEventDestroy(ev);
+    if (ctx->marks) cudaStreamDestroy(ctx->marks);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
@@ -1238,7 +1248,16 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         }
         CK(cudaEventRecord(ctx->ev_late, ctx->side), "event");
     }
-    CK(cudaEventRecordWithFlags(ctx->ev0, st, evflags), "event");
+    // Timing marks branch off st: ev0 (the frame's start) and ev1 (the raster
+    // pass's start) are recorded on `marks` once st reaches them, and st
+    // rejoins the branch before ev2, so no kernel waits on an event node.
+    auto mark = [&](cudaEvent_t ev) {
+        cudaError_t e = cudaEventRecord(ctx->ev_mark_fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->marks, ctx->ev_mark_fork, 0);
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev, ctx->marks, evflags);
+        return e;
+    };
+    CK(mark(ctx->ev0), "timing mark");
     // counters, super-chunk rectangles and slice keys, then setup launched
     // programmatically dependent on that launch (nothing may come between the
     // two on st)
@@ -1254,7 +1273,7 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
     // to let textures still on their way arrive during the visibility launch.
     const bool compiled_split = fv.vis_keys != 0 && !fv.ext && !fv.any_scissor;
     const bool split = fv.vis_keys != 0 && (any_late || compiled_split);
-    CK(cudaEventRecordWithFlags(ctx->ev1, st, evflags), "event");
+    CK(mark(ctx->ev1), "timing mark");
     if (split) {
         FrameView f = fv;
         f.vis_own = ctx->d_vis.as<uint32_t>();
@@ -1279,6 +1298,8 @@ int record_run(rsrgpu_ctx* ctx, cudaStream_t st, bool captured) {
         if (any_late) CK(cudaStreamWaitEvent(st, ctx->ev_late, 0), "stream wait");
         CK(launch_raster(fv, st), "raster_kernel");
     }
+    CK(cudaEventRecord(ctx->ev_mark_join, ctx->marks), "event");
+    CK(cudaStreamWaitEvent(st, ctx->ev_mark_join, 0), "stream wait");
     CK(cudaEventRecordWithFlags(ctx->ev2, st, evflags), "event");
     // outputs written in place need no copy back
     bool copies = false;
