@@ -399,6 +399,9 @@ def measure_frame(gpu, sc, args, stream, flush, world, clocks=None):
 # the kernels change).
 RASTER_WARP_INST = {"textured_sphere_1080p": 21_308_959 + 15_164_016, "plain_640x360": 166_223_473 + 3_089_735}
 RASTER_PASS = "raster pass (raster_vis_kernel + shade_pixels_kernel)"
+# the window rsrgpu_last_timings reports for it (CUDA events in the replayed frame graph)
+RASTER_WINDOW = ("end of binning (a timing mark on a graph branch that waits for bin_kernel) "
+                 "to the end of shading (an event after shade_pixels_kernel on its stream)")
 
 
 def issue_roofline(kernel_ms, inst, sm_mhz, num_sms):
@@ -449,7 +452,7 @@ def run_gpu(args):
     frame_s = head["ms_per_step"] / 1e3
     roof = issue_roofline(head["raster_ms"], RASTER_WARP_INST["textured_sphere_1080p"], sm_mhz, num_sms) or {
         "bound": "issue", "achieved": None, "peak": None, "unit": "Gwarp-inst/s", "frac": None}
-    roof.update({"kernel": RASTER_PASS, "avg_launch_ms": head["raster_ms"], "traffic": None,
+    roof.update({"kernel": RASTER_PASS, "avg_launch_ms": head["raster_ms"], "window": RASTER_WINDOW, "traffic": None,
                  "hbm": {"scope": "whole frame (setup, bin, raster)", "compulsory_bytes": comp,
                          "achieved_gbs": comp / frame_s / 1e9, "peak_gbs": peak, "frac": comp / frame_s / 1e9 / peak,
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}})

@@ -315,7 +315,11 @@ int rsrgpu_dump_tiles(rsrgpu_ctx* ctx, uint8_t* out, size_t capacity, size_t* ne
 int rsrgpu_dump_clipped(rsrgpu_ctx* ctx, rsrgpu_clipped_vertex* out, int capacity, int* count);
 int rsrgpu_get_stats(rsrgpu_ctx* ctx, rsrgpu_stats* out);
 
-/* Device timing of the last run's kernels (CUDA events on the run stream). */
+/* Device timing of the last run (CUDA events in the run's work): total_ms from
+ * the frame's start (after any input gather) to the end of the raster pass,
+ * raster_ms from the end of binning to the end of the raster pass.  The start
+ * marks are recorded on a branch that waits for the run stream's work before
+ * them, so no kernel waits for them. */
 int rsrgpu_last_timings(rsrgpu_ctx* ctx, float* total_ms, float* raster_ms);
 
 int rsrgpu_last_error(rsrgpu_ctx* ctx, char* buf, size_t len);
