@@ -108,6 +108,25 @@ def test_device_resident_inputs(gpu, cpu):
     assert np.array_equal(dep.cpu().numpy().view(np.uint32), od.view(np.uint32))
 
 
+def test_run_timings(gpu):
+    """rsrgpu_last_timings: the raster pass (from the end of binning) lies
+    within the frame (from its start), on the first run and on graph replays."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.plain_raster(seed=12, ntris=4000)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in sc.arrays.items()}
+    col = torch.zeros(sc.width * sc.height, dtype=torch.int32, device="cuda")
+    dep = torch.zeros(sc.width * sc.height, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    gpu.Reset(sc.width, sc.height, sc.tile_blocks)
+    gpu.Run(sc.record(ref=dev.__getitem__, color=col, depth=dep, gamma=False), stream=stream)
+    gpu.Wait()
+    for _ in range(3):
+        total, raster = gpu.timings()
+        assert 0.0 < raster <= total
+        gpu.run(stream)
+        gpu.Wait()
+
+
 def test_repeat_determinism(gpu):
     sc = scenes.textured_sphere(divs=5, width=640, height=360, tile_blocks=(4, 4))
     a = render_scene(gpu, sc, True)
